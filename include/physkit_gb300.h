@@ -1,0 +1,167 @@
+/*
+ * physkit_gb300.h — C ABI of the GB300-native PhysKit world step.
+ *
+ * The reference has no plugin or operator interface; its drop-in seam is the virtual
+ * world_base::step_impl(dt) (include/physkit/core/world.h:340, overridden by world at world.h:423
+ * and implemented in src/world.cpp:20-56). This ABI is what a C++ `gpu_world : world_base`
+ * override (or any FFI) binds: body creation/removal replaces world_base::create_rigid /
+ * remove_rigid (world.h:202-218), pk_world_step replaces world_base::step's call of step_impl
+ * (world.h:234-242), and the read-back calls replace get_rigid (world.h:220-224) and the
+ * on_collision / on_collision_exit callbacks (world.h:327-338).
+ *
+ * Conventions: plain C types, caller-owned descriptors (copied), library-owned device memory,
+ * int status returns (0 = PK_OK, negative = error), no exceptions across the ABI. One world
+ * object is single-threaded like the reference (swappable_queue.h:13); distinct world objects
+ * may be used from distinct threads. All device work of a world runs on its own CUDA stream.
+ *
+ * A world object may hold several independent sub-worlds ("worlds" below) that are stepped
+ * together by the same launches (the batched form); max_worlds = 1 is the plain single world.
+ */
+#ifndef PHYSKIT_GB300_H
+#define PHYSKIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PK_OK 0
+#define PK_ERR_INVALID (-1)       /* bad argument (e.g. missing shape: object.h:121 throws) */
+#define PK_ERR_STALE_HANDLE (-2)  /* handle generation mismatch (arena.h:234-244) */
+#define PK_ERR_CAPACITY (-3)      /* a fixed capacity given at creation is exhausted */
+#define PK_ERR_CUDA (-4)          /* a CUDA runtime call failed; pk_last_cuda_error() tells which */
+#define PK_ERR_DEVICE_STATUS (-5) /* the step finished but flagged a status bit (pk_step_info.status) */
+#define PK_ERR_NO_DEVICE (-6)     /* no CUDA device: this library has no CPU fallback */
+
+/* pk_step_info.status bits */
+#define PK_STATUS_PAIR_OVERFLOW 1   /* more overlap pairs than max_pairs: extra pairs dropped */
+#define PK_STATUS_EPA_CAP 2         /* an EPA polytope hit the fixed face/horizon capacity */
+#define PK_STATUS_COLOUR_CAP 4      /* more than 512 colouring rounds in one world */
+#define PK_STATUS_TRAVERSAL_STACK 8 /* LBVH traversal stack overflow */
+#define PK_STATUS_NAN 16            /* a non-finite position appeared */
+
+enum
+{
+    PK_PRECISION_F64 = 0, /* FP64 throughout; arithmetic order identical to the FP64 oracle */
+    PK_PRECISION_F32 = 1  /* FP32 state and geometry; FP64 accumulated impulses */
+};
+enum
+{
+    PK_BODY_DYNAMIC = 0, /* body_type::dynam (object.h:9-13) */
+    PK_BODY_STATIC = 1   /* body_type::stat: infinite mass, never integrated (object.h:81-85) */
+};
+
+typedef struct pk_world pk_world;
+
+typedef struct pk_world_desc
+{
+    double gravity[3];            /* world_desc gravity, default (0,-9.81,0): world.h:43-47 */
+    int32_t solver_iterations;    /* world_desc solver_iterations, default 10: world.h:48 */
+    int32_t precision;            /* PK_PRECISION_* */
+    int32_t max_bodies;           /* body slots over all worlds */
+    int32_t max_pairs;            /* broadphase pairs (0: 8 per body) */
+    int32_t max_worlds;           /* independent worlds stepped together (1: plain world) */
+    int32_t max_bodies_per_world; /* 0: max_bodies */
+    int32_t max_shape_vertices;   /* 0: 65536 */
+    int32_t max_shapes;           /* 0: 1024 */
+} pk_world_desc;
+
+typedef struct pk_body_desc /* object_desc (object.h:15-109) */
+{
+    int32_t type;   /* PK_BODY_* */
+    int32_t shape;  /* from pk_shape_*; object.h:61-65 (shared mesh) */
+    int32_t world;  /* sub-world index, 0 for the plain world */
+    int32_t reserved;
+    double pos[3];
+    double quat[4]; /* w, x, y, z (lin_alg.h:428-432) */
+    double vel[3];
+    double ang_vel[3];
+    double mass;        /* ignored for static bodies (infinite) */
+    double inertia[9];  /* local inertia tensor, row-major; inverted here like particle.h:126-131 */
+    double restitution; /* default 0.5 (object.h:107) */
+    double friction;    /* default 0.5 (object.h:108) */
+} pk_body_desc;
+
+typedef struct pk_step_info
+{
+    int32_t pairs;  /* broadphase pairs of the last step (all worlds) */
+    int32_t leaves; /* bodies in the LBVH of the last step */
+    int32_t status; /* PK_STATUS_* bits seen since the previous synchronize */
+    int32_t reserved;
+} pk_step_info;
+
+/* Primitive shape for pk_collide: kind 0 aabb (p = min3 max3), 1 obb (p = center3 quat4 half3),
+ * 2 mesh instance (p = pos3 quat4, shape = mesh id). */
+typedef struct pk_collide_shape
+{
+    int32_t kind;
+    int32_t shape;
+    double p[10];
+} pk_collide_shape;
+
+void pk_world_desc_init(pk_world_desc *desc);
+void pk_body_desc_init(pk_body_desc *desc);
+
+/* world_base(world_desc) / world(world_desc) (world.h:188-190, 382-385). */
+int pk_world_create(const pk_world_desc *desc, pk_world **out);
+void pk_world_destroy(pk_world *w);
+
+/* mesh::make / box / sphere / pyramid (mesh.h:219-236, mesh.cpp:16-137). Shapes are shared. */
+int pk_shape_mesh(pk_world *w, const double *verts, int32_t nverts, const int32_t *tris, int32_t ntris,
+                  int32_t *out_shape);
+int pk_shape_box(pk_world *w, double hx, double hy, double hz, int32_t *out_shape);
+int pk_shape_sphere(pk_world *w, double radius, int32_t stacks, int32_t sectors, int32_t *out_shape);
+int pk_shape_pyramid(pk_world *w, double base_half, double height, int32_t *out_shape);
+
+/* world_base::create_rigid (world.h:202-208) for n bodies; handles are arena ids
+ * (slot | generation << 32, arena.h:179-206). Bodies join the broadphase with exact bounds. */
+int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out_handles);
+/* world_base::remove_rigid (world.h:209-218): drops the body, its pairs and manifolds. */
+int pk_body_remove(pk_world *w, uint64_t handle);
+/* Retire a whole sub-world (all its bodies) and free its slots for reuse. */
+int pk_world_clear(pk_world *w, int32_t world);
+int pk_world_set_active(pk_world *w, int32_t world, int32_t active);
+int pk_world_set_gravity(pk_world *w, int32_t world, const double gravity[3]);
+
+/* One world step: world::step_impl (src/world.cpp:20-56) on the device. pk_world_step waits for
+ * completion and returns PK_ERR_DEVICE_STATUS if a status bit was raised. */
+int pk_world_step(pk_world *w, double dt);
+int pk_world_step_async(pk_world *w, double dt);
+int pk_world_synchronize(pk_world *w, pk_step_info *info);
+/* Record the step for a fixed dt as CUDA graphs; pk_world_step_graph replays one step async. */
+int pk_world_capture(pk_world *w, double dt);
+int pk_world_step_graph(pk_world *w);
+/* The CUDA stream (cudaStream_t) the world's work runs on. */
+void *pk_world_stream(pk_world *w);
+
+/* Per slot: pos3 quat4 vel3 ang_vel3 alive = 14 doubles (particle.h:135-149). */
+int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);
+/* Overwrite pos/quat/vel/ang_vel of one body and refresh its cached world inertia. */
+int pk_world_write_body(pk_world *w, uint64_t handle, const double *state13);
+/* Sorted broadphase pairs of the last step. keys use the reference layout
+ * (min_local << 32 | max_local, collision_phases.h:63-69); worlds gives each pair's world. */
+int pk_world_read_pairs(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t cap, int32_t *n);
+/* Manifolds of the last step in key order: 4 contacts x 13 doubles each
+ * (normal3 local_a3 local_b3 depth normal_impulse tangent_impulse2), collision_phases.h:75-99. */
+int pk_world_read_manifolds(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *counts, double *contacts,
+                            int32_t cap, int32_t *n);
+/* Begin (1) / end (2) collision events of the last step (collision_phases.h:309-318). */
+int pk_world_read_events(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *kinds, int32_t cap, int32_t *n);
+/* Solver colour of each manifold with contact rows in the last step (key order). */
+int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t cap, int32_t *n,
+                          int32_t *ncolours_world0);
+
+/* Narrowphase (gjk_epa, collision.cpp:512-518) on n primitive shape pairs; out has 10 doubles per
+ * pair: normal3 world_a3 world_b3 depth. hit[i] = 1 on collision. */
+int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
+               int32_t *hit);
+
+int pk_last_cuda_error(void);
+const char *pk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

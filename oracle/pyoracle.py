@@ -272,3 +272,21 @@ def sincos(x):
     s, c = C.c_double(), C.c_double()
     lib().pko_sincos(float(x), C.byref(s), C.byref(c))
     return s.value, c.value
+
+
+def load_scene(ow: "OracleWorld", scene):
+    """Create a physkit_gb300.scenes.Scene (one world) in an oracle world, in record order."""
+    ids = []
+    for s in scene.shapes:
+        if s[0] == "box":
+            ids.append(ow.box(*s[1:4]))
+        elif s[0] == "sphere":
+            ids.append(ow.sphere(s[1], s[2], s[3]))
+        else:
+            ids.append(ow.mesh(s[1], s[2]))
+    handles = []
+    for r in scene.bodies:
+        handles.append(ow.add(ids[int(r["shape"])], r["pos"], r["quat"], r["vel"], r["ang_vel"],
+                              float(r["mass"]), np.asarray(r["inertia"]).reshape(3, 3),
+                              float(r["restitution"]), float(r["friction"]), static=bool(r["type"] == 1)))
+    return handles

@@ -1,0 +1,636 @@
+// pk_capi.cu — the C ABI (include/physkit_gb300.h) over the device engine.
+//
+// Host-side bookkeeping mirrors the reference's world_base: each sub-world owns a generational
+// arena of local indices (detail/arena.h:169-267: a free stack of indices, generations bumped on
+// removal), and the local index is what pair keys are built from (world.h:206). Each local index
+// of a world is bound to one device slot for its lifetime, so results do not depend on where in
+// device memory a world lives.
+#include "../../include/physkit_gb300.h"
+#include "pk_engine_api.h"
+#include "pk_math.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace
+{
+int g_last_cuda = 0;
+
+struct SlotInfo
+{
+    int world = -1;
+    int local = -1;
+    uint32_t gen = 0;
+    bool alive = false;
+    bool is_static = false;
+};
+
+struct SubWorld
+{
+    std::vector<int> local_slot;   // local index -> device slot (-1 when never bound)
+    std::vector<uint32_t> local_gen;
+    std::vector<int> free_locals;  // arena free stack (arena.h:208-232)
+    std::vector<char> local_alive;
+    double gravity[3] = {0.0, -9.81, 0.0};
+    int active = 1;
+};
+
+int bits_for(long long v)
+{
+    int b = 1;
+    while ((1LL << b) < v) ++b;
+    return b;
+}
+} // namespace
+
+struct pk_world
+{
+    pk::EngineBase *eng = nullptr;
+    pk::EngineConfig cfg;
+    pk_world_desc desc;
+    std::vector<double> verts;   // all shape vertices
+    std::vector<int> ranges;     // (start, count) per shape
+    std::vector<double> boxes;   // local aabb per shape
+    std::vector<SubWorld> worlds;
+    std::vector<SlotInfo> slots;
+    std::vector<int> free_slots;
+    int nslots = 0;
+    int steps = 0;
+    bool shapes_dirty = false;
+};
+
+extern "C" {
+
+void pk_world_desc_init(pk_world_desc *d)
+{
+    std::memset(d, 0, sizeof(*d));
+    d->gravity[0] = 0.0;
+    d->gravity[1] = -9.81;
+    d->gravity[2] = 0.0;
+    d->solver_iterations = 10;
+    d->precision = PK_PRECISION_F64;
+    d->max_bodies = 4096;
+    d->max_pairs = 0;
+    d->max_worlds = 1;
+    d->max_bodies_per_world = 0;
+    d->max_shape_vertices = 0;
+    d->max_shapes = 0;
+}
+
+void pk_body_desc_init(pk_body_desc *d)
+{
+    std::memset(d, 0, sizeof(*d));
+    d->type = PK_BODY_DYNAMIC;
+    d->quat[0] = 1.0;
+    d->mass = 1.0;
+    d->inertia[0] = d->inertia[4] = d->inertia[8] = 1.0;
+    d->restitution = 0.5;
+    d->friction = 0.5;
+}
+
+int pk_last_cuda_error(void) { return g_last_cuda; }
+const char *pk_version(void) { return "physkit_gb300 0.1.0 (sm_103a)"; }
+
+int pk_world_create(const pk_world_desc *desc, pk_world **out)
+{
+    if (!desc || !out) return PK_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_NO_DEVICE;
+    }
+    if (desc->max_bodies <= 0 || desc->max_worlds <= 0 || desc->solver_iterations < 0) return PK_ERR_INVALID;
+    if (desc->precision != PK_PRECISION_F64 && desc->precision != PK_PRECISION_F32) return PK_ERR_INVALID;
+    auto *w = new (std::nothrow) pk_world;
+    if (!w) return PK_ERR_CAPACITY;
+    w->desc = *desc;
+    pk::EngineConfig &c = w->cfg;
+    c.body_cap = desc->max_bodies;
+    c.pair_cap = desc->max_pairs > 0 ? desc->max_pairs : 8 * desc->max_bodies;
+    c.max_worlds = desc->max_worlds;
+    c.vert_cap = desc->max_shape_vertices > 0 ? desc->max_shape_vertices : 65536;
+    c.shape_cap = desc->max_shapes > 0 ? desc->max_shapes : 1024;
+    c.iterations = desc->solver_iterations;
+    int per_world = desc->max_bodies_per_world > 0 ? desc->max_bodies_per_world : desc->max_bodies;
+    c.lbits = bits_for(per_world);
+    c.wbits = bits_for((long long)desc->max_worlds + 1);
+    if (c.wbits + 2 * c.lbits > 64 || c.wbits + 30 > 64)
+    {
+        delete w;
+        return PK_ERR_INVALID;
+    }
+    int sms = 148;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto blocks_for = [&](long long n)
+    {
+        long long b = (n + 4095) / 4096;
+        if (b > 2LL * sms) b = 2LL * sms;
+        return int(b < 1 ? 1 : b);
+    };
+    c.sort_blocks_bodies = blocks_for(c.body_cap);
+    c.sort_blocks_pairs = blocks_for(c.pair_cap);
+    w->eng = desc->precision == PK_PRECISION_F64 ? pk::make_engine_f64() : pk::make_engine_f32();
+    int rc = w->eng->init(c);
+    if (rc)
+    {
+        g_last_cuda = w->eng->last_error();
+        delete w->eng;
+        delete w;
+        return PK_ERR_CUDA;
+    }
+    w->worlds.resize(size_t(desc->max_worlds));
+    w->slots.resize(size_t(desc->max_bodies));
+    for (int i = 0; i < desc->max_worlds; ++i)
+    {
+        SubWorld &sw = w->worlds[size_t(i)];
+        for (int k = 0; k < 3; ++k) sw.gravity[k] = desc->gravity[k];
+        double gn = std::sqrt(sw.gravity[0] * sw.gravity[0] + sw.gravity[1] * sw.gravity[1] +
+                              sw.gravity[2] * sw.gravity[2]);
+        if (w->eng->set_world(i, sw.gravity, gn, 1))
+        {
+            g_last_cuda = w->eng->last_error();
+            delete w->eng;
+            delete w;
+            return PK_ERR_CUDA;
+        }
+    }
+    *out = w;
+    return PK_OK;
+}
+
+void pk_world_destroy(pk_world *w)
+{
+    if (!w) return;
+    delete w->eng;
+    delete w;
+}
+
+static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
+{
+    size_t nv = v.size() / 3;
+    if (nv == 0) return PK_ERR_INVALID;
+    if (w->verts.size() / 3 + nv > size_t(w->cfg.vert_cap) || w->ranges.size() / 2 + 1 > size_t(w->cfg.shape_cap))
+        return PK_ERR_CAPACITY;
+    // aabb::from_points (bounds.h:33-49)
+    double mn[3] = {v[0], v[1], v[2]}, mx[3] = {v[0], v[1], v[2]};
+    for (size_t i = 1; i < nv; ++i)
+        for (int k = 0; k < 3; ++k)
+        {
+            double x = v[3 * i + k];
+            mn[k] = (x < mn[k]) ? x : mn[k];
+            mx[k] = (mx[k] < x) ? x : mx[k];
+        }
+    int id = int(w->ranges.size() / 2);
+    w->ranges.push_back(int(w->verts.size() / 3));
+    w->ranges.push_back(int(nv));
+    w->verts.insert(w->verts.end(), v.begin(), v.end());
+    for (int k = 0; k < 3; ++k) w->boxes.push_back(mn[k]);
+    for (int k = 0; k < 3; ++k) w->boxes.push_back(mx[k]);
+    w->shapes_dirty = true; // uploaded in one copy before the next use (flush_shapes)
+    if (out) *out = id;
+    return PK_OK;
+}
+
+static int flush_shapes(pk_world *w)
+{
+    if (!w->shapes_dirty) return PK_OK;
+    if (w->eng->set_shapes(w->verts, w->ranges, w->boxes))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    w->shapes_dirty = false;
+    return PK_OK;
+}
+
+int pk_shape_mesh(pk_world *w, const double *verts, int32_t nverts, const int32_t *tris, int32_t ntris, int32_t *out)
+{
+    if (!w || !verts || nverts <= 0 || ntris <= 0 || !tris) return PK_ERR_INVALID;
+    for (int i = 0; i < 3 * ntris; ++i)
+        if (tris[i] < 0 || tris[i] >= nverts) return PK_ERR_INVALID;
+    return add_shape(w, std::vector<double>(verts, verts + 3 * size_t(nverts)), out);
+}
+
+int pk_shape_box(pk_world *w, double hx, double hy, double hz, int32_t *out)
+{
+    if (!w) return PK_ERR_INVALID;
+    // mesh::box vertex order (mesh.cpp:31-40)
+    std::vector<double> v = {-hx, -hy, -hz, +hx, -hy, -hz, +hx, +hy, -hz, -hx, +hy, -hz,
+                             -hx, -hy, +hz, +hx, -hy, +hz, +hx, +hy, +hz, -hx, +hy, +hz};
+    return add_shape(w, v, out);
+}
+
+int pk_shape_sphere(pk_world *w, double r, int32_t stacks, int32_t sectors, int32_t *out)
+{
+    if (!w || stacks < 2 || sectors < 3) return PK_ERR_INVALID;
+    // mesh::sphere UV layout (mesh.cpp:60-115)
+    std::vector<double> v = {0.0, r, 0.0};
+    for (int i = 1; i < stacks; ++i)
+    {
+        double phi = M_PI * double(i) / double(stacks);
+        for (int j = 0; j < sectors; ++j)
+        {
+            double theta = 2.0 * M_PI * double(j) / double(sectors);
+            v.push_back(r * std::sin(phi) * std::cos(theta));
+            v.push_back(r * std::cos(phi));
+            v.push_back(r * std::sin(phi) * std::sin(theta));
+        }
+    }
+    v.push_back(0.0);
+    v.push_back(-r);
+    v.push_back(0.0);
+    return add_shape(w, v, out);
+}
+
+int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)
+{
+    if (!w) return PK_ERR_INVALID;
+    // mesh::pyramid (mesh.cpp:117-137)
+    std::vector<double> v = {-b, 0.0, -b, +b, 0.0, -b, +b, 0.0, +b, -b, 0.0, +b, 0.0, h, 0.0};
+    return add_shape(w, v, out);
+}
+
+int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out)
+{
+    if (!w || (n > 0 && !descs)) return PK_ERR_INVALID;
+    int nshapes = int(w->ranges.size() / 2);
+    for (int i = 0; i < n; ++i)
+    {
+        const pk_body_desc &d = descs[i];
+        if (d.shape < 0 || d.shape >= nshapes) return PK_ERR_INVALID; // object.h:121
+        if (d.world < 0 || d.world >= w->cfg.max_worlds) return PK_ERR_INVALID;
+        if (d.type != PK_BODY_DYNAMIC && d.type != PK_BODY_STATIC) return PK_ERR_INVALID;
+    }
+    if (int rc = flush_shapes(w)) return rc;
+    std::vector<int> slots;
+    std::vector<pk::HostBody> hb;
+    slots.reserve(size_t(n));
+    hb.reserve(size_t(n));
+    const long long per_world_cap = 1LL << w->cfg.lbits;
+    for (int i = 0; i < n; ++i)
+    {
+        const pk_body_desc &d = descs[i];
+        SubWorld &sw = w->worlds[size_t(d.world)];
+        int local;
+        if (!sw.free_locals.empty())
+        {
+            local = sw.free_locals.back();
+            sw.free_locals.pop_back();
+        }
+        else
+        {
+            if ((long long)sw.local_slot.size() >= per_world_cap) return PK_ERR_CAPACITY;
+            local = int(sw.local_slot.size());
+            sw.local_slot.push_back(-1);
+            sw.local_gen.push_back(0);
+            sw.local_alive.push_back(0);
+        }
+        int slot = sw.local_slot[size_t(local)];
+        if (slot < 0)
+        {
+            if (!w->free_slots.empty())
+            {
+                slot = w->free_slots.back();
+                w->free_slots.pop_back();
+            }
+            else
+            {
+                if (w->nslots >= w->cfg.body_cap)
+                {
+                    sw.free_locals.push_back(local);
+                    return PK_ERR_CAPACITY;
+                }
+                slot = w->nslots++;
+            }
+            sw.local_slot[size_t(local)] = slot;
+        }
+        sw.local_alive[size_t(local)] = 1;
+        SlotInfo &si = w->slots[size_t(slot)];
+        si.world = d.world;
+        si.local = local;
+        si.gen = sw.local_gen[size_t(local)];
+        si.alive = true;
+        si.is_static = d.type == PK_BODY_STATIC;
+
+        pk::HostBody h;
+        std::memset(&h, 0, sizeof(h));
+        h.world = d.world;
+        h.local = local;
+        h.shape = d.shape;
+        h.flags = 1 | (si.is_static ? 2 : 0);
+        h.created = w->steps;
+        for (int k = 0; k < 3; ++k)
+        {
+            h.pos[k] = d.pos[k];
+            h.vel[k] = d.vel[k];
+            h.ang_vel[k] = d.ang_vel[k];
+        }
+        for (int k = 0; k < 4; ++k) h.quat[k] = d.quat[k];
+        // particle(...) constructor (particle.h:121-133): inv_mass = 1/m, I^-1 of the local tensor,
+        // zeroed for static bodies (infinite mass, object.h:81-85)
+        h.mass = si.is_static ? std::numeric_limits<double>::infinity() : d.mass;
+        h.inv_mass = 1.0 / h.mass;
+        pk::M3<double> I;
+        for (int k = 0; k < 9; ++k) I.m[k] = d.inertia[k];
+        pk::M3<double> Ii = pk::inverse(I);
+        for (int k = 0; k < 9; ++k)
+        {
+            h.il[k] = d.inertia[k];
+            h.il_inv[k] = (h.inv_mass == 0.0) ? 0.0 : Ii.m[k];
+        }
+        h.restitution = d.restitution;
+        h.friction = d.friction;
+        slots.push_back(slot);
+        hb.push_back(h);
+        if (out) out[i] = uint64_t(uint32_t(slot)) | (uint64_t(si.gen) << 32);
+    }
+    if (w->eng->upload_bodies(slots.data(), hb.data(), n, w->nslots))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
+static SlotInfo *resolve(pk_world *w, uint64_t handle, int *slot_out)
+{
+    uint32_t slot = uint32_t(handle & 0xFFFFFFFFu), gen = uint32_t(handle >> 32);
+    if (slot >= uint32_t(w->nslots)) return nullptr;
+    SlotInfo &si = w->slots[slot];
+    if (!si.alive || si.gen != gen) return nullptr;
+    *slot_out = int(slot);
+    return &si;
+}
+
+static int kill_slot(pk_world *w, int slot)
+{
+    SlotInfo &si = w->slots[size_t(slot)];
+    SubWorld &sw = w->worlds[size_t(si.world)];
+    si.alive = false;
+    sw.local_alive[size_t(si.local)] = 0;
+    sw.local_gen[size_t(si.local)]++;
+    sw.free_locals.push_back(si.local);
+    si.gen = sw.local_gen[size_t(si.local)];
+    if (w->eng->kill_body(slot, si.world, si.local))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
+int pk_body_remove(pk_world *w, uint64_t handle)
+{
+    if (!w) return PK_ERR_INVALID;
+    int slot;
+    if (!resolve(w, handle, &slot)) return PK_ERR_STALE_HANDLE;
+    return kill_slot(w, slot);
+}
+
+int pk_world_clear(pk_world *w, int32_t world)
+{
+    if (!w || world < 0 || world >= w->cfg.max_worlds) return PK_ERR_INVALID;
+    SubWorld &sw = w->worlds[size_t(world)];
+    for (size_t l = 0; l < sw.local_slot.size(); ++l)
+    {
+        int slot = sw.local_slot[l];
+        if (slot >= 0 && w->slots[size_t(slot)].alive)
+        {
+            int rc = kill_slot(w, slot);
+            if (rc) return rc;
+        }
+        if (slot >= 0)
+        {
+            w->slots[size_t(slot)] = SlotInfo{};
+            w->free_slots.push_back(slot);
+        }
+    }
+    sw.local_slot.clear();
+    sw.local_gen.clear();
+    sw.local_alive.clear();
+    sw.free_locals.clear();
+    return PK_OK;
+}
+
+int pk_world_set_active(pk_world *w, int32_t world, int32_t active)
+{
+    if (!w || world < 0 || world >= w->cfg.max_worlds) return PK_ERR_INVALID;
+    SubWorld &sw = w->worlds[size_t(world)];
+    sw.active = active ? 1 : 0;
+    double gn = std::sqrt(sw.gravity[0] * sw.gravity[0] + sw.gravity[1] * sw.gravity[1] + sw.gravity[2] * sw.gravity[2]);
+    if (w->eng->set_world(world, sw.gravity, gn, sw.active)) return PK_ERR_CUDA;
+    return PK_OK;
+}
+
+int pk_world_set_gravity(pk_world *w, int32_t world, const double g[3])
+{
+    if (!w || !g || world < 0 || world >= w->cfg.max_worlds) return PK_ERR_INVALID;
+    SubWorld &sw = w->worlds[size_t(world)];
+    for (int k = 0; k < 3; ++k) sw.gravity[k] = g[k];
+    // constraint_solver keeps |g| for the restitution threshold (world.h:383)
+    double gn = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    if (w->eng->set_world(world, sw.gravity, gn, sw.active)) return PK_ERR_CUDA;
+    return PK_OK;
+}
+
+int pk_world_step_async(pk_world *w, double dt)
+{
+    if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
+    if (int frc = flush_shapes(w)) return frc;
+    int rc = w->eng->step(dt);
+    if (rc)
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    w->steps++;
+    return PK_OK;
+}
+
+int pk_world_synchronize(pk_world *w, pk_step_info *info)
+{
+    if (!w) return PK_ERR_INVALID;
+    pk::StepCounters c;
+    if (w->eng->synchronize(&c))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    if (info)
+    {
+        info->pairs = c.npairs;
+        info->leaves = c.nleaf;
+        info->status = c.status;
+        info->reserved = 0;
+    }
+    return c.status ? PK_ERR_DEVICE_STATUS : PK_OK;
+}
+
+int pk_world_step(pk_world *w, double dt)
+{
+    int rc = pk_world_step_async(w, dt);
+    if (rc) return rc;
+    return pk_world_synchronize(w, nullptr);
+}
+
+int pk_world_capture(pk_world *w, double dt)
+{
+    if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
+    if (int rc = flush_shapes(w)) return rc;
+    if (w->eng->capture_graph(dt))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
+int pk_world_step_graph(pk_world *w)
+{
+    if (!w) return PK_ERR_INVALID;
+    int rc = w->eng->launch_graph();
+    if (rc == -2) return PK_ERR_INVALID;
+    if (rc)
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    w->steps++;
+    return PK_OK;
+}
+
+void *pk_world_stream(pk_world *w) { return w ? w->eng->stream() : nullptr; }
+
+int pk_world_read_bodies(pk_world *w, double *out, int32_t cap, int32_t *n)
+{
+    if (!w) return PK_ERR_INVALID;
+    if (n) *n = w->nslots;
+    if (!out || cap <= 0) return PK_OK;
+    int m = cap < w->nslots ? cap : w->nslots;
+    if (w->eng->read_bodies(out, m) < 0) return PK_ERR_CUDA;
+    return PK_OK;
+}
+
+int pk_world_write_body(pk_world *w, uint64_t handle, const double *s)
+{
+    if (!w || !s) return PK_ERR_INVALID;
+    int slot;
+    if (!resolve(w, handle, &slot)) return PK_ERR_STALE_HANDLE;
+    if (w->eng->write_state(slot, s)) return PK_ERR_CUDA;
+    return PK_OK;
+}
+
+static void split_key(const pk_world *w, uint64_t k, uint64_t *ref, int32_t *world)
+{
+    int lb = w->cfg.lbits;
+    uint64_t mask = (uint64_t(1) << lb) - 1;
+    uint64_t lo = (k >> lb) & mask, hi = k & mask;
+    if (ref) *ref = (lo << 32) | hi;
+    if (world) *world = int32_t(k >> (2 * lb));
+}
+
+int pk_world_read_pairs(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t cap, int32_t *n)
+{
+    if (!w) return PK_ERR_INVALID;
+    int np = w->eng->read_pairs(nullptr, nullptr, 0);
+    if (np < 0) return PK_ERR_CUDA;
+    if (n) *n = np;
+    int m = cap < np ? cap : np;
+    if (m <= 0) return PK_OK;
+    std::vector<uint64_t> raw(static_cast<size_t>(m));
+    if (w->eng->read_pairs(raw.data(), nullptr, m) < 0) return PK_ERR_CUDA;
+    for (int i = 0; i < m; ++i) split_key(w, raw[size_t(i)], keys ? keys + i : nullptr, worlds ? worlds + i : nullptr);
+    return PK_OK;
+}
+
+int pk_world_read_manifolds(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *counts, double *contacts,
+                            int32_t cap, int32_t *n)
+{
+    if (!w) return PK_ERR_INVALID;
+    int np = w->eng->read_manifolds(nullptr, nullptr, nullptr, 0);
+    if (np < 0) return PK_ERR_CUDA;
+    if (n) *n = np;
+    int m = cap < np ? cap : np;
+    if (m <= 0) return PK_OK;
+    std::vector<uint64_t> raw(static_cast<size_t>(m));
+    if (w->eng->read_manifolds(raw.data(), counts, contacts, m) < 0) return PK_ERR_CUDA;
+    for (int i = 0; i < m; ++i) split_key(w, raw[size_t(i)], keys ? keys + i : nullptr, worlds ? worlds + i : nullptr);
+    return PK_OK;
+}
+
+int pk_world_read_events(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *kinds, int32_t cap, int32_t *n)
+{
+    if (!w) return PK_ERR_INVALID;
+    int ne = w->eng->read_events(nullptr, nullptr, 0);
+    if (ne < 0) return PK_ERR_CUDA;
+    if (n) *n = ne;
+    int m = cap < ne ? cap : ne;
+    if (m <= 0) return PK_OK;
+    std::vector<uint64_t> raw(static_cast<size_t>(m));
+    std::vector<int> kd(static_cast<size_t>(m));
+    if (w->eng->read_events(raw.data(), kd.data(), m) < 0) return PK_ERR_CUDA;
+    for (int i = 0; i < m; ++i)
+    {
+        split_key(w, raw[size_t(i)], keys ? keys + i : nullptr, worlds ? worlds + i : nullptr);
+        if (kinds) kinds[i] = kd[size_t(i)];
+    }
+    return PK_OK;
+}
+
+int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t cap, int32_t *n, int32_t *nc0)
+{
+    if (!w) return PK_ERR_INVALID;
+    int nc = 0;
+    int na = w->eng->read_colours(nullptr, nullptr, 0, &nc);
+    if (na < 0) return PK_ERR_CUDA;
+    if (n) *n = na;
+    if (nc0) *nc0 = nc;
+    int m = cap < na ? cap : na;
+    if (m <= 0) return PK_OK;
+    std::vector<uint64_t> raw(static_cast<size_t>(m));
+    std::vector<int> col(static_cast<size_t>(m));
+    if (w->eng->read_colours(raw.data(), col.data(), m, &nc) < 0) return PK_ERR_CUDA;
+    for (int i = 0; i < m; ++i)
+    {
+        split_key(w, raw[size_t(i)], keys ? keys + i : nullptr, nullptr);
+        if (colours) colours[i] = col[size_t(i)];
+    }
+    return PK_OK;
+}
+
+int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out, int32_t *hit)
+{
+    if (!w || n < 0 || (n > 0 && (!a || !b || !out || !hit))) return PK_ERR_INVALID;
+    int nshapes = int(w->ranges.size() / 2);
+    for (int i = 0; i < n; ++i)
+    {
+        for (const pk_collide_shape *s : {a + i, b + i})
+        {
+            if (s->kind < 0 || s->kind > 2) return PK_ERR_INVALID;
+            if (s->kind == 2 && (s->shape < 0 || s->shape >= nshapes)) return PK_ERR_INVALID;
+        }
+    }
+    if (int rc = flush_shapes(w)) return rc;
+    std::vector<int> status(size_t(n > 0 ? n : 1));
+    static_assert(sizeof(pk_collide_shape) == 4 + 4 + 80, "layout shared with the device ShapeSpec");
+    if (w->eng->collide(a, b, n, out, hit, status.data()))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
+} // extern "C"

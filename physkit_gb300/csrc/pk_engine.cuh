@@ -1,0 +1,1132 @@
+// pk_engine.cuh — the GPU world step: body state in HBM, one kernel per stage.
+//
+// Stage order is that of world::step_impl (src/world.cpp:20-56):
+//   k_integrate_vel   gravity + semi-implicit velocity update (integrate.h:36-40, particle.h:72-79),
+//                     world AABB of the rotated mesh bounds (mesh.cpp:398, bounds.h:144-158) and the
+//                     fat-box hysteresis of dynamic_bvh::update_leaf (bvh.cpp:475-514)
+//   k_morton + radix sort + k_lbvh_build + k_lbvh_refit      per-step LBVH over the fat boxes
+//   k_traverse + radix sort                                  overlap pairs (collision_phases.h:377-436)
+//   k_narrow          GJK/EPA + manifold update + begin/end events (collision_phases.h:244-320)
+//   k_contact_setup   contact Jacobians (constraint.h:874-953, 1052-1104)
+//   k_solve_world     colouring + warm start + sequential impulses, one CTA per world
+//                     (constraint.h:1107-1201)
+//   k_integrate_pos   position/orientation update and cached inertia (integrate.h:42-46,
+//                     particle.h:140-146)
+// The pair set equals the reference's incremental one: a pair of bodies of one world exists when
+// their fat boxes overlap (inclusive compares), not both are static, and one of them was
+// reinserted in the tree at or after the step in which the younger of the two was created.
+#pragma once
+
+#include "pk_math.cuh"
+#include "pk_narrow.cuh"
+#include "pk_sort.cuh"
+
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+#include <vector>
+
+namespace pk
+{
+
+enum : uint32_t
+{
+    BODY_ALIVE = 1u,
+    BODY_STATIC = 2u,
+};
+
+// Device status bits (OR-ed into a word the host reads after a step).
+enum : int
+{
+    ST_PAIR_OVERFLOW = 1 << 0,
+    ST_EPA_CAP = 1 << 1,
+    ST_COLOUR_CAP = 1 << 2,
+    ST_TRAVERSAL_STACK = 1 << 3,
+    ST_NAN = 1 << 4,
+};
+
+constexpr int kMaxColours = 512;
+constexpr uint32_t kLeafBit = 0x80000000u;
+
+template <class T> struct Pose
+{
+    T p[3];
+    T q[4];
+};
+template <class T> struct Vel
+{
+    T v[3];
+    T w[3];
+};
+template <class T> struct Params
+{
+    T mass, inv_mass, restitution, friction;
+    T il[9];
+    T il_inv[9];
+};
+struct Meta
+{
+    uint32_t world, local, shape, flags;
+    int32_t created, reinserted;
+};
+template <class T> struct Contact
+{
+    T n[3], la[3], lb[3], depth;
+    double imp[3];
+};
+template <class T> struct Manifold
+{
+    int n;
+    int pad;
+    Contact<T> c[4];
+};
+template <class T> struct Row
+{
+    T n[3], wa_n[3], wb_n[3];
+    T meff_n, bias;
+    T t1[3], wa_t1[3], wb_t1[3];
+    T meff_t1;
+    T t2[3], wa_t2[3], wb_t2[3];
+    T meff_t2;
+    T inv11, inv12, inv22, mu;
+    double acc[3];
+};
+template <class T> struct WorldParams
+{
+    T g[3];
+    T gnorm;
+    int active;
+    int pad;
+};
+
+template <class T> struct Dev
+{
+    // bodies
+    Pose<T> *pose;
+    Vel<T> *vel;
+    T *iw;
+    T *iwinv;
+    Params<T> *prm;
+    Aabb<T> *tbox;
+    Meta *meta;
+    const int *nslots;
+    // shapes
+    const T *verts;
+    const int2 *shape_range;
+    const Aabb<T> *shape_box;
+    // worlds
+    WorldParams<T> *wp;
+    unsigned *wbounds;
+    int *wroot;
+    int *mstart;
+    int *mend;
+    int max_worlds;
+    // broadphase
+    uint64_t *mkey;
+    uint64_t *mval;
+    int *nleaf;
+    float4 *nodes;
+    int *parent;     // parent of internal node i
+    int *leaf_parent;
+    int *refit_flag;
+    // pairs
+    uint64_t *pkey;
+    uint64_t *pval;
+    int *npairs;
+    int pair_cap;
+    // manifolds
+    Manifold<T> *man_old;
+    uint64_t *key_old;
+    int *npairs_old;
+    Manifold<T> *man_new;
+    uint8_t *event;
+    Row<T> *rows;
+    uint8_t *rowmask;
+    int *colour;
+    uint32_t *owner;
+    uint32_t *order;
+    int *ncolours;
+    // control
+    int *status;
+    int *epoch;
+    int lbits, wbits, iterations;
+};
+
+// ------------------------------------------------------------------------------------------------
+// helpers
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned f2ord(float f)
+{
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u)
+{ return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u); }
+
+__device__ __forceinline__ float down_f(double x) { return __double2float_rd(x); }
+__device__ __forceinline__ float up_f(double x) { return __double2float_ru(x); }
+__device__ __forceinline__ float down_f(float x) { return x; }
+__device__ __forceinline__ float up_f(float x) { return x; }
+
+template <class T> __device__ __forceinline__ V3<T> ld3(const T *a) { return {a[0], a[1], a[2]}; }
+template <class T> __device__ __forceinline__ void st3(T *a, V3<T> v)
+{
+    a[0] = v.x;
+    a[1] = v.y;
+    a[2] = v.z;
+}
+template <class T> __device__ __forceinline__ Qt<T> ldq(const T *a) { return {a[0], a[1], a[2], a[3]}; }
+
+__device__ __forceinline__ uint32_t spread10(uint32_t v)
+{
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+#define PK_GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += blockDim.x * gridDim.x)
+
+// ------------------------------------------------------------------------------------------------
+// step begin: per-world resets
+// ------------------------------------------------------------------------------------------------
+template <class T> __global__ void k_begin_step(Dev<T> d)
+{
+    PK_GRID_STRIDE(w, d.max_worlds)
+    {
+        d.wbounds[6 * w + 0] = d.wbounds[6 * w + 1] = d.wbounds[6 * w + 2] = 0xFFFFFFFFu;
+        d.wbounds[6 * w + 3] = d.wbounds[6 * w + 4] = d.wbounds[6 * w + 5] = 0u;
+        d.wroot[w] = -1;
+        d.mstart[w] = 0;
+        d.mend[w] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        *d.npairs = 0;
+        *d.nleaf = 0;
+        *d.epoch += 1;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// velocity integration, world AABB, fat-box hysteresis, world bounds for Morton codes
+// ------------------------------------------------------------------------------------------------
+template <class T> __device__ __forceinline__ Aabb<T> world_bounds(const Aabb<T> &lb, Qt<T> q, V3<T> p)
+{
+    // aabb * quat: corner 0 is the min corner, corners 1..7 follow bit order (bounds.h:65-71, 144-158)
+    V3<T> p0 = rotate(q, lb.mn);
+    Aabb<T> r{p0, p0};
+#pragma unroll
+    for (unsigned i = 1; i < 8; ++i)
+    {
+        V3<T> c{(i & 1) ? lb.mx.x : lb.mn.x, (i & 2) ? lb.mx.y : lb.mn.y, (i & 4) ? lb.mx.z : lb.mn.z};
+        V3<T> pt = rotate(q, c);
+        r.mn.x = tmin(r.mn.x, pt.x);
+        r.mn.y = tmin(r.mn.y, pt.y);
+        r.mn.z = tmin(r.mn.z, pt.z);
+        r.mx.x = tmax(r.mx.x, pt.x);
+        r.mx.y = tmax(r.mx.y, pt.y);
+        r.mx.z = tmax(r.mx.z, pt.z);
+    }
+    return {r.mn + p, r.mx + p};
+}
+
+template <class T> __global__ void k_integrate_vel(Dev<T> d, T dt)
+{
+    const int n = *d.nslots;
+    const int epoch = *d.epoch;
+    PK_GRID_STRIDE(i, n)
+    {
+        Meta m = d.meta[i];
+        if (!(m.flags & BODY_ALIVE)) continue;
+        if (!d.wp[m.world].active) continue;
+        Aabb<T> tb = d.tbox[i];
+        if (!(m.flags & BODY_STATIC))
+        {
+            const Params<T> &pr = d.prm[i];
+            const WorldParams<T> &wp = d.wp[m.world];
+            Vel<T> ve = d.vel[i];
+            V3<T> v = ld3(ve.v), w = ld3(ve.w);
+            // apply_force(g*m): acc = 0 + (g*m)*inv_mass; v += acc*dt
+            V3<T> acc = (ld3(wp.g) * pr.mass) * pr.inv_mass;
+            v = v + acc * dt;
+            // angular_accel = I_w^-1 (tau - w x (I_w w)), tau = 0
+            V3<T> c = cross(w, matvec(d.iw + 9 * i, w));
+            V3<T> zero{T(0), T(0), T(0)};
+            V3<T> aa = matvec(d.iwinv + 9 * i, zero - c);
+            w = w + aa * dt;
+            st3(ve.v, v);
+            st3(ve.w, w);
+            d.vel[i] = ve;
+            const Pose<T> &ps = d.pose[i];
+            Aabb<T> tru = world_bounds(d.shape_box[m.shape], ldq(ps.q), ld3(ps.p));
+            if (!aabb_contains(tb, tru))
+            {
+                const T margin = T(0.1);
+                V3<T> mv{margin, margin, margin};
+                Aabb<T> nb{tru.mn - mv, tru.mx + mv};
+                V3<T> disp = v * dt;
+                if (disp.x < T(0)) nb.mn.x = nb.mn.x + disp.x; else nb.mx.x = nb.mx.x + disp.x;
+                if (disp.y < T(0)) nb.mn.y = nb.mn.y + disp.y; else nb.mx.y = nb.mx.y + disp.y;
+                if (disp.z < T(0)) nb.mn.z = nb.mn.z + disp.z; else nb.mx.z = nb.mx.z + disp.z;
+                tb = nb;
+                d.tbox[i] = nb;
+                d.meta[i].reinserted = epoch;
+            }
+        }
+        // world bounds of the fat-box centres (for the Morton quantisation only)
+        float cx = float(T(0.5) * (tb.mn.x + tb.mx.x));
+        float cy = float(T(0.5) * (tb.mn.y + tb.mx.y));
+        float cz = float(T(0.5) * (tb.mn.z + tb.mx.z));
+        unsigned *wb = d.wbounds + 6 * m.world;
+        atomicMin(wb + 0, f2ord(cx));
+        atomicMin(wb + 1, f2ord(cy));
+        atomicMin(wb + 2, f2ord(cz));
+        atomicMax(wb + 3, f2ord(cx));
+        atomicMax(wb + 4, f2ord(cy));
+        atomicMax(wb + 5, f2ord(cz));
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// LBVH: Morton keys (world id above 30 Morton bits), Karras build, bottom-up refit
+// ------------------------------------------------------------------------------------------------
+template <class T> __global__ void k_morton(Dev<T> d)
+{
+    const int n = *d.nslots;
+    const uint64_t dead = (uint64_t(d.max_worlds) << 30) | 0x3FFFFFFFull;
+    PK_GRID_STRIDE(i, n)
+    {
+        Meta m = d.meta[i];
+        uint64_t key = dead;
+        if ((m.flags & BODY_ALIVE) && d.wp[m.world].active)
+        {
+            Aabb<T> tb = d.tbox[i];
+            const unsigned *wb = d.wbounds + 6 * m.world;
+            float c[3] = {float(T(0.5) * (tb.mn.x + tb.mx.x)), float(T(0.5) * (tb.mn.y + tb.mx.y)),
+                          float(T(0.5) * (tb.mn.z + tb.mx.z))};
+            uint32_t code = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                float lo = ord2f(wb[a]), hi = ord2f(wb[3 + a]);
+                float ext = hi - lo;
+                float u = ext > 0.f ? (c[a] - lo) / ext : 0.f;
+                u = fminf(fmaxf(u, 0.f), 1.f);
+                uint32_t q = min(1023u, uint32_t(u * 1024.f));
+                code |= spread10(q) << (2 - a);
+            }
+            key = (uint64_t(m.world) << 30) | code;
+            atomicAdd(d.nleaf, 1);
+        }
+        d.mkey[i] = key;
+        d.mval[i] = uint64_t(i);
+    }
+}
+
+__device__ __forceinline__ int lbvh_delta(const uint64_t *k, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a == b) return 64 + __clz(uint32_t(i) ^ uint32_t(j));
+    return __clzll(a ^ b);
+}
+
+template <class T> __global__ void k_lbvh_build(Dev<T> d, const uint64_t *__restrict__ skey)
+{
+    const int n = *d.nleaf;
+    PK_GRID_STRIDE(i, n - 1)
+    {
+        int dir = (lbvh_delta(skey, n, i, i + 1) - lbvh_delta(skey, n, i, i - 1)) >= 0 ? 1 : -1;
+        int dmin = lbvh_delta(skey, n, i, i - dir);
+        int lmax = 2;
+        while (lbvh_delta(skey, n, i, i + lmax * dir) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (lbvh_delta(skey, n, i, i + (l + t) * dir) > dmin) l += t;
+        int j = i + l * dir;
+        int dnode = lbvh_delta(skey, n, i, j);
+        int s = 0;
+        int div = 2;
+        int t = (l + div - 1) / div;
+        while (true)
+        {
+            if (lbvh_delta(skey, n, i, i + (s + t) * dir) > dnode) s += t;
+            if (t <= 1) break;
+            div <<= 1;
+            t = (l + div - 1) / div;
+        }
+        int gamma = i + s * dir + min(dir, 0);
+        int first = min(i, j), last = max(i, j);
+        uint32_t left = (first == gamma) ? (uint32_t(gamma) | kLeafBit) : uint32_t(gamma);
+        uint32_t right = (last == gamma + 1) ? (uint32_t(gamma + 1) | kLeafBit) : uint32_t(gamma + 1);
+        d.nodes[4 * i + 0].w = __uint_as_float(left);
+        d.nodes[4 * i + 2].w = __uint_as_float(right);
+        if (left & kLeafBit)
+            d.leaf_parent[gamma] = i;
+        else
+            d.parent[gamma] = i;
+        if (right & kLeafBit)
+            d.leaf_parent[gamma + 1] = i;
+        else
+            d.parent[gamma + 1] = i;
+        if (i == 0) d.parent[0] = -1;
+        // the node spanning exactly one world's leaves is that world's root
+        uint64_t wf = skey[first] >> 30, wl = skey[last] >> 30;
+        if (wf == wl && (first == 0 || (skey[first - 1] >> 30) != wf) && (last == n - 1 || (skey[last + 1] >> 30) != wl))
+            d.wroot[wf] = i;
+    }
+    // single-leaf worlds
+    PK_GRID_STRIDE(j, n)
+    {
+        uint64_t w = skey[j] >> 30;
+        if ((j == 0 || (skey[j - 1] >> 30) != w) && (j == n - 1 || (skey[j + 1] >> 30) != w))
+            d.wroot[w] = int(uint32_t(j) | kLeafBit);
+    }
+}
+
+template <class T> __global__ void k_lbvh_refit(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int n = *d.nleaf;
+    if (n < 2) return;
+    PK_GRID_STRIDE(j, n)
+    {
+        int slot = int(sval[j]);
+        Aabb<T> b = d.tbox[slot];
+        float mn[3] = {down_f(b.mn.x), down_f(b.mn.y), down_f(b.mn.z)};
+        float mx[3] = {up_f(b.mx.x), up_f(b.mx.y), up_f(b.mx.z)};
+        int p = d.leaf_parent[j];
+        uint32_t me = uint32_t(j) | kLeafBit;
+        while (true)
+        {
+            int c = (__float_as_uint(d.nodes[4 * p].w) == me) ? 0 : 1;
+            float4 *slotp = d.nodes + 4 * p + 2 * c;
+            float wv = slotp[0].w;
+            __stcg(slotp + 0, make_float4(mn[0], mn[1], mn[2], wv));
+            __stcg(slotp + 1, make_float4(mx[0], mx[1], mx[2], 0.f));
+            __threadfence();
+            if (atomicAdd(d.refit_flag + p, 1) == 0) break;
+            __threadfence();
+            float4 a0 = __ldcg(d.nodes + 4 * p + 0), a1 = __ldcg(d.nodes + 4 * p + 1);
+            float4 b0 = __ldcg(d.nodes + 4 * p + 2), b1 = __ldcg(d.nodes + 4 * p + 3);
+            mn[0] = fminf(a0.x, b0.x);
+            mn[1] = fminf(a0.y, b0.y);
+            mn[2] = fminf(a0.z, b0.z);
+            mx[0] = fmaxf(a1.x, b1.x);
+            mx[1] = fmaxf(a1.y, b1.y);
+            mx[2] = fmaxf(a1.z, b1.z);
+            int pp = d.parent[p];
+            if (pp < 0) break;
+            me = uint32_t(p);
+            p = pp;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// pair search: each dynamic body walks its world's subtree
+// ------------------------------------------------------------------------------------------------
+template <class T> __device__ __forceinline__ bool pair_allowed(const Meta &a, const Meta &b)
+{
+    int re = a.reinserted > b.reinserted ? a.reinserted : b.reinserted;
+    int cr = a.created > b.created ? a.created : b.created;
+    return re >= cr;
+}
+
+template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int n = *d.nslots;
+    PK_GRID_STRIDE(i, n)
+    {
+        Meta mi = d.meta[i];
+        if (!(mi.flags & BODY_ALIVE) || (mi.flags & BODY_STATIC) || !d.wp[mi.world].active) continue;
+        int root = d.wroot[mi.world];
+        if (root < 0 || (uint32_t(root) & kLeafBit)) continue;
+        Aabb<T> qb = d.tbox[i];
+        float qmn[3] = {down_f(qb.mn.x), down_f(qb.mn.y), down_f(qb.mn.z)};
+        float qmx[3] = {up_f(qb.mx.x), up_f(qb.mx.y), up_f(qb.mx.z)};
+        int stack[96];
+        int sp = 0;
+        stack[sp++] = root;
+        while (sp > 0)
+        {
+            int node = stack[--sp];
+            const float4 *nd = d.nodes + 4 * node;
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+            {
+                float4 bmn = nd[2 * c], bmx = nd[2 * c + 1];
+                if (!(bmn.x <= qmx[0] && bmx.x >= qmn[0] && bmn.y <= qmx[1] && bmx.y >= qmn[1] &&
+                      bmn.z <= qmx[2] && bmx.z >= qmn[2]))
+                    continue;
+                uint32_t ch = __float_as_uint(bmn.w);
+                if (ch & kLeafBit)
+                {
+                    int sj = int(sval[ch & ~kLeafBit]);
+                    if (sj == i) continue;
+                    Meta mj = d.meta[sj];
+                    bool sj_static = (mj.flags & BODY_STATIC) != 0;
+                    if (!sj_static && mj.local < mi.local) continue; // dynamic pairs once, from the lower index
+                    if (!aabb_intersects(qb, d.tbox[sj])) continue;
+                    if (!pair_allowed<T>(mi, mj)) continue;
+                    uint32_t lo = min(mi.local, mj.local), hi = max(mi.local, mj.local);
+                    uint32_t slo = (mi.local < mj.local) ? uint32_t(i) : uint32_t(sj);
+                    uint32_t shi = (mi.local < mj.local) ? uint32_t(sj) : uint32_t(i);
+                    uint64_t key = (uint64_t(mi.world) << (2 * d.lbits)) | (uint64_t(lo) << d.lbits) | uint64_t(hi);
+                    int slot = atomicAdd(d.npairs, 1);
+                    if (slot < d.pair_cap)
+                    {
+                        d.pkey[slot] = key;
+                        d.pval[slot] = (uint64_t(slo) << 32) | shi;
+                    }
+                    else
+                        atomicOr(d.status, ST_PAIR_OVERFLOW);
+                }
+                else if (sp < 96)
+                    stack[sp++] = int(ch);
+                else
+                    atomicOr(d.status, ST_TRAVERSAL_STACK);
+            }
+        }
+    }
+}
+
+template <class T> __global__ void k_clamp_pairs(Dev<T> d)
+{
+    if (*d.npairs > d.pair_cap) *d.npairs = d.pair_cap;
+}
+
+// ------------------------------------------------------------------------------------------------
+// narrowphase + manifold update (collision_phases.h:244-320)
+// ------------------------------------------------------------------------------------------------
+template <class T> __device__ __forceinline__ ShapeRef<T> body_shape(const Dev<T> &d, int slot)
+{
+    ShapeRef<T> s;
+    const Meta m = d.meta[slot];
+    int2 r = d.shape_range[m.shape];
+    s.kind = SHAPE_MESH;
+    s.nverts = r.y;
+    s.verts = d.verts + 3 * r.x;
+    const Pose<T> &p = d.pose[slot];
+    s.pos = ld3(p.p);
+    s.q = ldq(p.q);
+    return s;
+}
+
+template <class T> __device__ __forceinline__ void add_contact(Manifold<T> &m, const Contact<T> &c)
+{
+    if (m.n < 4)
+    {
+        m.c[m.n++] = c;
+        return;
+    }
+    // manifold::add_reduce (collision_phases.h:139-198)
+    Contact<T> pool[5] = {m.c[0], m.c[1], m.c[2], m.c[3], c};
+    int best[4] = {0, 1, 2, 3};
+    for (int i = 1; i < 5; ++i)
+        if (pool[i].depth > pool[best[0]].depth) best[0] = i;
+    T md = T(-1);
+    for (int i = 0; i < 5; ++i)
+    {
+        if (i == best[0]) continue;
+        T d2 = sqnorm(ld3(pool[i].la) - ld3(pool[best[0]].la));
+        if (d2 > md)
+        {
+            md = d2;
+            best[1] = i;
+        }
+    }
+    T ma = T(-1);
+    V3<T> e0 = ld3(pool[best[1]].la) - ld3(pool[best[0]].la);
+    for (int i = 0; i < 5; ++i)
+    {
+        if (i == best[0] || i == best[1]) continue;
+        V3<T> e1 = ld3(pool[i].la) - ld3(pool[best[0]].la);
+        T a2 = sqnorm(cross(e0, e1));
+        if (a2 > ma)
+        {
+            ma = a2;
+            best[2] = i;
+        }
+    }
+    md = T(-1);
+    for (int i = 0; i < 5; ++i)
+    {
+        if (i == best[0] || i == best[1] || i == best[2]) continue;
+        T d2 = sqnorm(ld3(pool[i].la) - ld3(pool[best[2]].la));
+        if (d2 > md)
+        {
+            md = d2;
+            best[3] = i;
+        }
+    }
+    for (int k = 0; k < 4; ++k) m.c[k] = pool[best[k]];
+    m.n = 4;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_narrow(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
+{
+    const int np = *d.npairs;
+    const int nold = *d.npairs_old;
+    const T d2eps = T(0.005 * 0.005), breaking = T(0.05), drift2_eps = T(0.06);
+    PK_GRID_STRIDE(p, np)
+    {
+        uint64_t key = skey[p];
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        int world = int(key >> (2 * d.lbits));
+        if (p == 0 || (skey[p - 1] >> (2 * d.lbits)) != uint64_t(world)) d.mstart[world] = p;
+        if (p == np - 1 || (skey[p + 1] >> (2 * d.lbits)) != uint64_t(world)) d.mend[world] = p + 1;
+        // old manifold of the same pair (binary search over last step's sorted keys)
+        int lo = 0, hi = nold;
+        while (lo < hi)
+        {
+            int mid = (lo + hi) >> 1;
+            if (d.key_old[mid] < key) lo = mid + 1; else hi = mid;
+        }
+        Manifold<T> old;
+        old.n = 0;
+        if (lo < nold && d.key_old[lo] == key) old = d.man_old[lo];
+
+        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+        EpaState<T> es;
+        Collision<T> col;
+        int nps = 0;
+        bool hit = gjk_epa(A, B, es, col, &nps);
+        if (nps) atomicOr(d.status, ST_EPA_CAP);
+        Contact<T> nc;
+        if (hit)
+        {
+            st3(nc.n, col.normal);
+            st3(nc.la, rotate(conj(A.q), col.world_a - A.pos));
+            st3(nc.lb, rotate(conj(B.q), col.world_b - B.pos));
+            nc.depth = col.depth;
+            nc.imp[0] = nc.imp[1] = nc.imp[2] = 0.0;
+        }
+        Manifold<T> nm;
+        nm.n = 0;
+        nm.pad = 0;
+        for (int k = 0; k < old.n; ++k)
+        {
+            Contact<T> oc = old.c[k];
+            if (hit)
+            {
+                if (sqnorm(ld3(nc.la) - ld3(oc.la)) < d2eps || sqnorm(ld3(nc.lb) - ld3(oc.lb)) < d2eps)
+                {
+                    nc.imp[0] = oc.imp[0];
+                    nc.imp[1] = oc.imp[1];
+                    nc.imp[2] = oc.imp[2];
+                    continue;
+                }
+            }
+            V3<T> wa = rotate(A.q, ld3(oc.la)) + A.pos;
+            V3<T> wb = rotate(B.q, ld3(oc.lb)) + B.pos;
+            V3<T> normal = hit ? ld3(nc.n) : ld3(oc.n);
+            V3<T> rel = wb - wa;
+            T depth = dot(rel, normal);
+            V3<T> pa = wa + normal * depth;
+            T drift2 = sqnorm(pa - wb);
+            if (depth > -breaking && drift2 < drift2_eps)
+            {
+                oc.depth = depth;
+                st3(oc.n, normal);
+                add_contact(nm, oc);
+            }
+        }
+        if (hit) add_contact(nm, nc);
+        bool was = old.n != 0, is = nm.n != 0;
+        d.event[p] = (!was && is) ? 1 : ((was && !is) ? 2 : 0);
+        d.man_new[p] = nm;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// contact rows (build_contact_jacobian, constraint.h:874-953; setup_contacts :1052-1104)
+// ------------------------------------------------------------------------------------------------
+template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__restrict__ skey,
+                                                   const uint64_t *__restrict__ sval, T dt)
+{
+    const int np = *d.npairs;
+    PK_GRID_STRIDE(p, np)
+    {
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        int world = int(skey[p] >> (2 * d.lbits));
+        const Manifold<T> &m = d.man_new[p];
+        const Pose<T> &PA = d.pose[sa];
+        const Pose<T> &PB = d.pose[sb];
+        const Params<T> &ra = d.prm[sa];
+        const Params<T> &rb = d.prm[sb];
+        const Vel<T> &VA = d.vel[sa];
+        const Vel<T> &VB = d.vel[sb];
+        const T *Ia = d.iwinv + 9 * sa;
+        const T *Ib = d.iwinv + 9 * sb;
+        Qt<T> qa = ldq(PA.q), qb = ldq(PB.q);
+        V3<T> xa = ld3(PA.p), xb = ld3(PB.p);
+        const T rthr = T(2) * d.wp[world].gnorm * dt;
+        uint8_t mask = 0;
+        for (int k = 0; k < m.n; ++k)
+        {
+            const Contact<T> &c = m.c[k];
+            V3<T> nn = normalized(ld3(c.n));
+            V3<T> lnb = rotate(conj(qb), nn);
+            V3<T> r_a = rotate(qa, ld3(c.la));
+            V3<T> r_b = rotate(qb, ld3(c.lb));
+            V3<T> n = rotate(qb, lnb);
+            T pen = dot((xb + r_b) - (xa + r_a), n);
+            if (pen <= T(0)) continue;
+            Row<T> row;
+            // normal row
+            V3<T> wa = cross(r_a, n), wb = -cross(r_b, n);
+            V3<T> ka = matvec(Ia, wa), kb = matvec(Ib, wb);
+            row.meff_n = T(1) / (ra.inv_mass + rb.inv_mass + dot(wa, ka) + dot(wb, kb));
+            V3<T> vca = ld3(VA.v) + cross(ld3(VA.w), r_a);
+            V3<T> vcb = ld3(VB.v) + cross(ld3(VB.w), r_b);
+            T vreln = dot(vca - vcb, n);
+            T e = tmax(ra.restitution, rb.restitution);
+            T rbias = T(0);
+            if (vreln < -rthr) rbias = e * vreln;
+            T bbias = (T(-0.1) / dt) * tmax(T(0), pen - T(0.005));
+            row.bias = tmin(bbias, rbias);
+            st3(row.n, n);
+            st3(row.wa_n, wa);
+            st3(row.wb_n, wb);
+            // friction rows on the orthonormal basis of n (constraint.h:104-113)
+            T sign = copysign_one(n.z);
+            T a_ = T(-1) / (sign + n.z);
+            T b_ = n.x * n.y * a_;
+            V3<T> t1{T(1) + sign * n.x * n.x * a_, sign * b_, -sign * n.x};
+            V3<T> t2{b_, sign + n.y * n.y * a_, -n.y};
+            V3<T> wa1 = cross(r_a, t1), wb1 = -cross(r_b, t1);
+            V3<T> ka1 = matvec(Ia, wa1), kb1 = matvec(Ib, wb1);
+            row.meff_t1 = T(1) / (ra.inv_mass + rb.inv_mass + dot(wa1, ka1) + dot(wb1, kb1));
+            V3<T> wa2 = cross(r_a, t2), wb2 = -cross(r_b, t2);
+            V3<T> ka2 = matvec(Ia, wa2), kb2 = matvec(Ib, wb2);
+            row.meff_t2 = T(1) / (ra.inv_mass + rb.inv_mass + dot(wa2, ka2) + dot(wb2, kb2));
+            st3(row.t1, t1);
+            st3(row.wa_t1, wa1);
+            st3(row.wb_t1, wb1);
+            st3(row.t2, t2);
+            st3(row.wa_t2, wa2);
+            st3(row.wb_t2, wb2);
+            row.mu = pk_sqrt(ra.friction * rb.friction);
+            T m11 = T(1) / row.meff_t1, m22 = T(1) / row.meff_t2;
+            T m12 = dot(wa1, matvec(Ia, wa2)) + dot(wb1, matvec(Ib, wb2));
+            T det = m11 * m22 - m12 * m12;
+            if (det > T(0))
+            {
+                row.inv11 = m22 / det;
+                row.inv22 = m11 / det;
+                row.inv12 = -m12 / det;
+            }
+            else
+            {
+                row.inv11 = row.meff_t1;
+                row.inv22 = row.meff_t2;
+                row.inv12 = T(0);
+            }
+            row.acc[0] = c.imp[0];
+            row.acc[1] = c.imp[1];
+            row.acc[2] = c.imp[2];
+            d.rows[4 * p + k] = row;
+            mask |= uint8_t(1u << k);
+        }
+        d.rowmask[p] = mask;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// solver: one CTA per world; colouring, warm start, iterations (constraint.h:1107-1201)
+// ------------------------------------------------------------------------------------------------
+template <class T> struct BodyRef
+{
+    Vel<T> *v;
+    const T *iwinv;
+    T inv_mass;
+    bool is_static;
+};
+
+template <class T> __device__ __forceinline__ T jv(const T *J, const T *Wa, const T *Wb, const Vel<T> &a, const Vel<T> &b)
+{
+    // J_v.v_a + J_w_a.w_a - J_v.v_b + J_w_b.w_b (constraint.h:52-53), left to right
+    return dot(ld3(J), ld3(a.v)) + dot(ld3(Wa), ld3(a.w)) - dot(ld3(J), ld3(b.v)) + dot(ld3(Wb), ld3(b.w));
+}
+
+template <class T> __device__ __forceinline__ void apply_imp(BodyRef<T> &a, BodyRef<T> &b, V3<T> J, V3<T> Wa, V3<T> Wb, T lam)
+{
+    if (!a.is_static)
+    {
+        V3<T> v = ld3(a.v->v) + (J * lam) * a.inv_mass;
+        V3<T> w = ld3(a.v->w) + matvec(a.iwinv, Wa * lam);
+        st3(a.v->v, v);
+        st3(a.v->w, w);
+    }
+    if (!b.is_static)
+    {
+        V3<T> v = ld3(b.v->v) + ((-J) * lam) * b.inv_mass;
+        V3<T> w = ld3(b.v->w) + matvec(b.iwinv, Wb * lam);
+        st3(b.v->v, v);
+        st3(b.v->w, w);
+    }
+}
+
+template <class T> __device__ __forceinline__ void warm_row(BodyRef<T> &a, BodyRef<T> &b, const T *J, const T *Wa, const T *Wb, double acc)
+{
+    if (acc == 0.0) return;
+    apply_imp(a, b, ld3(J), ld3(Wa), ld3(Wb), T(acc));
+}
+
+template <class T> __device__ __forceinline__ void solve_contact(BodyRef<T> &A, BodyRef<T> &B, Row<T> &r)
+{
+    // normal row: jacobian_row::apply (constraint.h:49-71), gamma = 0
+    {
+        T Jv = jv(r.n, r.wa_n, r.wb_n, *A.v, *B.v);
+        T cfp = T(0) * T(r.acc[0]);
+        T lambda = -(Jv + r.bias + cfp) * r.meff_n;
+        double old = r.acc[0];
+        double v = old + double(lambda);
+        double lo = 0.0, hi = 1.7976931348623157e308;
+        double acc = (v < lo) ? lo : ((hi < v) ? hi : v);
+        r.acc[0] = acc;
+        T applied = T(acc - old);
+        apply_imp(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), applied);
+    }
+    // coupled 2D friction with circular cone clamp (constraint.h:1138-1187)
+    T maxf = r.mu * T(r.acc[0]);
+    T Jv1 = jv(r.t1, r.wa_t1, r.wb_t1, *A.v, *B.v);
+    T Jv2 = jv(r.t2, r.wa_t2, r.wb_t2, *A.v, *B.v);
+    T b1 = Jv1 + T(0), b2 = Jv2 + T(0);
+    T l1 = -(r.inv11 * b1 + r.inv12 * b2);
+    T l2 = -(r.inv12 * b1 + r.inv22 * b2);
+    double o1 = r.acc[1], o2 = r.acc[2];
+    double n1 = o1 + double(l1), n2 = o2 + double(l2);
+    double mag = pk_sqrt(n1 * n1 + n2 * n2);
+    if (mag > double(maxf))
+    {
+        n1 = n1 * (double(maxf) / mag);
+        n2 = n2 * (double(maxf) / mag);
+    }
+    r.acc[1] = n1;
+    r.acc[2] = n2;
+    T a1 = T(n1 - o1), a2 = T(n2 - o2);
+    if (!A.is_static)
+    {
+        V3<T> imp = ld3(r.t1) * a1 + ld3(r.t2) * a2;
+        V3<T> v = ld3(A.v->v) + imp * A.inv_mass;
+        V3<T> w = ld3(A.v->w) + matvec(A.iwinv, ld3(r.wa_t1) * a1 + ld3(r.wa_t2) * a2);
+        st3(A.v->v, v);
+        st3(A.v->w, w);
+    }
+    if (!B.is_static)
+    {
+        V3<T> imp = (-ld3(r.t1)) * a1 - ld3(r.t2) * a2;
+        V3<T> v = ld3(B.v->v) + imp * B.inv_mass;
+        V3<T> w = ld3(B.v->w) + matvec(B.iwinv, ld3(r.wb_t1) * a1 + ld3(r.wb_t2) * a2);
+        st3(B.v->v, v);
+        st3(B.v->w, w);
+    }
+}
+
+template <class T> __device__ __forceinline__ BodyRef<T> body_ref(const Dev<T> &d, int s)
+{
+    BodyRef<T> r;
+    r.v = d.vel + s;
+    r.iwinv = d.iwinv + 9 * s;
+    r.inv_mass = d.prm[s].inv_mass;
+    r.is_static = (d.meta[s].flags & BODY_STATIC) != 0;
+    return r;
+}
+
+template <class T> __global__ void __launch_bounds__(512) k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    __shared__ int ccount[kMaxColours];
+    __shared__ int cstart[kMaxColours];
+    __shared__ int cursor[kMaxColours];
+    __shared__ int remaining;
+    __shared__ int nrounds;
+    const int w = blockIdx.x;
+    if (w >= d.max_worlds || !d.wp[w].active) return;
+    const int ms = d.mstart[w], me = d.mend[w];
+    if (me <= ms) return;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int p = ms + tid; p < me; p += nt) d.colour[p] = d.rowmask[p] ? -1 : -2;
+    for (int c = tid; c < kMaxColours; c += nt)
+    {
+        ccount[c] = 0;
+        cursor[c] = 0;
+    }
+    __syncthreads();
+    int round = 0;
+    while (true)
+    {
+        for (int p = ms + tid; p < me; p += nt)
+        {
+            if (d.colour[p] != -1) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            if (!(d.meta[a].flags & BODY_STATIC)) d.owner[a] = 0xFFFFFFFFu;
+            if (!(d.meta[b].flags & BODY_STATIC)) d.owner[b] = 0xFFFFFFFFu;
+        }
+        if (tid == 0) remaining = 0;
+        __syncthreads();
+        for (int p = ms + tid; p < me; p += nt)
+        {
+            if (d.colour[p] != -1) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            if (!(d.meta[a].flags & BODY_STATIC)) atomicMin(d.owner + a, uint32_t(p));
+            if (!(d.meta[b].flags & BODY_STATIC)) atomicMin(d.owner + b, uint32_t(p));
+        }
+        __syncthreads();
+        int left = 0;
+        for (int p = ms + tid; p < me; p += nt)
+        {
+            if (d.colour[p] != -1) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            bool oka = (d.meta[a].flags & BODY_STATIC) || d.owner[a] == uint32_t(p);
+            bool okb = (d.meta[b].flags & BODY_STATIC) || d.owner[b] == uint32_t(p);
+            if (oka && okb)
+                d.colour[p] = round;
+            else
+                ++left;
+        }
+        if (left) atomicAdd(&remaining, left);
+        __syncthreads();
+        ++round;
+        if (remaining == 0) break;
+        if (round >= kMaxColours)
+        {
+            if (tid == 0) atomicOr(d.status, ST_COLOUR_CAP);
+            break;
+        }
+        __syncthreads();
+    }
+    const int ncol = round;
+    for (int p = ms + tid; p < me; p += nt)
+    {
+        int c = d.colour[p];
+        if (c >= 0 && c < kMaxColours) atomicAdd(&ccount[c], 1);
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+        int s = 0;
+        for (int c = 0; c < ncol; ++c)
+        {
+            cstart[c] = s;
+            s += ccount[c];
+        }
+        nrounds = ncol;
+        d.ncolours[w] = ncol;
+    }
+    __syncthreads();
+    for (int p = ms + tid; p < me; p += nt)
+    {
+        int c = d.colour[p];
+        if (c >= 0 && c < kMaxColours) d.order[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = uint32_t(p);
+    }
+    __syncthreads();
+
+    // warm start, colour by colour
+    for (int c = 0; c < nrounds; ++c)
+    {
+        for (int k = tid; k < ccount[c]; k += nt)
+        {
+            int p = int(d.order[ms + cstart[c] + k]);
+            uint64_t v = sval[p];
+            BodyRef<T> A = body_ref(d, int(v >> 32)), B = body_ref(d, int(v & 0xFFFFFFFFu));
+            uint8_t mask = d.rowmask[p];
+            for (int q = 0; q < 4; ++q)
+            {
+                if (!(mask & (1u << q))) continue;
+                const Row<T> &r = d.rows[4 * p + q];
+                warm_row(A, B, r.n, r.wa_n, r.wb_n, r.acc[0]);
+                warm_row(A, B, r.t1, r.wa_t1, r.wb_t1, r.acc[1]);
+                warm_row(A, B, r.t2, r.wa_t2, r.wb_t2, r.acc[2]);
+            }
+        }
+        __syncthreads();
+    }
+    for (int it = 0; it < d.iterations; ++it)
+    {
+        for (int c = 0; c < nrounds; ++c)
+        {
+            for (int k = tid; k < ccount[c]; k += nt)
+            {
+                int p = int(d.order[ms + cstart[c] + k]);
+                uint64_t v = sval[p];
+                BodyRef<T> A = body_ref(d, int(v >> 32)), B = body_ref(d, int(v & 0xFFFFFFFFu));
+                uint8_t mask = d.rowmask[p];
+                for (int q = 0; q < 4; ++q)
+                {
+                    if (!(mask & (1u << q))) continue;
+                    solve_contact(A, B, d.rows[4 * p + q]);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // write back accumulated impulses into the manifold cache
+    for (int p = ms + tid; p < me; p += nt)
+    {
+        uint8_t mask = d.rowmask[p];
+        for (int q = 0; q < 4; ++q)
+        {
+            if (!(mask & (1u << q))) continue;
+            const Row<T> &r = d.rows[4 * p + q];
+            Contact<T> &c = d.man_new[p].c[q];
+            c.imp[0] = r.acc[0];
+            c.imp[1] = r.acc[1];
+            c.imp[2] = r.acc[2];
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// position integration + cached inertia (integrate.h:20-46, particle.h:140-146)
+// ------------------------------------------------------------------------------------------------
+template <class T> __global__ void k_integrate_pos(Dev<T> d, T dt)
+{
+    const int n = *d.nslots;
+    PK_GRID_STRIDE(i, n)
+    {
+        Meta m = d.meta[i];
+        if (!(m.flags & BODY_ALIVE) || (m.flags & BODY_STATIC) || !d.wp[m.world].active) continue;
+        Pose<T> ps = d.pose[i];
+        Vel<T> ve = d.vel[i];
+        V3<T> v = ld3(ve.v), w = ld3(ve.w);
+        V3<T> x = ld3(ps.p) + v * dt;
+        V3<T> ang = w * dt;
+        T mag = norm(ang);
+        Qt<T> dq;
+        if (mag < T(1e-12))
+        {
+            V3<T> h = ang * T(0.5);
+            dq = qnormalized(Qt<T>{T(1), h.x, h.y, h.z});
+        }
+        else
+        {
+            V3<T> ax = ang / mag;
+            T s, c;
+            sincos_det(T(0.5) * mag, &s, &c);
+            dq = Qt<T>{c, s * ax.x, s * ax.y, s * ax.z};
+        }
+        Qt<T> q = qmul(dq, ldq(ps.q));
+        st3(ps.p, x);
+        ps.q[0] = q.w;
+        ps.q[1] = q.x;
+        ps.q[2] = q.y;
+        ps.q[3] = q.z;
+        d.pose[i] = ps;
+        M3<T> R = to_matrix(q), Rt = transpose(R);
+        M3<T> il, ili;
+        for (int k = 0; k < 9; ++k)
+        {
+            il.m[k] = d.prm[i].il[k];
+            ili.m[k] = d.prm[i].il_inv[k];
+        }
+        M3<T> iw = matmul(matmul(R, il), Rt);
+        M3<T> iwi = matmul(matmul(R, ili), Rt);
+        bool bad = false;
+        for (int k = 0; k < 9; ++k)
+        {
+            d.iw[9 * i + k] = iw.m[k];
+            d.iwinv[9 * i + k] = iwi.m[k];
+        }
+        if (!(x.x == x.x) || !(x.y == x.y) || !(x.z == x.z)) bad = true;
+        if (bad) atomicOr(d.status, ST_NAN);
+    }
+}
+
+template <class T> __global__ void k_finish(Dev<T> d, const uint64_t *__restrict__ skey)
+{
+    const int np = *d.npairs;
+    PK_GRID_STRIDE(p, np) d.key_old[p] = skey[p];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d.npairs_old = np;
+}
+
+// Removal of a body invalidates the cached manifolds of its pairs (collision_phases.h:38-52).
+template <class T> __global__ void k_purge_pairs(Dev<T> d, uint32_t world, uint32_t local)
+{
+    const int n = *d.npairs_old;
+    const uint64_t mask = (uint64_t(1) << d.lbits) - 1;
+    PK_GRID_STRIDE(p, n)
+    {
+        uint64_t k = d.key_old[p];
+        uint32_t w = uint32_t(k >> (2 * d.lbits));
+        uint32_t lo = uint32_t((k >> d.lbits) & mask), hi = uint32_t(k & mask);
+        if (w == world && (lo == local || hi == local)) d.man_old[p].n = 0;
+    }
+}
+
+// Standalone narrowphase over primitive shape pairs (known-answer checks of collision.cpp).
+struct ShapeSpec
+{
+    int kind;  // SHAPE_AABB / SHAPE_OBB / SHAPE_MESH
+    int shape; // mesh shape id
+    double p[10];
+};
+template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const ShapeSpec *sb, int n, const T *verts,
+                                                   const int2 *ranges, double *out, int *hit, int *status)
+{
+    PK_GRID_STRIDE(i, n)
+    {
+        ShapeRef<T> s[2];
+        const ShapeSpec *sp[2] = {sa + i, sb + i};
+        for (int k = 0; k < 2; ++k)
+        {
+            const ShapeSpec &q = *sp[k];
+            ShapeRef<T> &r = s[k];
+            r.kind = q.kind;
+            r.nverts = 0;
+            r.verts = nullptr;
+            r.q = Qt<T>{T(1), T(0), T(0), T(0)};
+            r.pos = r.a = r.b = V3<T>{T(0), T(0), T(0)};
+            if (q.kind == SHAPE_AABB)
+            {
+                r.a = V3<T>{T(q.p[0]), T(q.p[1]), T(q.p[2])};
+                r.b = V3<T>{T(q.p[3]), T(q.p[4]), T(q.p[5])};
+            }
+            else if (q.kind == SHAPE_OBB)
+            {
+                r.pos = V3<T>{T(q.p[0]), T(q.p[1]), T(q.p[2])};
+                r.q = Qt<T>{T(q.p[3]), T(q.p[4]), T(q.p[5]), T(q.p[6])};
+                r.b = V3<T>{T(q.p[7]), T(q.p[8]), T(q.p[9])};
+            }
+            else
+            {
+                r.pos = V3<T>{T(q.p[0]), T(q.p[1]), T(q.p[2])};
+                r.q = Qt<T>{T(q.p[3]), T(q.p[4]), T(q.p[5]), T(q.p[6])};
+                int2 rg = ranges[q.shape];
+                r.verts = verts + 3 * rg.x;
+                r.nverts = rg.y;
+            }
+        }
+        EpaState<T> es;
+        Collision<T> c;
+        int st = 0;
+        bool h = gjk_epa(s[0], s[1], es, c, &st);
+        hit[i] = h ? 1 : 0;
+        status[i] = st;
+        double *o = out + 10 * i;
+        if (h)
+        {
+            o[0] = double(c.normal.x);
+            o[1] = double(c.normal.y);
+            o[2] = double(c.normal.z);
+            o[3] = double(c.world_a.x);
+            o[4] = double(c.world_a.y);
+            o[5] = double(c.world_a.z);
+            o[6] = double(c.world_b.x);
+            o[7] = double(c.world_b.y);
+            o[8] = double(c.world_b.z);
+            o[9] = double(c.depth);
+        }
+    }
+}
+
+} // namespace pk

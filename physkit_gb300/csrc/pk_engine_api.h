@@ -1,0 +1,69 @@
+// pk_engine_api.h — precision-independent interface between the C ABI layer and the device engine.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace pk
+{
+
+struct EngineConfig
+{
+    int body_cap = 0;
+    int pair_cap = 0;
+    int max_worlds = 1;
+    int vert_cap = 0;
+    int shape_cap = 0;
+    int iterations = 10;
+    int lbits = 1;   // bits of a world-local body index in pair keys
+    int wbits = 1;   // bits of a world index in Morton keys (max_worlds itself must fit)
+    int sort_blocks_bodies = 1;
+    int sort_blocks_pairs = 1;
+};
+
+// One body as the host staged it (double precision; converted to the engine's scalar on upload).
+struct HostBody
+{
+    int world, local, shape, flags, created;
+    double pos[3], quat[4], vel[3], ang_vel[3];
+    double mass, inv_mass, restitution, friction;
+    double il[9], il_inv[9];
+};
+
+struct StepCounters
+{
+    int npairs = 0;
+    int nleaf = 0;
+    int status = 0;
+};
+
+class EngineBase
+{
+public:
+    virtual ~EngineBase() = default;
+    virtual int precision_bits() const = 0;
+    virtual int init(const EngineConfig &cfg) = 0;
+    virtual int set_shapes(const std::vector<double> &verts, const std::vector<int> &ranges,
+                           const std::vector<double> &boxes) = 0;
+    virtual int set_world(int w, const double g[3], double gnorm, int active) = 0;
+    virtual int upload_bodies(const int *slots, const HostBody *b, int n, int nslots) = 0;
+    virtual int kill_body(int slot, int world, int local) = 0;
+    virtual int step(double dt) = 0;                 // enqueue only
+    virtual int synchronize(StepCounters *c) = 0;   // wait + read counters, clears status
+    virtual int read_bodies(double *out14, int nslots) = 0;
+    virtual int write_state(int slot, const double *state13) = 0;
+    virtual int read_pairs(uint64_t *keys, uint64_t *slots, int cap) = 0;
+    virtual int read_manifolds(uint64_t *keys, int *counts, double *contacts13, int cap) = 0;
+    virtual int read_events(uint64_t *keys, int *kinds, int cap) = 0;
+    virtual int read_colours(uint64_t *keys, int *colours, int cap, int *ncolours_world0) = 0;
+    virtual int collide(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) = 0;
+    virtual int capture_graph(double dt) = 0;        // record the step as CUDA graphs
+    virtual int launch_graph() = 0;                  // replay one captured step
+    virtual void *stream() = 0;
+    virtual int last_error() const = 0;
+};
+
+EngineBase *make_engine_f64();
+EngineBase *make_engine_f32();
+
+} // namespace pk

@@ -1,0 +1,570 @@
+// pk_engine_host.cuh — device buffers and the launch sequence of one world step.
+//
+// Included by pk_engine_f64.cu (FP64, -fmad=false: the parity form) and pk_engine_f32.cu (FP32 bulk
+// arithmetic with FP64 accumulated impulses: the precision form).
+#pragma once
+
+#include "pk_engine.cuh"
+#include "pk_engine_api.h"
+
+#include <cstring>
+#include <cuda_runtime.h>
+
+namespace pk
+{
+
+#define PK_CUDA(x)                                                                                     \
+    do                                                                                                 \
+    {                                                                                                  \
+        cudaError_t e_ = (x);                                                                          \
+        if (e_ != cudaSuccess)                                                                         \
+        {                                                                                              \
+            last_err_ = int(e_);                                                                       \
+            std::fprintf(stderr, "physkit_gb300: %s failed: %s\n", #x, cudaGetErrorString(e_));        \
+            return -int(e_) - 1000;                                                                    \
+        }                                                                                              \
+    } while (0)
+
+template <class T> __device__ __forceinline__ void refresh_one(Dev<T> d, int s)
+{
+    // particle::update_derived_state (particle.h:140-146)
+    Qt<T> q = ldq(d.pose[s].q);
+    M3<T> R = to_matrix(q), Rt = transpose(R);
+    M3<T> il, ili;
+    for (int k = 0; k < 9; ++k)
+    {
+        il.m[k] = d.prm[s].il[k];
+        ili.m[k] = d.prm[s].il_inv[k];
+    }
+    M3<T> iw = matmul(matmul(R, il), Rt);
+    M3<T> iwi = matmul(matmul(R, ili), Rt);
+    for (int k = 0; k < 9; ++k)
+    {
+        d.iw[9 * s + k] = iw.m[k];
+        d.iwinv[9 * s + k] = iwi.m[k];
+    }
+}
+
+template <class T>
+__global__ void k_install_bodies(Dev<T> d, const int *slots, const Pose<T> *pose, const Vel<T> *vel,
+                                 const Params<T> *prm, const Meta *meta, int n)
+{
+    PK_GRID_STRIDE(i, n)
+    {
+        int s = slots[i];
+        d.pose[s] = pose[i];
+        d.vel[s] = vel[i];
+        d.prm[s] = prm[i];
+        d.meta[s] = meta[i];
+        // dynamic_bvh::add stores the exact (not fattened) bounds (bvh.h:294-302)
+        d.tbox[s] = world_bounds(d.shape_box[meta[i].shape], ldq(pose[i].q), ld3(pose[i].p));
+        refresh_one(d, s);
+    }
+}
+
+template <class T> __global__ void k_refresh_derived(Dev<T> d, int first, int n)
+{
+    PK_GRID_STRIDE(i, n) refresh_one(d, first + i);
+}
+
+template <class T> __global__ void k_kill_body(Dev<T> d, int slot) { d.meta[slot].flags = 0; }
+
+template <class T> class Engine final : public EngineBase
+{
+public:
+    ~Engine() override { release(); }
+
+    int precision_bits() const override { return int(sizeof(T) * 8); }
+    int last_error() const override { return last_err_; }
+    void *stream() override { return st_; }
+
+    int init(const EngineConfig &cfg) override
+    {
+        cfg_ = cfg;
+        int dev = 0;
+        PK_CUDA(cudaGetDevice(&dev));
+        PK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+        PK_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        const size_t N = size_t(cfg.body_cap), P = size_t(cfg.pair_cap), W = size_t(cfg.max_worlds);
+        Dev<T> &d = d_;
+        std::memset(&d, 0, sizeof(d));
+        d.max_worlds = cfg.max_worlds;
+        d.pair_cap = cfg.pair_cap;
+        d.lbits = cfg.lbits;
+        d.wbits = cfg.wbits;
+        d.iterations = cfg.iterations;
+        PK_CUDA(alloc(&d.pose, N));
+        PK_CUDA(alloc(&d.vel, N));
+        PK_CUDA(alloc(&d.iw, 9 * N));
+        PK_CUDA(alloc(&d.iwinv, 9 * N));
+        PK_CUDA(alloc(&d.prm, N));
+        PK_CUDA(alloc(&d.tbox, N));
+        PK_CUDA(alloc(&d.meta, N));
+        PK_CUDA(cudaMemset(d.meta, 0, sizeof(Meta) * N));
+        PK_CUDA(alloc(&counters_, 8));
+        PK_CUDA(cudaMemset(counters_, 0, sizeof(int) * 8));
+        d.nslots = counters_ + 0;
+        d.nleaf = counters_ + 1;
+        d.npairs = counters_ + 2;
+        d.npairs_old = counters_ + 3;
+        d.status = counters_ + 4;
+        d.epoch = counters_ + 5;
+        int minus1 = -1;
+        PK_CUDA(cudaMemcpy(d.epoch, &minus1, sizeof(int), cudaMemcpyHostToDevice));
+        PK_CUDA(alloc(&d.wp, W));
+        PK_CUDA(cudaMemset(d.wp, 0, sizeof(WorldParams<T>) * W));
+        PK_CUDA(alloc(&d.wbounds, 6 * W));
+        PK_CUDA(alloc(&d.wroot, W));
+        PK_CUDA(alloc(&d.mstart, W));
+        PK_CUDA(alloc(&d.mend, W));
+        PK_CUDA(alloc(&d.ncolours, W));
+        PK_CUDA(cudaMemset(d.ncolours, 0, sizeof(int) * W));
+        for (int k = 0; k < 2; ++k)
+        {
+            PK_CUDA(alloc(&mkey_[k], N));
+            PK_CUDA(alloc(&mval_[k], N));
+            PK_CUDA(alloc(&pkey_[k], P));
+            PK_CUDA(alloc(&pval_[k], P));
+            PK_CUDA(alloc(&man_[k], P));
+        }
+        PK_CUDA(alloc(&d.nodes, 4 * N));
+        PK_CUDA(alloc(&d.parent, N));
+        PK_CUDA(alloc(&d.leaf_parent, N));
+        PK_CUDA(alloc(&d.refit_flag, N));
+        PK_CUDA(alloc(&d.key_old, P));
+        PK_CUDA(alloc(&d.event, P));
+        PK_CUDA(alloc(&d.rows, 4 * P));
+        PK_CUDA(alloc(&d.rowmask, P));
+        PK_CUDA(alloc(&d.colour, P));
+        PK_CUDA(alloc(&d.order, P));
+        PK_CUDA(alloc(&d.owner, N));
+        int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
+        PK_CUDA(alloc(&hist_, size_t(kSortRadix) * hb));
+        PK_CUDA(alloc(&d.verts, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
+        PK_CUDA(alloc(&shape_range_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
+        PK_CUDA(alloc(&shape_box_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
+        d.shape_range = shape_range_;
+        d.shape_box = shape_box_;
+        d.man_old = man_[0];
+        d.man_new = man_[1];
+        PK_CUDA(cudaDeviceSynchronize());
+        return 0;
+    }
+
+    int set_shapes(const std::vector<double> &verts, const std::vector<int> &ranges,
+                   const std::vector<double> &boxes) override
+    {
+        size_t nv = verts.size() / 3, ns = ranges.size() / 2;
+        if (nv > size_t(cfg_.vert_cap) || ns > size_t(cfg_.shape_cap)) return -3;
+        std::vector<T> v(verts.size());
+        for (size_t i = 0; i < verts.size(); ++i) v[i] = T(verts[i]);
+        std::vector<Aabb<T>> b(ns);
+        for (size_t i = 0; i < ns; ++i)
+            b[i] = Aabb<T>{{T(boxes[6 * i]), T(boxes[6 * i + 1]), T(boxes[6 * i + 2])},
+                           {T(boxes[6 * i + 3]), T(boxes[6 * i + 4]), T(boxes[6 * i + 5])}};
+        PK_CUDA(cudaMemcpyAsync(const_cast<T *>(d_.verts), v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaMemcpyAsync(shape_range_, ranges.data(), sizeof(int) * ranges.size(), cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaMemcpyAsync(shape_box_, b.data(), sizeof(Aabb<T>) * ns, cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int set_world(int w, const double g[3], double gnorm, int active) override
+    {
+        WorldParams<T> p;
+        p.g[0] = T(g[0]);
+        p.g[1] = T(g[1]);
+        p.g[2] = T(g[2]);
+        p.gnorm = T(gnorm);
+        p.active = active;
+        p.pad = 0;
+        PK_CUDA(cudaMemcpyAsync(d_.wp + w, &p, sizeof(p), cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int upload_bodies(const int *slots, const HostBody *b, int n, int nslots) override
+    {
+        if (n > 0)
+        {
+            std::vector<int> sl(slots, slots + n);
+            std::vector<Pose<T>> pose(n);
+            std::vector<Vel<T>> vel(n);
+            std::vector<Params<T>> prm(n);
+            std::vector<Meta> meta(n);
+            for (int i = 0; i < n; ++i)
+            {
+                const HostBody &h = b[i];
+                for (int k = 0; k < 3; ++k)
+                {
+                    pose[i].p[k] = T(h.pos[k]);
+                    vel[i].v[k] = T(h.vel[k]);
+                    vel[i].w[k] = T(h.ang_vel[k]);
+                }
+                for (int k = 0; k < 4; ++k) pose[i].q[k] = T(h.quat[k]);
+                prm[i].mass = T(h.mass);
+                prm[i].inv_mass = T(h.inv_mass);
+                prm[i].restitution = T(h.restitution);
+                prm[i].friction = T(h.friction);
+                for (int k = 0; k < 9; ++k)
+                {
+                    prm[i].il[k] = T(h.il[k]);
+                    prm[i].il_inv[k] = T(h.il_inv[k]);
+                }
+                meta[i] = Meta{uint32_t(h.world), uint32_t(h.local), uint32_t(h.shape), uint32_t(h.flags), h.created, -1};
+            }
+            int *dsl;
+            Pose<T> *dpose;
+            Vel<T> *dvel;
+            Params<T> *dprm;
+            Meta *dmeta;
+            PK_CUDA(cudaMallocAsync(&dsl, sizeof(int) * n, st_));
+            PK_CUDA(cudaMallocAsync(&dpose, sizeof(Pose<T>) * n, st_));
+            PK_CUDA(cudaMallocAsync(&dvel, sizeof(Vel<T>) * n, st_));
+            PK_CUDA(cudaMallocAsync(&dprm, sizeof(Params<T>) * n, st_));
+            PK_CUDA(cudaMallocAsync(&dmeta, sizeof(Meta) * n, st_));
+            PK_CUDA(cudaMemcpyAsync(dsl, sl.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st_));
+            PK_CUDA(cudaMemcpyAsync(dpose, pose.data(), sizeof(Pose<T>) * n, cudaMemcpyHostToDevice, st_));
+            PK_CUDA(cudaMemcpyAsync(dvel, vel.data(), sizeof(Vel<T>) * n, cudaMemcpyHostToDevice, st_));
+            PK_CUDA(cudaMemcpyAsync(dprm, prm.data(), sizeof(Params<T>) * n, cudaMemcpyHostToDevice, st_));
+            PK_CUDA(cudaMemcpyAsync(dmeta, meta.data(), sizeof(Meta) * n, cudaMemcpyHostToDevice, st_));
+            k_install_bodies<T><<<grid(n), 256, 0, st_>>>(d_, dsl, dpose, dvel, dprm, dmeta, n);
+            PK_CUDA(cudaGetLastError());
+            PK_CUDA(cudaFreeAsync(dsl, st_));
+            PK_CUDA(cudaFreeAsync(dpose, st_));
+            PK_CUDA(cudaFreeAsync(dvel, st_));
+            PK_CUDA(cudaFreeAsync(dprm, st_));
+            PK_CUDA(cudaFreeAsync(dmeta, st_));
+        }
+        nslots_ = nslots;
+        PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.nslots), &nslots_, sizeof(int), cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int kill_body(int slot, int world, int local) override
+    {
+        k_kill_body<T><<<1, 1, 0, st_>>>(d_, slot);
+        Dev<T> d = d_;
+        d.man_old = man_[parity_];
+        k_purge_pairs<T><<<grid(cfg_.pair_cap), 256, 0, st_>>>(d, uint32_t(world), uint32_t(local));
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int step(double dt) override
+    {
+        int rc = enqueue_step(T(dt), parity_);
+        if (rc) return rc;
+        parity_ ^= 1;
+        return 0;
+    }
+
+    int capture_graph(double dt) override
+    {
+        for (int k = 0; k < 2; ++k)
+        {
+            if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
+            graph_exec_[k] = nullptr;
+        }
+        for (int k = 0; k < 2; ++k)
+        {
+            cudaGraph_t g;
+            PK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_step(T(dt), k);
+            cudaError_t e = cudaStreamEndCapture(st_, &g);
+            if (rc) return rc;
+            PK_CUDA(e);
+            PK_CUDA(cudaGraphInstantiate(&graph_exec_[k], g, 0));
+            cudaGraphDestroy(g);
+        }
+        return 0;
+    }
+
+    int launch_graph() override
+    {
+        if (!graph_exec_[parity_]) return -2;
+        PK_CUDA(cudaGraphLaunch(graph_exec_[parity_], st_));
+        parity_ ^= 1;
+        return 0;
+    }
+
+    int synchronize(StepCounters *c) override
+    {
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaGetLastError());
+        int h[8];
+        PK_CUDA(cudaMemcpy(h, counters_, sizeof(h), cudaMemcpyDeviceToHost));
+        if (c)
+        {
+            c->nleaf = h[1];
+            c->npairs = h[2];
+            c->status = h[4];
+        }
+        int zero = 0;
+        PK_CUDA(cudaMemcpy(counters_ + 4, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        return 0;
+    }
+
+    int read_bodies(double *out, int n) override
+    {
+        if (n > nslots_) n = nslots_;
+        std::vector<Pose<T>> pose(n);
+        std::vector<Vel<T>> vel(n);
+        std::vector<Meta> meta(n);
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(pose.data(), d_.pose, sizeof(Pose<T>) * n, cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(vel.data(), d_.vel, sizeof(Vel<T>) * n, cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(meta.data(), d_.meta, sizeof(Meta) * n, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; ++i)
+        {
+            double *o = out + 14 * i;
+            for (int k = 0; k < 3; ++k)
+            {
+                o[k] = double(pose[i].p[k]);
+                o[7 + k] = double(vel[i].v[k]);
+                o[10 + k] = double(vel[i].w[k]);
+            }
+            for (int k = 0; k < 4; ++k) o[3 + k] = double(pose[i].q[k]);
+            o[13] = (meta[i].flags & BODY_ALIVE) ? 1.0 : 0.0;
+        }
+        return n;
+    }
+
+    int write_state(int slot, const double *s) override
+    {
+        Pose<T> p;
+        Vel<T> v;
+        for (int k = 0; k < 3; ++k)
+        {
+            p.p[k] = T(s[k]);
+            v.v[k] = T(s[7 + k]);
+            v.w[k] = T(s[10 + k]);
+        }
+        for (int k = 0; k < 4; ++k) p.q[k] = T(s[3 + k]);
+        PK_CUDA(cudaMemcpy(d_.pose + slot, &p, sizeof(p), cudaMemcpyHostToDevice));
+        PK_CUDA(cudaMemcpy(d_.vel + slot, &v, sizeof(v), cudaMemcpyHostToDevice));
+        k_refresh_derived<T><<<1, 32, 0, st_>>>(d_, slot, 1);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int read_pairs(uint64_t *keys, uint64_t *slots, int cap) override
+    {
+        int np = 0;
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(&np, d_.npairs_old, sizeof(int), cudaMemcpyDeviceToHost));
+        int n = np < cap ? np : cap;
+        if (n > 0 && keys) PK_CUDA(cudaMemcpy(keys, d_.key_old, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        if (n > 0 && slots && last_sval_) PK_CUDA(cudaMemcpy(slots, last_sval_, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+        return np;
+    }
+
+    int read_manifolds(uint64_t *keys, int *counts, double *contacts, int cap) override
+    {
+        int np = 0;
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(&np, d_.npairs_old, sizeof(int), cudaMemcpyDeviceToHost));
+        int n = np < cap ? np : cap;
+        if (n > 0)
+        {
+            std::vector<Manifold<T>> m(n);
+            PK_CUDA(cudaMemcpy(m.data(), man_[parity_], sizeof(Manifold<T>) * n, cudaMemcpyDeviceToHost));
+            if (keys) PK_CUDA(cudaMemcpy(keys, d_.key_old, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+            for (int i = 0; i < n; ++i)
+            {
+                if (counts) counts[i] = m[i].n;
+                if (!contacts) continue;
+                for (int k = 0; k < 4; ++k)
+                {
+                    double *o = contacts + (size_t(i) * 4 + k) * 13;
+                    const Contact<T> &c = m[i].c[k];
+                    if (k >= m[i].n)
+                    {
+                        for (int z = 0; z < 13; ++z) o[z] = 0.0;
+                        continue;
+                    }
+                    for (int z = 0; z < 3; ++z)
+                    {
+                        o[z] = double(c.n[z]);
+                        o[3 + z] = double(c.la[z]);
+                        o[6 + z] = double(c.lb[z]);
+                    }
+                    o[9] = double(c.depth);
+                    o[10] = c.imp[0];
+                    o[11] = c.imp[1];
+                    o[12] = c.imp[2];
+                }
+            }
+        }
+        return np;
+    }
+
+    int read_events(uint64_t *keys, int *kinds, int cap) override
+    {
+        int np = 0;
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(&np, d_.npairs_old, sizeof(int), cudaMemcpyDeviceToHost));
+        if (np == 0) return 0;
+        std::vector<uint8_t> ev(np);
+        std::vector<uint64_t> k(np);
+        PK_CUDA(cudaMemcpy(ev.data(), d_.event, np, cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(k.data(), d_.key_old, sizeof(uint64_t) * np, cudaMemcpyDeviceToHost));
+        int cnt = 0;
+        for (int i = 0; i < np; ++i)
+        {
+            if (!ev[i]) continue;
+            if (cnt < cap)
+            {
+                if (keys) keys[cnt] = k[i];
+                if (kinds) kinds[cnt] = ev[i];
+            }
+            ++cnt;
+        }
+        return cnt;
+    }
+
+    int read_colours(uint64_t *keys, int *colours, int cap, int *nc0) override
+    {
+        int np = 0;
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(&np, d_.npairs_old, sizeof(int), cudaMemcpyDeviceToHost));
+        std::vector<int> col(np > 0 ? np : 1);
+        std::vector<uint64_t> k(np > 0 ? np : 1);
+        if (np > 0)
+        {
+            PK_CUDA(cudaMemcpy(col.data(), d_.colour, sizeof(int) * np, cudaMemcpyDeviceToHost));
+            PK_CUDA(cudaMemcpy(k.data(), d_.key_old, sizeof(uint64_t) * np, cudaMemcpyDeviceToHost));
+        }
+        if (nc0) PK_CUDA(cudaMemcpy(nc0, d_.ncolours, sizeof(int), cudaMemcpyDeviceToHost));
+        int cnt = 0;
+        for (int i = 0; i < np; ++i)
+        {
+            if (col[i] < 0) continue;
+            if (cnt < cap)
+            {
+                if (keys) keys[cnt] = k[i];
+                if (colours) colours[cnt] = col[i];
+            }
+            ++cnt;
+        }
+        return cnt;
+    }
+
+    int collide(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) override
+    {
+        if (n <= 0) return 0;
+        ShapeSpec *da, *db;
+        double *dout;
+        int *dhit, *dst;
+        PK_CUDA(cudaMalloc(&da, sizeof(ShapeSpec) * n));
+        PK_CUDA(cudaMalloc(&db, sizeof(ShapeSpec) * n));
+        PK_CUDA(cudaMalloc(&dout, sizeof(double) * 10 * n));
+        PK_CUDA(cudaMalloc(&dhit, sizeof(int) * n));
+        PK_CUDA(cudaMalloc(&dst, sizeof(int) * n));
+        PK_CUDA(cudaMemcpy(da, specs_a, sizeof(ShapeSpec) * n, cudaMemcpyHostToDevice));
+        PK_CUDA(cudaMemcpy(db, specs_b, sizeof(ShapeSpec) * n, cudaMemcpyHostToDevice));
+        PK_CUDA(cudaMemset(dout, 0, sizeof(double) * 10 * n));
+        k_collide_batch<T><<<(n + 127) / 128, 128, 0, st_>>>(da, db, n, d_.verts, shape_range_, dout, dhit, dst);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(out, dout, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(hit, dhit, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(status, dst, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        cudaFree(da);
+        cudaFree(db);
+        cudaFree(dout);
+        cudaFree(dhit);
+        cudaFree(dst);
+        return 0;
+    }
+
+private:
+    EngineConfig cfg_{};
+    Dev<T> d_{};
+    cudaStream_t st_ = nullptr;
+    int sms_ = 1;
+    int nslots_ = 0;
+    int parity_ = 0;
+    int last_err_ = 0;
+    int *counters_ = nullptr;
+    uint64_t *mkey_[2] = {nullptr, nullptr}, *mval_[2] = {nullptr, nullptr};
+    uint64_t *pkey_[2] = {nullptr, nullptr}, *pval_[2] = {nullptr, nullptr};
+    Manifold<T> *man_[2] = {nullptr, nullptr};
+    uint64_t *last_sval_ = nullptr;
+    uint32_t *hist_ = nullptr;
+    int2 *shape_range_ = nullptr;
+    Aabb<T> *shape_box_ = nullptr;
+    cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+
+    template <class U> cudaError_t alloc(U **p, size_t n)
+    {
+        if (n == 0) n = 1;
+        return cudaMalloc(reinterpret_cast<void **>(p), sizeof(U) * n);
+    }
+    template <class U> cudaError_t alloc(const U **p, size_t n)
+    {
+        if (n == 0) n = 1;
+        return cudaMalloc(const_cast<void **>(reinterpret_cast<const void **>(p)), sizeof(U) * n);
+    }
+    int grid(int n) const
+    {
+        int g = (n + 255) / 256;
+        int cap = sms_ * 8;
+        if (g > cap) g = cap;
+        return g < 1 ? 1 : g;
+    }
+    void release()
+    {
+        for (int k = 0; k < 2; ++k)
+            if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
+        void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
+                      d_.wroot, d_.mstart, d_.mend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
+                      pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
+                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.rows, d_.rowmask, d_.colour,
+                      d_.order, d_.owner, hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_};
+        for (void *p : ps)
+            if (p) cudaFree(p);
+        if (st_) cudaStreamDestroy(st_);
+        st_ = nullptr;
+    }
+
+    int enqueue_step(T dt, int parity)
+    {
+        Dev<T> d = d_;
+        d.man_old = man_[parity];
+        d.man_new = man_[parity ^ 1];
+        const int N = cfg_.body_cap;
+        const int gb = grid(N);
+        const int gp = grid(cfg_.pair_cap);
+        k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
+        k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
+        k_morton<T><<<gb, 256, 0, st_>>>(d);
+        // sort all slots by (world, Morton); dead slots sort to the end
+        bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nslots, cfg_.wbits + 30,
+                                        cfg_.sort_blocks_bodies, hist_, st_);
+        const uint64_t *skey = in1 ? mkey_[1] : mkey_[0];
+        const uint64_t *sval = in1 ? mval_[1] : mval_[0];
+        k_lbvh_build<T><<<gb, 256, 0, st_>>>(d, skey);
+        PK_CUDA(cudaMemsetAsync(d.refit_flag, 0, sizeof(int) * size_t(N), st_));
+        k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
+        k_traverse<T><<<gb, 128, 0, st_>>>(d, sval);
+        k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
+        bool p1 = radix_sort<uint64_t>(pkey_[0], pval_[0], pkey_[1], pval_[1], d.npairs,
+                                       cfg_.wbits + 2 * cfg_.lbits, cfg_.sort_blocks_pairs, hist_, st_);
+        const uint64_t *pk = p1 ? pkey_[1] : pkey_[0];
+        const uint64_t *pv = p1 ? pval_[1] : pval_[0];
+        last_sval_ = const_cast<uint64_t *>(pv);
+        k_narrow<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pk, pv);
+        k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
+        k_solve_world<T><<<cfg_.max_worlds, 512, 0, st_>>>(d, pv);
+        k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
+        k_finish<T><<<gp, 256, 0, st_>>>(d, pk);
+        PK_CUDA(cudaGetLastError());
+        return 0;
+    }
+};
+
+} // namespace pk

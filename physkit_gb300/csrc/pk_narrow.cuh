@@ -1,0 +1,521 @@
+// pk_narrow.cuh — GJK boolean test + EPA penetration for one shape pair (device and host).
+//
+// Follows src/collision.cpp:10-518 branch for branch: GJK from direction (1,0,0) with the
+// line/triangle/tetrahedron Voronoi cases (collision.cpp:12-162, <=100 iterations), simplex
+// padding (collision.cpp:191-248), EPA with a min-distance face heap, silhouette flood fill and
+// <=64 expansions (collision.cpp:251-509). The face heap uses the sift rules of the libstdc++
+// std::push_heap / std::pop_heap that the reference calls (collision.cpp:390-408), so ties
+// between equally distant faces resolve the same way.
+//
+// Storage is fixed-size per call (no heap allocation on the device). Exceeding a cap sets a
+// status bit and returns the best face so far; callers report it.
+#pragma once
+
+#include "pk_math.cuh"
+
+namespace pk
+{
+
+enum : int
+{
+    PK_NP_FACE_CAP = 1 << 0,
+    PK_NP_HORIZON_CAP = 1 << 1,
+    PK_NP_STACK_CAP = 1 << 2,
+};
+
+constexpr int kMaxPoly = 4 + 64;
+constexpr int kMaxFaces = 256;
+constexpr int kMaxHorizon = 64;
+constexpr uint16_t kNull16 = 0xFFFF;
+
+enum : int
+{
+    SHAPE_AABB = 0,
+    SHAPE_OBB = 1,
+    SHAPE_MESH = 2,
+};
+
+// A posed convex shape: aabb (a=min, b=max), obb (pos=center, q, b=half) or mesh instance
+// (pos, q, vertex list).
+template <class T> struct ShapeRef
+{
+    int kind;
+    int nverts;
+    const T *verts; // xyz interleaved, local frame
+    V3<T> a, b, pos;
+    Qt<T> q;
+
+    PK_HD V3<T> support(V3<T> d) const
+    {
+        if (kind == SHAPE_AABB)
+        {
+            T sx = d.x >= T(0) ? T(1) : T(-1), sy = d.y >= T(0) ? T(1) : T(-1), sz = d.z >= T(0) ? T(1) : T(-1);
+            return {sx > T(0) ? b.x : a.x, sy > T(0) ? b.y : a.y, sz > T(0) ? b.z : a.z};
+        }
+        if (kind == SHAPE_OBB)
+        {
+            // obb::support (bounds.h:539-548)
+            V3<T> ld = rotate(conj(q), d);
+            V3<T> s{ld.x >= T(0) ? T(1) : T(-1), ld.y >= T(0) ? T(1) : T(-1), ld.z >= T(0) ? T(1) : T(-1)};
+            return pos + rotate(q, V3<T>{s.x * b.x, s.y * b.y, s.z * b.z});
+        }
+        // mesh::instance::support -> mesh::support: first strictly maximal vertex
+        // (mesh.cpp:341-358, 442-448)
+        V3<T> ld = rotate(conj(q), d);
+        int best = 0;
+        T bd = verts[0] * ld.x + verts[1] * ld.y + verts[2] * ld.z;
+        for (int i = 1; i < nverts; ++i)
+        {
+            T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
+            if (v > bd)
+            {
+                bd = v;
+                best = i;
+            }
+        }
+        V3<T> lv{verts[3 * best], verts[3 * best + 1], verts[3 * best + 2]};
+        return rotate(q, lv) + pos;
+    }
+};
+
+template <class T> struct SupPt
+{
+    V3<T> p, pa, pb;
+};
+
+template <class T> struct Collision
+{
+    V3<T> normal, world_a, world_b;
+    T depth;
+};
+
+template <class T> PK_HD SupPt<T> minkowski(const ShapeRef<T> &A, const ShapeRef<T> &B, V3<T> d)
+{
+    V3<T> pa = A.support(d);
+    V3<T> pb = B.support(-d);
+    return {pa - pb, pa, pb};
+}
+
+template <class T> struct Simplex
+{
+    SupPt<T> v[4];
+    int n;
+    PK_HD void push(const SupPt<T> &p) { v[n++] = p; }
+    PK_HD void erase(int i)
+    {
+        for (int k = i; k + 1 < n; ++k) v[k] = v[k + 1];
+        --n;
+    }
+};
+
+template <class T> PK_HD void gjk_triangle(Simplex<T> &s, V3<T> &dir)
+{
+    const SupPt<T> a = s.v[2], b = s.v[1], c = s.v[0];
+    V3<T> ab = b.p - a.p, ac = c.p - a.p, ao = -a.p;
+    V3<T> abc = cross(ab, ac);
+    V3<T> ab_perp = cross(ab, abc);
+    if (dot(ab_perp, ao) > T(0))
+    {
+        s.erase(0);
+        V3<T> tr = cross(cross(ab, ao), ab);
+        dir = (sqnorm(tr) < T(1e-12)) ? normalized(ao) : normalized(tr);
+        return;
+    }
+    V3<T> ac_perp = cross(abc, ac);
+    if (dot(ac_perp, ao) > T(0))
+    {
+        s.erase(1);
+        V3<T> tr = cross(cross(ac, ao), ac);
+        dir = (sqnorm(tr) < T(1e-12)) ? normalized(ao) : normalized(tr);
+        return;
+    }
+    if (dot(abc, ao) <= T(0))
+    {
+        SupPt<T> t = s.v[0];
+        s.v[0] = s.v[1];
+        s.v[1] = t;
+        dir = normalized(-abc);
+    }
+    else
+        dir = normalized(abc);
+}
+
+// Returns true when the simplex encloses the origin (collision.cpp:149-162).
+template <class T> PK_HD bool gjk_simplex(Simplex<T> &s, V3<T> &dir)
+{
+    if (s.n == 2)
+    {
+        const SupPt<T> a = s.v[1], b = s.v[0];
+        V3<T> ab = b.p - a.p, ao = -a.p;
+        if (dot(ab, ao) > T(0))
+        {
+            V3<T> tr = cross(cross(ab, ao), ab);
+            if (sqnorm(tr) < T(1e-12))
+            {
+                V3<T> ab_hat = normalized(ab);
+                V3<T> perp = cross(ab_hat, V3<T>{T(0), T(1), T(0)});
+                if (sqnorm(perp) < T(1e-12)) perp = cross(ab_hat, V3<T>{T(0), T(0), T(1)});
+                dir = normalized(perp);
+            }
+            else
+                dir = normalized(tr);
+        }
+        else
+        {
+            s.erase(0);
+            dir = normalized(ao);
+        }
+        return false;
+    }
+    if (s.n == 3)
+    {
+        gjk_triangle(s, dir);
+        return false;
+    }
+    if (s.n == 4)
+    {
+        const SupPt<T> a = s.v[3], b = s.v[2], c = s.v[1], d = s.v[0];
+        V3<T> ao = -a.p;
+        V3<T> abc = cross(b.p - a.p, c.p - a.p);
+        V3<T> acd = cross(c.p - a.p, d.p - a.p);
+        V3<T> adb = cross(d.p - a.p, b.p - a.p);
+        if (dot(abc, d.p - a.p) > T(0)) abc = -abc;
+        if (dot(acd, b.p - a.p) > T(0)) acd = -acd;
+        if (dot(adb, c.p - a.p) > T(0)) adb = -adb;
+        if (dot(abc, ao) > T(0))
+        {
+            s.n = 0;
+            s.push(c);
+            s.push(b);
+            s.push(a);
+            dir = normalized(abc);
+            gjk_triangle(s, dir);
+            return false;
+        }
+        if (dot(acd, ao) > T(0))
+        {
+            s.n = 0;
+            s.push(d);
+            s.push(c);
+            s.push(a);
+            dir = normalized(acd);
+            gjk_triangle(s, dir);
+            return false;
+        }
+        if (dot(adb, ao) > T(0))
+        {
+            s.n = 0;
+            s.push(b);
+            s.push(d);
+            s.push(a);
+            dir = normalized(adb);
+            gjk_triangle(s, dir);
+            return false;
+        }
+        return true;
+    }
+    return false;
+}
+
+// gjk_collision (collision.cpp:165-189). Returns true with the enclosing simplex.
+template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s)
+{
+    s.n = 0;
+    V3<T> dir{T(1), T(0), T(0)};
+    SupPt<T> pt = minkowski(A, B, dir);
+    s.push(pt);
+    if (sqnorm(pt.p) < T(1e-12)) return true;
+    dir = -normalized(pt.p);
+    for (int iter = 0; iter < 100; ++iter)
+    {
+        SupPt<T> np = minkowski(A, B, dir);
+        if (dot(np.p, dir) <= T(0)) return false;
+        s.push(np);
+        if (gjk_simplex(s, dir)) return true;
+    }
+    return false;
+}
+
+template <class T> PK_HD bool pad_simplex(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s)
+{
+    int n0 = s.n;
+    if (n0 <= 1)
+    {
+        V3<T> dir{T(1), T(0), T(0)};
+        SupPt<T> p2 = minkowski(A, B, dir);
+        if (sqnorm(p2.p - s.v[0].p) < T(1e-6)) p2 = minkowski(A, B, -dir);
+        s.push(p2);
+    }
+    if (n0 <= 2)
+    {
+        V3<T> line = s.v[1].p - s.v[0].p;
+        V3<T> dir = cross(normalized(line), V3<T>{T(0), T(1), T(0)});
+        if (sqnorm(dir) < T(1e-6)) dir = cross(normalized(line), V3<T>{T(0), T(0), T(1)});
+        dir = normalized(dir);
+        SupPt<T> p3 = minkowski(A, B, dir);
+        if (sqnorm(cross(line, p3.p - s.v[0].p)) < T(1e-6)) p3 = minkowski(A, B, -dir);
+        s.push(p3);
+    }
+    if (n0 <= 3)
+    {
+        V3<T> ab = s.v[1].p - s.v[0].p, ac = s.v[2].p - s.v[0].p;
+        V3<T> dir = normalized(cross(ab, ac));
+        SupPt<T> p4 = minkowski(A, B, dir);
+        if (tabs(dot(p4.p - s.v[0].p, dir)) < T(1e-6)) p4 = minkowski(A, B, -dir);
+        s.push(p4);
+    }
+    V3<T> ad = s.v[0].p - s.v[3].p, bd = s.v[1].p - s.v[3].p, cd = s.v[2].p - s.v[3].p;
+    return tabs(dot(ad, cross(bd, cd))) > T(1e-12);
+}
+
+template <class T> struct EpaFace
+{
+    uint16_t v[3];
+    uint16_t adj[3];
+    V3<T> n;
+    T d;
+    uint8_t obsolete;
+};
+
+template <class T> struct EpaState
+{
+    SupPt<T> poly[kMaxPoly];
+    EpaFace<T> faces[kMaxFaces];
+    uint16_t heap[kMaxFaces];
+    int npoly, nfaces, nheap;
+    int status;
+
+    // heap comparison used by the reference: comp(f1, f2) = dist(f1) > dist(f2)
+    PK_HD bool comp(uint16_t f1, uint16_t f2) const { return faces[f1].d > faces[f2].d; }
+
+    // libstdc++ __push_heap
+    PK_HD void sift_up(int hole, int top, uint16_t value)
+    {
+        int parent = (hole - 1) / 2;
+        while (hole > top && comp(heap[parent], value))
+        {
+            heap[hole] = heap[parent];
+            hole = parent;
+            parent = (hole - 1) / 2;
+        }
+        heap[hole] = value;
+    }
+    PK_HD void push_face(uint16_t f)
+    {
+        heap[nheap++] = f;
+        sift_up(nheap - 1, 0, heap[nheap - 1]);
+    }
+    // libstdc++ pop_heap = move the top to the back, then __adjust_heap on [0, len-1)
+    PK_HD uint16_t pop_top()
+    {
+        int len = nheap;
+        if (len > 1)
+        {
+            uint16_t value = heap[len - 1];
+            heap[len - 1] = heap[0];
+            int n = len - 1;
+            int hole = 0, top = 0, second = 0;
+            while (second < (n - 1) / 2)
+            {
+                second = 2 * (second + 1);
+                if (comp(heap[second], heap[second - 1])) second--;
+                heap[hole] = heap[second];
+                hole = second;
+            }
+            if ((n & 1) == 0 && second == (n - 2) / 2)
+            {
+                second = 2 * (second + 1);
+                heap[hole] = heap[second - 1];
+                hole = second - 1;
+            }
+            sift_up(hole, top, value);
+        }
+        return heap[--nheap];
+    }
+    PK_HD int pop_face()
+    {
+        while (nheap > 0)
+        {
+            uint16_t f = pop_top();
+            if (!faces[f].obsolete) return f;
+        }
+        return -1;
+    }
+    PK_HD void init_face(int f, int i, int j, int k, int opp)
+    {
+        EpaFace<T> &fc = faces[f];
+        fc.v[0] = uint16_t(i);
+        fc.v[1] = uint16_t(j);
+        fc.v[2] = uint16_t(k);
+        fc.adj[0] = fc.adj[1] = fc.adj[2] = kNull16;
+        fc.obsolete = 0;
+        V3<T> ab = poly[j].p - poly[i].p, ac = poly[k].p - poly[i].p;
+        V3<T> n = cross(ab, ac);
+        if (sqnorm(n) < T(1e-12))
+            n = V3<T>{T(0), T(0), T(0)};
+        else
+            n = normalized(n);
+        if (opp >= 0 && dot(n, poly[opp].p - poly[i].p) > T(0))
+        {
+            uint16_t t = fc.v[1];
+            fc.v[1] = fc.v[2];
+            fc.v[2] = t;
+            n = -n;
+        }
+        fc.n = n;
+        fc.d = dot(n, poly[i].p);
+    }
+    PK_HD void link(int f1, int f2, int va, int vb)
+    {
+        EpaFace<T> &a = faces[f1];
+        EpaFace<T> &b = faces[f2];
+        int e1 = (a.v[0] == va) ? 0 : (a.v[1] == va ? 1 : 2);
+        int e2 = (b.v[0] == vb) ? 0 : (b.v[1] == vb ? 1 : 2);
+        a.adj[e1] = uint16_t(f2);
+        b.adj[e2] = uint16_t(f1);
+    }
+    PK_HD Collision<T> barycentric(const EpaFace<T> &f) const
+    {
+        const SupPt<T> &p0 = poly[f.v[0]], &p1 = poly[f.v[1]], &p2 = poly[f.v[2]];
+        V3<T> pm = f.n * f.d;
+        V3<T> v0 = p1.p - p0.p, v1 = p2.p - p0.p, v2 = pm - p0.p;
+        T d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1);
+        T d20 = dot(v2, v0), d21 = dot(v2, v1);
+        T denom = d00 * d11 - d01 * d01;
+        T v = (d11 * d20 - d01 * d21) / denom;
+        T w = (d00 * d21 - d01 * d20) / denom;
+        T u = T(1) - v - w;
+        Collision<T> c;
+        c.normal = -f.n;
+        c.world_a = u * p0.pa + v * p1.pa + w * p2.pa;
+        c.world_b = u * p0.pb + v * p1.pb + w * p2.pb;
+        c.depth = f.d;
+        return c;
+    }
+};
+
+struct HorizonEdge
+{
+    uint16_t start, end, adj;
+};
+
+// epa_solver::solve (collision.cpp:411-504). Returns true with a collision.
+template <class T>
+PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T> &e, Collision<T> &out)
+{
+    e.status = 0;
+    if (s.n < 4 && !pad_simplex(A, B, s)) return false;
+    e.npoly = 4;
+    for (int i = 0; i < 4; ++i) e.poly[i] = s.v[i];
+    e.nfaces = 0;
+    e.nheap = 0;
+    const int init[4][4] = {{0, 1, 2, 3}, {0, 2, 3, 1}, {0, 3, 1, 2}, {1, 3, 2, 0}};
+    for (int f = 0; f < 4; ++f)
+    {
+        e.init_face(f, init[f][0], init[f][1], init[f][2], init[f][3]);
+        e.nfaces = f + 1;
+        e.push_face(uint16_t(f));
+    }
+    for (int i = 0; i < 4; ++i)
+        for (int j = i + 1; j < 4; ++j)
+            for (int e1 = 0; e1 < 3; ++e1)
+            {
+                uint16_t u1 = e.faces[i].v[e1], v1 = e.faces[i].v[(e1 + 1) % 3];
+                for (int e2 = 0; e2 < 3; ++e2)
+                {
+                    uint16_t u2 = e.faces[j].v[e2], v2 = e.faces[j].v[(e2 + 1) % 3];
+                    if (u1 == v2 && v1 == u2)
+                    {
+                        e.faces[i].adj[e1] = uint16_t(j);
+                        e.faces[j].adj[e2] = uint16_t(i);
+                    }
+                }
+            }
+
+    HorizonEdge horizon[kMaxHorizon];
+    uint16_t stack[kMaxFaces];
+    uint16_t nf[kMaxHorizon];
+    const T tol = T(1e-6);
+    for (int iter = 0; iter < 64; ++iter)
+    {
+        int mf = e.pop_face();
+        if (mf < 0) break;
+        const EpaFace<T> minf = e.faces[mf];
+        SupPt<T> p = minkowski(A, B, minf.n);
+        T pd = dot(minf.n, p.p);
+        if (pd - minf.d < tol)
+        {
+            out = e.barycentric(minf);
+            return true;
+        }
+        // find_silhouette (collision.cpp:315-353): depth-first flood over visible faces
+        int nh = 0, sp = 0;
+        stack[sp++] = uint16_t(mf);
+        e.faces[mf].obsolete = 1;
+        while (sp > 0)
+        {
+            int cur = stack[--sp];
+            for (int i = 0; i < 3; ++i)
+            {
+                uint16_t n = e.faces[cur].adj[i];
+                if (n == kNull16) continue;
+                EpaFace<T> &nb = e.faces[n];
+                if (nb.obsolete) continue;
+                if (dot(nb.n, p.p) > nb.d + tol)
+                {
+                    nb.obsolete = 1;
+                    if (sp < kMaxFaces)
+                        stack[sp++] = n;
+                    else
+                        e.status |= PK_NP_STACK_CAP;
+                }
+                else if (nh < kMaxHorizon)
+                    horizon[nh++] = {e.faces[cur].v[i], e.faces[cur].v[(i + 1) % 3], n};
+                else
+                    e.status |= PK_NP_HORIZON_CAP;
+            }
+        }
+        if (nh == 0) break;
+        if (e.nfaces + nh > kMaxFaces)
+        {
+            e.status |= PK_NP_FACE_CAP;
+            break;
+        }
+        e.poly[e.npoly] = p;
+        int pi = e.npoly++;
+        for (int h = 0; h < nh; ++h)
+        {
+            int f = e.nfaces++;
+            e.init_face(f, horizon[h].start, horizon[h].end, pi, -1);
+            e.link(f, horizon[h].adj, horizon[h].start, horizon[h].end);
+            e.push_face(uint16_t(f));
+            nf[h] = uint16_t(f);
+        }
+        for (int i = 0; i < nh; ++i)
+            for (int j = i + 1; j < nh; ++j)
+            {
+                if (horizon[i].end == horizon[j].start)
+                    e.link(nf[i], nf[j], horizon[i].end, pi);
+                else if (horizon[i].start == horizon[j].end)
+                    e.link(nf[j], nf[i], horizon[j].end, pi);
+            }
+    }
+    int mf = e.pop_face();
+    if (mf < 0) return false;
+    out = e.barycentric(e.faces[mf]);
+    return true;
+}
+
+// gjk_epa (collision.cpp:512-518)
+template <class T>
+PK_HD bool gjk_epa(const ShapeRef<T> &A, const ShapeRef<T> &B, EpaState<T> &e, Collision<T> &out, int *status)
+{
+    Simplex<T> s;
+    *status = 0;
+    if (!gjk(A, B, s)) return false;
+    bool hit = epa(A, B, s, e, out);
+    *status = e.status;
+    return hit;
+}
+
+} // namespace pk

@@ -1,0 +1,150 @@
+// pk_sort.cuh — stable LSD radix sort of (u64 key, u64 value) pairs whose element count lives in
+// device memory, so the launches can be captured in a CUDA graph once and replayed every step.
+//
+// One pass per 8-bit digit, three kernels per pass:
+//   hist    : each CTA counts the digits of its contiguous chunk           -> hist[digit][cta]
+//   scan    : one CTA turns the digit-major table into exclusive offsets
+//   scatter : each CTA walks its chunk in 256-element tiles, ranks equal digits inside a warp with
+//             __match_any_sync, combines warps through shared-memory counters, and writes each
+//             element to offset + running count + rank (stable).
+// Traffic per pass and element: read key+value twice (hist reads keys only), write key+value once.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pk
+{
+
+constexpr int kSortThreads = 256;
+constexpr int kSortRadix = 256;
+
+__device__ __forceinline__ void sort_chunk(int n, int nblocks, int b, int &lo, int &hi)
+{
+    int per = (n + nblocks - 1) / nblocks;
+    per = (per + kSortThreads - 1) / kSortThreads * kSortThreads;
+    lo = min(n, b * per);
+    hi = min(n, lo + per);
+}
+
+static __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint64_t *__restrict__ keys, const int *n_ptr,
+                                                            int shift, uint32_t *__restrict__ hist)
+{
+    __shared__ uint32_t h[kSortRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int lo, hi;
+    sort_chunk(*n_ptr, gridDim.x, blockIdx.x, lo, hi);
+    for (int i = lo + threadIdx.x; i < hi; i += kSortThreads)
+        atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
+    __syncthreads();
+    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of `count` entries with one CTA of 1024 threads.
+static __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist, int count)
+{
+    __shared__ uint32_t part[1024];
+    int per = (count + 1023) / 1024;
+    int lo = threadIdx.x * per, hi = min(count, lo + per);
+    uint32_t s = 0;
+    for (int i = lo; i < hi; ++i) s += hist[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1)
+    {
+        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+    for (int i = lo; i < hi; ++i)
+    {
+        uint32_t v = hist[i];
+        hist[i] = run;
+        run += v;
+    }
+}
+
+template <class V>
+__global__ void __launch_bounds__(kSortThreads)
+    k_sort_scatter(const uint64_t *__restrict__ kin, const V *__restrict__ vin, uint64_t *__restrict__ kout,
+                   V *__restrict__ vout, const int *n_ptr, int shift, const uint32_t *__restrict__ hist)
+{
+    constexpr int W = kSortThreads / 32;
+    __shared__ uint32_t base[kSortRadix];
+    __shared__ uint32_t running[kSortRadix];
+    __shared__ uint32_t wcnt[W][kSortRadix + 1];
+    __shared__ uint32_t tile_total[kSortRadix];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    base[t] = hist[t * gridDim.x + blockIdx.x];
+    running[t] = 0;
+    int lo, hi;
+    sort_chunk(*n_ptr, gridDim.x, blockIdx.x, lo, hi);
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int tile = lo; tile < hi; tile += kSortThreads)
+    {
+        for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
+        if (t == 0)
+            for (int w = 0; w < W; ++w) wcnt[w][kSortRadix] = 0;
+        __syncthreads();
+        int i = tile + t;
+        bool valid = i < hi;
+        uint64_t k = valid ? kin[i] : 0;
+        V v = valid ? vin[i] : V(0);
+        int d = valid ? int((k >> shift) & 0xFF) : kSortRadix;
+        unsigned same = __match_any_sync(0xFFFFFFFFu, d);
+        int rank = __popc(same & lt_mask);
+        if (rank == 0) wcnt[warp][d] = __popc(same);
+        __syncthreads();
+        {
+            uint32_t s = 0;
+            for (int w = 0; w < W; ++w)
+            {
+                uint32_t c = wcnt[w][t];
+                wcnt[w][t] = s;
+                s += c;
+            }
+            tile_total[t] = s;
+        }
+        __syncthreads();
+        if (valid)
+        {
+            uint32_t dst = base[d] + running[d] + wcnt[warp][d] + uint32_t(rank);
+            kout[dst] = k;
+            vout[dst] = v;
+        }
+        __syncthreads();
+        running[t] += tile_total[t];
+        __syncthreads();
+    }
+}
+
+// Host-side launcher. Sorts [0, *n_dev) of (k0, v0) by the low `bits` bits of the key; ping-pongs
+// with (k1, v1). Returns true when the result ends in (k1, v1).
+template <class V>
+inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_dev, int bits, int nblocks,
+                       uint32_t *hist, cudaStream_t st)
+{
+    int passes = (bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    uint64_t *ka = k0, *kb = k1;
+    V *va = v0, *vb = v1;
+    for (int p = 0; p < passes; ++p)
+    {
+        int shift = 8 * p;
+        k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n_dev, shift, hist);
+        k_sort_scan<<<1, 1024, 0, st>>>(hist, kSortRadix * nblocks);
+        k_sort_scatter<V><<<nblocks, kSortThreads, 0, st>>>(ka, va, kb, vb, n_dev, shift, hist);
+        uint64_t *tk = ka;
+        ka = kb;
+        kb = tk;
+        V *tv = va;
+        va = vb;
+        vb = tv;
+    }
+    return (passes & 1) != 0;
+}
+
+} // namespace pk

@@ -1,0 +1,321 @@
+"""Seeded synthetic scenes for the world-step workloads (no dataset is involved).
+
+Every scene is a list of shapes plus a structured array of body descriptors (world.BODY_DTYPE)
+that both the device library and the FP64 oracle consume unchanged, so their inputs are identical.
+
+  config1  1,000 dynamic boxes (half-extents U[0.1,0.5] m, density 1000 kg/m^3) above a static
+           ground box (100 x 1 x 100 m, top at y = 0), uniform random orientation, at rest.
+  config2  N convex bodies in a 200 m cube: 1/3 UV spheres (r ~ lognormal(ln 0.3, 0.4)),
+           1/3 boxes (half-extents U[0.1,0.6]), 1/3 hulls of 16 points on a sphere of radius
+           U[0.2,0.6]; velocities N(0, 1 m/s) per axis.
+  config3  W independent worlds with log-uniform body counts in [nmin, nmax]; each a pile of
+           boxes/spheres/hulls dropped into a 5 m walled bin (static floor + 4 walls).
+  config5  spheres (r ~ lognormal(ln 0.05, 0.3)) poured into a 20 x 20 m open box.
+
+Mass properties (the reference's mesh::mass_center / inertia_tensor throw, mesh.cpp:154-166):
+box m = rho*8*hx*hy*hz, I = m/3 diag(hy^2+hz^2, hx^2+hz^2, hx^2+hy^2); sphere m = rho*4/3*pi*r^3,
+I = 2/5 m r^2; hull m = rho*volume(hull), I = the box inertia of its local AABB.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from .world import BODY_DTYPE
+
+RHO = 1000.0
+SEED_BASE = 0x50484B0000000000
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    shapes: list            # ("box", hx, hy, hz) | ("sphere", r, stacks, sectors) | ("mesh", verts, tris)
+    bodies: np.ndarray      # BODY_DTYPE records; "shape" indexes `shapes`
+    nworlds: int = 1
+    gravity: tuple = (0.0, -9.81, 0.0)
+    dt: float = 1.0 / 120.0
+    steps: int = 240
+    iterations: int = 10
+
+    @property
+    def n_dynamic(self):
+        return int(np.count_nonzero(self.bodies["type"] == 0))
+
+    def vertex_count(self):
+        n = 0
+        for s in self.shapes:
+            if s[0] == "box":
+                n += 8
+            elif s[0] == "sphere":
+                n += 2 + (s[2] - 1) * s[3]
+            else:
+                n += len(s[1])
+        return n
+
+    def world_slice(self, w):
+        """The bodies of world w, in creation order (their local arena indices)."""
+        return self.bodies[self.bodies["world"] == w]
+
+
+def rng_for(config: int, seed: int | None = None):
+    s = SEED_BASE + config if seed is None else seed
+    return np.random.Generator(np.random.PCG64(s))
+
+
+def random_quats(rng, n):
+    """Shoemake's uniform random unit quaternions, returned (w, x, y, z)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1.0 - u1), np.sqrt(u1)
+    x, y = a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2)
+    z, w = b * np.sin(2 * np.pi * u3), b * np.cos(2 * np.pi * u3)
+    return np.stack([w, x, y, z], axis=1)
+
+
+def box_mass(hx, hy, hz):
+    m = RHO * 8.0 * hx * hy * hz
+    return m, np.array([m / 3.0 * (hy * hy + hz * hz), m / 3.0 * (hx * hx + hz * hz), m / 3.0 * (hx * hx + hy * hy)])
+
+
+def sphere_mass(r):
+    m = RHO * 4.0 / 3.0 * math.pi * r ** 3
+    i = 0.4 * m * r * r
+    return m, np.array([i, i, i])
+
+
+def hull_shape(rng, scale):
+    """16 points uniform on a sphere of radius `scale`, triangulated by their convex hull."""
+    from scipy.spatial import ConvexHull
+
+    p = rng.normal(size=(16, 3))
+    p = p / np.linalg.norm(p, axis=1, keepdims=True) * scale
+    hull = ConvexHull(p)
+    tris = hull.simplices.copy()
+    # orient every triangle outward (signed-tetrahedron volume of mesh::volume, mesh.cpp:139-151)
+    c = p.mean(axis=0)
+    for t in tris:
+        a, b, d = p[t[0]], p[t[1]], p[t[2]]
+        if np.dot(np.cross(b - a, d - a), a - c) < 0:
+            t[1], t[2] = t[2], t[1]
+    vol = float(abs(hull.volume))
+    lo, hi = p.min(axis=0), p.max(axis=0)
+    he = 0.5 * (hi - lo)
+    m = RHO * vol
+    I = np.array([m / 3.0 * (he[1] ** 2 + he[2] ** 2), m / 3.0 * (he[0] ** 2 + he[2] ** 2),
+                  m / 3.0 * (he[0] ** 2 + he[1] ** 2)])
+    # centre the vertices on their AABB so the body position is the shape's middle
+    p = p - 0.5 * (hi + lo)
+    return ("mesh", p, tris), m, I
+
+
+def _records(n):
+    r = np.zeros(n, dtype=BODY_DTYPE)
+    r["quat"][:, 0] = 1.0
+    r["restitution"] = 0.5
+    r["friction"] = 0.5
+    r["mass"] = 1.0
+    r["inertia"][:, [0, 4, 8]] = 1.0
+    return r
+
+
+def _static(shape, pos, world=0):
+    r = _records(1)
+    r["type"] = 1
+    r["shape"] = shape
+    r["pos"] = pos
+    r["world"] = world
+    return r
+
+
+def config1(n=1000, seed=None, ground=True, restitution=0.0, friction=0.5):
+    rng = rng_for(1, seed)
+    shapes, recs = [], []
+    if ground:
+        shapes.append(("box", 100.0, 0.5, 100.0))
+        recs.append(_static(0, (0.0, -0.5, 0.0)))
+    he = rng.uniform(0.1, 0.5, size=(n, 3))
+    q = random_quats(rng, n)
+    r = _records(n)
+    for i in range(n):
+        hx, hy, hz = he[i]
+        shapes.append(("box", float(hx), float(hy), float(hz)))
+        m, I = box_mass(hx, hy, hz)
+        h = math.sqrt(hx * hx + hy * hy + hz * hz)
+        r[i]["shape"] = len(shapes) - 1
+        r[i]["mass"] = m
+        r[i]["inertia"] = np.diag(I).reshape(-1)
+        r[i]["pos"] = (rng.uniform(-10, 10), rng.uniform(h, 20 + h), rng.uniform(-10, 10))
+        r[i]["quat"] = q[i]
+    r["restitution"] = restitution
+    r["friction"] = friction
+    recs.append(r)
+    return Scene("config1: %d boxes on a static ground, FP64, dt=1/120, 240 steps, 10 iterations" % n,
+                 shapes, np.concatenate(recs), 1, dt=1 / 120, steps=240, iterations=10)
+
+
+def _mixed_body(rng, kind, shapes, size_scale=1.0):
+    if kind == 0:
+        r = float(np.exp(rng.normal(math.log(0.3), 0.4))) * size_scale
+        shapes.append(("sphere", r, 16, 32))
+        m, I = sphere_mass(r)
+        return m, I, r
+    if kind == 1:
+        he = rng.uniform(0.1, 0.6, 3) * size_scale
+        shapes.append(("box", float(he[0]), float(he[1]), float(he[2])))
+        m, I = box_mass(*he)
+        return m, I, float(np.linalg.norm(he))
+    sh, m, I = hull_shape(rng, float(rng.uniform(0.2, 0.6)) * size_scale)
+    shapes.append(sh)
+    return m, I, float(np.max(np.linalg.norm(sh[1], axis=1)))
+
+
+def config2(n=100_000, seed=None, extent=200.0):
+    rng = rng_for(2, seed)
+    shapes = []
+    r = _records(n)
+    q = random_quats(rng, n)
+    for i in range(n):
+        m, I, _ = _mixed_body(rng, i % 3, shapes)
+        r[i]["shape"] = len(shapes) - 1
+        r[i]["mass"] = m
+        r[i]["inertia"] = np.diag(I).reshape(-1)
+    r["pos"] = rng.uniform(-extent / 2, extent / 2, size=(n, 3))
+    r["vel"] = rng.normal(0.0, 1.0, size=(n, 3))
+    r["quat"] = q
+    return Scene("config2: %d mixed convex bodies in a %g m cube, dt=1/120, 120 steps" % (n, extent),
+                 shapes, r, 1, gravity=(0.0, -9.81, 0.0), dt=1 / 120, steps=120, iterations=10)
+
+
+def bin_statics(shapes, world, half=2.5, wall_h=6.0, thick=0.25):
+    """Static floor + 4 walls of a (2*half) m square bin; shapes shared across worlds."""
+    recs = []
+    floor, wall_x, wall_z = 0, 1, 2
+    recs.append(_static(floor, (0.0, -thick, 0.0), world))
+    recs.append(_static(wall_x, (half + thick, wall_h, 0.0), world))
+    recs.append(_static(wall_x, (-half - thick, wall_h, 0.0), world))
+    recs.append(_static(wall_z, (0.0, wall_h, half + thick), world))
+    recs.append(_static(wall_z, (0.0, wall_h, -half - thick), world))
+    return recs
+
+
+def config3(nworlds=4096, nmin=8, nmax=2048, seed=None, kinds=(0, 1, 2), half=2.5, max_shapes_per_kind=None):
+    """Batched piles. Shapes are shared between worlds: each world draws its bodies from a pool of
+    shapes generated once (`max_shapes_per_kind` per kind), like meshes shared via shared_ptr
+    (object.h:61-65)."""
+    rng = rng_for(3, seed)
+    thick, wall_h = 0.25, 6.0
+    shapes = [("box", half + thick, thick, half + thick), ("box", thick, wall_h, half + 2 * thick),
+              ("box", half + 2 * thick, wall_h, thick)]
+    pool = {k: [] for k in kinds}
+    npool = max_shapes_per_kind or 64
+    for k in kinds:
+        for _ in range(npool):
+            m, I, rad = _mixed_body(rng, k, shapes, size_scale=0.5)
+            pool[k].append((len(shapes) - 1, m, I, rad))
+    counts = np.round(np.exp(rng.uniform(math.log(nmin), math.log(nmax), nworlds))).astype(int)
+    recs = []
+    for w in range(nworlds):
+        recs += bin_statics(shapes, w, half, wall_h, thick)
+        n = int(counts[w])
+        r = _records(n)
+        kk = rng.integers(0, len(kinds), n)
+        pick = rng.integers(0, npool, n)
+        q = random_quats(rng, n)
+        height = 0.5 + n * 0.02
+        for i in range(n):
+            sid, m, I, rad = pool[kinds[kk[i]]][pick[i]]
+            r[i]["shape"] = sid
+            r[i]["mass"] = m
+            r[i]["inertia"] = np.diag(I).reshape(-1)
+            lim = max(half - rad, 0.0)
+            r[i]["pos"] = (rng.uniform(-lim, lim), rng.uniform(rad, rad + height), rng.uniform(-lim, lim))
+            r[i]["quat"] = q[i]
+        r["world"] = w
+        r["restitution"] = 0.0
+        recs.append(r)
+    return Scene("config3: %d worlds, %d-%d bodies each (log-uniform), boxes/spheres/hulls in %g m bins, "
+                 "dt=1/120, 240 steps" % (nworlds, nmin, nmax, 2 * half),
+                 shapes, np.concatenate(recs), nworlds, dt=1 / 120, steps=240, iterations=10)
+
+
+def config5(n=1_000_000, seed=None, half=10.0, nradii=32):
+    """Spheres poured into a 20 x 20 m open box; radii drawn from a pool of `nradii` lognormal
+    radii so the UV meshes are shared."""
+    rng = rng_for(5, seed)
+    thick, wall_h = 0.25, 10.0
+    shapes = [("box", half + thick, thick, half + thick), ("box", thick, wall_h, half + 2 * thick),
+              ("box", half + 2 * thick, wall_h, thick)]
+    radii = np.exp(rng.normal(math.log(0.05), 0.3, nradii))
+    for rr in radii:
+        shapes.append(("sphere", float(rr), 16, 32))
+    recs = bin_statics(shapes, 0, half, wall_h, thick)
+    r = _records(n)
+    pick = rng.integers(0, nradii, n)
+    for i in range(n):
+        m, I = sphere_mass(radii[pick[i]])
+        r[i]["shape"] = 3 + pick[i]
+        r[i]["mass"] = m
+        r[i]["inertia"] = np.diag(I).reshape(-1)
+    r["pos"][:, 0] = rng.uniform(-half + 0.2, half - 0.2, n)
+    r["pos"][:, 2] = rng.uniform(-half + 0.2, half - 0.2, n)
+    r["pos"][:, 1] = rng.uniform(0.1, 0.1 + n * 2e-5, n)
+    r["quat"] = random_quats(rng, n)
+    r["restitution"] = 0.0
+    recs.append(r)
+    return Scene("config5: %d spheres in a 20x20 m box, dt=1/240, 480 steps, 20 iterations" % n,
+                 shapes, np.concatenate(recs), 1, dt=1 / 240, steps=480, iterations=20)
+
+
+def small_pile(n=60, seed=7, extent=3.0, kinds=(1,), ground=True, restitution=0.0):
+    """A small pile for parity tests: bodies close together above a ground box."""
+    rng = rng_for(9, seed)
+    shapes, recs = [], []
+    if ground:
+        shapes.append(("box", 20.0, 0.5, 20.0))
+        recs.append(_static(0, (0.0, -0.5, 0.0)))
+    r = _records(n)
+    q = random_quats(rng, n)
+    for i in range(n):
+        m, I, rad = _mixed_body(rng, kinds[i % len(kinds)], shapes, size_scale=0.8)
+        r[i]["shape"] = len(shapes) - 1
+        r[i]["mass"] = m
+        r[i]["inertia"] = np.diag(I).reshape(-1)
+        r[i]["pos"] = (rng.uniform(-extent, extent), rng.uniform(rad, rad + 4.0), rng.uniform(-extent, extent))
+        r[i]["quat"] = q[i]
+    r["restitution"] = restitution
+    recs.append(r)
+    return Scene("small pile", shapes, np.concatenate(recs), 1)
+
+
+def load(world, scene: Scene, shape_offset_map=None):
+    """Create the scene's shapes and bodies in a physkit_gb300.World; returns body handles."""
+    ids = []
+    for s in scene.shapes:
+        if s[0] == "box":
+            ids.append(world.mesh_box(*s[1:4]))
+        elif s[0] == "sphere":
+            ids.append(world.mesh_sphere(s[1], s[2], s[3]))
+        else:
+            ids.append(world.mesh_make(s[1], s[2]))
+    rec = scene.bodies.copy()
+    rec["shape"] = np.asarray(ids, dtype=np.int32)[rec["shape"]]
+    return world.create_rigids(rec)
+
+
+def make_world(scene: Scene, precision="f64", pair_factor=8, iterations=None, max_bodies_per_world=0):
+    from .world import World, world_desc
+
+    nb = len(scene.bodies)
+    per_world = max_bodies_per_world or (nb if scene.nworlds == 1 else
+                                         int(np.bincount(scene.bodies["world"]).max()))
+    d = (world_desc.make().with_gravity(scene.gravity)
+         .with_solver_iterations(iterations if iterations is not None else scene.iterations)
+         .with_precision(precision)
+         .with_capacity(max_bodies=nb, max_pairs=max(pair_factor * nb, 1024), max_worlds=scene.nworlds,
+                        max_bodies_per_world=per_world, max_shape_vertices=scene.vertex_count() + 16,
+                        max_shapes=len(scene.shapes) + 4))
+    w = World(d)
+    handles = load(w, scene)
+    return w, handles

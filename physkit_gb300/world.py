@@ -1,0 +1,450 @@
+"""Python mirror of the reference's world API over the C ABI (include/physkit_gb300.h).
+
+Names follow the reference: world_desc (core/world.h:23-49), object_desc (core/object.h:15-109),
+world::create_rigid / remove_rigid / get_rigid / step (core/world.h:202-242), mesh::box / sphere /
+pyramid / make (collision/mesh.h:219-236). Invalid input raises ValueError like the reference's
+std::invalid_argument (object.h:121); stale handles give None like get_rigid's std::nullopt.
+
+The device library is required: there is no CPU fallback. Without a CUDA device, World() raises
+RuntimeError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_lock = threading.Lock()
+
+PK_OK = 0
+PK_ERR_INVALID = -1
+PK_ERR_STALE_HANDLE = -2
+PK_ERR_CAPACITY = -3
+PK_ERR_CUDA = -4
+PK_ERR_DEVICE_STATUS = -5
+PK_ERR_NO_DEVICE = -6
+PRECISION = {"f64": 0, "f32": 1}
+
+STATUS_BITS = {1: "pair_overflow", 2: "epa_cap", 4: "colour_cap", 8: "traversal_stack", 16: "nan"}
+
+
+class WorldDescC(C.Structure):
+    _fields_ = [("gravity", C.c_double * 3), ("solver_iterations", C.c_int32), ("precision", C.c_int32),
+                ("max_bodies", C.c_int32), ("max_pairs", C.c_int32), ("max_worlds", C.c_int32),
+                ("max_bodies_per_world", C.c_int32), ("max_shape_vertices", C.c_int32),
+                ("max_shapes", C.c_int32)]
+
+
+BODY_DTYPE = np.dtype([("type", np.int32), ("shape", np.int32), ("world", np.int32), ("reserved", np.int32),
+                       ("pos", np.float64, 3), ("quat", np.float64, 4), ("vel", np.float64, 3),
+                       ("ang_vel", np.float64, 3), ("mass", np.float64), ("inertia", np.float64, 9),
+                       ("restitution", np.float64), ("friction", np.float64)], align=True)
+assert BODY_DTYPE.itemsize == 216
+
+
+class StepInfoC(C.Structure):
+    _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
+class CollideShapeC(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("shape", C.c_int32), ("p", C.c_double * 10)]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load libphyskit_gb300.so (building it in-tree first if it is missing or stale)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.build()
+        L = C.CDLL(path)
+        P = C.POINTER
+        vp, dp, i32p, u64p = C.c_void_p, P(C.c_double), P(C.c_int32), P(C.c_uint64)
+        sig = {
+            "pk_world_desc_init": (None, [P(WorldDescC)]),
+            "pk_world_create": (C.c_int, [P(WorldDescC), P(C.c_void_p)]),
+            "pk_world_destroy": (None, [vp]),
+            "pk_shape_mesh": (C.c_int, [vp, dp, C.c_int32, i32p, C.c_int32, i32p]),
+            "pk_shape_box": (C.c_int, [vp, C.c_double, C.c_double, C.c_double, i32p]),
+            "pk_shape_sphere": (C.c_int, [vp, C.c_double, C.c_int32, C.c_int32, i32p]),
+            "pk_shape_pyramid": (C.c_int, [vp, C.c_double, C.c_double, i32p]),
+            "pk_body_add": (C.c_int, [vp, C.c_void_p, C.c_int32, u64p]),
+            "pk_body_remove": (C.c_int, [vp, C.c_uint64]),
+            "pk_world_clear": (C.c_int, [vp, C.c_int32]),
+            "pk_world_set_active": (C.c_int, [vp, C.c_int32, C.c_int32]),
+            "pk_world_set_gravity": (C.c_int, [vp, C.c_int32, dp]),
+            "pk_world_step": (C.c_int, [vp, C.c_double]),
+            "pk_world_step_async": (C.c_int, [vp, C.c_double]),
+            "pk_world_synchronize": (C.c_int, [vp, P(StepInfoC)]),
+            "pk_world_capture": (C.c_int, [vp, C.c_double]),
+            "pk_world_step_graph": (C.c_int, [vp]),
+            "pk_world_stream": (C.c_void_p, [vp]),
+            "pk_world_read_bodies": (C.c_int, [vp, dp, C.c_int32, i32p]),
+            "pk_world_write_body": (C.c_int, [vp, C.c_uint64, dp]),
+            "pk_world_read_pairs": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p]),
+            "pk_world_read_manifolds": (C.c_int, [vp, u64p, i32p, i32p, dp, C.c_int32, i32p]),
+            "pk_world_read_events": (C.c_int, [vp, u64p, i32p, i32p, C.c_int32, i32p]),
+            "pk_world_read_colours": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p, i32p]),
+            "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
+            "pk_last_cuda_error": (C.c_int, []),
+            "pk_version": (C.c_char_p, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _check(rc, what):
+    if rc == PK_OK:
+        return
+    if rc == PK_ERR_INVALID:
+        raise ValueError(f"{what}: invalid argument")
+    if rc == PK_ERR_CAPACITY:
+        raise MemoryError(f"{what}: capacity exhausted")
+    if rc == PK_ERR_NO_DEVICE:
+        raise RuntimeError(f"{what}: no CUDA device (physkit_gb300 has no CPU fallback)")
+    if rc == PK_ERR_CUDA:
+        raise RuntimeError(f"{what}: CUDA error {lib().pk_last_cuda_error()}")
+    raise RuntimeError(f"{what}: error {rc}")
+
+
+class world_desc:
+    """world_desc (core/world.h:23-49) plus the device capacities of this implementation."""
+
+    def __init__(self):
+        self.gravity = (0.0, -9.81, 0.0)
+        self.solver_iterations = 10
+        self.precision = "f64"
+        self.max_bodies = 4096
+        self.max_pairs = 0
+        self.max_worlds = 1
+        self.max_bodies_per_world = 0
+        self.max_shape_vertices = 0
+        self.max_shapes = 0
+
+    @staticmethod
+    def make():
+        return world_desc()
+
+    def with_gravity(self, g):
+        self.gravity = tuple(float(x) for x in g)
+        return self
+
+    def with_solver_iterations(self, n):
+        self.solver_iterations = int(n)
+        return self
+
+    def with_precision(self, p):
+        if p not in PRECISION:
+            raise ValueError(f"precision must be one of {list(PRECISION)}")
+        self.precision = p
+        return self
+
+    def with_capacity(self, max_bodies, max_pairs=0, max_worlds=1, max_bodies_per_world=0,
+                      max_shape_vertices=0, max_shapes=0):
+        self.max_bodies, self.max_pairs, self.max_worlds = int(max_bodies), int(max_pairs), int(max_worlds)
+        self.max_bodies_per_world = int(max_bodies_per_world)
+        self.max_shape_vertices, self.max_shapes = int(max_shape_vertices), int(max_shapes)
+        return self
+
+    def to_c(self):
+        d = WorldDescC()
+        lib().pk_world_desc_init(C.byref(d))
+        for k in range(3):
+            d.gravity[k] = self.gravity[k]
+        d.solver_iterations = self.solver_iterations
+        d.precision = PRECISION[self.precision]
+        d.max_bodies = self.max_bodies
+        d.max_pairs = self.max_pairs
+        d.max_worlds = self.max_worlds
+        d.max_bodies_per_world = self.max_bodies_per_world
+        d.max_shape_vertices = self.max_shape_vertices
+        d.max_shapes = self.max_shapes
+        return d
+
+
+class object_desc:
+    """object_desc (core/object.h:15-109): builder for one rigid body."""
+
+    def __init__(self, static=False):
+        self.static = static
+        self.pos = (0.0, 0.0, 0.0)
+        self.vel = (0.0, 0.0, 0.0)
+        self.mass = 1.0
+        self.orientation = (1.0, 0.0, 0.0, 0.0)
+        self.ang_vel = (0.0, 0.0, 0.0)
+        self.inertia = np.eye(3)
+        self.mesh = None
+        self.restitution = 0.5
+        self.friction = 0.5
+        self.world = 0
+
+    @staticmethod
+    def dynam():
+        return object_desc(False)
+
+    @staticmethod
+    def stat():
+        return object_desc(True)
+
+    def with_pos(self, p):
+        self.pos = tuple(map(float, p))
+        return self
+
+    def with_vel(self, v):
+        self.vel = tuple(map(float, v))
+        return self
+
+    def with_mass(self, m):
+        self.mass = float(m)
+        return self
+
+    def with_orientation(self, q):
+        self.orientation = tuple(map(float, q))
+        return self
+
+    def with_ang_vel(self, w):
+        self.ang_vel = tuple(map(float, w))
+        return self
+
+    def with_inertia_tensor(self, inertia):
+        a = np.asarray(inertia, dtype=np.float64)
+        self.inertia = np.diag(a) if a.shape == (3,) else a.reshape(3, 3)
+        return self
+
+    def with_mesh(self, shape_id):
+        self.mesh = shape_id
+        return self
+
+    def with_restitution(self, r):
+        self.restitution = float(r)
+        return self
+
+    def with_friction(self, f):
+        self.friction = float(f)
+        return self
+
+    def in_world(self, w):
+        self.world = int(w)
+        return self
+
+    def record(self):
+        if self.mesh is None:
+            raise ValueError("Object must have a mesh")  # object.h:121
+        r = np.zeros(1, dtype=BODY_DTYPE)
+        r["type"] = 1 if self.static else 0
+        r["shape"] = self.mesh
+        r["world"] = self.world
+        r["pos"] = self.pos
+        r["quat"] = self.orientation
+        r["vel"] = self.vel
+        r["ang_vel"] = self.ang_vel
+        r["mass"] = self.mass
+        r["inertia"] = self.inertia.reshape(-1)
+        r["restitution"] = self.restitution
+        r["friction"] = self.friction
+        return r
+
+
+class World:
+    """A device-resident world (or batch of independent worlds) behind the C ABI."""
+
+    def __init__(self, desc: world_desc | None = None):
+        self.desc = desc or world_desc()
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.pk_world_create(C.byref(self.desc.to_c()), C.byref(h)), "pk_world_create")
+        self.h = h
+        self.last_info = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pk_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # meshes (mesh.h:219-236) ------------------------------------------------------------------
+    def mesh_box(self, hx, hy, hz):
+        out = C.c_int32()
+        _check(self.L.pk_shape_box(self.h, hx, hy, hz, C.byref(out)), "pk_shape_box")
+        return out.value
+
+    def mesh_sphere(self, r, stacks=16, sectors=32):
+        out = C.c_int32()
+        _check(self.L.pk_shape_sphere(self.h, r, stacks, sectors, C.byref(out)), "pk_shape_sphere")
+        return out.value
+
+    def mesh_pyramid(self, b, h):
+        out = C.c_int32()
+        _check(self.L.pk_shape_pyramid(self.h, b, h, C.byref(out)), "pk_shape_pyramid")
+        return out.value
+
+    def mesh_make(self, verts, tris):
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64).reshape(-1))
+        t = np.ascontiguousarray(np.asarray(tris, dtype=np.int32).reshape(-1))
+        out = C.c_int32()
+        _check(self.L.pk_shape_mesh(self.h, _ptr(v, C.c_double), len(v) // 3, _ptr(t, C.c_int32), len(t) // 3,
+                                    C.byref(out)), "pk_shape_mesh")
+        return out.value
+
+    # bodies ------------------------------------------------------------------------------------
+    def create_rigid(self, desc: object_desc):
+        return int(self.create_rigids(desc.record())[0])
+
+    def create_rigids(self, records: np.ndarray):
+        rec = np.ascontiguousarray(records, dtype=BODY_DTYPE)
+        n = len(rec)
+        out = np.zeros(max(n, 1), dtype=np.uint64)
+        _check(self.L.pk_body_add(self.h, rec.ctypes.data, n, _ptr(out, C.c_uint64)), "pk_body_add")
+        return out[:n]
+
+    def remove_rigid(self, handle):
+        rc = self.L.pk_body_remove(self.h, C.c_uint64(int(handle)))
+        if rc == PK_ERR_STALE_HANDLE:
+            return False
+        _check(rc, "pk_body_remove")
+        return True
+
+    def clear_world(self, w):
+        _check(self.L.pk_world_clear(self.h, int(w)), "pk_world_clear")
+
+    def set_active(self, w, active):
+        _check(self.L.pk_world_set_active(self.h, int(w), int(bool(active))), "pk_world_set_active")
+
+    # stepping ----------------------------------------------------------------------------------
+    def step(self, dt, check=True):
+        rc = self.L.pk_world_step(self.h, float(dt))
+        if rc == PK_ERR_DEVICE_STATUS and not check:
+            return
+        _check(rc, "pk_world_step")
+
+    def step_async(self, dt):
+        _check(self.L.pk_world_step_async(self.h, float(dt)), "pk_world_step_async")
+
+    def capture(self, dt):
+        _check(self.L.pk_world_capture(self.h, float(dt)), "pk_world_capture")
+
+    def step_graph(self):
+        _check(self.L.pk_world_step_graph(self.h), "pk_world_step_graph")
+
+    def synchronize(self):
+        info = StepInfoC()
+        rc = self.L.pk_world_synchronize(self.h, C.byref(info))
+        if rc not in (PK_OK, PK_ERR_DEVICE_STATUS):
+            _check(rc, "pk_world_synchronize")
+        self.last_info = {"pairs": info.pairs, "leaves": info.leaves, "status": info.status,
+                          "flags": [v for k, v in STATUS_BITS.items() if info.status & k]}
+        return self.last_info
+
+    def stream(self):
+        return self.L.pk_world_stream(self.h)
+
+    # reads -------------------------------------------------------------------------------------
+    def bodies(self):
+        n = C.c_int32()
+        self.L.pk_world_read_bodies(self.h, None, 0, C.byref(n))
+        out = np.zeros((max(n.value, 1), 14))
+        _check(self.L.pk_world_read_bodies(self.h, _ptr(out, C.c_double), n.value, C.byref(n)),
+               "pk_world_read_bodies")
+        return out[: n.value]
+
+    def get_rigid(self, handle):
+        """world_base::get_rigid (world.h:220-224): state row, or None for a stale handle."""
+        slot = int(handle) & 0xFFFFFFFF
+        b = self.bodies()
+        if slot >= len(b) or b[slot, 13] == 0.0:
+            return None
+        return b[slot]
+
+    def write_body(self, handle, state13):
+        s = np.ascontiguousarray(state13, dtype=np.float64)
+        _check(self.L.pk_world_write_body(self.h, C.c_uint64(int(handle)), _ptr(s, C.c_double)),
+               "pk_world_write_body")
+
+    def pairs(self, with_worlds=False):
+        n = C.c_int32()
+        self.L.pk_world_read_pairs(self.h, None, None, 0, C.byref(n))
+        k = np.zeros(max(n.value, 1), dtype=np.uint64)
+        w = np.zeros(max(n.value, 1), dtype=np.int32)
+        _check(self.L.pk_world_read_pairs(self.h, _ptr(k, C.c_uint64), _ptr(w, C.c_int32), n.value, C.byref(n)),
+               "pk_world_read_pairs")
+        return (k[: n.value], w[: n.value]) if with_worlds else k[: n.value]
+
+    def manifolds(self, with_worlds=False):
+        n = C.c_int32()
+        self.L.pk_world_read_manifolds(self.h, None, None, None, None, 0, C.byref(n))
+        m = max(n.value, 1)
+        k = np.zeros(m, dtype=np.uint64)
+        w = np.zeros(m, dtype=np.int32)
+        c = np.zeros(m, dtype=np.int32)
+        ct = np.zeros((m, 4, 13))
+        _check(self.L.pk_world_read_manifolds(self.h, _ptr(k, C.c_uint64), _ptr(w, C.c_int32), _ptr(c, C.c_int32),
+                                              _ptr(ct, C.c_double), n.value, C.byref(n)), "pk_world_read_manifolds")
+        r = (k[: n.value], c[: n.value], ct[: n.value])
+        return r + (w[: n.value],) if with_worlds else r
+
+    def events(self, with_worlds=False):
+        n = C.c_int32()
+        self.L.pk_world_read_events(self.h, None, None, None, 0, C.byref(n))
+        m = max(n.value, 1)
+        k = np.zeros(m, dtype=np.uint64)
+        w = np.zeros(m, dtype=np.int32)
+        kd = np.zeros(m, dtype=np.int32)
+        _check(self.L.pk_world_read_events(self.h, _ptr(k, C.c_uint64), _ptr(w, C.c_int32), _ptr(kd, C.c_int32),
+                                           n.value, C.byref(n)), "pk_world_read_events")
+        r = (k[: n.value], kd[: n.value])
+        return r + (w[: n.value],) if with_worlds else r
+
+    def colours(self):
+        n = C.c_int32()
+        nc = C.c_int32()
+        self.L.pk_world_read_colours(self.h, None, None, 0, C.byref(n), C.byref(nc))
+        m = max(n.value, 1)
+        k = np.zeros(m, dtype=np.uint64)
+        col = np.zeros(m, dtype=np.int32)
+        _check(self.L.pk_world_read_colours(self.h, _ptr(k, C.c_uint64), _ptr(col, C.c_int32), n.value, C.byref(n),
+                                            C.byref(nc)), "pk_world_read_colours")
+        return k[: n.value], col[: n.value], nc.value
+
+    def collide(self, shapes_a, shapes_b):
+        """gjk_epa on primitive shape pairs; each shape is (kind, params list, mesh id)."""
+        n = len(shapes_a)
+        A = (CollideShapeC * max(n, 1))()
+        B = (CollideShapeC * max(n, 1))()
+        for i, (sa, sb) in enumerate(zip(shapes_a, shapes_b)):
+            for dst, (kind, params, sid) in ((A[i], sa), (B[i], sb)):
+                dst.kind = kind
+                dst.shape = sid
+                for k, v in enumerate(params):
+                    dst.p[k] = v
+        out = np.zeros((max(n, 1), 10))
+        hit = np.zeros(max(n, 1), dtype=np.int32)
+        _check(self.L.pk_collide(self.h, A, B, n, _ptr(out, C.c_double), _ptr(hit, C.c_int32)), "pk_collide")
+        return hit[:n].astype(bool), out[:n]

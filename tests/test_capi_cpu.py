@@ -1,0 +1,52 @@
+"""CPU-side checks of the C ABI library: it builds for sm_103a, loads, exports every symbol that
+include/*.h declares, and refuses to run without a device (no CPU fallback)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(pk_[a-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    from physkit_gb300 import build
+
+    path = build.build()
+    L = C.CDLL(path)
+    names = declared_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_descriptor_layouts_match_header():
+    from physkit_gb300 import world
+
+    assert world.BODY_DTYPE.itemsize == 216
+    assert C.sizeof(world.WorldDescC) == 56
+    assert C.sizeof(world.CollideShapeC) == 88
+
+
+def test_no_device_is_an_error_not_a_fallback():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from physkit_gb300 import World, lib
+
+    L = lib()
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        World()
+    assert L.pk_version().decode().startswith("physkit_gb300")

@@ -1,0 +1,154 @@
+"""World-step parity on the GPU (through the C ABI) against the FP64 oracle.
+
+FP64 form: the oracle runs the reference's step with the solver in the GPU's colour order; every
+step the pair set, manifolds, colours, events and body states must be bit-identical.
+FP32 form: per-quantity error against the FP64 oracle over a short horizon, with the tolerances
+written in each test.
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from physkit_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def run_pair(scene, steps, precision="f64", check_every=1, graph=False):
+    world, handles = scenes.make_world(scene, precision=precision)
+    ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+    pyoracle.load_scene(ow, scene)
+    return world, ow, handles
+
+
+def compare_step(world, ow, step):
+    gp, op = world.pairs(), ow.pairs()
+    assert np.array_equal(gp, op), f"pair sets differ at step {step}: {len(gp)} vs {len(op)}"
+    gk, gc, gct = world.manifolds()
+    ok, oc, oct_ = ow.manifolds()
+    assert np.array_equal(gk, ok)
+    assert np.array_equal(gc, oc), f"contact counts differ at step {step}"
+    assert np.array_equal(gct, oct_), f"contacts differ at step {step}: {np.abs(gct - oct_).max()}"
+    gck, gcol, gnc = world.colours()
+    ock, ocol, onc = ow.colours()
+    assert np.array_equal(gck, ock) and np.array_equal(gcol, ocol) and gnc == onc, f"colours differ at step {step}"
+    ge, gkind = world.events()
+    oe, okind = ow.events()
+    assert np.array_equal(np.sort(ge), np.sort(oe))
+    gb, ob = world.bodies(), ow.bodies()
+    assert np.array_equal(gb[:, :13], ob[:, :13]), f"body state differs at step {step}: {np.abs(gb[:, :13] - ob[:, :13]).max()}"
+
+
+def test_fp64_small_box_pile_bit_identical():
+    scene = scenes.small_pile(n=60, seed=11)
+    world, ow, _ = run_pair(scene, 0)
+    for step in range(150):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        compare_step(world, ow, step)
+    world.close()
+
+
+def test_fp64_mixed_shapes_bit_identical():
+    # boxes, UV spheres (482 vertices) and 16-point hulls
+    scene = scenes.small_pile(n=45, seed=5, kinds=(0, 1, 2))
+    world, ow, _ = run_pair(scene, 0)
+    for step in range(120):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        compare_step(world, ow, step)
+    world.close()
+
+
+def test_fp64_config1_1000_boxes_240_steps():
+    scene = scenes.config1()
+    world, ow, _ = run_pair(scene, 0)
+    for step in range(scene.steps):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        assert np.array_equal(world.pairs(), ow.pairs()), f"pair set differs at step {step}"
+        if step % 20 == 19:
+            compare_step(world, ow, step)
+    compare_step(world, ow, scene.steps)
+    world.close()
+
+
+def test_fp64_remove_and_add_bodies():
+    # world_base::remove_rigid / create_rigid between steps (world.h:202-218)
+    scene = scenes.small_pile(n=40, seed=2)
+    world, ow, handles = run_pair(scene, 0)
+    oh = list(range(len(handles)))
+    for step in range(100):
+        if step == 40:
+            for i in (5, 17, 30):
+                assert world.remove_rigid(int(handles[i]))
+                assert ow.remove(int(handles[i]))
+            assert not world.remove_rigid(int(handles[5]))  # stale handle
+        if step == 60:
+            rec = scene.bodies[[6, 7]].copy()
+            rec["pos"][:, 1] += 3.0
+            gh = world.create_rigids(rec.copy())  # shape ids equal scene indices (loaded in order)
+            for r in rec:
+                ow.add(int(r["shape"]), r["pos"], r["quat"], r["vel"], r["ang_vel"], float(r["mass"]),
+                       np.asarray(r["inertia"]).reshape(3, 3), float(r["restitution"]), float(r["friction"]))
+            assert [int(h) & 0xFFFFFFFF for h in gh] == [30, 17]  # the arena's free stack is LIFO
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        compare_step(world, ow, step)
+    world.close()
+
+
+def test_fp64_graph_replay_matches_plain_steps():
+    scene = scenes.small_pile(n=50, seed=4)
+    a, _ = scenes.make_world(scene, precision="f64")
+    b, _ = scenes.make_world(scene, precision="f64")
+    b.capture(scene.dt)
+    for _ in range(80):
+        a.step(scene.dt)
+        b.step_graph()
+    b.synchronize()
+    assert np.array_equal(a.bodies(), b.bodies())
+    assert np.array_equal(a.pairs(), b.pairs())
+    a.close()
+    b.close()
+
+
+def test_batched_worlds_equal_alone_and_oracle():
+    # each world of a batch gives the same bits as the world run alone and as the FP64 oracle
+    scene = scenes.config3(nworlds=6, nmin=8, nmax=80, seed=21)
+    batch, _ = scenes.make_world(scene, precision="f64")
+    for _ in range(60):
+        batch.step(scene.dt)
+    bb = batch.bodies()
+    for w in range(scene.nworlds):
+        sub = scenes.Scene("world %d" % w, scene.shapes, scene.world_slice(w).copy(), 1)
+        sub.bodies["world"] = 0
+        alone, _ = scenes.make_world(sub, precision="f64")
+        ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+        pyoracle.load_scene(ow, sub)
+        for _ in range(60):
+            alone.step(scene.dt)
+            ow.step(scene.dt)
+        mine = bb[scene.bodies["world"] == w]
+        assert np.array_equal(mine, alone.bodies())
+        assert np.array_equal(mine[:, :13], ow.bodies()[:, :13])
+        alone.close()
+        ow.close()
+    batch.close()
+
+
+def test_fp32_error_against_fp64_oracle():
+    # precision form: FP32 bulk arithmetic, FP64 accumulated impulses. Free flight + first contacts
+    # over 60 steps of config1: positions within 1e-4 relative of the FP64 oracle.
+    scene = scenes.config1(n=300)
+    world, _ = scenes.make_world(scene, precision="f32")
+    ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+    pyoracle.load_scene(ow, scene)
+    for _ in range(60):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+    g, o = world.bodies(), ow.bodies()
+    dyn = scene.bodies["type"] == 0
+    rel = np.linalg.norm(g[dyn, 0:3] - o[dyn, 0:3], axis=1) / np.maximum(np.linalg.norm(o[dyn, 0:3], axis=1), 1.0)
+    assert rel.max() < 1e-4, rel.max()
+    world.close()
