@@ -1,0 +1,356 @@
+"""World-step throughput benchmark (body-steps/s) on the batched-worlds workload.
+
+Workload (headline): 4,096 independent worlds with log-uniform body counts in [8, 2048] (~1.5 M
+dynamic bodies: UV spheres, boxes and 16-point hulls dropped into 5 m walled bins), FP32 bulk
+arithmetic with FP64 accumulated impulses, dt = 1/120, 10 solver iterations. One step = one
+world-step of every world. Inputs are synthetic (seeded generator in physkit_gb300/scenes.py).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: dynamic bodies x K / device time of K steps (CUDA events on the world's stream, max over
+ranks); e2e: the same metric through the C ABI with a host read-back of every body's state after
+each step (pk_world_step + pk_world_read_bodies, wall clock). The reference arm times the FP64 CPU
+restatement of the reference step (oracle/) on a bounded sample of the same worlds with all host
+cores. Under torchrun each rank steps its own independent batch (weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "world-step throughput, batched worlds (body-steps/s)"
+UNIT = "body-steps/s"
+
+# Algorithmic bytes per unit (FP32 SoA compulsory traffic; each datum once per kernel pass).
+BYTES = {
+    "integrate_vel": ("body", 152.0),
+    "morton_sort": ("body", 64.0),
+    "lbvh_build_refit": ("body", 90.0),
+    "traverse": ("body", 56.0),
+    "pair_sort": ("pair", 16.0 * 6),
+    "narrow": ("pair", 504.0),
+    "contact_setup": ("contact", 150.0),
+    "solve": ("contact_iter", 250.0),
+    "integrate_pos": ("body", 116.0),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--nmin", type=int, default=8)
+    ap.add_argument("--nmax", type=int, default=2048)
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--cpu-sample-worlds", type=int, default=24)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def config_dict(a, scene, world_size):
+    return {"workload": f"batched worlds: {a.worlds} worlds x log-uniform[{a.nmin},{a.nmax}] bodies "
+                        f"(spheres/boxes/hulls in 5 m bins), {a.precision.upper()} bulk + FP64 impulses, "
+                        f"dt=1/120, 10 iterations",
+            "worlds_per_gpu": a.worlds, "dynamic_bodies_per_gpu": scene.n_dynamic if scene else None,
+            "parallelism": f"replicas x{world_size} (independent worlds per GPU, no collective)",
+            "l2": "inputs larger than L2 (device-resident body state > 129 MB)",
+            "seed": "scenes.config3 seed 0x50484B0000000003 + rank"}
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks
+# ------------------------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.index = index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU baseline: the FP64 oracle on a bounded sample of the same worlds
+# ------------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    scene_kw, worlds, steps, warmup, barrier, out_q = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import pyoracle
+    from physkit_gb300 import scenes
+
+    scene = scenes.config3(**scene_kw)
+    ows, nb = [], 0
+    for w in worlds:
+        sub = scenes.Scene("w", scene.shapes, scene.world_slice(w).copy(), 1)
+        ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="key")
+        pyoracle.load_scene(ow, sub)
+        ows.append(ow)
+        nb += sub.n_dynamic
+    for _ in range(warmup):
+        for ow in ows:
+            ow.step(scene.dt)
+    if barrier is not None:
+        barrier.wait()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for ow in ows:
+            ow.step(scene.dt)
+    t1 = time.perf_counter()
+    if barrier is not None:
+        barrier.wait()
+    out_q.put((nb, t1 - t0))
+
+
+def cpu_baseline(scene_kw, worlds, steps, warmup, procs):
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    shards = [worlds[i::procs] for i in range(procs)]
+    shards = [s for s in shards if s]
+    q = ctx.Queue()
+    barrier = ctx.Barrier(len(shards) + 1) if len(shards) > 1 else None
+    ps = [ctx.Process(target=_cpu_worker, args=((scene_kw, s, steps, warmup, barrier, q),)) for s in shards]
+    for p in ps:
+        p.start()
+    if barrier is not None:
+        barrier.wait()
+        t0 = time.perf_counter()
+        barrier.wait()
+        wall = time.perf_counter() - t0
+    res = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    nb = sum(r[0] for r in res)
+    if barrier is None:
+        wall = res[0][1]
+    return nb * steps / wall, nb, wall
+
+
+# ------------------------------------------------------------------------------------------------
+def run_reference(a, rank, world_size):
+    if rank != 0:
+        return
+    ncpu = os.cpu_count() or 1
+    sample = min(a.worlds, max(4 * ncpu, a.cpu_sample_worlds))
+    steps = max(1, min(a.steps, 10))
+    kw = {"nworlds": a.worlds, "nmin": a.nmin, "nmax": a.nmax}
+    value, nb, wall = cpu_baseline(kw, list(range(sample)), steps, min(a.warmup, 3), ncpu)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(a, None, world_size),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncpu, "kind": "port",
+                             "sample": f"FP64 oracle restating the reference step, first {sample} of the "
+                                       f"{a.worlds} worlds ({nb} dynamic bodies), {steps} steps per "
+                                       f"process after warm-up, {ncpu} processes"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a, rank, world_size, local_rank):
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    from physkit_gb300 import scenes
+
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+
+    scene = scenes.config3(nworlds=a.worlds, nmin=a.nmin, nmax=a.nmax, seed=scenes.SEED_BASE + 3 + rank)
+    world, _ = scenes.make_world(scene, precision=a.precision, pair_factor=6)
+    nb = scene.n_dynamic
+    dt = scene.dt
+    for _ in range(a.warmup):
+        world.step_async(dt)
+    world.synchronize()
+
+    stream = torch.cuda.ExternalStream(world.stream())
+    world.set_timing(True)
+    world.stage_times()  # clear
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local_rank)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(a.steps):
+        world.step_async(dt)
+    ev1.record(stream)
+    info = world.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    stages = world.stage_times()
+    world.set_timing(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / a.steps
+    value = nb * world_size * a.steps / (ms / 1e3)
+
+    # counts for the roofline model (last step)
+    keys, counts, _ = world.manifolds()
+    P = len(keys)
+    Cn = int(counts.sum())
+    units = {"body": nb, "pair": P, "contact": Cn, "contact_iter": Cn * (scene.iterations + 1)}
+    per_stage = {k: v[0] / max(v[1], 1) for k, v in stages.items()}
+    dom = max(per_stage, key=per_stage.get)
+    unit, bpu = BYTES[dom]
+    achieved = bpu * units[unit] / (per_stage[dom] / 1e3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get(dom)
+
+    # end to end through the C ABI: step + host read-back of every body's state
+    host = np.zeros((len(scene.bodies), 14))
+    n_e2e = max(3, min(a.steps, 20))
+    world.step(dt)
+    world.bodies()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        world.step(dt, check=False)
+        host[:] = world.bodies()
+    e2e_s = time.perf_counter() - t0
+    bpb = 28 + 24 + 24 if a.precision == "f32" else 56 + 48 + 24
+    e2e = {"value": nb * world_size * n_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": len(scene.bodies) * bpb,
+           "note": "pk_world_step (synchronous) + pk_world_read_bodies into host memory every step; "
+                   "dt is the only per-step input (a kernel argument)"}
+    world.close()
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": a.precision, "data": "synthetic",
+           "config": config_dict(a, scene, world_size), "e2e": e2e,
+           "gpu_launches": info["launches"] * a.steps, "clocks": clk,
+           "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                        "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": traffic,
+                        "model": f"{bpu:g} B per {unit} x {units[unit]} {unit}s per launch"},
+           "stage_ms_per_step": {k: round(v, 4) for k, v in per_stage.items()},
+           "counts": {"pairs": P, "contacts": Cn, "status": info["flags"]}}
+
+    if rank == 0 and not a.no_plain:
+        out["plain_single_world"] = plain_world(a)
+        out["batched_vs_plain"] = value / world_size / out["plain_single_world"]["value"]
+    if rank == 0 and not a.no_cpu_baseline:
+        kw = {"nworlds": a.worlds, "nmin": a.nmin, "nmax": a.nmax}
+        sample = list(range(min(a.cpu_sample_worlds, a.worlds)))
+        csteps = max(1, min(a.steps, 10))
+        v, cnb, wall = cpu_baseline(kw, sample, csteps, min(a.warmup, 3), 1)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"FP64 oracle, worlds 0-{len(sample) - 1} of the batch ({cnb} dynamic "
+                                         f"bodies), {csteps} steps after {min(a.warmup, 3)} warm-up steps, "
+                                         f"1 thread, {wall:.1f} s"}
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def plain_world(a):
+    """The plain single-world GPU step on one world of the same size class (config 1: 1,000 boxes on
+    a ground box), replayed from a captured CUDA graph."""
+    import torch
+    from physkit_gb300 import scenes
+
+    scene = scenes.config1()
+    world, _ = scenes.make_world(scene, precision=a.precision)
+    world.capture(scene.dt)
+    for _ in range(5):
+        world.step_graph()
+    world.synchronize()
+    stream = torch.cuda.ExternalStream(world.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 100
+    ev0.record(stream)
+    for _ in range(n):
+        world.step_graph()
+    ev1.record(stream)
+    world.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    world.close()
+    return {"workload": "config1: 1,000 boxes + ground, one world, CUDA-graph replay", "value": scene.n_dynamic * n / (ms / 1e3),
+            "unit": UNIT, "ms_per_step": ms / n}
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", str(a.gpus)))
+    if "RANK" not in os.environ:
+        world_size = 1  # without torchrun this process is the only rank
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank, world_size)
+    else:
+        run_ours(a, rank, world_size, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -88,8 +88,8 @@ typedef struct pk_step_info
 {
     int32_t pairs;  /* broadphase pairs of the last step (all worlds) */
     int32_t leaves; /* bodies in the LBVH of the last step */
-    int32_t status; /* PK_STATUS_* bits seen since the previous synchronize */
-    int32_t reserved;
+    int32_t status;   /* PK_STATUS_* bits seen since the previous synchronize */
+    int32_t launches; /* kernels launched by one step */
 } pk_step_info;
 
 /* Primitive shape for pk_collide: kind 0 aabb (p = min3 max3), 1 obb (p = center3 quat4 half3),
@@ -135,6 +135,13 @@ int pk_world_capture(pk_world *w, double dt);
 int pk_world_step_graph(pk_world *w);
 /* The CUDA stream (cudaStream_t) the world's work runs on. */
 void *pk_world_stream(pk_world *w);
+
+/* Stage timing: with timing on, plain (non-graph) steps record CUDA events around each stage;
+ * pk_world_read_stage_times returns the summed milliseconds and step counts per stage since the
+ * last read. The reference has no timers; this is the per-stage trace of the step. */
+int pk_world_set_timing(pk_world *w, int32_t enable);
+int pk_world_read_stage_times(pk_world *w, double *total_ms, int32_t *counts, int32_t cap, int32_t *nstages);
+const char *pk_stage_name(int32_t stage);
 
 /* Per slot: pos3 quat4 vel3 ang_vel3 alive = 14 doubles (particle.h:135-149). */
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);

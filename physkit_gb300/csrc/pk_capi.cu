@@ -19,6 +19,13 @@
 
 #include <cuda_runtime.h>
 
+namespace pk
+{
+const char *const kStageNames[kStages] = {"integrate_vel", "morton_sort", "lbvh_build_refit", "traverse",
+                                          "pair_sort",     "narrow",      "contact_setup",    "solve",
+                                          "integrate_pos"};
+}
+
 namespace
 {
 int g_last_cuda = 0;
@@ -473,7 +480,7 @@ int pk_world_synchronize(pk_world *w, pk_step_info *info)
         info->pairs = c.npairs;
         info->leaves = c.nleaf;
         info->status = c.status;
-        info->reserved = 0;
+        info->launches = c.launches;
     }
     return c.status ? PK_ERR_DEVICE_STATUS : PK_OK;
 }
@@ -512,6 +519,38 @@ int pk_world_step_graph(pk_world *w)
 }
 
 void *pk_world_stream(pk_world *w) { return w ? w->eng->stream() : nullptr; }
+
+int pk_world_set_timing(pk_world *w, int32_t enable)
+{
+    if (!w) return PK_ERR_INVALID;
+    w->eng->set_timing(enable);
+    return PK_OK;
+}
+
+int pk_world_read_stage_times(pk_world *w, double *total_ms, int32_t *counts, int32_t cap, int32_t *nstages)
+{
+    if (!w) return PK_ERR_INVALID;
+    double ms[pk::kStages];
+    int cnt[pk::kStages];
+    if (w->eng->read_stage_times(ms, cnt) < 0)
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    if (nstages) *nstages = pk::kStages;
+    for (int k = 0; k < pk::kStages && k < cap; ++k)
+    {
+        if (total_ms) total_ms[k] = ms[k];
+        if (counts) counts[k] = cnt[k];
+    }
+    return PK_OK;
+}
+
+const char *pk_stage_name(int32_t stage)
+{
+    if (stage < 0 || stage >= pk::kStages) return nullptr;
+    return pk::kStageNames[stage];
+}
 
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap, int32_t *n)
 {

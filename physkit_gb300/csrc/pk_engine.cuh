@@ -850,9 +850,21 @@ template <class T> __global__ void __launch_bounds__(512) k_solve_world(Dev<T> d
     const int w = blockIdx.x;
     if (w >= d.max_worlds || !d.wp[w].active) return;
     const int ms = d.mstart[w], me = d.mend[w];
-    if (me <= ms) return;
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int p = ms + tid; p < me; p += nt) d.colour[p] = d.rowmask[p] ? -1 : -2;
+    if (me <= ms)
+    {
+        if (tid == 0) d.ncolours[w] = 0;
+        return;
+    }
+    if (tid == 0) remaining = 0;
+    __syncthreads();
+    int active = 0;
+    for (int p = ms + tid; p < me; p += nt)
+    {
+        d.colour[p] = d.rowmask[p] ? -1 : -2;
+        active += d.rowmask[p] ? 1 : 0;
+    }
+    if (active) atomicAdd(&remaining, active);
     for (int c = tid; c < kMaxColours; c += nt)
     {
         ccount[c] = 0;
@@ -860,8 +872,9 @@ template <class T> __global__ void __launch_bounds__(512) k_solve_world(Dev<T> d
     }
     __syncthreads();
     int round = 0;
-    while (true)
+    while (remaining > 0)
     {
+        __syncthreads();
         for (int p = ms + tid; p < me; p += nt)
         {
             if (d.colour[p] != -1) continue;
@@ -897,13 +910,11 @@ template <class T> __global__ void __launch_bounds__(512) k_solve_world(Dev<T> d
         if (left) atomicAdd(&remaining, left);
         __syncthreads();
         ++round;
-        if (remaining == 0) break;
-        if (round >= kMaxColours)
+        if (round >= kMaxColours && remaining > 0)
         {
             if (tid == 0) atomicOr(d.status, ST_COLOUR_CAP);
             break;
         }
-        __syncthreads();
     }
     const int ncol = round;
     for (int p = ms + tid; p < me; p += nt)

@@ -35,7 +35,11 @@ struct StepCounters
     int npairs = 0;
     int nleaf = 0;
     int status = 0;
+    int launches = 0; // kernels one step launches
 };
+
+constexpr int kStages = 9;
+extern const char *const kStageNames[kStages];
 
 class EngineBase
 {
@@ -60,6 +64,8 @@ public:
     virtual int capture_graph(double dt) = 0;        // record the step as CUDA graphs
     virtual int launch_graph() = 0;                  // replay one captured step
     virtual void *stream() = 0;
+    virtual int set_timing(int enable) = 0;                 // CUDA events around each stage
+    virtual int read_stage_times(double *ms, int *count) = 0; // totals since the last read
     virtual int last_error() const = 0;
 };
 

@@ -69,6 +69,11 @@ template <class T> __global__ void k_refresh_derived(Dev<T> d, int first, int n)
 
 template <class T> __global__ void k_kill_body(Dev<T> d, int slot) { d.meta[slot].flags = 0; }
 
+static __global__ void k_zero_ints(int *p, int n)
+{
+    PK_GRID_STRIDE(i, n) p[i] = 0;
+}
+
 template <class T> class Engine final : public EngineBase
 {
 public:
@@ -272,7 +277,9 @@ public:
         {
             cudaGraph_t g;
             PK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+            capturing_ = true;
             int rc = enqueue_step(T(dt), k);
+            capturing_ = false;
             cudaError_t e = cudaStreamEndCapture(st_, &g);
             if (rc) return rc;
             PK_CUDA(e);
@@ -290,10 +297,31 @@ public:
         return 0;
     }
 
+    int set_timing(int enable) override
+    {
+        timing_ = enable != 0;
+        return 0;
+    }
+
+    int read_stage_times(double *ms, int *count) override
+    {
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(accumulate_stage_times());
+        for (int k = 0; k < kStages; ++k)
+        {
+            ms[k] = stage_ms_[k];
+            count[k] = stage_n_[k];
+            stage_ms_[k] = 0.0;
+            stage_n_[k] = 0;
+        }
+        return kStages;
+    }
+
     int synchronize(StepCounters *c) override
     {
         PK_CUDA(cudaStreamSynchronize(st_));
         PK_CUDA(cudaGetLastError());
+        PK_CUDA(accumulate_stage_times());
         int h[8];
         PK_CUDA(cudaMemcpy(h, counters_, sizeof(h), cudaMemcpyDeviceToHost));
         if (c)
@@ -301,6 +329,7 @@ public:
             c->nleaf = h[1];
             c->npairs = h[2];
             c->status = h[4];
+            c->launches = launches_;
         }
         int zero = 0;
         PK_CUDA(cudaMemcpy(counters_ + 4, &zero, sizeof(int), cudaMemcpyHostToDevice));
@@ -498,6 +527,42 @@ private:
     int2 *shape_range_ = nullptr;
     Aabb<T> *shape_box_ = nullptr;
     cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+    bool timing_ = false;
+    bool capturing_ = false;
+    int launches_ = 0;
+    std::vector<cudaEvent_t> events_; // kStages + 1 per timed step
+    int timed_steps_ = 0;
+    double stage_ms_[kStages] = {};
+    int stage_n_[kStages] = {};
+
+    cudaError_t mark(int stage)
+    {
+        if (!timing_ || capturing_) return cudaSuccess;
+        size_t idx = size_t(timed_steps_) * (kStages + 1) + size_t(stage);
+        while (events_.size() <= idx)
+        {
+            cudaEvent_t e;
+            cudaError_t err = cudaEventCreate(&e);
+            if (err != cudaSuccess) return err;
+            events_.push_back(e);
+        }
+        return cudaEventRecord(events_[idx], st_);
+    }
+    cudaError_t accumulate_stage_times()
+    {
+        for (int s = 0; s < timed_steps_; ++s)
+            for (int k = 0; k < kStages; ++k)
+            {
+                float ms = 0.f;
+                cudaError_t e = cudaEventElapsedTime(&ms, events_[size_t(s) * (kStages + 1) + k],
+                                                     events_[size_t(s) * (kStages + 1) + k + 1]);
+                if (e != cudaSuccess) return e;
+                stage_ms_[k] += ms;
+                stage_n_[k] += 1;
+            }
+        timed_steps_ = 0;
+        return cudaSuccess;
+    }
 
     template <class U> cudaError_t alloc(U **p, size_t n)
     {
@@ -527,6 +592,7 @@ private:
                       d_.order, d_.owner, hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_};
         for (void *p : ps)
             if (p) cudaFree(p);
+        for (cudaEvent_t e : events_) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         st_ = nullptr;
     }
@@ -536,32 +602,49 @@ private:
         Dev<T> d = d_;
         d.man_old = man_[parity];
         d.man_new = man_[parity ^ 1];
+        d.mkey = mkey_[0]; // Morton keys are written here, the radix sort ping-pongs with [1]
+        d.mval = mval_[0];
+        d.pkey = pkey_[0]; // pairs are emitted here, the radix sort ping-pongs with [1]
+        d.pval = pval_[0];
         const int N = cfg_.body_cap;
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
+        const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
+        launches_ = 13 + 3 * mpasses + 3 * ppasses;
+        PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
+        PK_CUDA(mark(1));
         k_morton<T><<<gb, 256, 0, st_>>>(d);
         // sort all slots by (world, Morton); dead slots sort to the end
         bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nslots, cfg_.wbits + 30,
                                         cfg_.sort_blocks_bodies, hist_, st_);
         const uint64_t *skey = in1 ? mkey_[1] : mkey_[0];
         const uint64_t *sval = in1 ? mval_[1] : mval_[0];
+        PK_CUDA(mark(2));
         k_lbvh_build<T><<<gb, 256, 0, st_>>>(d, skey);
-        PK_CUDA(cudaMemsetAsync(d.refit_flag, 0, sizeof(int) * size_t(N), st_));
+        k_zero_ints<<<gb, 256, 0, st_>>>(d.refit_flag, N);
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
+        PK_CUDA(mark(3));
         k_traverse<T><<<gb, 128, 0, st_>>>(d, sval);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
+        PK_CUDA(mark(4));
         bool p1 = radix_sort<uint64_t>(pkey_[0], pval_[0], pkey_[1], pval_[1], d.npairs,
                                        cfg_.wbits + 2 * cfg_.lbits, cfg_.sort_blocks_pairs, hist_, st_);
         const uint64_t *pk = p1 ? pkey_[1] : pkey_[0];
         const uint64_t *pv = p1 ? pval_[1] : pval_[0];
         last_sval_ = const_cast<uint64_t *>(pv);
+        PK_CUDA(mark(5));
         k_narrow<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pk, pv);
+        PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
+        PK_CUDA(mark(7));
         k_solve_world<T><<<cfg_.max_worlds, 512, 0, st_>>>(d, pv);
+        PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk);
+        PK_CUDA(mark(9));
+        if (timing_ && !capturing_) ++timed_steps_;
         PK_CUDA(cudaGetLastError());
         return 0;
     }

@@ -48,7 +48,7 @@ assert BODY_DTYPE.itemsize == 216
 
 
 class StepInfoC(C.Structure):
-    _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("launches", C.c_int32)]
 
 
 class CollideShapeC(C.Structure):
@@ -95,6 +95,9 @@ def lib():
             "pk_world_read_events": (C.c_int, [vp, u64p, i32p, i32p, C.c_int32, i32p]),
             "pk_world_read_colours": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p, i32p]),
             "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
+            "pk_world_set_timing": (C.c_int, [vp, C.c_int32]),
+            "pk_world_read_stage_times": (C.c_int, [vp, dp, i32p, C.c_int32, i32p]),
+            "pk_stage_name": (C.c_char_p, [C.c_int32]),
             "pk_last_cuda_error": (C.c_int, []),
             "pk_version": (C.c_char_p, []),
         }
@@ -360,11 +363,24 @@ class World:
         if rc not in (PK_OK, PK_ERR_DEVICE_STATUS):
             _check(rc, "pk_world_synchronize")
         self.last_info = {"pairs": info.pairs, "leaves": info.leaves, "status": info.status,
+                          "launches": info.launches,
                           "flags": [v for k, v in STATUS_BITS.items() if info.status & k]}
         return self.last_info
 
     def stream(self):
         return self.L.pk_world_stream(self.h)
+
+    def set_timing(self, enable=True):
+        _check(self.L.pk_world_set_timing(self.h, int(bool(enable))), "pk_world_set_timing")
+
+    def stage_times(self):
+        """{stage: (total ms, steps)} accumulated since the last call (CUDA events per stage)."""
+        ms = np.zeros(16)
+        cnt = np.zeros(16, dtype=np.int32)
+        n = C.c_int32()
+        _check(self.L.pk_world_read_stage_times(self.h, _ptr(ms, C.c_double), _ptr(cnt, C.c_int32), 16,
+                                                C.byref(n)), "pk_world_read_stage_times")
+        return {self.L.pk_stage_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(n.value)}
 
     # reads -------------------------------------------------------------------------------------
     def bodies(self):
