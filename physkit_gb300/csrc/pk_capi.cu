@@ -63,7 +63,9 @@ struct pk_world
     pk::EngineConfig cfg;
     pk_world_desc desc;
     std::vector<double> verts;   // all shape vertices
-    std::vector<int> ranges;     // (start, count) per shape
+    std::vector<int> ranges;     // (vertex start, vertex count, cluster start, cluster count) per shape
+    std::vector<double> clusters; // (centre xyz, radius) per cluster of 8 consecutive vertices
+    std::vector<double> rmax;     // bounding radius of each shape about its origin
     std::vector<double> boxes;   // local aabb per shape
     std::vector<SubWorld> worlds;
     std::vector<SlotInfo> slots;
@@ -188,7 +190,7 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
 {
     size_t nv = v.size() / 3;
     if (nv == 0) return PK_ERR_INVALID;
-    if (w->verts.size() / 3 + nv > size_t(w->cfg.vert_cap) || w->ranges.size() / 2 + 1 > size_t(w->cfg.shape_cap))
+    if (w->verts.size() / 3 + nv > size_t(w->cfg.vert_cap) || w->ranges.size() / 4 + 1 > size_t(w->cfg.shape_cap))
         return PK_ERR_CAPACITY;
     // aabb::from_points (bounds.h:33-49)
     double mn[3] = {v[0], v[1], v[2]}, mx[3] = {v[0], v[1], v[2]};
@@ -199,9 +201,38 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
             mn[k] = (x < mn[k]) ? x : mn[k];
             mx[k] = (mx[k] < x) ? x : mx[k];
         }
-    int id = int(w->ranges.size() / 2);
+    int id = int(w->ranges.size() / 4);
+    // Bounding spheres of blocks of 8 consecutive vertices (large meshes only): they let the
+    // device support search skip blocks that cannot hold the maximum.
+    double rm = 0.0;
+    for (size_t i = 0; i < nv; ++i)
+        rm = std::fmax(rm, std::sqrt(v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]));
+    int cstart = int(w->clusters.size() / 4), ncl = 0;
+    if (nv > 32)
+    {
+        for (size_t b = 0; b < nv; b += 8)
+        {
+            size_t e = b + 8 < nv ? b + 8 : nv;
+            double c[3] = {0, 0, 0};
+            for (size_t i = b; i < e; ++i)
+                for (int k = 0; k < 3; ++k) c[k] += v[3 * i + k] / double(e - b);
+            double r = 0.0;
+            for (size_t i = b; i < e; ++i)
+            {
+                double dx = v[3 * i] - c[0], dy = v[3 * i + 1] - c[1], dz = v[3 * i + 2] - c[2];
+                r = std::fmax(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+            // widen so the bound still holds after rounding the centre and radius to FP32
+            r = r * (1.0 + 1e-9) + 1e-6 * rm;
+            w->clusters.insert(w->clusters.end(), {c[0], c[1], c[2], r});
+            ++ncl;
+        }
+    }
     w->ranges.push_back(int(w->verts.size() / 3));
     w->ranges.push_back(int(nv));
+    w->ranges.push_back(cstart);
+    w->ranges.push_back(ncl);
+    w->rmax.push_back(rm);
     w->verts.insert(w->verts.end(), v.begin(), v.end());
     for (int k = 0; k < 3; ++k) w->boxes.push_back(mn[k]);
     for (int k = 0; k < 3; ++k) w->boxes.push_back(mx[k]);
@@ -213,7 +244,7 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
 static int flush_shapes(pk_world *w)
 {
     if (!w->shapes_dirty) return PK_OK;
-    if (w->eng->set_shapes(w->verts, w->ranges, w->boxes))
+    if (w->eng->set_shapes(w->verts, w->ranges, w->boxes, w->clusters, w->rmax))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
@@ -272,7 +303,7 @@ int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)
 int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out)
 {
     if (!w || (n > 0 && !descs)) return PK_ERR_INVALID;
-    int nshapes = int(w->ranges.size() / 2);
+    int nshapes = int(w->ranges.size() / 4);
     for (int i = 0; i < n; ++i)
     {
         const pk_body_desc &d = descs[i];
@@ -652,7 +683,7 @@ int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t
 int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out, int32_t *hit)
 {
     if (!w || n < 0 || (n > 0 && (!a || !b || !out || !hit))) return PK_ERR_INVALID;
-    int nshapes = int(w->ranges.size() / 2);
+    int nshapes = int(w->ranges.size() / 4);
     for (int i = 0; i < n; ++i)
     {
         for (const pk_collide_shape *s : {a + i, b + i})

@@ -112,8 +112,10 @@ template <class T> struct Dev
     const int *nslots;
     // shapes
     const T *verts;
-    const int2 *shape_range;
+    const int4 *shape_range; // vertex start, vertex count, cluster start, cluster count
     const Aabb<T> *shape_box;
+    const T *clusters;       // 4 per cluster: centre xyz, radius
+    const T *shape_rmax;     // bounding radius about the shape origin
     // worlds
     WorldParams<T> *wp;
     unsigned *wbounds;
@@ -505,10 +507,13 @@ template <class T> __device__ __forceinline__ ShapeRef<T> body_shape(const Dev<T
 {
     ShapeRef<T> s;
     const Meta m = d.meta[slot];
-    int2 r = d.shape_range[m.shape];
+    int4 r = d.shape_range[m.shape];
     s.kind = SHAPE_MESH;
     s.nverts = r.y;
     s.verts = d.verts + 3 * r.x;
+    s.ncl = r.w;
+    s.cl = d.clusters + 4 * r.z;
+    s.rmax = d.shape_rmax[m.shape];
     const Pose<T> &p = d.pose[slot];
     s.pos = ld3(p.p);
     s.q = ldq(p.q);
@@ -595,7 +600,12 @@ __global__ void __launch_bounds__(128) k_narrow(Dev<T> d, const uint64_t *__rest
         EpaState<T> es;
         Collision<T> col;
         int nps = 0;
-        bool hit = gjk_epa(A, B, es, col, &nps);
+        // Bounding spheres apart by more than the rounding margin: the shapes are disjoint and the
+        // reference's GJK returns no collision for them (collision.cpp:181-182), so skip it.
+        V3<T> dc = B.pos - A.pos;
+        T rs = A.rmax + B.rmax;
+        T cull = rs + (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
+        bool hit = (sqnorm(dc) > cull * cull) ? false : gjk_epa(A, B, es, col, &nps);
         if (nps) atomicOr(d.status, ST_EPA_CAP);
         Contact<T> nc;
         if (hit)
@@ -1082,7 +1092,8 @@ struct ShapeSpec
     double p[10];
 };
 template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const ShapeSpec *sb, int n, const T *verts,
-                                                   const int2 *ranges, double *out, int *hit, int *status)
+                                                   const int4 *ranges, const T *clusters, const T *rmax,
+                                                   double *out, int *hit, int *status)
 {
     PK_GRID_STRIDE(i, n)
     {
@@ -1095,6 +1106,9 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
             r.kind = q.kind;
             r.nverts = 0;
             r.verts = nullptr;
+            r.ncl = 0;
+            r.cl = nullptr;
+            r.rmax = T(0);
             r.q = Qt<T>{T(1), T(0), T(0), T(0)};
             r.pos = r.a = r.b = V3<T>{T(0), T(0), T(0)};
             if (q.kind == SHAPE_AABB)
@@ -1112,9 +1126,12 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
             {
                 r.pos = V3<T>{T(q.p[0]), T(q.p[1]), T(q.p[2])};
                 r.q = Qt<T>{T(q.p[3]), T(q.p[4]), T(q.p[5]), T(q.p[6])};
-                int2 rg = ranges[q.shape];
+                int4 rg = ranges[q.shape];
                 r.verts = verts + 3 * rg.x;
                 r.nverts = rg.y;
+                r.ncl = rg.w;
+                r.cl = clusters + 4 * rg.z;
+                r.rmax = rmax[q.shape];
             }
         }
         EpaState<T> es;

@@ -47,8 +47,11 @@ public:
     virtual ~EngineBase() = default;
     virtual int precision_bits() const = 0;
     virtual int init(const EngineConfig &cfg) = 0;
+    // ranges: 4 ints per shape (vertex start, vertex count, cluster start, cluster count);
+    // clusters: 4 doubles per cluster (centre, radius); rmax: bounding radius per shape.
     virtual int set_shapes(const std::vector<double> &verts, const std::vector<int> &ranges,
-                           const std::vector<double> &boxes) = 0;
+                           const std::vector<double> &boxes, const std::vector<double> &clusters,
+                           const std::vector<double> &rmax) = 0;
     virtual int set_world(int w, const double g[3], double gnorm, int active) = 0;
     virtual int upload_bodies(const int *slots, const HostBody *b, int n, int nslots) = 0;
     virtual int kill_body(int slot, int world, int local) = 0;

@@ -148,8 +148,10 @@ public:
         PK_CUDA(alloc(&d.verts, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
         PK_CUDA(alloc(&shape_range_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
         PK_CUDA(alloc(&shape_box_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
+        PK_CUDA(alloc(&shape_rmax_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
         d.shape_range = shape_range_;
         d.shape_box = shape_box_;
+        d.shape_rmax = shape_rmax_;
         d.man_old = man_[0];
         d.man_new = man_[1];
         PK_CUDA(cudaDeviceSynchronize());
@@ -157,9 +159,10 @@ public:
     }
 
     int set_shapes(const std::vector<double> &verts, const std::vector<int> &ranges,
-                   const std::vector<double> &boxes) override
+                   const std::vector<double> &boxes, const std::vector<double> &clusters,
+                   const std::vector<double> &rmax) override
     {
-        size_t nv = verts.size() / 3, ns = ranges.size() / 2;
+        size_t nv = verts.size() / 3, ns = ranges.size() / 4, nc = clusters.size() / 4;
         if (nv > size_t(cfg_.vert_cap) || ns > size_t(cfg_.shape_cap)) return -3;
         std::vector<T> v(verts.size());
         for (size_t i = 0; i < verts.size(); ++i) v[i] = T(verts[i]);
@@ -167,9 +170,22 @@ public:
         for (size_t i = 0; i < ns; ++i)
             b[i] = Aabb<T>{{T(boxes[6 * i]), T(boxes[6 * i + 1]), T(boxes[6 * i + 2])},
                            {T(boxes[6 * i + 3]), T(boxes[6 * i + 4]), T(boxes[6 * i + 5])}};
+        std::vector<T> c(clusters.size() > 0 ? clusters.size() : 4);
+        for (size_t i = 0; i < clusters.size(); ++i) c[i] = T(clusters[i]);
+        std::vector<T> r(ns);
+        for (size_t i = 0; i < ns; ++i) r[i] = T(rmax[i]);
+        if (nc > clusters_cap_)
+        {
+            if (clusters_) cudaFree(clusters_);
+            clusters_cap_ = nc + nc / 2 + 16;
+            PK_CUDA(cudaMalloc(&clusters_, sizeof(T) * 4 * clusters_cap_));
+        }
+        d_.clusters = clusters_;
         PK_CUDA(cudaMemcpyAsync(const_cast<T *>(d_.verts), v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaMemcpyAsync(shape_range_, ranges.data(), sizeof(int) * ranges.size(), cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaMemcpyAsync(shape_box_, b.data(), sizeof(Aabb<T>) * ns, cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaMemcpyAsync(shape_rmax_, r.data(), sizeof(T) * ns, cudaMemcpyHostToDevice, st_));
+        if (nc) PK_CUDA(cudaMemcpyAsync(clusters_, c.data(), sizeof(T) * 4 * nc, cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaStreamSynchronize(st_));
         return 0;
     }
@@ -349,6 +365,11 @@ public:
         for (int i = 0; i < n; ++i)
         {
             double *o = out + 14 * i;
+            if (!(meta[i].flags & BODY_ALIVE))
+            {
+                for (int k = 0; k < 14; ++k) o[k] = 0.0; // no body in this slot
+                continue;
+            }
             for (int k = 0; k < 3; ++k)
             {
                 o[k] = double(pose[i].p[k]);
@@ -496,7 +517,8 @@ public:
         PK_CUDA(cudaMemcpy(da, specs_a, sizeof(ShapeSpec) * n, cudaMemcpyHostToDevice));
         PK_CUDA(cudaMemcpy(db, specs_b, sizeof(ShapeSpec) * n, cudaMemcpyHostToDevice));
         PK_CUDA(cudaMemset(dout, 0, sizeof(double) * 10 * n));
-        k_collide_batch<T><<<(n + 127) / 128, 128, 0, st_>>>(da, db, n, d_.verts, shape_range_, dout, dhit, dst);
+        k_collide_batch<T><<<(n + 127) / 128, 128, 0, st_>>>(da, db, n, d_.verts, shape_range_, d_.clusters,
+                                                              shape_rmax_, dout, dhit, dst);
         PK_CUDA(cudaGetLastError());
         PK_CUDA(cudaStreamSynchronize(st_));
         PK_CUDA(cudaMemcpy(out, dout, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost));
@@ -524,8 +546,11 @@ private:
     Manifold<T> *man_[2] = {nullptr, nullptr};
     uint64_t *last_sval_ = nullptr;
     uint32_t *hist_ = nullptr;
-    int2 *shape_range_ = nullptr;
+    int4 *shape_range_ = nullptr;
     Aabb<T> *shape_box_ = nullptr;
+    T *shape_rmax_ = nullptr;
+    T *clusters_ = nullptr;
+    size_t clusters_cap_ = 0;
     cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
     bool timing_ = false;
     bool capturing_ = false;
@@ -589,7 +614,8 @@ private:
                       d_.wroot, d_.mstart, d_.mend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.rows, d_.rowmask, d_.colour,
-                      d_.order, d_.owner, hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_};
+                      d_.order, d_.owner, hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
+                      shape_rmax_, clusters_};
         for (void *p : ps)
             if (p) cudaFree(p);
         for (cudaEvent_t e : events_) cudaEventDestroy(e);

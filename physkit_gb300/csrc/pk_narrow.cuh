@@ -24,8 +24,8 @@ enum : int
 };
 
 constexpr int kMaxPoly = 4 + 64;
-constexpr int kMaxFaces = 256;
-constexpr int kMaxHorizon = 64;
+constexpr int kMaxFaces = 512;
+constexpr int kMaxHorizon = 96;
 constexpr uint16_t kNull16 = 0xFFFF;
 
 enum : int
@@ -35,8 +35,21 @@ enum : int
     SHAPE_MESH = 2,
 };
 
+template <class T> struct EpsOf;
+template <> struct EpsOf<double>
+{
+    static constexpr double v = 2.220446049250313e-16;
+};
+template <> struct EpsOf<float>
+{
+    static constexpr float v = 1.1920929e-07f;
+};
+
+constexpr int kClusterSize = 8;
+
 // A posed convex shape: aabb (a=min, b=max), obb (pos=center, q, b=half) or mesh instance
-// (pos, q, vertex list).
+// (pos, q, vertex list). Large meshes carry clusters of kClusterSize consecutive vertices with a
+// bounding sphere each (cx, cy, cz, radius) and the shape's bounding radius `rmax`.
 template <class T> struct ShapeRef
 {
     int kind;
@@ -44,6 +57,59 @@ template <class T> struct ShapeRef
     const T *verts; // xyz interleaved, local frame
     V3<T> a, b, pos;
     Qt<T> q;
+    int ncl;
+    const T *cl;
+    T rmax;
+
+    // First strictly maximal vertex of v.ld over the vertex list, in index order.
+    PK_HD int argmax_linear(V3<T> ld, int lo, int hi, int best, T &bd) const
+    {
+        for (int i = lo; i < hi; ++i)
+        {
+            T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
+            if (best < 0 || v > bd)
+            {
+                bd = v;
+                best = i;
+            }
+        }
+        return best;
+    }
+    // Same result as argmax_linear over all vertices: clusters whose bound (with a margin that
+    // covers the rounding of both the bound and every vertex dot product) is below the value of a
+    // vertex already seen cannot hold the maximum or a tie with it, so they are skipped; the rest
+    // are scanned in index order.
+    PK_HD int argmax_clustered(V3<T> ld) const
+    {
+        T dn = norm(ld);
+        T margin = T(64) * EpsOf<T>::v * rmax * dn;
+        int kb = 0;
+        T ub_best = T(0);
+        for (int k = 0; k < ncl; ++k)
+        {
+            const T *c = cl + 4 * k;
+            T ub = c[0] * ld.x + c[1] * ld.y + c[2] * ld.z + c[3] * dn;
+            if (k == 0 || ub > ub_best)
+            {
+                ub_best = ub;
+                kb = k;
+            }
+        }
+        T B;
+        int lo = kb * kClusterSize, hi = lo + kClusterSize < nverts ? lo + kClusterSize : nverts;
+        argmax_linear(ld, lo, hi, -1, B);
+        int best = -1;
+        T bd = T(0);
+        for (int k = 0; k < ncl; ++k)
+        {
+            const T *c = cl + 4 * k;
+            T ub = c[0] * ld.x + c[1] * ld.y + c[2] * ld.z + c[3] * dn + margin;
+            if (ub < B) continue;
+            int l = k * kClusterSize, h = l + kClusterSize < nverts ? l + kClusterSize : nverts;
+            best = argmax_linear(ld, l, h, best, bd);
+        }
+        return best;
+    }
 
     PK_HD V3<T> support(V3<T> d) const
     {
@@ -62,16 +128,13 @@ template <class T> struct ShapeRef
         // mesh::instance::support -> mesh::support: first strictly maximal vertex
         // (mesh.cpp:341-358, 442-448)
         V3<T> ld = rotate(conj(q), d);
-        int best = 0;
-        T bd = verts[0] * ld.x + verts[1] * ld.y + verts[2] * ld.z;
-        for (int i = 1; i < nverts; ++i)
+        int best;
+        if (ncl > 0)
+            best = argmax_clustered(ld);
+        else
         {
-            T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
-            if (v > bd)
-            {
-                bd = v;
-                best = i;
-            }
+            T bd;
+            best = argmax_linear(ld, 0, nverts, -1, bd);
         }
         V3<T> lv{verts[3 * best], verts[3 * best + 1], verts[3 * best + 2]};
         return rotate(q, lv) + pos;
