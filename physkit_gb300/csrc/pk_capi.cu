@@ -9,6 +9,7 @@
 #include "pk_engine_api.h"
 #include "pk_math.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -73,6 +74,7 @@ struct pk_world
     int nslots = 0;
     int steps = 0;
     bool shapes_dirty = false;
+    bool order_dirty = false; // solver schedule needs recomputing (bodies added or removed)
 };
 
 extern "C" {
@@ -241,6 +243,25 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
     return PK_OK;
 }
 
+// Solver CTAs take worlds largest first so the longest solves start earliest.
+static int flush_order(pk_world *w)
+{
+    if (!w->order_dirty) return PK_OK;
+    int nw = w->cfg.max_worlds;
+    std::vector<int> cnt(static_cast<size_t>(nw), 0), order(static_cast<size_t>(nw));
+    for (int s = 0; s < w->nslots; ++s)
+        if (w->slots[size_t(s)].alive && !w->slots[size_t(s)].is_static) cnt[size_t(w->slots[size_t(s)].world)]++;
+    for (int i = 0; i < nw; ++i) order[size_t(i)] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[size_t(a)] > cnt[size_t(b)]; });
+    if (w->eng->set_world_order(order.data(), nw))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    w->order_dirty = false;
+    return PK_OK;
+}
+
 static int flush_shapes(pk_world *w)
 {
     if (!w->shapes_dirty) return PK_OK;
@@ -399,6 +420,7 @@ int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
     }
+    w->order_dirty = true;
     return PK_OK;
 }
 
@@ -421,6 +443,7 @@ static int kill_slot(pk_world *w, int slot)
     sw.local_gen[size_t(si.local)]++;
     sw.free_locals.push_back(si.local);
     si.gen = sw.local_gen[size_t(si.local)];
+    w->order_dirty = true;
     if (w->eng->kill_body(slot, si.world, si.local))
     {
         g_last_cuda = w->eng->last_error();
@@ -487,6 +510,7 @@ int pk_world_step_async(pk_world *w, double dt)
 {
     if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
     if (int frc = flush_shapes(w)) return frc;
+    if (int orc = flush_order(w)) return orc;
     int rc = w->eng->step(dt);
     if (rc)
     {
@@ -527,6 +551,7 @@ int pk_world_capture(pk_world *w, double dt)
 {
     if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
     if (int rc = flush_shapes(w)) return rc;
+    if (int orc = flush_order(w)) return orc;
     if (w->eng->capture_graph(dt))
     {
         g_last_cuda = w->eng->last_error();

@@ -142,12 +142,19 @@ template <class T> struct Dev
     int *npairs_old;
     Manifold<T> *man_new;
     uint8_t *event;
+    int *old_idx;          // per pair: index of last step's manifold or -1
+    int *gjk_list;         // pairs queued for GJK
+    int *gjk_count;
+    int *epa_list;         // pairs queued for EPA
+    Simplex<T> *epa_simplex;
+    int *epa_count;
     Row<T> *rows;
     uint8_t *rowmask;
     int *colour;
     uint32_t *owner;
     uint32_t *order;
     int *ncolours;
+    const int *world_order; // solver CTA -> world, largest worlds first
     // control
     int *status;
     int *epoch;
@@ -208,6 +215,8 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
     {
         *d.npairs = 0;
         *d.nleaf = 0;
+        *d.gjk_count = 0;
+        *d.epa_count = 0;
         *d.epoch += 1;
     }
 }
@@ -571,12 +580,82 @@ template <class T> __device__ __forceinline__ void add_contact(Manifold<T> &m, c
     m.n = 4;
 }
 
+// Slot in a compacted list for every active lane of the warp: one atomic per warp.
+__device__ __forceinline__ int warp_push(int *counter)
+{
+    unsigned m = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// The manifold update of narrow_phase::calculate for one pair given its new contact (if any):
+// warm-start transfer, re-projection of old contacts, reduction to four and begin/end events
+// (collision_phases.h:261-318).
 template <class T>
-__global__ void __launch_bounds__(128) k_narrow(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
+__device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const ShapeRef<T> &A, const ShapeRef<T> &B,
+                                bool hit, const Collision<T> &col)
+{
+    const T d2eps = T(0.005 * 0.005), breaking = T(0.05), drift2_eps = T(0.06);
+    Manifold<T> old;
+    old.n = 0;
+    if (old_idx >= 0) old = d.man_old[old_idx];
+    Contact<T> nc;
+    if (hit)
+    {
+        st3(nc.n, col.normal);
+        st3(nc.la, rotate(conj(A.q), col.world_a - A.pos));
+        st3(nc.lb, rotate(conj(B.q), col.world_b - B.pos));
+        nc.depth = col.depth;
+        nc.imp[0] = nc.imp[1] = nc.imp[2] = 0.0;
+    }
+    Manifold<T> nm;
+    nm.n = 0;
+    nm.pad = 0;
+    for (int k = 0; k < old.n; ++k)
+    {
+        Contact<T> oc = old.c[k];
+        if (hit)
+        {
+            if (sqnorm(ld3(nc.la) - ld3(oc.la)) < d2eps || sqnorm(ld3(nc.lb) - ld3(oc.lb)) < d2eps)
+            {
+                nc.imp[0] = oc.imp[0];
+                nc.imp[1] = oc.imp[1];
+                nc.imp[2] = oc.imp[2];
+                continue;
+            }
+        }
+        V3<T> wa = rotate(A.q, ld3(oc.la)) + A.pos;
+        V3<T> wb = rotate(B.q, ld3(oc.lb)) + B.pos;
+        V3<T> normal = hit ? ld3(nc.n) : ld3(oc.n);
+        V3<T> rel = wb - wa;
+        T depth = dot(rel, normal);
+        V3<T> pa = wa + normal * depth;
+        T drift2 = sqnorm(pa - wb);
+        if (depth > -breaking && drift2 < drift2_eps)
+        {
+            oc.depth = depth;
+            st3(oc.n, normal);
+            add_contact(nm, oc);
+        }
+    }
+    if (hit) add_contact(nm, nc);
+    bool was = old.n != 0, is = nm.n != 0;
+    d.event[p] = (!was && is) ? 1 : ((was && !is) ? 2 : 0);
+    d.man_new[p] = nm;
+}
+
+// Narrowphase pass 1: per pair, find last step's manifold, then either settle the pair at once
+// (bounding spheres apart by more than the rounding margin: disjoint shapes, for which the
+// reference's GJK returns no collision, collision.cpp:181-182) or queue it for GJK.
+template <class T>
+__global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
 {
     const int np = *d.npairs;
     const int nold = *d.npairs_old;
-    const T d2eps = T(0.005 * 0.005), breaking = T(0.05), drift2_eps = T(0.06);
     PK_GRID_STRIDE(p, np)
     {
         uint64_t key = skey[p];
@@ -585,71 +664,72 @@ __global__ void __launch_bounds__(128) k_narrow(Dev<T> d, const uint64_t *__rest
         int world = int(key >> (2 * d.lbits));
         if (p == 0 || (skey[p - 1] >> (2 * d.lbits)) != uint64_t(world)) d.mstart[world] = p;
         if (p == np - 1 || (skey[p + 1] >> (2 * d.lbits)) != uint64_t(world)) d.mend[world] = p + 1;
-        // old manifold of the same pair (binary search over last step's sorted keys)
         int lo = 0, hi = nold;
         while (lo < hi)
         {
             int mid = (lo + hi) >> 1;
             if (d.key_old[mid] < key) lo = mid + 1; else hi = mid;
         }
-        Manifold<T> old;
-        old.n = 0;
-        if (lo < nold && d.key_old[lo] == key) old = d.man_old[lo];
-
+        int old_idx = (lo < nold && d.key_old[lo] == key) ? lo : -1;
+        d.old_idx[p] = old_idx;
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
-        EpaState<T> es;
-        Collision<T> col;
-        int nps = 0;
-        // Bounding spheres apart by more than the rounding margin: the shapes are disjoint and the
-        // reference's GJK returns no collision for them (collision.cpp:181-182), so skip it.
         V3<T> dc = B.pos - A.pos;
         T rs = A.rmax + B.rmax;
         T cull = rs + (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
-        bool hit = (sqnorm(dc) > cull * cull) ? false : gjk_epa(A, B, es, col, &nps);
-        if (nps) atomicOr(d.status, ST_EPA_CAP);
-        Contact<T> nc;
-        if (hit)
+        if (sqnorm(dc) > cull * cull)
         {
-            st3(nc.n, col.normal);
-            st3(nc.la, rotate(conj(A.q), col.world_a - A.pos));
-            st3(nc.lb, rotate(conj(B.q), col.world_b - B.pos));
-            nc.depth = col.depth;
-            nc.imp[0] = nc.imp[1] = nc.imp[2] = 0.0;
+            Collision<T> none;
+            manifold_update(d, p, old_idx, A, B, false, none);
         }
-        Manifold<T> nm;
-        nm.n = 0;
-        nm.pad = 0;
-        for (int k = 0; k < old.n; ++k)
+        else
+            d.gjk_list[warp_push(d.gjk_count)] = p;
+    }
+}
+
+// Narrowphase pass 2: GJK (collision.cpp:165-189) over the queued pairs; enclosing simplices are
+// queued for EPA, the rest are settled without a new contact.
+template <class T>
+__global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int n = *d.gjk_count;
+    PK_GRID_STRIDE(i, n)
+    {
+        int p = d.gjk_list[i];
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+        Simplex<T> s;
+        if (gjk(A, B, s))
         {
-            Contact<T> oc = old.c[k];
-            if (hit)
-            {
-                if (sqnorm(ld3(nc.la) - ld3(oc.la)) < d2eps || sqnorm(ld3(nc.lb) - ld3(oc.lb)) < d2eps)
-                {
-                    nc.imp[0] = oc.imp[0];
-                    nc.imp[1] = oc.imp[1];
-                    nc.imp[2] = oc.imp[2];
-                    continue;
-                }
-            }
-            V3<T> wa = rotate(A.q, ld3(oc.la)) + A.pos;
-            V3<T> wb = rotate(B.q, ld3(oc.lb)) + B.pos;
-            V3<T> normal = hit ? ld3(nc.n) : ld3(oc.n);
-            V3<T> rel = wb - wa;
-            T depth = dot(rel, normal);
-            V3<T> pa = wa + normal * depth;
-            T drift2 = sqnorm(pa - wb);
-            if (depth > -breaking && drift2 < drift2_eps)
-            {
-                oc.depth = depth;
-                st3(oc.n, normal);
-                add_contact(nm, oc);
-            }
+            int j = warp_push(d.epa_count);
+            d.epa_list[j] = p;
+            d.epa_simplex[j] = s;
         }
-        if (hit) add_contact(nm, nc);
-        bool was = old.n != 0, is = nm.n != 0;
-        d.event[p] = (!was && is) ? 1 : ((was && !is) ? 2 : 0);
-        d.man_new[p] = nm;
+        else
+        {
+            Collision<T> none;
+            manifold_update(d, p, d.old_idx[p], A, B, false, none);
+        }
+    }
+}
+
+// Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, then the manifold update.
+template <class T>
+__global__ void __launch_bounds__(128) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int n = *d.epa_count;
+    PK_GRID_STRIDE(j, n)
+    {
+        int p = d.epa_list[j];
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+        Simplex<T> s = d.epa_simplex[j];
+        EpaState<T> es;
+        Collision<T> col;
+        bool hit = epa(A, B, s, es, col);
+        if (es.status) atomicOr(d.status, ST_EPA_CAP);
+        manifold_update(d, p, d.old_idx[p], A, B, hit, col);
     }
 }
 
@@ -850,15 +930,16 @@ template <class T> __device__ __forceinline__ BodyRef<T> body_ref(const Dev<T> &
     return r;
 }
 
-template <class T> __global__ void __launch_bounds__(512) k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval)
+template <class T> __global__ void __launch_bounds__(256) k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
     __shared__ int remaining;
     __shared__ int nrounds;
-    const int w = blockIdx.x;
-    if (w >= d.max_worlds || !d.wp[w].active) return;
+    if (int(blockIdx.x) >= d.max_worlds) return;
+    const int w = d.world_order[blockIdx.x];
+    if (!d.wp[w].active) return;
     const int ms = d.mstart[w], me = d.mend[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     if (me <= ms)

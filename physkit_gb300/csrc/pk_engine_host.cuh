@@ -106,14 +106,16 @@ public:
         PK_CUDA(alloc(&d.tbox, N));
         PK_CUDA(alloc(&d.meta, N));
         PK_CUDA(cudaMemset(d.meta, 0, sizeof(Meta) * N));
-        PK_CUDA(alloc(&counters_, 8));
-        PK_CUDA(cudaMemset(counters_, 0, sizeof(int) * 8));
+        PK_CUDA(alloc(&counters_, 16));
+        PK_CUDA(cudaMemset(counters_, 0, sizeof(int) * 16));
         d.nslots = counters_ + 0;
         d.nleaf = counters_ + 1;
         d.npairs = counters_ + 2;
         d.npairs_old = counters_ + 3;
         d.status = counters_ + 4;
         d.epoch = counters_ + 5;
+        d.gjk_count = counters_ + 6;
+        d.epa_count = counters_ + 7;
         int minus1 = -1;
         PK_CUDA(cudaMemcpy(d.epoch, &minus1, sizeof(int), cudaMemcpyHostToDevice));
         PK_CUDA(alloc(&d.wp, W));
@@ -124,6 +126,14 @@ public:
         PK_CUDA(alloc(&d.mend, W));
         PK_CUDA(alloc(&d.ncolours, W));
         PK_CUDA(cudaMemset(d.ncolours, 0, sizeof(int) * W));
+        {
+            int *wo;
+            PK_CUDA(alloc(&wo, W));
+            std::vector<int> ident(W);
+            for (size_t i = 0; i < W; ++i) ident[i] = int(i);
+            PK_CUDA(cudaMemcpy(wo, ident.data(), sizeof(int) * W, cudaMemcpyHostToDevice));
+            d.world_order = wo;
+        }
         for (int k = 0; k < 2; ++k)
         {
             PK_CUDA(alloc(&mkey_[k], N));
@@ -138,6 +148,10 @@ public:
         PK_CUDA(alloc(&d.refit_flag, N));
         PK_CUDA(alloc(&d.key_old, P));
         PK_CUDA(alloc(&d.event, P));
+        PK_CUDA(alloc(&d.old_idx, P));
+        PK_CUDA(alloc(&d.gjk_list, P));
+        PK_CUDA(alloc(&d.epa_list, P));
+        PK_CUDA(alloc(&d.epa_simplex, P));
         PK_CUDA(alloc(&d.rows, 4 * P));
         PK_CUDA(alloc(&d.rowmask, P));
         PK_CUDA(alloc(&d.colour, P));
@@ -263,6 +277,14 @@ public:
         return 0;
     }
 
+    int set_world_order(const int *order, int n) override
+    {
+        if (n != cfg_.max_worlds) return -3;
+        PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_order), order, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
     int kill_body(int slot, int world, int local) override
     {
         k_kill_body<T><<<1, 1, 0, st_>>>(d_, slot);
@@ -338,7 +360,7 @@ public:
         PK_CUDA(cudaStreamSynchronize(st_));
         PK_CUDA(cudaGetLastError());
         PK_CUDA(accumulate_stage_times());
-        int h[8];
+        int h[16];
         PK_CUDA(cudaMemcpy(h, counters_, sizeof(h), cudaMemcpyDeviceToHost));
         if (c)
         {
@@ -613,8 +635,9 @@ private:
         void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
                       d_.wroot, d_.mstart, d_.mend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
-                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.rows, d_.rowmask, d_.colour,
-                      d_.order, d_.owner, hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
+                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.old_idx, d_.gjk_list,
+                      d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour,
+                      d_.order, d_.owner, const_cast<int *>(d_.world_order), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_};
         for (void *p : ps)
             if (p) cudaFree(p);
@@ -636,7 +659,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 13 + 3 * mpasses + 3 * ppasses;
+        launches_ = 15 + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -661,11 +684,13 @@ private:
         const uint64_t *pv = p1 ? pval_[1] : pval_[0];
         last_sval_ = const_cast<uint64_t *>(pv);
         PK_CUDA(mark(5));
-        k_narrow<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pk, pv);
+        k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
+        k_narrow_gjk<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
+        k_narrow_epa<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         PK_CUDA(mark(7));
-        k_solve_world<T><<<cfg_.max_worlds, 512, 0, st_>>>(d, pv);
+        k_solve_world<T><<<cfg_.max_worlds, 256, 0, st_>>>(d, pv);
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk);
