@@ -165,6 +165,21 @@ int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t
 int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
                int32_t *hit);
 
+/* Allocation-free variant of pk_collide (this entry point has no counterpart in the reference).
+ * For callers that cannot allocate device memory at call time: code running inside a strict
+ * memory budget, or under an allocator that must not see per-call cudaMalloc/cudaFree. Nothing
+ * is allocated: the device staging for the descriptors and results is a fixed array inside the
+ * library, holding at most PK_COLLIDE_NOALLOC_MAX pairs (about 1 MiB, kept by every GPU that
+ * loads the library until the process exits). Larger n returns PK_ERR_CAPACITY. Inputs and
+ * outputs are the caller's host arrays, as for pk_collide, and the results are the same.
+ * The first call on a device looks up the array's device address; make that first call before
+ * any stream capture. All calls share the one array: calls whose GPU work overlaps (several
+ * threads, or several world objects on one device) race and must be serialised by the caller.
+ * The world's shapes must already be on the device (after a pk_body_add, a step or a pk_collide). */
+#define PK_COLLIDE_NOALLOC_MAX 4096
+int pk_collide_noalloc(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
+                       int32_t *hit);
+
 int pk_last_cuda_error(void);
 const char *pk_version(void);
 

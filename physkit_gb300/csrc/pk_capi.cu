@@ -15,6 +15,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -77,6 +78,56 @@ struct pk_world
     bool order_dirty = false; // solver schedule needs recomputing (bodies added or removed)
 };
 
+// Allocation-free narrowphase (pk_collide_noalloc). Its device staging lives in this file-scope
+// array instead of memory from cudaMalloc: pair descriptors in, results out, for at most
+// PK_COLLIDE_NOALLOC_MAX pairs per call. Every GPU that loads this library holds the array
+// (about 1 MiB) until the process exits.
+namespace
+{
+constexpr int kNoAllocMax = PK_COLLIDE_NOALLOC_MAX;
+constexpr size_t kNoAllocSpecs = sizeof(pk_collide_shape) * kNoAllocMax; // one side's descriptors
+constexpr size_t kNoAllocOut = sizeof(double) * 10 * kNoAllocMax;
+constexpr size_t kNoAllocInts = sizeof(int32_t) * kNoAllocMax;
+constexpr size_t kNoAllocBytes = 2 * kNoAllocSpecs + kNoAllocOut + 2 * kNoAllocInts;
+} // namespace
+
+static __device__ __align__(256) unsigned char g_collide_scratch[kNoAllocBytes];
+
+namespace
+{
+// Device address of g_collide_scratch, looked up once per device (with that device current):
+// in host code the array's name is only a host-side stand-in, not a device address.
+constexpr int kMaxDevices = 64;
+unsigned char *g_scratch_ptr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
+
+int scratch_for_current_device(unsigned char **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) return PK_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev])
+    {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_collide_scratch);
+        if (e != cudaSuccess)
+        {
+            g_last_cuda = int(e);
+            return PK_ERR_CUDA;
+        }
+        g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return PK_OK;
+}
+} // namespace
+
 extern "C" {
 
 void pk_world_desc_init(pk_world_desc *d)
@@ -104,6 +155,52 @@ void pk_body_desc_init(pk_body_desc *d)
     d->inertia[0] = d->inertia[4] = d->inertia[8] = 1.0;
     d->restitution = 0.5;
     d->friction = 0.5;
+}
+
+int pk_collide_noalloc(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
+                       int32_t *hit)
+{
+    if (!w || n < 0 || (n > 0 && (!a || !b || !out || !hit))) return PK_ERR_INVALID;
+    if (n > kNoAllocMax) return PK_ERR_CAPACITY; // larger batches: split them, or use pk_collide
+    int nshapes = int(w->ranges.size() / 4);
+    for (int i = 0; i < n; ++i)
+        for (const pk_collide_shape *s : {a + i, b + i})
+        {
+            if (s->kind < 0 || s->kind > 2) return PK_ERR_INVALID;
+            if (s->kind == 2 && (s->shape < 0 || s->shape >= nshapes)) return PK_ERR_INVALID;
+        }
+    if (n == 0) return PK_OK;
+    if (w->shapes_dirty) return PK_ERR_INVALID; // shapes are uploaded by a step, a body add or pk_collide first
+    unsigned char *base = nullptr;
+    if (int rc = scratch_for_current_device(&base)) return rc;
+    unsigned char *da = base, *db = base + kNoAllocSpecs;
+    double *dout = reinterpret_cast<double *>(base + 2 * kNoAllocSpecs);
+    int32_t *dhit = reinterpret_cast<int32_t *>(base + 2 * kNoAllocSpecs + kNoAllocOut);
+    int32_t *dst = dhit + kNoAllocMax;
+    cudaStream_t st = static_cast<cudaStream_t>(w->eng->stream());
+    size_t spec_bytes = sizeof(pk_collide_shape) * size_t(n);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(da, a, spec_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(db, b, spec_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        // the array keeps the previous call's results: misses leave `out` untouched, so clear it
+        (e = cudaMemsetAsync(dout, 0, sizeof(double) * 10 * size_t(n), st)) != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    if (w->eng->collide_device(da, db, n, dout, dhit, dst))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    if ((e = cudaMemcpyAsync(out, dout, sizeof(double) * 10 * size_t(n), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(hit, dhit, sizeof(int32_t) * size_t(n), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
 }
 
 int pk_last_cuda_error(void) { return g_last_cuda; }

@@ -65,6 +65,9 @@ public:
     virtual int read_events(uint64_t *keys, int *kinds, int cap) = 0;
     virtual int read_colours(uint64_t *keys, int *colours, int cap, int *ncolours_world0) = 0;
     virtual int collide(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) = 0;
+    // Same narrowphase launch on device buffers the caller provides; allocates nothing.
+    virtual int collide_device(const void *specs_a_dev, const void *specs_b_dev, int n, double *out_dev,
+                               int *hit_dev, int *status_dev) = 0;
     virtual int capture_graph(double dt) = 0;        // record the step as CUDA graphs
     virtual int launch_graph() = 0;                  // replay one captured step
     virtual void *stream() = 0;

@@ -554,6 +554,16 @@ public:
         return 0;
     }
 
+    int collide_device(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) override
+    {
+        if (n <= 0) return 0;
+        k_collide_batch<T><<<(n + 127) / 128, 128, 0, st_>>>(static_cast<const ShapeSpec *>(specs_a),
+                                                              static_cast<const ShapeSpec *>(specs_b), n, d_.verts,
+                                                              shape_range_, d_.clusters, shape_rmax_, out, hit, status);
+        PK_CUDA(cudaGetLastError());
+        return 0;
+    }
+
 private:
     EngineConfig cfg_{};
     Dev<T> d_{};

@@ -95,6 +95,7 @@ def lib():
             "pk_world_read_events": (C.c_int, [vp, u64p, i32p, i32p, C.c_int32, i32p]),
             "pk_world_read_colours": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p, i32p]),
             "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
+            "pk_collide_noalloc": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_world_set_timing": (C.c_int, [vp, C.c_int32]),
             "pk_world_read_stage_times": (C.c_int, [vp, dp, i32p, C.c_int32, i32p]),
             "pk_stage_name": (C.c_char_p, [C.c_int32]),
@@ -449,8 +450,9 @@ class World:
                                             C.byref(nc)), "pk_world_read_colours")
         return k[: n.value], col[: n.value], nc.value
 
-    def collide(self, shapes_a, shapes_b):
-        """gjk_epa on primitive shape pairs; each shape is (kind, params list, mesh id)."""
+    def collide(self, shapes_a, shapes_b, noalloc=False):
+        """gjk_epa on primitive shape pairs; each shape is (kind, params list, mesh id).
+        noalloc=True goes through pk_collide_noalloc (no device allocation; at most 4096 pairs)."""
         n = len(shapes_a)
         A = (CollideShapeC * max(n, 1))()
         B = (CollideShapeC * max(n, 1))()
@@ -462,5 +464,7 @@ class World:
                     dst.p[k] = v
         out = np.zeros((max(n, 1), 10))
         hit = np.zeros(max(n, 1), dtype=np.int32)
-        _check(self.L.pk_collide(self.h, A, B, n, _ptr(out, C.c_double), _ptr(hit, C.c_int32)), "pk_collide")
+        fn = self.L.pk_collide_noalloc if noalloc else self.L.pk_collide
+        _check(fn(self.h, A, B, n, _ptr(out, C.c_double), _ptr(hit, C.c_int32)),
+               "pk_collide_noalloc" if noalloc else "pk_collide")
         return hit[:n].astype(bool), out[:n]
