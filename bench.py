@@ -293,7 +293,9 @@ def run_ours(a, rank, world_size, local_rank):
                         "traffic": traffic,
                         "model": f"{bpu:g} B per {unit} x {units[unit]} {unit}s per launch"},
            "stage_ms_per_step": {k: round(v, 4) for k, v in per_stage.items()},
-           "counts": {"pairs": P, "contacts": Cn, "status": info["flags"]}}
+           "counts": {"pairs": P, "contacts": Cn, "gjk": info["gjk"], "epa": info["epa"],
+                      "gjk_large_mesh": info["gjk_large_mesh"], "epa_large_mesh": info["epa_large_mesh"],
+                      "status": info["flags"]}}
 
     if rank == 0 and not a.no_plain:
         out["plain_single_world"] = plain_world(a)

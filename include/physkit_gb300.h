@@ -90,6 +90,10 @@ typedef struct pk_step_info
     int32_t leaves; /* bodies in the LBVH of the last step */
     int32_t status;   /* PK_STATUS_* bits seen since the previous synchronize */
     int32_t launches; /* kernels launched by one step */
+    int32_t gjk;      /* pairs that reached GJK in the last step (after the bounding-sphere cull) */
+    int32_t epa;      /* pairs that reached EPA (GJK found them intersecting) */
+    int32_t gjk_large_mesh; /* of those, pairs involving a mesh above 32 vertices */
+    int32_t epa_large_mesh;
 } pk_step_info;
 
 /* Primitive shape for pk_collide: kind 0 aabb (p = min3 max3), 1 obb (p = center3 quat4 half3),

@@ -633,6 +633,10 @@ int pk_world_synchronize(pk_world *w, pk_step_info *info)
         info->leaves = c.nleaf;
         info->status = c.status;
         info->launches = c.launches;
+        info->gjk = c.gjk;
+        info->epa = c.epa;
+        info->gjk_large_mesh = c.gjk_heavy;
+        info->epa_large_mesh = c.epa_heavy;
     }
     return c.status ? PK_ERR_DEVICE_STATUS : PK_OK;
 }

@@ -143,11 +143,15 @@ template <class T> struct Dev
     Manifold<T> *man_new;
     uint8_t *event;
     int *old_idx;          // per pair: index of last step's manifold or -1
-    int *gjk_list;         // pairs queued for GJK
-    int *gjk_count;
-    int *epa_list;         // pairs queued for EPA
+    // GJK / EPA work lists. Pairs involving a large (clustered) mesh fill a list from its end,
+    // the others from its start, so each warp works on one cost class; heavy items run first.
+    int *gjk_list;
+    int *gjk_count;        // light items
+    int *gjk_count_heavy;
+    int *epa_list;
     Simplex<T> *epa_simplex;
     int *epa_count;
+    int *epa_count_heavy;
     Row<T> *rows;
     uint8_t *rowmask;
     int *colour;
@@ -217,6 +221,8 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.nleaf = 0;
         *d.gjk_count = 0;
         *d.epa_count = 0;
+        *d.gjk_count_heavy = 0;
+        *d.epa_count_heavy = 0;
         *d.epoch += 1;
     }
 }
@@ -681,27 +687,38 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
             Collision<T> none;
             manifold_update(d, p, old_idx, A, B, false, none);
         }
+        else if (A.ncl > 0 || B.ncl > 0)
+            d.gjk_list[d.pair_cap - 1 - warp_push(d.gjk_count_heavy)] = p;
         else
             d.gjk_list[warp_push(d.gjk_count)] = p;
     }
 }
+
+// Work item i of a two-class list: heavy items (stored from the end) first, then light ones.
+__device__ __forceinline__ int list_slot(int i, int nheavy, int cap)
+{ return i < nheavy ? cap - 1 - i : i - nheavy; }
 
 // Narrowphase pass 2: GJK (collision.cpp:165-189) over the queued pairs; enclosing simplices are
 // queued for EPA, the rest are settled without a new contact.
 template <class T>
 __global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    const int n = *d.gjk_count;
+    const int nh = *d.gjk_count_heavy;
+    const int n = nh + *d.gjk_count;
     PK_GRID_STRIDE(i, n)
     {
-        int p = d.gjk_list[i];
+        int p = d.gjk_list[list_slot(i, nh, d.pair_cap)];
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         Simplex<T> s;
         if (gjk(A, B, s))
         {
-            int j = warp_push(d.epa_count);
+            int j;
+            if (A.ncl > 0 || B.ncl > 0)
+                j = d.pair_cap - 1 - warp_push(d.epa_count_heavy);
+            else
+                j = warp_push(d.epa_count);
             d.epa_list[j] = p;
             d.epa_simplex[j] = s;
         }
@@ -717,9 +734,11 @@ __global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__
 template <class T>
 __global__ void __launch_bounds__(128) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    const int n = *d.epa_count;
-    PK_GRID_STRIDE(j, n)
+    const int nh = *d.epa_count_heavy;
+    const int n = nh + *d.epa_count;
+    PK_GRID_STRIDE(i, n)
     {
+        int j = list_slot(i, nh, d.pair_cap);
         int p = d.epa_list[j];
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);

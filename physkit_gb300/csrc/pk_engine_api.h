@@ -36,6 +36,7 @@ struct StepCounters
     int nleaf = 0;
     int status = 0;
     int launches = 0; // kernels one step launches
+    int gjk = 0, gjk_heavy = 0, epa = 0, epa_heavy = 0; // narrowphase work items of the last step
 };
 
 constexpr int kStages = 9;

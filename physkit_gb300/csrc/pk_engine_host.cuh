@@ -116,6 +116,8 @@ public:
         d.epoch = counters_ + 5;
         d.gjk_count = counters_ + 6;
         d.epa_count = counters_ + 7;
+        d.gjk_count_heavy = counters_ + 8;
+        d.epa_count_heavy = counters_ + 9;
         int minus1 = -1;
         PK_CUDA(cudaMemcpy(d.epoch, &minus1, sizeof(int), cudaMemcpyHostToDevice));
         PK_CUDA(alloc(&d.wp, W));
@@ -368,6 +370,10 @@ public:
             c->npairs = h[2];
             c->status = h[4];
             c->launches = launches_;
+            c->gjk = h[6] + h[8];
+            c->gjk_heavy = h[8];
+            c->epa = h[7] + h[9];
+            c->epa_heavy = h[9];
         }
         int zero = 0;
         PK_CUDA(cudaMemcpy(counters_ + 4, &zero, sizeof(int), cudaMemcpyHostToDevice));

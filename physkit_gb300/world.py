@@ -48,7 +48,8 @@ assert BODY_DTYPE.itemsize == 216
 
 
 class StepInfoC(C.Structure):
-    _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("launches", C.c_int32)]
+    _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("launches", C.c_int32),
+                ("gjk", C.c_int32), ("epa", C.c_int32), ("gjk_large_mesh", C.c_int32), ("epa_large_mesh", C.c_int32)]
 
 
 class CollideShapeC(C.Structure):
@@ -364,7 +365,8 @@ class World:
         if rc not in (PK_OK, PK_ERR_DEVICE_STATUS):
             _check(rc, "pk_world_synchronize")
         self.last_info = {"pairs": info.pairs, "leaves": info.leaves, "status": info.status,
-                          "launches": info.launches,
+                          "launches": info.launches, "gjk": info.gjk, "epa": info.epa,
+                          "gjk_large_mesh": info.gjk_large_mesh, "epa_large_mesh": info.epa_large_mesh,
                           "flags": [v for k, v in STATUS_BITS.items() if info.status & k]}
         return self.last_info
 
