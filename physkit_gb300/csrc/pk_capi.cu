@@ -348,9 +348,19 @@ static int flush_order(pk_world *w)
     std::vector<int> cnt(static_cast<size_t>(nw), 0), order(static_cast<size_t>(nw));
     for (int s = 0; s < w->nslots; ++s)
         if (w->slots[size_t(s)].alive && !w->slots[size_t(s)].is_static) cnt[size_t(w->slots[size_t(s)].world)]++;
-    for (int i = 0; i < nw; ++i) order[size_t(i)] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[size_t(a)] > cnt[size_t(b)]; });
-    if (w->eng->set_world_order(order.data(), nw))
+    std::vector<int> nlocal(static_cast<size_t>(nw));
+    for (int i = 0; i < nw; ++i)
+    {
+        order[size_t(i)] = i;
+        nlocal[size_t(i)] = int(w->worlds[size_t(i)].local_slot.size());
+    }
+    // largest first by local indices in use (this also keeps the worlds that need the large
+    // solver cache contiguous at the front), then by dynamic bodies
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (nlocal[size_t(a)] != nlocal[size_t(b)]) return nlocal[size_t(a)] > nlocal[size_t(b)];
+        return cnt[size_t(a)] > cnt[size_t(b)];
+    });
+    if (w->eng->set_world_order(order.data(), nlocal.data(), nw))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;

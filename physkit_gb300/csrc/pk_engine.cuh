@@ -159,6 +159,7 @@ template <class T> struct Dev
     uint32_t *order;
     int *ncolours;
     const int *world_order; // solver CTA -> world, largest worlds first
+    const int *world_nlocal; // local indices in use per world (bounds the shared-memory cache)
     // control
     int *status;
     int *epoch;
@@ -654,9 +655,54 @@ __device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const Shape
     d.man_new[p] = nm;
 }
 
-// Narrowphase pass 1: per pair, find last step's manifold, then either settle the pair at once
-// (bounding spheres apart by more than the rounding margin: disjoint shapes, for which the
-// reference's GJK returns no collision, collision.cpp:181-182) or queue it for GJK.
+// Separating-axis test of the two bodies' oriented local AABBs (15 axes). True only when some axis
+// separates them by more than `margin`: then the shapes inside are disjoint too.
+template <class T>
+__device__ __forceinline__ bool obb_separated(const Aabb<T> &la, Qt<T> qa, V3<T> pa, const Aabb<T> &lb, Qt<T> qb,
+                                              V3<T> pb, T margin)
+{
+    M3<T> Ra = to_matrix(qa), Rb = to_matrix(qb);
+    V3<T> ha = (la.mx - la.mn) * T(0.5), hb = (lb.mx - lb.mn) * T(0.5);
+    V3<T> ca = pa + matvec(Ra.m, (la.mx + la.mn) * T(0.5));
+    V3<T> cb = pb + matvec(Rb.m, (lb.mx + lb.mn) * T(0.5));
+    V3<T> t = cb - ca;
+    // axes of A and B are the columns of Ra, Rb
+    T a[3] = {ha.x, ha.y, ha.z}, b[3] = {hb.x, hb.y, hb.z};
+    T C[3][3], AC[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+        {
+            C[i][j] = Ra.m[i] * Rb.m[j] + Ra.m[3 + i] * Rb.m[3 + j] + Ra.m[6 + i] * Rb.m[6 + j];
+            AC[i][j] = tabs(C[i][j]) + T(1e-6);
+        }
+    T ta[3];
+    for (int i = 0; i < 3; ++i) ta[i] = Ra.m[i] * t.x + Ra.m[3 + i] * t.y + Ra.m[6 + i] * t.z;
+    for (int i = 0; i < 3; ++i)
+        if (tabs(ta[i]) > a[i] + b[0] * AC[i][0] + b[1] * AC[i][1] + b[2] * AC[i][2] + margin) return true;
+    for (int j = 0; j < 3; ++j)
+    {
+        T tb = ta[0] * C[0][j] + ta[1] * C[1][j] + ta[2] * C[2][j];
+        if (tabs(tb) > b[j] + a[0] * AC[0][j] + a[1] * AC[1][j] + a[2] * AC[2][j] + margin) return true;
+    }
+    for (int i = 0; i < 3; ++i)
+    {
+        int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+        for (int j = 0; j < 3; ++j)
+        {
+            int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+            T tt = tabs(ta[i2] * C[i1][j] - ta[i1] * C[i2][j]);
+            T ra = a[i1] * AC[i2][j] + a[i2] * AC[i1][j];
+            T rb = b[j1] * AC[i][j2] + b[j2] * AC[i][j1];
+            if (tt > ra + rb + margin) return true;
+        }
+    }
+    return false;
+}
+
+// Narrowphase pass 1: per pair, find last step's manifold, then either settle the pair at once or
+// queue it for GJK. A pair is settled without a new contact when the bodies' bounding spheres or
+// their oriented local boxes are apart by more than a rounding margin: the shapes are then
+// disjoint, and the reference's GJK returns no collision for them (collision.cpp:181-182).
 template <class T>
 __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
 {
@@ -682,7 +728,10 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
         V3<T> dc = B.pos - A.pos;
         T rs = A.rmax + B.rmax;
         T cull = rs + (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
-        if (sqnorm(dc) > cull * cull)
+        const T margin = (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
+        if (sqnorm(dc) > cull * cull ||
+            obb_separated(d.shape_box[d.meta[sa].shape], A.q, A.pos, d.shape_box[d.meta[sb].shape], B.q, B.pos,
+                          margin + T(1e-5) * rs))
         {
             Collision<T> none;
             manifold_update(d, p, old_idx, A, B, false, none);
@@ -939,26 +988,34 @@ template <class T> __device__ __forceinline__ void solve_contact(BodyRef<T> &A, 
     }
 }
 
-template <class T> __device__ __forceinline__ BodyRef<T> body_ref(const Dev<T> &d, int s)
+// Solver view of a body: its velocities live in the CTA's shared-memory cache (indexed by the
+// world-local index) when `cache` is set, else in global memory.
+template <class T> __device__ __forceinline__ BodyRef<T> body_ref(const Dev<T> &d, int s, Vel<T> *cache)
 {
     BodyRef<T> r;
-    r.v = d.vel + s;
+    const Meta m = d.meta[s];
+    r.is_static = (m.flags & BODY_STATIC) != 0;
+    r.v = (cache && !r.is_static) ? cache + m.local : d.vel + s;
     r.iwinv = d.iwinv + 9 * s;
     r.inv_mass = d.prm[s].inv_mass;
-    r.is_static = (d.meta[s].flags & BODY_STATIC) != 0;
     return r;
 }
 
-template <class T> __global__ void __launch_bounds__(256) k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval)
+template <class T>
+__global__ void __launch_bounds__(256)
+    k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies)
 {
+    extern __shared__ __align__(16) unsigned char solve_smem[];
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
     __shared__ int remaining;
     __shared__ int nrounds;
-    if (int(blockIdx.x) >= d.max_worlds) return;
-    const int w = d.world_order[blockIdx.x];
+    const int blk = first_block + int(blockIdx.x);
+    if (blk >= d.max_worlds) return;
+    const int w = d.world_order[blk];
     if (!d.wp[w].active) return;
+    Vel<T> *cache = (d.world_nlocal[w] <= cache_bodies) ? reinterpret_cast<Vel<T> *>(solve_smem) : nullptr;
     const int ms = d.mstart[w], me = d.mend[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     if (me <= ms)
@@ -1052,6 +1109,19 @@ template <class T> __global__ void __launch_bounds__(256) k_solve_world(Dev<T> d
     }
     __syncthreads();
 
+    if (cache)
+    {
+        // velocities of the world's dynamic bodies that take part in contacts
+        for (int p = ms + tid; p < me; p += nt)
+        {
+            if (!d.rowmask[p]) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            if (!(d.meta[a].flags & BODY_STATIC)) cache[d.meta[a].local] = d.vel[a];
+            if (!(d.meta[b].flags & BODY_STATIC)) cache[d.meta[b].local] = d.vel[b];
+        }
+        __syncthreads();
+    }
     // warm start, colour by colour
     for (int c = 0; c < nrounds; ++c)
     {
@@ -1059,7 +1129,7 @@ template <class T> __global__ void __launch_bounds__(256) k_solve_world(Dev<T> d
         {
             int p = int(d.order[ms + cstart[c] + k]);
             uint64_t v = sval[p];
-            BodyRef<T> A = body_ref(d, int(v >> 32)), B = body_ref(d, int(v & 0xFFFFFFFFu));
+            BodyRef<T> A = body_ref(d, int(v >> 32), cache), B = body_ref(d, int(v & 0xFFFFFFFFu), cache);
             uint8_t mask = d.rowmask[p];
             for (int q = 0; q < 4; ++q)
             {
@@ -1080,7 +1150,7 @@ template <class T> __global__ void __launch_bounds__(256) k_solve_world(Dev<T> d
             {
                 int p = int(d.order[ms + cstart[c] + k]);
                 uint64_t v = sval[p];
-                BodyRef<T> A = body_ref(d, int(v >> 32)), B = body_ref(d, int(v & 0xFFFFFFFFu));
+                BodyRef<T> A = body_ref(d, int(v >> 32), cache), B = body_ref(d, int(v & 0xFFFFFFFFu), cache);
                 uint8_t mask = d.rowmask[p];
                 for (int q = 0; q < 4; ++q)
                 {
@@ -1089,6 +1159,17 @@ template <class T> __global__ void __launch_bounds__(256) k_solve_world(Dev<T> d
                 }
             }
             __syncthreads();
+        }
+    }
+    if (cache)
+    {
+        for (int p = ms + tid; p < me; p += nt)
+        {
+            if (!d.rowmask[p]) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            if (!(d.meta[a].flags & BODY_STATIC)) d.vel[a] = cache[d.meta[a].local];
+            if (!(d.meta[b].flags & BODY_STATIC)) d.vel[b] = cache[d.meta[b].local];
         }
     }
     // write back accumulated impulses into the manifold cache

@@ -56,7 +56,8 @@ public:
     virtual int set_world(int w, const double g[3], double gnorm, int active) = 0;
     virtual int upload_bodies(const int *slots, const HostBody *b, int n, int nslots) = 0;
     virtual int kill_body(int slot, int world, int local) = 0;
-    virtual int set_world_order(const int *order, int n) = 0; // solver schedule, largest first
+    // solver schedule (largest worlds first) and local indices in use per world
+    virtual int set_world_order(const int *order, const int *nlocal, int n) = 0;
     virtual int step(double dt) = 0;                 // enqueue only
     virtual int synchronize(StepCounters *c) = 0;   // wait + read counters, clears status
     virtual int read_bodies(double *out14, int nslots) = 0;

@@ -129,13 +129,18 @@ public:
         PK_CUDA(alloc(&d.ncolours, W));
         PK_CUDA(cudaMemset(d.ncolours, 0, sizeof(int) * W));
         {
-            int *wo;
+            int *wo, *wn;
             PK_CUDA(alloc(&wo, W));
+            PK_CUDA(alloc(&wn, W));
             std::vector<int> ident(W);
             for (size_t i = 0; i < W; ++i) ident[i] = int(i);
             PK_CUDA(cudaMemcpy(wo, ident.data(), sizeof(int) * W, cudaMemcpyHostToDevice));
+            PK_CUDA(cudaMemset(wn, 0x7F, sizeof(int) * W)); // "too large to cache" until set
             d.world_order = wo;
+            d.world_nlocal = wn;
         }
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(kMaxSolveSmem)));
         for (int k = 0; k < 2; ++k)
         {
             PK_CUDA(alloc(&mkey_[k], N));
@@ -279,11 +284,24 @@ public:
         return 0;
     }
 
-    int set_world_order(const int *order, int n) override
+    int set_world_order(const int *order, const int *nlocal, int n) override
     {
         if (n != cfg_.max_worlds) return -3;
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_order), order, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_nlocal), nlocal, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaStreamSynchronize(st_));
+        // Worlds above kSmallWorld local indices get their own launch with a cache sized for the
+        // largest world (if it fits in shared memory); the others share a small cache.
+        big_worlds_ = 0;
+        int maxl = 0;
+        for (int i = 0; i < n; ++i)
+        {
+            int nl = nlocal[order[i]];
+            if (nl > kSmallWorld) ++big_worlds_;
+            maxl = nl > maxl ? nl : maxl;
+        }
+        int limit = int(kMaxSolveSmem / sizeof(Vel<T>));
+        big_cache_ = maxl <= limit ? maxl : 0;
         return 0;
     }
 
@@ -590,6 +608,10 @@ private:
     T *clusters_ = nullptr;
     size_t clusters_cap_ = 0;
     cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+    static constexpr int kSmallWorld = 512;
+    static constexpr size_t kMaxSolveSmem = 160 * 1024;
+    int big_worlds_ = 0;
+    int big_cache_ = 0;
     bool timing_ = false;
     bool capturing_ = false;
     int launches_ = 0;
@@ -653,7 +675,8 @@ private:
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.old_idx, d_.gjk_list,
                       d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour,
-                      d_.order, d_.owner, const_cast<int *>(d_.world_order), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
+                      d_.order, d_.owner, const_cast<int *>(d_.world_order),
+                      const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_};
         for (void *p : ps)
             if (p) cudaFree(p);
@@ -675,7 +698,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 15 + 3 * mpasses + 3 * ppasses;
+        launches_ = 14 + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -706,7 +729,11 @@ private:
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         PK_CUDA(mark(7));
-        k_solve_world<T><<<cfg_.max_worlds, 256, 0, st_>>>(d, pv);
+        if (big_worlds_ > 0)
+            k_solve_world<T><<<big_worlds_, 256, sizeof(Vel<T>) * size_t(big_cache_), st_>>>(d, pv, 0, big_cache_);
+        if (cfg_.max_worlds > big_worlds_)
+            k_solve_world<T><<<cfg_.max_worlds - big_worlds_, 256, sizeof(Vel<T>) * kSmallWorld, st_>>>(
+                d, pv, big_worlds_, kSmallWorld);
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk);
