@@ -154,7 +154,9 @@ template <class T> struct Dev
     int *epa_count_heavy;
     Row<T> *rows;
     uint8_t *rowmask;
-    int *colour;
+    int *colour;      // solver scratch: compacted active manifolds of each world
+    int *colour_tmp;  // solver scratch: colour of each compacted manifold
+    int *pair_colour; // colour of each pair of the last step (-2: no contact rows)
     uint32_t *owner;
     uint32_t *order;
     int *ncolours;
@@ -893,55 +895,58 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
             mask |= uint8_t(1u << k);
         }
         d.rowmask[p] = mask;
+        d.pair_colour[p] = -2;
     }
 }
 
 // ------------------------------------------------------------------------------------------------
 // solver: one CTA per world; colouring, warm start, iterations (constraint.h:1107-1201)
 // ------------------------------------------------------------------------------------------------
-template <class T> struct BodyRef
+// A body as the solver sees it while one thread processes one manifold: velocities and the world
+// inverse inertia in registers, loaded once and stored once per manifold. Within a colour no
+// other thread touches the same dynamic body, so the result equals updating memory in place.
+template <class T> struct SBody
 {
-    Vel<T> *v;
-    const T *iwinv;
+    V3<T> v, w;
+    T I[9];
     T inv_mass;
     bool is_static;
 };
 
-template <class T> __device__ __forceinline__ T jv(const T *J, const T *Wa, const T *Wb, const Vel<T> &a, const Vel<T> &b)
+template <class T> __device__ __forceinline__ T jv_reg(const T *J, const T *Wa, const T *Wb, const SBody<T> &a, const SBody<T> &b)
 {
     // J_v.v_a + J_w_a.w_a - J_v.v_b + J_w_b.w_b (constraint.h:52-53), left to right
-    return dot(ld3(J), ld3(a.v)) + dot(ld3(Wa), ld3(a.w)) - dot(ld3(J), ld3(b.v)) + dot(ld3(Wb), ld3(b.w));
+    return dot(ld3(J), a.v) + dot(ld3(Wa), a.w) - dot(ld3(J), b.v) + dot(ld3(Wb), b.w);
 }
 
-template <class T> __device__ __forceinline__ void apply_imp(BodyRef<T> &a, BodyRef<T> &b, V3<T> J, V3<T> Wa, V3<T> Wb, T lam)
+template <class T> __device__ __forceinline__ void apply_reg(SBody<T> &a, SBody<T> &b, V3<T> J, V3<T> Wa, V3<T> Wb, T lam)
 {
+    // apply_impulse / apply_angular_impulse (particle.h:88-93); static bodies are not written
     if (!a.is_static)
     {
-        V3<T> v = ld3(a.v->v) + (J * lam) * a.inv_mass;
-        V3<T> w = ld3(a.v->w) + matvec(a.iwinv, Wa * lam);
-        st3(a.v->v, v);
-        st3(a.v->w, w);
+        a.v = a.v + (J * lam) * a.inv_mass;
+        a.w = a.w + matvec(a.I, Wa * lam);
     }
     if (!b.is_static)
     {
-        V3<T> v = ld3(b.v->v) + ((-J) * lam) * b.inv_mass;
-        V3<T> w = ld3(b.v->w) + matvec(b.iwinv, Wb * lam);
-        st3(b.v->v, v);
-        st3(b.v->w, w);
+        b.v = b.v + ((-J) * lam) * b.inv_mass;
+        b.w = b.w + matvec(b.I, Wb * lam);
     }
 }
 
-template <class T> __device__ __forceinline__ void warm_row(BodyRef<T> &a, BodyRef<T> &b, const T *J, const T *Wa, const T *Wb, double acc)
+template <class T> __device__ __forceinline__ void warm_contact(SBody<T> &A, SBody<T> &B, const Row<T> &r)
 {
-    if (acc == 0.0) return;
-    apply_imp(a, b, ld3(J), ld3(Wa), ld3(Wb), T(acc));
+    // jacobian_row::warm_start for the three rows (constraint.h:73-87, 1125-1130)
+    if (r.acc[0] != 0.0) apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), T(r.acc[0]));
+    if (r.acc[1] != 0.0) apply_reg(A, B, ld3(r.t1), ld3(r.wa_t1), ld3(r.wb_t1), T(r.acc[1]));
+    if (r.acc[2] != 0.0) apply_reg(A, B, ld3(r.t2), ld3(r.wa_t2), ld3(r.wb_t2), T(r.acc[2]));
 }
 
-template <class T> __device__ __forceinline__ void solve_contact(BodyRef<T> &A, BodyRef<T> &B, Row<T> &r)
+template <class T> __device__ __forceinline__ void solve_contact(SBody<T> &A, SBody<T> &B, Row<T> &r)
 {
     // normal row: jacobian_row::apply (constraint.h:49-71), gamma = 0
     {
-        T Jv = jv(r.n, r.wa_n, r.wb_n, *A.v, *B.v);
+        T Jv = jv_reg(r.n, r.wa_n, r.wb_n, A, B);
         T cfp = T(0) * T(r.acc[0]);
         T lambda = -(Jv + r.bias + cfp) * r.meff_n;
         double old = r.acc[0];
@@ -949,13 +954,12 @@ template <class T> __device__ __forceinline__ void solve_contact(BodyRef<T> &A, 
         double lo = 0.0, hi = 1.7976931348623157e308;
         double acc = (v < lo) ? lo : ((hi < v) ? hi : v);
         r.acc[0] = acc;
-        T applied = T(acc - old);
-        apply_imp(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), applied);
+        apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), T(acc - old));
     }
     // coupled 2D friction with circular cone clamp (constraint.h:1138-1187)
     T maxf = r.mu * T(r.acc[0]);
-    T Jv1 = jv(r.t1, r.wa_t1, r.wb_t1, *A.v, *B.v);
-    T Jv2 = jv(r.t2, r.wa_t2, r.wb_t2, *A.v, *B.v);
+    T Jv1 = jv_reg(r.t1, r.wa_t1, r.wb_t1, A, B);
+    T Jv2 = jv_reg(r.t2, r.wa_t2, r.wb_t2, A, B);
     T b1 = Jv1 + T(0), b2 = Jv2 + T(0);
     T l1 = -(r.inv11 * b1 + r.inv12 * b2);
     T l2 = -(r.inv12 * b1 + r.inv22 * b2);
@@ -973,32 +977,65 @@ template <class T> __device__ __forceinline__ void solve_contact(BodyRef<T> &A, 
     if (!A.is_static)
     {
         V3<T> imp = ld3(r.t1) * a1 + ld3(r.t2) * a2;
-        V3<T> v = ld3(A.v->v) + imp * A.inv_mass;
-        V3<T> w = ld3(A.v->w) + matvec(A.iwinv, ld3(r.wa_t1) * a1 + ld3(r.wa_t2) * a2);
-        st3(A.v->v, v);
-        st3(A.v->w, w);
+        A.v = A.v + imp * A.inv_mass;
+        A.w = A.w + matvec(A.I, ld3(r.wa_t1) * a1 + ld3(r.wa_t2) * a2);
     }
     if (!B.is_static)
     {
         V3<T> imp = (-ld3(r.t1)) * a1 - ld3(r.t2) * a2;
-        V3<T> v = ld3(B.v->v) + imp * B.inv_mass;
-        V3<T> w = ld3(B.v->w) + matvec(B.iwinv, ld3(r.wb_t1) * a1 + ld3(r.wb_t2) * a2);
-        st3(B.v->v, v);
-        st3(B.v->w, w);
+        B.v = B.v + imp * B.inv_mass;
+        B.w = B.w + matvec(B.I, ld3(r.wb_t1) * a1 + ld3(r.wb_t2) * a2);
     }
 }
 
-// Solver view of a body: its velocities live in the CTA's shared-memory cache (indexed by the
-// world-local index) when `cache` is set, else in global memory.
-template <class T> __device__ __forceinline__ BodyRef<T> body_ref(const Dev<T> &d, int s, Vel<T> *cache)
+template <class T> __device__ __forceinline__ void load_sbody(const Dev<T> &d, int s, const Vel<T> *cache, SBody<T> &b)
 {
-    BodyRef<T> r;
     const Meta m = d.meta[s];
-    r.is_static = (m.flags & BODY_STATIC) != 0;
-    r.v = (cache && !r.is_static) ? cache + m.local : d.vel + s;
-    r.iwinv = d.iwinv + 9 * s;
-    r.inv_mass = d.prm[s].inv_mass;
-    return r;
+    b.is_static = (m.flags & BODY_STATIC) != 0;
+    const Vel<T> ve = (cache && !b.is_static) ? cache[m.local] : d.vel[s];
+    b.v = ld3(ve.v);
+    b.w = ld3(ve.w);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) b.I[k] = d.iwinv[9 * s + k];
+    b.inv_mass = d.prm[s].inv_mass;
+}
+
+template <class T> __device__ __forceinline__ void store_sbody(const Dev<T> &d, int s, Vel<T> *cache, const SBody<T> &b)
+{
+    if (b.is_static) return;
+    Vel<T> ve;
+    st3(ve.v, b.v);
+    st3(ve.w, b.w);
+    if (cache)
+        cache[d.meta[s].local] = ve;
+    else
+        d.vel[s] = ve;
+}
+
+// One manifold: warm start (warm = true) or one Gauss-Seidel pass over its contacts in order.
+template <class T> __device__ __forceinline__ void solve_manifold(const Dev<T> &d, int p, uint64_t sv, Vel<T> *cache, bool warm)
+{
+    int sa = int(sv >> 32), sb = int(sv & 0xFFFFFFFFu);
+    SBody<T> A, B;
+    load_sbody(d, sa, cache, A);
+    load_sbody(d, sb, cache, B);
+    const uint8_t mask = d.rowmask[p];
+    for (int q = 0; q < 4; ++q)
+    {
+        if (!(mask & (1u << q))) continue;
+        Row<T> r = d.rows[4 * p + q];
+        if (warm)
+            warm_contact(A, B, r);
+        else
+        {
+            solve_contact(A, B, r);
+            d.rows[4 * p + q].acc[0] = r.acc[0];
+            d.rows[4 * p + q].acc[1] = r.acc[1];
+            d.rows[4 * p + q].acc[2] = r.acc[2];
+        }
+    }
+    store_sbody(d, sa, cache, A);
+    store_sbody(d, sb, cache, B);
 }
 
 template <class T>
@@ -1009,68 +1046,95 @@ __global__ void __launch_bounds__(256)
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
+    __shared__ int wsum[8];
     __shared__ int remaining;
-    __shared__ int nrounds;
+    __shared__ int nactive;
     const int blk = first_block + int(blockIdx.x);
     if (blk >= d.max_worlds) return;
     const int w = d.world_order[blk];
     if (!d.wp[w].active) return;
-    Vel<T> *cache = (d.world_nlocal[w] <= cache_bodies) ? reinterpret_cast<Vel<T> *>(solve_smem) : nullptr;
     const int ms = d.mstart[w], me = d.mend[w];
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     if (me <= ms)
     {
         if (tid == 0) d.ncolours[w] = 0;
         return;
     }
-    if (tid == 0) remaining = 0;
+    const bool fits = d.world_nlocal[w] <= cache_bodies;
+    Vel<T> *cache = fits ? reinterpret_cast<Vel<T> *>(solve_smem) : nullptr;
+    uint32_t *sowner = fits ? reinterpret_cast<uint32_t *>(solve_smem) : nullptr; // during colouring only
+    int *act = d.colour + ms; // compacted active manifolds of this world, ascending p
+
+    // 1. compact the manifolds that have contact rows (stable: ascending pair index)
+    if (tid == 0) nactive = 0;
     __syncthreads();
-    int active = 0;
-    for (int p = ms + tid; p < me; p += nt)
+    for (int base = ms; base < me; base += nt)
     {
-        d.colour[p] = d.rowmask[p] ? -1 : -2;
-        active += d.rowmask[p] ? 1 : 0;
+        int p = base + tid;
+        bool a = p < me && d.rowmask[p] != 0;
+        unsigned bal = __ballot_sync(0xFFFFFFFFu, a);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        int off = nactive;
+        for (int k = 0; k < warp; ++k) off += wsum[k];
+        if (a) act[off + __popc(bal & ((1u << lane) - 1u))] = p;
+        __syncthreads();
+        if (tid == 0)
+            for (int k = 0; k < nt / 32; ++k) nactive += wsum[k];
+        __syncthreads();
     }
-    if (active) atomicAdd(&remaining, active);
+    const int na = nactive;
+    int *colour = d.colour_tmp + ms; // colour of act[k]
+    for (int k = tid; k < na; k += nt) colour[k] = -1;
     for (int c = tid; c < kMaxColours; c += nt)
     {
         ccount[c] = 0;
         cursor[c] = 0;
     }
+    if (tid == 0) remaining = na;
     __syncthreads();
+
+    // 2. colouring: each uncoloured manifold claims its dynamic bodies with its index; the winners
+    //    of all their bodies take the round number
     int round = 0;
     while (remaining > 0)
     {
         __syncthreads();
-        for (int p = ms + tid; p < me; p += nt)
+        for (int k = tid; k < na; k += nt)
         {
-            if (d.colour[p] != -1) continue;
+            if (colour[k] != -1) continue;
+            int p = act[k];
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            if (!(d.meta[a].flags & BODY_STATIC)) d.owner[a] = 0xFFFFFFFFu;
-            if (!(d.meta[b].flags & BODY_STATIC)) d.owner[b] = 0xFFFFFFFFu;
+            const Meta ma = d.meta[a], mb = d.meta[b];
+            if (!(ma.flags & BODY_STATIC)) { if (sowner) sowner[ma.local] = 0xFFFFFFFFu; else d.owner[a] = 0xFFFFFFFFu; }
+            if (!(mb.flags & BODY_STATIC)) { if (sowner) sowner[mb.local] = 0xFFFFFFFFu; else d.owner[b] = 0xFFFFFFFFu; }
         }
         if (tid == 0) remaining = 0;
         __syncthreads();
-        for (int p = ms + tid; p < me; p += nt)
+        for (int k = tid; k < na; k += nt)
         {
-            if (d.colour[p] != -1) continue;
+            if (colour[k] != -1) continue;
+            int p = act[k];
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            if (!(d.meta[a].flags & BODY_STATIC)) atomicMin(d.owner + a, uint32_t(p));
-            if (!(d.meta[b].flags & BODY_STATIC)) atomicMin(d.owner + b, uint32_t(p));
+            const Meta ma = d.meta[a], mb = d.meta[b];
+            if (!(ma.flags & BODY_STATIC)) { if (sowner) atomicMin(sowner + ma.local, uint32_t(k)); else atomicMin(d.owner + a, uint32_t(k)); }
+            if (!(mb.flags & BODY_STATIC)) { if (sowner) atomicMin(sowner + mb.local, uint32_t(k)); else atomicMin(d.owner + b, uint32_t(k)); }
         }
         __syncthreads();
         int left = 0;
-        for (int p = ms + tid; p < me; p += nt)
+        for (int k = tid; k < na; k += nt)
         {
-            if (d.colour[p] != -1) continue;
+            if (colour[k] != -1) continue;
+            int p = act[k];
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            bool oka = (d.meta[a].flags & BODY_STATIC) || d.owner[a] == uint32_t(p);
-            bool okb = (d.meta[b].flags & BODY_STATIC) || d.owner[b] == uint32_t(p);
+            const Meta ma = d.meta[a], mb = d.meta[b];
+            bool oka = (ma.flags & BODY_STATIC) || (sowner ? sowner[ma.local] : d.owner[a]) == uint32_t(k);
+            bool okb = (mb.flags & BODY_STATIC) || (sowner ? sowner[mb.local] : d.owner[b]) == uint32_t(k);
             if (oka && okb)
-                d.colour[p] = round;
+                colour[k] = round;
             else
                 ++left;
         }
@@ -1084,9 +1148,9 @@ __global__ void __launch_bounds__(256)
         }
     }
     const int ncol = round;
-    for (int p = ms + tid; p < me; p += nt)
+    for (int k = tid; k < na; k += nt)
     {
-        int c = d.colour[p];
+        int c = colour[k];
         if (c >= 0 && c < kMaxColours) atomicAdd(&ccount[c], 1);
     }
     __syncthreads();
@@ -1098,83 +1162,58 @@ __global__ void __launch_bounds__(256)
             cstart[c] = s;
             s += ccount[c];
         }
-        nrounds = ncol;
         d.ncolours[w] = ncol;
     }
     __syncthreads();
-    for (int p = ms + tid; p < me; p += nt)
+    for (int k = tid; k < na; k += nt)
     {
-        int c = d.colour[p];
-        if (c >= 0 && c < kMaxColours) d.order[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = uint32_t(p);
+        int c = colour[k];
+        if (c >= 0 && c < kMaxColours) d.order[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = uint32_t(act[k]);
     }
     __syncthreads();
-
+    // per-pair colour for read-back (-2: no contact rows)
+    for (int k = tid; k < na; k += nt) d.pair_colour[act[k]] = colour[k];
     if (cache)
     {
-        // velocities of the world's dynamic bodies that take part in contacts
-        for (int p = ms + tid; p < me; p += nt)
+        // the owner table is done; the shared memory now caches body velocities
+        for (int k = tid; k < na; k += nt)
         {
-            if (!d.rowmask[p]) continue;
-            uint64_t v = sval[p];
+            uint64_t v = sval[act[k]];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
             if (!(d.meta[a].flags & BODY_STATIC)) cache[d.meta[a].local] = d.vel[a];
             if (!(d.meta[b].flags & BODY_STATIC)) cache[d.meta[b].local] = d.vel[b];
         }
-        __syncthreads();
     }
-    // warm start, colour by colour
-    for (int c = 0; c < nrounds; ++c)
+    __syncthreads();
+
+    // 3. warm start, then the iterations, colour by colour
+    for (int it = -1; it < d.iterations; ++it)
     {
-        for (int k = tid; k < ccount[c]; k += nt)
+        for (int c = 0; c < ncol; ++c)
         {
-            int p = int(d.order[ms + cstart[c] + k]);
-            uint64_t v = sval[p];
-            BodyRef<T> A = body_ref(d, int(v >> 32), cache), B = body_ref(d, int(v & 0xFFFFFFFFu), cache);
-            uint8_t mask = d.rowmask[p];
-            for (int q = 0; q < 4; ++q)
+            const int cs = ms + cstart[c], cn = ccount[c];
+            for (int k = tid; k < cn; k += nt)
             {
-                if (!(mask & (1u << q))) continue;
-                const Row<T> &r = d.rows[4 * p + q];
-                warm_row(A, B, r.n, r.wa_n, r.wb_n, r.acc[0]);
-                warm_row(A, B, r.t1, r.wa_t1, r.wb_t1, r.acc[1]);
-                warm_row(A, B, r.t2, r.wa_t2, r.wb_t2, r.acc[2]);
-            }
-        }
-        __syncthreads();
-    }
-    for (int it = 0; it < d.iterations; ++it)
-    {
-        for (int c = 0; c < nrounds; ++c)
-        {
-            for (int k = tid; k < ccount[c]; k += nt)
-            {
-                int p = int(d.order[ms + cstart[c] + k]);
-                uint64_t v = sval[p];
-                BodyRef<T> A = body_ref(d, int(v >> 32), cache), B = body_ref(d, int(v & 0xFFFFFFFFu), cache);
-                uint8_t mask = d.rowmask[p];
-                for (int q = 0; q < 4; ++q)
-                {
-                    if (!(mask & (1u << q))) continue;
-                    solve_contact(A, B, d.rows[4 * p + q]);
-                }
+                int p = int(d.order[cs + k]);
+                solve_manifold(d, p, sval[p], cache, it < 0);
             }
             __syncthreads();
         }
     }
     if (cache)
     {
-        for (int p = ms + tid; p < me; p += nt)
+        for (int k = tid; k < na; k += nt)
         {
-            if (!d.rowmask[p]) continue;
-            uint64_t v = sval[p];
+            uint64_t v = sval[act[k]];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
             if (!(d.meta[a].flags & BODY_STATIC)) d.vel[a] = cache[d.meta[a].local];
             if (!(d.meta[b].flags & BODY_STATIC)) d.vel[b] = cache[d.meta[b].local];
         }
     }
-    // write back accumulated impulses into the manifold cache
-    for (int p = ms + tid; p < me; p += nt)
+    // 4. write the accumulated impulses back into the manifold cache
+    for (int k = tid; k < na; k += nt)
     {
+        int p = act[k];
         uint8_t mask = d.rowmask[p];
         for (int q = 0; q < 4; ++q)
         {

@@ -162,6 +162,8 @@ public:
         PK_CUDA(alloc(&d.rows, 4 * P));
         PK_CUDA(alloc(&d.rowmask, P));
         PK_CUDA(alloc(&d.colour, P));
+        PK_CUDA(alloc(&d.colour_tmp, P));
+        PK_CUDA(alloc(&d.pair_colour, P));
         PK_CUDA(alloc(&d.order, P));
         PK_CUDA(alloc(&d.owner, N));
         int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
@@ -531,7 +533,7 @@ public:
         std::vector<uint64_t> k(np > 0 ? np : 1);
         if (np > 0)
         {
-            PK_CUDA(cudaMemcpy(col.data(), d_.colour, sizeof(int) * np, cudaMemcpyDeviceToHost));
+            PK_CUDA(cudaMemcpy(col.data(), d_.pair_colour, sizeof(int) * np, cudaMemcpyDeviceToHost));
             PK_CUDA(cudaMemcpy(k.data(), d_.key_old, sizeof(uint64_t) * np, cudaMemcpyDeviceToHost));
         }
         if (nc0) PK_CUDA(cudaMemcpy(nc0, d_.ncolours, sizeof(int), cudaMemcpyDeviceToHost));
@@ -674,7 +676,7 @@ private:
                       d_.wroot, d_.mstart, d_.mend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.old_idx, d_.gjk_list,
-                      d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour,
+                      d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_};
