@@ -295,6 +295,8 @@ def run_ours(a, rank, world_size, local_rank):
            "stage_ms_per_step": {k: round(v, 4) for k, v in per_stage.items()},
            "counts": {"pairs": P, "contacts": Cn, "gjk": info["gjk"], "epa": info["epa"],
                       "gjk_large_mesh": info["gjk_large_mesh"], "epa_large_mesh": info["epa_large_mesh"],
+                      "gjk_iterations": info["gjk_iterations"], "epa_iterations": info["epa_iterations"],
+                      "epa_iterations_large_mesh": info["epa_iterations_large_mesh"],
                       "status": info["flags"]}}
 
     if rank == 0 and not a.no_plain:

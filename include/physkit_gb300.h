@@ -94,6 +94,9 @@ typedef struct pk_step_info
     int32_t epa;      /* pairs that reached EPA (GJK found them intersecting) */
     int32_t gjk_large_mesh; /* of those, pairs involving a mesh above 32 vertices */
     int32_t epa_large_mesh;
+    int64_t gjk_iterations; /* GJK iterations summed over the last step's pairs */
+    int64_t epa_iterations; /* EPA expansions summed over the last step's pairs */
+    int64_t epa_iterations_large_mesh;
 } pk_step_info;
 
 /* Primitive shape for pk_collide: kind 0 aabb (p = min3 max3), 1 obb (p = center3 quat4 half3),

@@ -647,6 +647,9 @@ int pk_world_synchronize(pk_world *w, pk_step_info *info)
         info->epa = c.epa;
         info->gjk_large_mesh = c.gjk_heavy;
         info->epa_large_mesh = c.epa_heavy;
+        info->gjk_iterations = c.gjk_iters;
+        info->epa_iterations = c.epa_iters;
+        info->epa_iterations_large_mesh = c.epa_iters_heavy;
     }
     return c.status ? PK_ERR_DEVICE_STATUS : PK_OK;
 }

@@ -152,6 +152,7 @@ template <class T> struct Dev
     Simplex<T> *epa_simplex;
     int *epa_count;
     int *epa_count_heavy;
+    unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
     Row<T> *rows;
     uint8_t *rowmask;
     int *colour;      // solver scratch: compacted active manifolds of each world
@@ -226,6 +227,7 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.epa_count = 0;
         *d.gjk_count_heavy = 0;
         *d.epa_count_heavy = 0;
+        d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
         *d.epoch += 1;
     }
 }
@@ -763,7 +765,9 @@ __global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         Simplex<T> s;
-        if (gjk(A, B, s))
+        bool enclosed = gjk(A, B, s);
+        atomicAdd(d.np_iters, (unsigned long long)s.iters);
+        if (enclosed)
         {
             int j;
             if (A.ncl > 0 || B.ncl > 0)
@@ -799,6 +803,8 @@ __global__ void __launch_bounds__(128) k_narrow_epa(Dev<T> d, const uint64_t *__
         Collision<T> col;
         bool hit = epa(A, B, s, es, col);
         if (es.status) atomicOr(d.status, ST_EPA_CAP);
+        atomicAdd(d.np_iters + 1, (unsigned long long)es.iters);
+        if (A.ncl > 0 || B.ncl > 0) atomicAdd(d.np_iters + 2, (unsigned long long)es.iters);
         manifold_update(d, p, d.old_idx[p], A, B, hit, col);
     }
 }

@@ -37,6 +37,7 @@ struct StepCounters
     int status = 0;
     int launches = 0; // kernels one step launches
     int gjk = 0, gjk_heavy = 0, epa = 0, epa_heavy = 0; // narrowphase work items of the last step
+    long long gjk_iters = 0, epa_iters = 0, epa_iters_heavy = 0;
 };
 
 constexpr int kStages = 9;

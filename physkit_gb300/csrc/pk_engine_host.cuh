@@ -118,6 +118,7 @@ public:
         d.epa_count = counters_ + 7;
         d.gjk_count_heavy = counters_ + 8;
         d.epa_count_heavy = counters_ + 9;
+        d.np_iters = reinterpret_cast<unsigned long long *>(counters_ + 10); // counters 10..15
         int minus1 = -1;
         PK_CUDA(cudaMemcpy(d.epoch, &minus1, sizeof(int), cudaMemcpyHostToDevice));
         PK_CUDA(alloc(&d.wp, W));
@@ -394,6 +395,11 @@ public:
             c->gjk_heavy = h[8];
             c->epa = h[7] + h[9];
             c->epa_heavy = h[9];
+            unsigned long long it[3];
+            std::memcpy(it, h + 10, sizeof(it));
+            c->gjk_iters = (long long)it[0];
+            c->epa_iters = (long long)it[1];
+            c->epa_iters_heavy = (long long)it[2];
         }
         int zero = 0;
         PK_CUDA(cudaMemcpy(counters_ + 4, &zero, sizeof(int), cudaMemcpyHostToDevice));

@@ -163,6 +163,7 @@ template <class T> struct Simplex
 {
     SupPt<T> v[4];
     int n;
+    int iters; // GJK iterations used
     PK_HD void push(const SupPt<T> &p) { v[n++] = p; }
     PK_HD void erase(int i)
     {
@@ -284,6 +285,7 @@ template <class T> PK_HD bool gjk_simplex(Simplex<T> &s, V3<T> &dir)
 template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s)
 {
     s.n = 0;
+    s.iters = 0;
     V3<T> dir{T(1), T(0), T(0)};
     SupPt<T> pt = minkowski(A, B, dir);
     s.push(pt);
@@ -291,6 +293,7 @@ template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Si
     dir = -normalized(pt.p);
     for (int iter = 0; iter < 100; ++iter)
     {
+        s.iters = iter + 1;
         SupPt<T> np = minkowski(A, B, dir);
         if (dot(np.p, dir) <= T(0)) return false;
         s.push(np);
@@ -347,6 +350,7 @@ template <class T> struct EpaState
     uint16_t heap[kMaxFaces];
     int npoly, nfaces, nheap;
     int status;
+    int iters; // EPA expansions used
 
     // heap comparison used by the reference: comp(f1, f2) = dist(f1) > dist(f2)
     PK_HD bool comp(uint16_t f1, uint16_t f2) const { return faces[f1].d > faces[f2].d; }
@@ -467,6 +471,7 @@ template <class T>
 PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T> &e, Collision<T> &out)
 {
     e.status = 0;
+    e.iters = 0;
     if (s.n < 4 && !pad_simplex(A, B, s)) return false;
     e.npoly = 4;
     for (int i = 0; i < 4; ++i) e.poly[i] = s.v[i];
@@ -501,6 +506,7 @@ PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaSta
     const T tol = T(1e-6);
     for (int iter = 0; iter < 64; ++iter)
     {
+        e.iters = iter + 1;
         int mf = e.pop_face();
         if (mf < 0) break;
         const EpaFace<T> minf = e.faces[mf];

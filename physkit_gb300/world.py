@@ -49,7 +49,8 @@ assert BODY_DTYPE.itemsize == 216
 
 class StepInfoC(C.Structure):
     _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("launches", C.c_int32),
-                ("gjk", C.c_int32), ("epa", C.c_int32), ("gjk_large_mesh", C.c_int32), ("epa_large_mesh", C.c_int32)]
+                ("gjk", C.c_int32), ("epa", C.c_int32), ("gjk_large_mesh", C.c_int32), ("epa_large_mesh", C.c_int32),
+                ("gjk_iterations", C.c_int64), ("epa_iterations", C.c_int64), ("epa_iterations_large_mesh", C.c_int64)]
 
 
 class CollideShapeC(C.Structure):
@@ -367,6 +368,8 @@ class World:
         self.last_info = {"pairs": info.pairs, "leaves": info.leaves, "status": info.status,
                           "launches": info.launches, "gjk": info.gjk, "epa": info.epa,
                           "gjk_large_mesh": info.gjk_large_mesh, "epa_large_mesh": info.epa_large_mesh,
+                          "gjk_iterations": info.gjk_iterations, "epa_iterations": info.epa_iterations,
+                          "epa_iterations_large_mesh": info.epa_iterations_large_mesh,
                           "flags": [v for k, v in STATUS_BITS.items() if info.status & k]}
         return self.last_info
 
