@@ -65,7 +65,7 @@ struct pk_world
     pk::EngineConfig cfg;
     pk_world_desc desc;
     std::vector<double> verts;   // all shape vertices
-    std::vector<int> ranges;     // (vertex start, vertex count, cluster start, cluster count) per shape
+    std::vector<int> ranges;     // 8 ints per shape: vertices, clusters, groups (start, count), 2 pad
     std::vector<double> clusters; // (centre xyz, radius) per cluster of 8 consecutive vertices
     std::vector<double> rmax;     // bounding radius of each shape about its origin
     std::vector<double> boxes;   // local aabb per shape
@@ -162,7 +162,7 @@ int pk_collide_noalloc(pk_world *w, const pk_collide_shape *a, const pk_collide_
 {
     if (!w || n < 0 || (n > 0 && (!a || !b || !out || !hit))) return PK_ERR_INVALID;
     if (n > kNoAllocMax) return PK_ERR_CAPACITY; // larger batches: split them, or use pk_collide
-    int nshapes = int(w->ranges.size() / 4);
+    int nshapes = int(w->ranges.size() / 8);
     for (int i = 0; i < n; ++i)
         for (const pk_collide_shape *s : {a + i, b + i})
         {
@@ -289,7 +289,7 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
 {
     size_t nv = v.size() / 3;
     if (nv == 0) return PK_ERR_INVALID;
-    if (w->verts.size() / 3 + nv > size_t(w->cfg.vert_cap) || w->ranges.size() / 4 + 1 > size_t(w->cfg.shape_cap))
+    if (w->verts.size() / 3 + nv > size_t(w->cfg.vert_cap) || w->ranges.size() / 8 + 1 > size_t(w->cfg.shape_cap))
         return PK_ERR_CAPACITY;
     // aabb::from_points (bounds.h:33-49)
     double mn[3] = {v[0], v[1], v[2]}, mx[3] = {v[0], v[1], v[2]};
@@ -300,7 +300,7 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
             mn[k] = (x < mn[k]) ? x : mn[k];
             mx[k] = (mx[k] < x) ? x : mx[k];
         }
-    int id = int(w->ranges.size() / 4);
+    int id = int(w->ranges.size() / 8);
     // Bounding spheres of blocks of 8 consecutive vertices (large meshes only): they let the
     // device support search skip blocks that cannot hold the maximum.
     double rm = 0.0;
@@ -327,10 +327,35 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
             ++ncl;
         }
     }
+    // groups of 8 consecutive blocks (64 vertices), bounded the same way
+    int gstart = int(w->clusters.size() / 4), ngr = 0;
+    if (ncl > 0)
+    {
+        for (size_t b = 0; b < nv; b += 64)
+        {
+            size_t e = b + 64 < nv ? b + 64 : nv;
+            double c[3] = {0, 0, 0};
+            for (size_t i = b; i < e; ++i)
+                for (int k = 0; k < 3; ++k) c[k] += v[3 * i + k] / double(e - b);
+            double r = 0.0;
+            for (size_t i = b; i < e; ++i)
+            {
+                double dx = v[3 * i] - c[0], dy = v[3 * i + 1] - c[1], dz = v[3 * i + 2] - c[2];
+                r = std::fmax(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+            r = r * (1.0 + 1e-9) + 1e-6 * rm;
+            w->clusters.insert(w->clusters.end(), {c[0], c[1], c[2], r});
+            ++ngr;
+        }
+    }
     w->ranges.push_back(int(w->verts.size() / 3));
     w->ranges.push_back(int(nv));
     w->ranges.push_back(cstart);
     w->ranges.push_back(ncl);
+    w->ranges.push_back(gstart);
+    w->ranges.push_back(ngr);
+    w->ranges.push_back(0);
+    w->ranges.push_back(0);
     w->rmax.push_back(rm);
     w->verts.insert(w->verts.end(), v.begin(), v.end());
     for (int k = 0; k < 3; ++k) w->boxes.push_back(mn[k]);
@@ -431,7 +456,7 @@ int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)
 int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out)
 {
     if (!w || (n > 0 && !descs)) return PK_ERR_INVALID;
-    int nshapes = int(w->ranges.size() / 4);
+    int nshapes = int(w->ranges.size() / 8);
     for (int i = 0; i < n; ++i)
     {
         const pk_body_desc &d = descs[i];
@@ -822,7 +847,7 @@ int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t
 int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out, int32_t *hit)
 {
     if (!w || n < 0 || (n > 0 && (!a || !b || !out || !hit))) return PK_ERR_INVALID;
-    int nshapes = int(w->ranges.size() / 4);
+    int nshapes = int(w->ranges.size() / 8);
     for (int i = 0; i < n; ++i)
     {
         for (const pk_collide_shape *s : {a + i, b + i})

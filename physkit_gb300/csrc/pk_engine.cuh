@@ -99,6 +99,13 @@ template <class T> struct WorldParams
     int pad;
 };
 
+// Where a shape's data lives: vertices, vertex-block bounds (clusters of 8) and bounds of groups of
+// 8 clusters, the latter two in one array of (centre xyz, radius) records.
+struct ShapeRange
+{
+    int vstart, nverts, cstart, ncl, gstart, ngr, pad0, pad1;
+};
+
 template <class T> struct Dev
 {
     // bodies
@@ -112,7 +119,7 @@ template <class T> struct Dev
     const int *nslots;
     // shapes
     const T *verts;
-    const int4 *shape_range; // vertex start, vertex count, cluster start, cluster count
+    const ShapeRange *shape_range;
     const Aabb<T> *shape_box;
     const T *clusters;       // 4 per cluster: centre xyz, radius
     const T *shape_rmax;     // bounding radius about the shape origin
@@ -527,12 +534,14 @@ template <class T> __device__ __forceinline__ ShapeRef<T> body_shape(const Dev<T
 {
     ShapeRef<T> s;
     const Meta m = d.meta[slot];
-    int4 r = d.shape_range[m.shape];
+    const ShapeRange r = d.shape_range[m.shape];
     s.kind = SHAPE_MESH;
-    s.nverts = r.y;
-    s.verts = d.verts + 3 * r.x;
-    s.ncl = r.w;
-    s.cl = d.clusters + 4 * r.z;
+    s.nverts = r.nverts;
+    s.verts = d.verts + 3 * r.vstart;
+    s.ncl = r.ncl;
+    s.cl = d.clusters + 4 * r.cstart;
+    s.ngr = r.ngr;
+    s.gr = d.clusters + 4 * r.gstart;
     s.rmax = d.shape_rmax[m.shape];
     const Pose<T> &p = d.pose[slot];
     s.pos = ld3(p.p);
@@ -1318,7 +1327,7 @@ struct ShapeSpec
     double p[10];
 };
 template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const ShapeSpec *sb, int n, const T *verts,
-                                                   const int4 *ranges, const T *clusters, const T *rmax,
+                                                   const ShapeRange *ranges, const T *clusters, const T *rmax,
                                                    double *out, int *hit, int *status)
 {
     PK_GRID_STRIDE(i, n)
@@ -1334,6 +1343,8 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
             r.verts = nullptr;
             r.ncl = 0;
             r.cl = nullptr;
+            r.ngr = 0;
+            r.gr = nullptr;
             r.rmax = T(0);
             r.q = Qt<T>{T(1), T(0), T(0), T(0)};
             r.pos = r.a = r.b = V3<T>{T(0), T(0), T(0)};
@@ -1352,11 +1363,13 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
             {
                 r.pos = V3<T>{T(q.p[0]), T(q.p[1]), T(q.p[2])};
                 r.q = Qt<T>{T(q.p[3]), T(q.p[4]), T(q.p[5]), T(q.p[6])};
-                int4 rg = ranges[q.shape];
-                r.verts = verts + 3 * rg.x;
-                r.nverts = rg.y;
-                r.ncl = rg.w;
-                r.cl = clusters + 4 * rg.z;
+                const ShapeRange rg = ranges[q.shape];
+                r.verts = verts + 3 * rg.vstart;
+                r.nverts = rg.nverts;
+                r.ncl = rg.ncl;
+                r.cl = clusters + 4 * rg.cstart;
+                r.ngr = rg.ngr;
+                r.gr = clusters + 4 * rg.gstart;
                 r.rmax = rmax[q.shape];
             }
         }

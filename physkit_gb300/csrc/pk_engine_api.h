@@ -49,8 +49,9 @@ public:
     virtual ~EngineBase() = default;
     virtual int precision_bits() const = 0;
     virtual int init(const EngineConfig &cfg) = 0;
-    // ranges: 4 ints per shape (vertex start, vertex count, cluster start, cluster count);
-    // clusters: 4 doubles per cluster (centre, radius); rmax: bounding radius per shape.
+    // ranges: 8 ints per shape (vertex start/count, cluster start/count, group start/count, 2 pad);
+    // clusters: 4 doubles per record (centre, radius), vertex blocks and groups of blocks;
+    // rmax: bounding radius per shape.
     virtual int set_shapes(const std::vector<double> &verts, const std::vector<int> &ranges,
                            const std::vector<double> &boxes, const std::vector<double> &clusters,
                            const std::vector<double> &rmax) = 0;

@@ -186,7 +186,7 @@ public:
                    const std::vector<double> &boxes, const std::vector<double> &clusters,
                    const std::vector<double> &rmax) override
     {
-        size_t nv = verts.size() / 3, ns = ranges.size() / 4, nc = clusters.size() / 4;
+        size_t nv = verts.size() / 3, ns = ranges.size() / 8, nc = clusters.size() / 4;
         if (nv > size_t(cfg_.vert_cap) || ns > size_t(cfg_.shape_cap)) return -3;
         std::vector<T> v(verts.size());
         for (size_t i = 0; i < verts.size(); ++i) v[i] = T(verts[i]);
@@ -610,7 +610,7 @@ private:
     Manifold<T> *man_[2] = {nullptr, nullptr};
     uint64_t *last_sval_ = nullptr;
     uint32_t *hist_ = nullptr;
-    int4 *shape_range_ = nullptr;
+    ShapeRange *shape_range_ = nullptr;
     Aabb<T> *shape_box_ = nullptr;
     T *shape_rmax_ = nullptr;
     T *clusters_ = nullptr;

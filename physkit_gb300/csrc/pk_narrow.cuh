@@ -59,6 +59,8 @@ template <class T> struct ShapeRef
     Qt<T> q;
     int ncl;
     const T *cl;
+    int ngr;       // groups of kClusterSize consecutive clusters (64 vertices), same layout
+    const T *gr;
     T rmax;
 
     // First strictly maximal vertex of v.ld over the vertex list, in index order.
@@ -83,13 +85,27 @@ template <class T> struct ShapeRef
     {
         T dn = norm(ld);
         T margin = T(64) * EpsOf<T>::v * rmax * dn;
-        int kb = 0;
+        // seed: the best cluster of the best group gives the value B of an actual vertex
+        int g0 = 0;
+        T ubg = T(0);
+        for (int g = 0; g < ngr; ++g)
+        {
+            const T *c = gr + 4 * g;
+            T ub = c[0] * ld.x + c[1] * ld.y + c[2] * ld.z + c[3] * dn;
+            if (g == 0 || ub > ubg)
+            {
+                ubg = ub;
+                g0 = g;
+            }
+        }
+        int klo = g0 * kClusterSize, khi = klo + kClusterSize < ncl ? klo + kClusterSize : ncl;
+        int kb = klo;
         T ub_best = T(0);
-        for (int k = 0; k < ncl; ++k)
+        for (int k = klo; k < khi; ++k)
         {
             const T *c = cl + 4 * k;
             T ub = c[0] * ld.x + c[1] * ld.y + c[2] * ld.z + c[3] * dn;
-            if (k == 0 || ub > ub_best)
+            if (k == klo || ub > ub_best)
             {
                 ub_best = ub;
                 kb = k;
@@ -98,15 +114,21 @@ template <class T> struct ShapeRef
         T B;
         int lo = kb * kClusterSize, hi = lo + kClusterSize < nverts ? lo + kClusterSize : nverts;
         argmax_linear(ld, lo, hi, -1, B);
+        // every vertex whose value can reach B lies in a cluster and a group whose bound reaches B
         int best = -1;
         T bd = T(0);
-        for (int k = 0; k < ncl; ++k)
+        for (int g = 0; g < ngr; ++g)
         {
-            const T *c = cl + 4 * k;
-            T ub = c[0] * ld.x + c[1] * ld.y + c[2] * ld.z + c[3] * dn + margin;
-            if (ub < B) continue;
-            int l = k * kClusterSize, h = l + kClusterSize < nverts ? l + kClusterSize : nverts;
-            best = argmax_linear(ld, l, h, best, bd);
+            const T *c = gr + 4 * g;
+            if (c[0] * ld.x + c[1] * ld.y + c[2] * ld.z + c[3] * dn + margin < B) continue;
+            int k1 = g * kClusterSize, k2 = k1 + kClusterSize < ncl ? k1 + kClusterSize : ncl;
+            for (int k = k1; k < k2; ++k)
+            {
+                const T *cc = cl + 4 * k;
+                if (cc[0] * ld.x + cc[1] * ld.y + cc[2] * ld.z + cc[3] * dn + margin < B) continue;
+                int l = k * kClusterSize, h = l + kClusterSize < nverts ? l + kClusterSize : nverts;
+                best = argmax_linear(ld, l, h, best, bd);
+            }
         }
         return best;
     }

@@ -51,16 +51,16 @@ static int check_heap(std::mt19937_64 &rng)
     return bad;
 }
 
-template <class T> static std::vector<T> make_clusters(const std::vector<double> &v, double &rm)
+template <class T> static std::vector<T> make_clusters(const std::vector<double> &v, double &rm, size_t block = 8)
 {
     size_t nv = v.size() / 3;
     rm = 0;
     for (size_t i = 0; i < nv; ++i)
         rm = std::fmax(rm, std::sqrt(v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]));
     std::vector<T> c;
-    for (size_t b = 0; b < nv; b += 8)
+    for (size_t b = 0; b < nv; b += block)
     {
-        size_t e = std::min(b + 8, nv);
+        size_t e = std::min(b + block, nv);
         double cc[3] = {0, 0, 0};
         for (size_t i = b; i < e; ++i)
             for (int k = 0; k < 3; ++k) cc[k] += v[3 * i + k] / double(e - b);
@@ -84,12 +84,15 @@ template <class T> static int check_support(const std::vector<double> &vd, std::
     std::vector<T> v(vd.begin(), vd.end());
     double rm;
     std::vector<T> cl = make_clusters<T>(vd, rm);
+    std::vector<T> gr = make_clusters<T>(vd, rm, 64);
     ShapeRef<T> s{};
     s.kind = SHAPE_MESH;
     s.nverts = int(v.size() / 3);
     s.verts = v.data();
     s.ncl = int(cl.size() / 4);
     s.cl = cl.data();
+    s.ngr = int(gr.size() / 4);
+    s.gr = gr.data();
     s.rmax = T(rm);
     std::normal_distribution<double> nd(0.0, 1.0);
     int bad = 0;
