@@ -18,7 +18,6 @@
 #pragma once
 
 #include "pk_math.cuh"
-#include "pk_epa_warp.cuh"
 #include "pk_narrow.cuh"
 #include "pk_sort.cuh"
 
@@ -795,20 +794,13 @@ __global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__
     }
 }
 
-// Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, one warp per pair with
-// the polytope in shared memory, then the manifold update.
-constexpr int kEpaWarpsPerBlock = 2;
-
+// Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, then the manifold update.
 template <class T>
-__global__ void __launch_bounds__(32 * kEpaWarpsPerBlock) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
+__global__ void __launch_bounds__(128) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    extern __shared__ __align__(16) unsigned char epa_smem[];
-    const int lane = threadIdx.x & 31;
-    WarpEpa<T> &W = reinterpret_cast<WarpEpa<T> *>(epa_smem)[threadIdx.x >> 5];
     const int nh = *d.epa_count_heavy;
     const int n = nh + *d.epa_count;
-    const int nwarps = gridDim.x * kEpaWarpsPerBlock;
-    for (int i = blockIdx.x * kEpaWarpsPerBlock + (threadIdx.x >> 5); i < n; i += nwarps)
+    PK_GRID_STRIDE(i, n)
     {
         int j = list_slot(i, nh, d.pair_cap);
         int p = d.epa_list[j];
@@ -816,16 +808,13 @@ __global__ void __launch_bounds__(32 * kEpaWarpsPerBlock) k_narrow_epa(Dev<T> d,
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         Simplex<T> s = d.epa_simplex[j];
+        EpaState<T> es;
         Collision<T> col;
-        bool hit = warp_epa(A, B, s, W, col, lane);
-        if (lane == 0)
-        {
-            if (W.e.status) atomicOr(d.status, ST_EPA_CAP);
-            atomicAdd(d.np_iters + 1, (unsigned long long)W.e.iters);
-            if (A.ncl > 0 || B.ncl > 0) atomicAdd(d.np_iters + 2, (unsigned long long)W.e.iters);
-            manifold_update(d, p, d.old_idx[p], A, B, hit, col);
-        }
-        __syncwarp();
+        bool hit = epa(A, B, s, es, col);
+        if (es.status) atomicOr(d.status, ST_EPA_CAP);
+        atomicAdd(d.np_iters + 1, (unsigned long long)es.iters);
+        if (A.ncl > 0 || B.ncl > 0) atomicAdd(d.np_iters + 2, (unsigned long long)es.iters);
+        manifold_update(d, p, d.old_idx[p], A, B, hit, col);
     }
 }
 

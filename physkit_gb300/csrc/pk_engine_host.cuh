@@ -142,8 +142,6 @@ public:
         }
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
-        PK_CUDA(cudaFuncSetAttribute(k_narrow_epa<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(sizeof(WarpEpa<T>) * kEpaWarpsPerBlock)));
         for (int k = 0; k < 2; ++k)
         {
             PK_CUDA(alloc(&mkey_[k], N));
@@ -735,7 +733,7 @@ private:
         PK_CUDA(mark(5));
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
-        k_narrow_epa<T><<<sms_ * 8, 32 * kEpaWarpsPerBlock, sizeof(WarpEpa<T>) * kEpaWarpsPerBlock, st_>>>(d, pv);
+        k_narrow_epa<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         PK_CUDA(mark(7));
