@@ -56,7 +56,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
 
     def compile_one(name):
         obj = os.path.join(OUT, name.replace(".cu", ".o"))
-        cmd = [nv, *ARCH, *COMMON, *UNITS[name], "-c", os.path.join(SRC, name), "-o", obj]
+        extra = os.environ.get("PK_NVCC_FLAGS", "").split()  # optional extra nvcc flags
+        cmd = [nv, *ARCH, *COMMON, *UNITS[name], *extra, "-c", os.path.join(SRC, name), "-o", obj]
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -762,8 +762,15 @@ __device__ __forceinline__ int list_slot(int i, int nheavy, int cap)
 
 // Narrowphase pass 2: GJK (collision.cpp:165-189) over the queued pairs; enclosing simplices are
 // queued for EPA, the rest are settled without a new contact.
+#ifndef PK_GJK_MIN_BLOCKS
+#define PK_GJK_MIN_BLOCKS 1
+#endif
+#ifndef PK_EPA_MIN_BLOCKS
+#define PK_EPA_MIN_BLOCKS 1
+#endif
+
 template <class T>
-__global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
+__global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.gjk_count_heavy;
     const int n = nh + *d.gjk_count;
@@ -796,7 +803,7 @@ __global__ void __launch_bounds__(128) k_narrow_gjk(Dev<T> d, const uint64_t *__
 
 // Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, then the manifold update.
 template <class T>
-__global__ void __launch_bounds__(128) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
+__global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.epa_count_heavy;
     const int n = nh + *d.epa_count;
