@@ -763,10 +763,10 @@ __device__ __forceinline__ int list_slot(int i, int nheavy, int cap)
 // Narrowphase pass 2: GJK (collision.cpp:165-189) over the queued pairs; enclosing simplices are
 // queued for EPA, the rest are settled without a new contact.
 #ifndef PK_GJK_MIN_BLOCKS
-#define PK_GJK_MIN_BLOCKS 1
+#define PK_GJK_MIN_BLOCKS 5
 #endif
 #ifndef PK_EPA_MIN_BLOCKS
-#define PK_EPA_MIN_BLOCKS 1
+#define PK_EPA_MIN_BLOCKS 4
 #endif
 
 template <class T>
