@@ -464,11 +464,14 @@ template <class T> __device__ __forceinline__ bool pair_allowed(const Meta &a, c
     return re >= cr;
 }
 
+// Threads take bodies in Morton (leaf) order, so a warp's queries are spatially close and walk
+// similar paths through the tree.
 template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    const int n = *d.nslots;
-    PK_GRID_STRIDE(i, n)
+    const int n = *d.nleaf;
+    PK_GRID_STRIDE(leaf, n)
     {
+        const int i = int(sval[leaf]);
         Meta mi = d.meta[i];
         if (!(mi.flags & BODY_ALIVE) || (mi.flags & BODY_STATIC) || !d.wp[mi.world].active) continue;
         int root = d.wroot[mi.world];

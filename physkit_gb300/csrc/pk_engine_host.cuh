@@ -722,7 +722,7 @@ private:
         k_zero_ints<<<gb, 256, 0, st_>>>(d.refit_flag, N);
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
         PK_CUDA(mark(3));
-        k_traverse<T><<<gb, 128, 0, st_>>>(d, sval);
+        k_traverse<T><<<(N + 127) / 128, 128, 0, st_>>>(d, sval);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
         PK_CUDA(mark(4));
         bool p1 = radix_sort<uint64_t>(pkey_[0], pval_[0], pkey_[1], pval_[1], d.npairs,

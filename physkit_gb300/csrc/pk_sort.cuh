@@ -48,7 +48,17 @@ static __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict_
     int per = (count + 1023) / 1024;
     int lo = threadIdx.x * per, hi = min(count, lo + per);
     uint32_t s = 0;
-    for (int i = lo; i < hi; ++i) s += hist[i];
+    int i = lo;
+    // eight independent loads in flight per thread instead of a chain of dependent ones
+    for (; i + 8 <= hi; i += 8)
+    {
+        uint32_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = hist[i + k];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s += v[k];
+    }
+    for (; i < hi; ++i) s += hist[i];
     part[threadIdx.x] = s;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1)
@@ -59,7 +69,20 @@ static __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict_
         __syncthreads();
     }
     uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-    for (int i = lo; i < hi; ++i)
+    i = lo;
+    for (; i + 8 <= hi; i += 8)
+    {
+        uint32_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = hist[i + k];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            hist[i + k] = run;
+            run += v[k];
+        }
+    }
+    for (; i < hi; ++i)
     {
         uint32_t v = hist[i];
         hist[i] = run;
