@@ -127,9 +127,14 @@ int pk_shape_pyramid(pk_world *w, double base_half, double height, int32_t *out_
 int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out_handles);
 /* world_base::remove_rigid (world.h:209-218): drops the body, its pairs and manifolds. */
 int pk_body_remove(pk_world *w, uint64_t handle);
-/* Retire a whole sub-world (all its bodies) and free its slots for reuse. */
+/* Retire a whole sub-world (all its bodies, pairs and manifolds) and free its slots for reuse. */
 int pk_world_clear(pk_world *w, int32_t world);
+/* Worlds that are not active sit out the following steps unchanged: no integration, and their
+ * pairs and manifolds are carried over, so a world's trajectory depends only on how many steps it
+ * took, not on which batched steps those were. */
 int pk_world_set_active(pk_world *w, int32_t world, int32_t active);
+/* One flag per world (n = max_worlds), enqueued on the world's stream (no synchronisation). */
+int pk_world_set_active_mask(pk_world *w, const uint8_t *mask, int32_t n);
 int pk_world_set_gravity(pk_world *w, int32_t world, const double gravity[3]);
 
 /* One world step: world::step_impl (src/world.cpp:20-56) on the device. pk_world_step waits for

@@ -596,24 +596,38 @@ int pk_world_clear(pk_world *w, int32_t world)
 {
     if (!w || world < 0 || world >= w->cfg.max_worlds) return PK_ERR_INVALID;
     SubWorld &sw = w->worlds[size_t(world)];
+    std::vector<int> dead;
     for (size_t l = 0; l < sw.local_slot.size(); ++l)
     {
         int slot = sw.local_slot[l];
-        if (slot >= 0 && w->slots[size_t(slot)].alive)
-        {
-            int rc = kill_slot(w, slot);
-            if (rc) return rc;
-        }
-        if (slot >= 0)
-        {
-            w->slots[size_t(slot)] = SlotInfo{};
-            w->free_slots.push_back(slot);
-        }
+        if (slot < 0) continue;
+        if (w->slots[size_t(slot)].alive) dead.push_back(slot);
+        w->slots[size_t(slot)] = SlotInfo{};
+        w->free_slots.push_back(slot);
+    }
+    // one kernel kills the bodies, one empties every cached manifold of the world
+    if (w->eng->kill_world(dead.data(), int(dead.size()), world))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
     }
     sw.local_slot.clear();
     sw.local_gen.clear();
     sw.local_alive.clear();
     sw.free_locals.clear();
+    w->order_dirty = true;
+    return PK_OK;
+}
+
+int pk_world_set_active_mask(pk_world *w, const uint8_t *mask, int32_t n)
+{
+    if (!w || !mask || n != w->cfg.max_worlds) return PK_ERR_INVALID;
+    for (int i = 0; i < n; ++i) w->worlds[size_t(i)].active = mask[i] ? 1 : 0;
+    if (w->eng->set_active_mask(mask, n))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
     return PK_OK;
 }
 

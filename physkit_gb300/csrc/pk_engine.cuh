@@ -146,6 +146,7 @@ template <class T> struct Dev
     // manifolds
     Manifold<T> *man_old;
     uint64_t *key_old;
+    uint64_t *val_old;     // slot pairs of last step's sorted pairs
     int *npairs_old;
     Manifold<T> *man_new;
     uint8_t *event;
@@ -740,6 +741,16 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
         }
         int old_idx = (lo < nold && d.key_old[lo] == key) ? lo : -1;
         d.old_idx[p] = old_idx;
+        if (!d.wp[world].active)
+        {
+            // carried pair of a world that sits out this step: unchanged, no event
+            if (old_idx >= 0)
+                d.man_new[p] = d.man_old[old_idx];
+            else
+                d.man_new[p].n = 0;
+            d.event[p] = 0;
+            continue;
+        }
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         V3<T> dc = B.pos - A.pos;
         T rs = A.rmax + B.rmax;
@@ -840,6 +851,12 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         int world = int(skey[p] >> (2 * d.lbits));
+        d.pair_colour[p] = -2;
+        if (!d.wp[world].active)
+        {
+            d.rowmask[p] = 0;
+            continue;
+        }
         const Manifold<T> &m = d.man_new[p];
         const Pose<T> &PA = d.pose[sa];
         const Pose<T> &PB = d.pose[sb];
@@ -920,7 +937,6 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
             mask |= uint8_t(1u << k);
         }
         d.rowmask[p] = mask;
-        d.pair_colour[p] = -2;
     }
 }
 
@@ -1308,10 +1324,58 @@ template <class T> __global__ void k_integrate_pos(Dev<T> d, T dt)
     }
 }
 
-template <class T> __global__ void k_finish(Dev<T> d, const uint64_t *__restrict__ skey)
+// Worlds that sit out this step keep last step's pairs (and, through them, their manifolds and
+// warm-start impulses), so a world's trajectory does not depend on which steps it skipped.
+template <class T> __global__ void k_carry_pairs(Dev<T> d)
+{
+    const int nold = *d.npairs_old;
+    PK_GRID_STRIDE(p, nold)
+    {
+        uint64_t key = d.key_old[p];
+        int world = int(key >> (2 * d.lbits));
+        if (d.wp[world].active) continue;
+        uint64_t val = d.val_old[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        if (!(d.meta[sa].flags & BODY_ALIVE) || !(d.meta[sb].flags & BODY_ALIVE)) continue;
+        int slot = atomicAdd(d.npairs, 1);
+        if (slot < d.pair_cap)
+        {
+            d.pkey[slot] = key;
+            d.pval[slot] = val;
+        }
+        else
+            atomicOr(d.status, ST_PAIR_OVERFLOW);
+    }
+}
+
+// Retiring a world: every cached manifold of its pairs becomes empty.
+template <class T> __global__ void k_purge_world(Dev<T> d, uint32_t world)
+{
+    const int n = *d.npairs_old;
+    PK_GRID_STRIDE(p, n)
+    {
+        if (uint32_t(d.key_old[p] >> (2 * d.lbits)) == world) d.man_old[p].n = 0;
+    }
+}
+
+template <class T> __global__ void k_kill_bodies(Dev<T> d, const int *slots, int n)
+{
+    PK_GRID_STRIDE(i, n) d.meta[slots[i]].flags = 0;
+}
+
+template <class T> __global__ void k_set_active(Dev<T> d, const uint8_t *mask, int n)
+{
+    PK_GRID_STRIDE(w, n) d.wp[w].active = mask[w] ? 1 : 0;
+}
+
+template <class T> __global__ void k_finish(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
 {
     const int np = *d.npairs;
-    PK_GRID_STRIDE(p, np) d.key_old[p] = skey[p];
+    PK_GRID_STRIDE(p, np)
+    {
+        d.key_old[p] = skey[p];
+        d.val_old[p] = sval[p];
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) *d.npairs_old = np;
 }
 

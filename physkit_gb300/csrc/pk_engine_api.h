@@ -58,6 +58,8 @@ public:
     virtual int set_world(int w, const double g[3], double gnorm, int active) = 0;
     virtual int upload_bodies(const int *slots, const HostBody *b, int n, int nslots) = 0;
     virtual int kill_body(int slot, int world, int local) = 0;
+    virtual int kill_world(const int *slots, int n, int world) = 0; // all bodies of a world at once
+    virtual int set_active_mask(const uint8_t *mask, int n) = 0;    // stream-ordered, no sync
     // solver schedule (largest worlds first) and local indices in use per world
     virtual int set_world_order(const int *order, const int *nlocal, int n) = 0;
     virtual int step(double dt) = 0;                 // enqueue only

@@ -155,6 +155,7 @@ public:
         PK_CUDA(alloc(&d.leaf_parent, N));
         PK_CUDA(alloc(&d.refit_flag, N));
         PK_CUDA(alloc(&d.key_old, P));
+        PK_CUDA(alloc(&d.val_old, P));
         PK_CUDA(alloc(&d.event, P));
         PK_CUDA(alloc(&d.old_idx, P));
         PK_CUDA(alloc(&d.gjk_list, P));
@@ -305,6 +306,34 @@ public:
         }
         int limit = int(kMaxSolveSmem / sizeof(Vel<T>));
         big_cache_ = maxl <= limit ? maxl : 0;
+        return 0;
+    }
+
+    int kill_world(const int *slots, int n, int world) override
+    {
+        Dev<T> d = d_;
+        d.man_old = man_[parity_];
+        if (n > 0)
+        {
+            int *ds;
+            PK_CUDA(cudaMallocAsync(&ds, sizeof(int) * size_t(n), st_));
+            PK_CUDA(cudaMemcpyAsync(ds, slots, sizeof(int) * size_t(n), cudaMemcpyHostToDevice, st_));
+            k_kill_bodies<T><<<grid(n), 256, 0, st_>>>(d, ds, n);
+            PK_CUDA(cudaFreeAsync(ds, st_));
+        }
+        k_purge_world<T><<<grid(cfg_.pair_cap), 256, 0, st_>>>(d, uint32_t(world));
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int set_active_mask(const uint8_t *mask, int n) override
+    {
+        if (n != cfg_.max_worlds) return -3;
+        if (!mask_dev_) PK_CUDA(cudaMalloc(&mask_dev_, size_t(cfg_.max_worlds)));
+        PK_CUDA(cudaMemcpyAsync(mask_dev_, mask, size_t(n), cudaMemcpyHostToDevice, st_));
+        k_set_active<T><<<grid(n), 256, 0, st_>>>(d_, mask_dev_, n);
+        PK_CUDA(cudaGetLastError());
         return 0;
     }
 
@@ -622,6 +651,7 @@ private:
     int big_cache_ = 0;
     bool timing_ = false;
     bool capturing_ = false;
+    uint8_t *mask_dev_ = nullptr;
     int launches_ = 0;
     std::vector<cudaEvent_t> events_; // kStages + 1 per timed step
     int timed_steps_ = 0;
@@ -681,11 +711,11 @@ private:
         void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
                       d_.wroot, d_.mstart, d_.mend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
-                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.event, d_.old_idx, d_.gjk_list,
+                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list,
                       d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
-                      shape_rmax_, clusters_};
+                      shape_rmax_, clusters_, mask_dev_};
         for (void *p : ps)
             if (p) cudaFree(p);
         for (cudaEvent_t e : events_) cudaEventDestroy(e);
@@ -706,7 +736,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 14 + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 15 + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -723,6 +753,7 @@ private:
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
         PK_CUDA(mark(3));
         k_traverse<T><<<(N + 127) / 128, 128, 0, st_>>>(d, sval);
+        k_carry_pairs<T><<<gp, 256, 0, st_>>>(d);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
         PK_CUDA(mark(4));
         bool p1 = radix_sort<uint64_t>(pkey_[0], pval_[0], pkey_[1], pval_[1], d.npairs,
@@ -744,7 +775,7 @@ private:
                 d, pv, big_worlds_, kSmallWorld);
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
-        k_finish<T><<<gp, 256, 0, st_>>>(d, pk);
+        k_finish<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         PK_CUDA(mark(9));
         if (timing_ && !capturing_) ++timed_steps_;
         PK_CUDA(cudaGetLastError());

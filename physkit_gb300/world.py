@@ -83,6 +83,7 @@ def lib():
             "pk_body_remove": (C.c_int, [vp, C.c_uint64]),
             "pk_world_clear": (C.c_int, [vp, C.c_int32]),
             "pk_world_set_active": (C.c_int, [vp, C.c_int32, C.c_int32]),
+            "pk_world_set_active_mask": (C.c_int, [vp, P(C.c_uint8), C.c_int32]),
             "pk_world_set_gravity": (C.c_int, [vp, C.c_int32, dp]),
             "pk_world_step": (C.c_int, [vp, C.c_double]),
             "pk_world_step_async": (C.c_int, [vp, C.c_double]),
@@ -339,10 +340,15 @@ class World:
         return True
 
     def clear_world(self, w):
+        """Retire world w: its bodies, pairs and manifolds go; its slots become free."""
         _check(self.L.pk_world_clear(self.h, int(w)), "pk_world_clear")
 
     def set_active(self, w, active):
         _check(self.L.pk_world_set_active(self.h, int(w), int(bool(active))), "pk_world_set_active")
+
+    def set_active_mask(self, mask):
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        _check(self.L.pk_world_set_active_mask(self.h, _ptr(m, C.c_uint8), len(m)), "pk_world_set_active_mask")
 
     # stepping ----------------------------------------------------------------------------------
     def step(self, dt, check=True):
