@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--cpu-sample-worlds", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--served-rates", default="1000,5000,20000",
+                    help="Poisson request rates (req/s) for the served form; empty to skip")
+    ap.add_argument("--served-seconds", type=float, default=2.0)
     return ap.parse_args()
 
 
@@ -302,6 +306,13 @@ def run_ours(a, rank, world_size, local_rank):
     if rank == 0 and not a.no_plain:
         out["plain_single_world"] = plain_world(a)
         out["batched_vs_plain"] = value / world_size / out["plain_single_world"]["value"]
+    if rank == 0 and not a.no_precision:
+        out["precision_f32_vs_f64"] = precision_report()
+    if rank == 0 and a.served_rates:
+        from physkit_gb300.serve import run_served
+
+        out["served"] = [run_served(rate=float(r), duration=a.served_seconds, warm_live=256, max_worlds=1024,
+                                    max_bodies=1_500_000) for r in a.served_rates.split(",")]
     if rank == 0 and not a.no_cpu_baseline:
         kw = {"nworlds": a.worlds, "nmin": a.nmin, "nmax": a.nmax}
         sample = list(range(min(a.cpu_sample_worlds, a.worlds)))
@@ -315,6 +326,36 @@ def run_ours(a, rank, world_size, local_rank):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def precision_report(steps=240, n=1000):
+    """FP32 precision form against FP64 on config 1 (1,000 boxes), 240 steps. The FP64 run is the
+    device FP64 form, which is bit-identical to the FP64 oracle (tests/test_gpu_world_parity.py)."""
+    import numpy as np
+    from physkit_gb300 import scenes
+
+    scene = scenes.config1(n=n)
+    w32, _ = scenes.make_world(scene, precision="f32")
+    w64, _ = scenes.make_world(scene, precision="f64")
+    dyn = scene.bodies["type"] == 0
+    rep = {}
+    for s in range(1, steps + 1):
+        w32.step(scene.dt, check=False)
+        w64.step(scene.dt, check=False)
+        if s in (60, 120, 240):
+            a, b = w32.bodies()[dyn], w64.bodies()[dyn]
+            dpos = np.linalg.norm(a[:, 0:3] - b[:, 0:3], axis=1)
+            scale = np.maximum(np.linalg.norm(b[:, 0:3], axis=1), 1.0)
+            dq = 1.0 - np.abs(np.sum(a[:, 3:7] * b[:, 3:7], axis=1))
+            dv = np.linalg.norm(a[:, 7:10] - b[:, 7:10], axis=1)
+            rep[f"step{s}"] = {"pos_rel_max": float((dpos / scale).max()), "pos_rel_p50": float(np.median(dpos / scale)),
+                               "pos_abs_max_m": float(dpos.max()), "quat_1mdot_max": float(dq.max()),
+                               "vel_abs_max_mps": float(dv.max()),
+                               "pairs_f32_vs_f64": [int(len(w32.pairs())), int(len(w64.pairs()))]}
+    w32.close()
+    w64.close()
+    rep["workload"] = f"config1: {n} boxes + ground, dt=1/120; FP32 form vs FP64 form"
+    return rep
 
 
 def plain_world(a):
