@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--served-rates", default="1000,5000,20000",
                     help="Poisson request rates (req/s) for the served form; empty to skip")
     ap.add_argument("--served-seconds", type=float, default=2.0)
@@ -224,6 +225,7 @@ def run_ours(a, rank, world_size, local_rank):
     for _ in range(a.warmup):
         world.step_async(dt)
     world.synchronize()
+    tuned = world.autotune(dt, 2) if not a.no_tune else None
 
     stream = torch.cuda.ExternalStream(world.stream())
     world.set_timing(True)
@@ -297,6 +299,7 @@ def run_ours(a, rank, world_size, local_rank):
                         "traffic": traffic,
                         "model": f"{bpu:g} B per {unit} x {units[unit]} {unit}s per launch"},
            "stage_ms_per_step": {k: round(v, 4) for k, v in per_stage.items()},
+           "autotune": tuned,
            "counts": {"pairs": P, "contacts": Cn, "gjk": info["gjk"], "epa": info["epa"],
                       "gjk_large_mesh": info["gjk_large_mesh"], "epa_large_mesh": info["epa_large_mesh"],
                       "gjk_iterations": info["gjk_iterations"], "epa_iterations": info["epa_iterations"],

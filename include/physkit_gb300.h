@@ -155,6 +155,23 @@ int pk_world_set_timing(pk_world *w, int32_t enable);
 int pk_world_read_stage_times(pk_world *w, double *total_ms, int32_t *counts, int32_t cap, int32_t *nstages);
 const char *pk_stage_name(int32_t stage);
 
+/* Autotuner: picks the launch shapes of the step (solver CTA size and the split between the
+ * solver's large- and small-world launches, narrowphase grid, traversal block size) by timing
+ * each stage over `steps_per_candidate` real steps per candidate. These steps advance the world
+ * like pk_world_step; launch shapes do not change results. Call before pk_world_capture. */
+typedef struct pk_tune_result
+{
+    int32_t solve_threads;
+    int32_t small_world;
+    int32_t narrow_grid;
+    int32_t traverse_threads;
+    double step_ms_before; /* summed stage times per step before and after tuning */
+    double step_ms_after;
+    int32_t steps_used;
+    int32_t reserved;
+} pk_tune_result;
+int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tune_result *out);
+
 /* Per slot: pos3 quat4 vel3 ang_vel3 alive = 14 doubles (particle.h:135-149). */
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);
 /* Overwrite pos/quat/vel/ang_vel of one body and refresh its cached world inertia. */

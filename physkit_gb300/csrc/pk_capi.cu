@@ -761,6 +761,117 @@ const char *pk_stage_name(int32_t stage)
     return pk::kStageNames[stage];
 }
 
+// Time `k` plain steps with per-stage CUDA events; returns mean ms per step of every stage.
+static int timed_steps(pk_world *w, double dt, int k, double *stage_ms)
+{
+    double ms[pk::kStages];
+    int cnt[pk::kStages];
+    if (w->eng->read_stage_times(ms, cnt) < 0) return PK_ERR_CUDA; // clear
+    for (int i = 0; i < k; ++i)
+        if (int rc = pk_world_step_async(w, dt)) return rc;
+    if (w->eng->synchronize(nullptr)) return PK_ERR_CUDA;
+    if (w->eng->read_stage_times(ms, cnt) < 0) return PK_ERR_CUDA;
+    for (int s = 0; s < pk::kStages; ++s) stage_ms[s] = cnt[s] ? ms[s] / cnt[s] : 0.0;
+    return PK_OK;
+}
+
+int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tune_result *out)
+{
+    if (!w || !(dt > 0.0) || steps_per_candidate < 1) return PK_ERR_INVALID;
+    if (int rc = flush_shapes(w)) return rc;
+    if (int rc = flush_order(w)) return rc;
+    const int k = steps_per_candidate;
+    int used = 0;
+    double st[pk::kStages];
+    auto total = [&](const double *x) {
+        double t = 0.0;
+        for (int i = 0; i < pk::kStages; ++i) t += x[i];
+        return t;
+    };
+    w->eng->set_timing(1);
+    pk::Tunables best = w->eng->tunables();
+    int rc = timed_steps(w, dt, k, st);
+    used += k;
+    if (rc) return rc;
+    const double before = total(st);
+    enum { S_TRAVERSE = 3, S_NARROW = 5, S_SOLVE = 7 };
+    // solver: CTA size x small-world split
+    {
+        double bt = 1e300;
+        pk::Tunables bc = best;
+        for (int th : {64, 128, 256})
+            for (int sw : {256, 512, 1024})
+            {
+                pk::Tunables t = best;
+                t.solve_threads = th;
+                t.small_world = sw;
+                w->eng->set_tunables(t);
+                if ((rc = timed_steps(w, dt, k, st))) return rc;
+                used += k;
+                if (st[S_SOLVE] < bt)
+                {
+                    bt = st[S_SOLVE];
+                    bc = t;
+                }
+            }
+        best = bc;
+    }
+    // narrowphase grid
+    {
+        double bt = 1e300;
+        pk::Tunables bc = best;
+        for (int g : {1, 2, 4})
+        {
+            pk::Tunables t = best;
+            t.narrow_grid = g;
+            w->eng->set_tunables(t);
+            if ((rc = timed_steps(w, dt, k, st))) return rc;
+            used += k;
+            if (st[S_NARROW] < bt)
+            {
+                bt = st[S_NARROW];
+                bc = t;
+            }
+        }
+        best = bc;
+    }
+    // traversal block size
+    {
+        double bt = 1e300;
+        pk::Tunables bc = best;
+        for (int th : {64, 128, 256})
+        {
+            pk::Tunables t = best;
+            t.traverse_threads = th;
+            w->eng->set_tunables(t);
+            if ((rc = timed_steps(w, dt, k, st))) return rc;
+            used += k;
+            if (st[S_TRAVERSE] < bt)
+            {
+                bt = st[S_TRAVERSE];
+                bc = t;
+            }
+        }
+        best = bc;
+    }
+    w->eng->set_tunables(best);
+    if ((rc = timed_steps(w, dt, k, st))) return rc;
+    used += k;
+    w->eng->set_timing(0);
+    if (out)
+    {
+        out->solve_threads = best.solve_threads;
+        out->small_world = best.small_world;
+        out->narrow_grid = best.narrow_grid;
+        out->traverse_threads = best.traverse_threads;
+        out->step_ms_before = before;
+        out->step_ms_after = total(st);
+        out->steps_used = used;
+        out->reserved = 0;
+    }
+    return PK_OK;
+}
+
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap, int32_t *n)
 {
     if (!w) return PK_ERR_INVALID;

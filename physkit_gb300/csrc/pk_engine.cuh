@@ -21,6 +21,7 @@
 #include "pk_narrow.cuh"
 #include "pk_sort.cuh"
 
+#include <cooperative_groups.h>
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -1029,13 +1030,24 @@ template <class T> __device__ __forceinline__ void solve_contact(SBody<T> &A, SB
     }
 }
 
-template <class T> __device__ __forceinline__ void load_sbody(const Dev<T> &d, int s, const Vel<T> *cache, SBody<T> &b)
+template <class T>
+__device__ __forceinline__ void load_sbody(const Dev<T> &d, int s, const Vel<T> *cache, SBody<T> &b, bool coherent)
 {
     const Meta m = d.meta[s];
     b.is_static = (m.flags & BODY_STATIC) != 0;
-    const Vel<T> ve = (cache && !b.is_static) ? cache[m.local] : d.vel[s];
-    b.v = ld3(ve.v);
-    b.w = ld3(ve.w);
+    if (coherent)
+    {
+        // other SMs wrote this body in earlier colours: read through L2, not a stale L1 line
+        const T *src = reinterpret_cast<const T *>(d.vel + s);
+        b.v = V3<T>{__ldcg(src + 0), __ldcg(src + 1), __ldcg(src + 2)};
+        b.w = V3<T>{__ldcg(src + 3), __ldcg(src + 4), __ldcg(src + 5)};
+    }
+    else
+    {
+        const Vel<T> ve = (cache && !b.is_static) ? cache[m.local] : d.vel[s];
+        b.v = ld3(ve.v);
+        b.w = ld3(ve.w);
+    }
 #pragma unroll
     for (int k = 0; k < 9; ++k) b.I[k] = d.iwinv[9 * s + k];
     b.inv_mass = d.prm[s].inv_mass;
@@ -1054,12 +1066,14 @@ template <class T> __device__ __forceinline__ void store_sbody(const Dev<T> &d, 
 }
 
 // One manifold: warm start (warm = true) or one Gauss-Seidel pass over its contacts in order.
-template <class T> __device__ __forceinline__ void solve_manifold(const Dev<T> &d, int p, uint64_t sv, Vel<T> *cache, bool warm)
+template <class T>
+__device__ __forceinline__ void solve_manifold(const Dev<T> &d, int p, uint64_t sv, Vel<T> *cache, bool warm,
+                                               bool coherent = false)
 {
     int sa = int(sv >> 32), sb = int(sv & 0xFFFFFFFFu);
     SBody<T> A, B;
-    load_sbody(d, sa, cache, A);
-    load_sbody(d, sb, cache, B);
+    load_sbody(d, sa, cache, A, coherent);
+    load_sbody(d, sb, cache, B, coherent);
     const uint8_t mask = d.rowmask[p];
     for (int q = 0; q < 4; ++q)
     {
@@ -1081,7 +1095,7 @@ template <class T> __device__ __forceinline__ void solve_manifold(const Dev<T> &
 
 template <class T>
 __global__ void __launch_bounds__(256)
-    k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies)
+    k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies, int grid_world)
 {
     extern __shared__ __align__(16) unsigned char solve_smem[];
     __shared__ int ccount[kMaxColours];
@@ -1093,7 +1107,7 @@ __global__ void __launch_bounds__(256)
     const int blk = first_block + int(blockIdx.x);
     if (blk >= d.max_worlds) return;
     const int w = d.world_order[blk];
-    if (!d.wp[w].active) return;
+    if (!d.wp[w].active || d.world_nlocal[w] > grid_world) return; // large worlds: k_solve_grid
     const int ms = d.mstart[w], me = d.mend[w];
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     if (me <= ms)
@@ -1255,6 +1269,144 @@ __global__ void __launch_bounds__(256)
     for (int k = tid; k < na; k += nt)
     {
         int p = act[k];
+        uint8_t mask = d.rowmask[p];
+        for (int q = 0; q < 4; ++q)
+        {
+            if (!(mask & (1u << q))) continue;
+            const Row<T> &r = d.rows[4 * p + q];
+            Contact<T> &c = d.man_new[p].c[q];
+            c.imp[0] = r.acc[0];
+            c.imp[1] = r.acc[1];
+            c.imp[2] = r.acc[2];
+        }
+    }
+}
+
+// The same colouring and colour-ordered sweeps for one world too large for a CTA: every block of a
+// cooperative launch takes part, and grid-wide barriers separate the phases. Claim priority is
+// the pair index itself (monotone in the compacted index the CTA solver uses), so the colours are
+// the same as the CTA solver's and the oracle's.
+struct GridScratch
+{
+    int ccount[kMaxColours];
+    int cstart[kMaxColours];
+    int cursor[kMaxColours];
+    int left[2];
+    int ncol;
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__restrict__ sval, int w, GridScratch *g)
+{
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    if (!d.wp[w].active) return;
+    const int ms = d.mstart[w], me = d.mend[w];
+    const int gtid = int(grid.thread_rank()), gn = int(grid.size());
+    if (me <= ms)
+    {
+        if (gtid == 0) d.ncolours[w] = 0;
+        return;
+    }
+    int *colour = d.colour_tmp;
+    for (int p = ms + gtid; p < me; p += gn) colour[p] = d.rowmask[p] ? -1 : -2;
+    for (int c = gtid; c < kMaxColours; c += gn) g->ccount[c] = g->cursor[c] = 0;
+    if (gtid == 0)
+    {
+        g->left[0] = 1; // any value > 0: first round runs
+        g->left[1] = 0;
+    }
+    grid.sync();
+    int round = 0;
+    int active_left = 1;
+    while (active_left > 0)
+    {
+        int *cnt = &g->left[round & 1];
+        for (int p = ms + gtid; p < me; p += gn)
+        {
+            if (colour[p] != -1) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            if (!(d.meta[a].flags & BODY_STATIC)) d.owner[a] = 0xFFFFFFFFu;
+            if (!(d.meta[b].flags & BODY_STATIC)) d.owner[b] = 0xFFFFFFFFu;
+        }
+        if (gtid == 0) *cnt = 0;
+        grid.sync();
+        for (int p = ms + gtid; p < me; p += gn)
+        {
+            if (colour[p] != -1) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            if (!(d.meta[a].flags & BODY_STATIC)) atomicMin(d.owner + a, uint32_t(p));
+            if (!(d.meta[b].flags & BODY_STATIC)) atomicMin(d.owner + b, uint32_t(p));
+        }
+        grid.sync();
+        int left = 0;
+        for (int p = ms + gtid; p < me; p += gn)
+        {
+            if (colour[p] != -1) continue;
+            uint64_t v = sval[p];
+            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
+            bool oka = (d.meta[a].flags & BODY_STATIC) || __ldcg(d.owner + a) == uint32_t(p);
+            bool okb = (d.meta[b].flags & BODY_STATIC) || __ldcg(d.owner + b) == uint32_t(p);
+            if (oka && okb)
+                colour[p] = round;
+            else
+                ++left;
+        }
+        if (left) atomicAdd(cnt, left);
+        grid.sync();
+        active_left = *((volatile int *)cnt);
+        ++round;
+        if (round >= kMaxColours && active_left > 0)
+        {
+            if (gtid == 0) atomicOr(d.status, ST_COLOUR_CAP);
+            break;
+        }
+    }
+    const int ncol_guess = round;
+    for (int p = ms + gtid; p < me; p += gn)
+    {
+        int c = colour[p];
+        if (c >= 0 && c < kMaxColours) atomicAdd(&g->ccount[c], 1);
+    }
+    grid.sync();
+    if (gtid == 0)
+    {
+        int s = 0, nc = 0;
+        for (int c = 0; c < ncol_guess; ++c)
+        {
+            g->cstart[c] = s;
+            s += g->ccount[c];
+            if (g->ccount[c] > 0) nc = c + 1;
+        }
+        g->ncol = nc;
+        d.ncolours[w] = nc;
+    }
+    grid.sync();
+    const int ncol = *((volatile int *)&g->ncol);
+    for (int p = ms + gtid; p < me; p += gn)
+    {
+        int c = colour[p];
+        if (c >= 0 && c < kMaxColours) d.order[ms + __ldcg(&g->cstart[c]) + atomicAdd(&g->cursor[c], 1)] = uint32_t(p);
+        d.pair_colour[p] = c >= 0 ? c : -2;
+    }
+    grid.sync();
+    for (int it = -1; it < d.iterations; ++it)
+    {
+        for (int c = 0; c < ncol; ++c)
+        {
+            const int cs = ms + __ldcg(&g->cstart[c]), cn = __ldcg(&g->ccount[c]);
+            for (int k = gtid; k < cn; k += gn)
+            {
+                int p = int(__ldcg(d.order + cs + k));
+                solve_manifold(d, p, sval[p], (Vel<T> *)nullptr, it < 0, true);
+            }
+            grid.sync();
+        }
+    }
+    for (int p = ms + gtid; p < me; p += gn)
+    {
         uint8_t mask = d.rowmask[p];
         for (int q = 0; q < 4; ++q)
         {

@@ -30,6 +30,17 @@ struct HostBody
     double il[9], il_inv[9];
 };
 
+// Launch shapes chosen at run time (by pk_world_autotune or left at these defaults). They do not
+// change results: colour-parallel solver updates are independent and the other kernels are
+// per-element.
+struct Tunables
+{
+    int solve_threads = 256;   // threads per solver CTA (one CTA per world)
+    int small_world = 512;     // worlds up to this many local indices share the small solver launch
+    int narrow_grid = 2;       // GJK/EPA grid = narrow_grid x the default grid
+    int traverse_threads = 128;
+};
+
 struct StepCounters
 {
     int npairs = 0;
@@ -79,6 +90,8 @@ public:
     virtual void *stream() = 0;
     virtual int set_timing(int enable) = 0;                 // CUDA events around each stage
     virtual int read_stage_times(double *ms, int *count) = 0; // totals since the last read
+    virtual int set_tunables(const Tunables &t) = 0;
+    virtual Tunables tunables() const = 0;
     virtual int last_error() const = 0;
 };
 

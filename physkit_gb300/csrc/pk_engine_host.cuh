@@ -142,6 +142,12 @@ public:
         }
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
+        {
+            int per_sm = 0;
+            PK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_grid<T>, 256, 0));
+            grid_blocks_ = sms_ * (per_sm > 0 ? per_sm : 1);
+            PK_CUDA(cudaMalloc(&grid_scratch_, sizeof(GridScratch)));
+        }
         for (int k = 0; k < 2; ++k)
         {
             PK_CUDA(alloc(&mkey_[k], N));
@@ -294,20 +300,43 @@ public:
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_order), order, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_nlocal), nlocal, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaStreamSynchronize(st_));
-        // Worlds above kSmallWorld local indices get their own launch with a cache sized for the
-        // largest world (if it fits in shared memory); the others share a small cache.
-        big_worlds_ = 0;
-        int maxl = 0;
-        for (int i = 0; i < n; ++i)
-        {
-            int nl = nlocal[order[i]];
-            if (nl > kSmallWorld) ++big_worlds_;
-            maxl = nl > maxl ? nl : maxl;
-        }
-        int limit = int(kMaxSolveSmem / sizeof(Vel<T>));
-        big_cache_ = maxl <= limit ? maxl : 0;
+        order_.assign(order, order + n);
+        nlocal_.assign(nlocal, nlocal + n);
+        split_worlds();
         return 0;
     }
+
+    // Worlds above tune_.small_world local indices get their own solver launch with a cache sized
+    // for the largest world (if it fits in shared memory); the others share a small cache.
+    void split_worlds()
+    {
+        big_worlds_ = 0;
+        int maxl = 0;
+        grid_worlds_.clear();
+        for (size_t i = 0; i < order_.size(); ++i)
+        {
+            int nl = nlocal_[size_t(order_[i])];
+            if (nl > kGridWorld)
+            {
+                grid_worlds_.push_back(order_[i]);
+                continue;
+            }
+            if (nl > tune_.small_world) ++big_worlds_;
+            maxl = nl > maxl ? nl : maxl;
+        }
+        // worlds handled by the grid solver sort first (largest first): skip them in the CTA launches
+        big_worlds_ += int(grid_worlds_.size());
+        int limit = int(kMaxSolveSmem / sizeof(Vel<T>));
+        big_cache_ = maxl <= limit ? maxl : 0;
+    }
+
+    int set_tunables(const Tunables &t) override
+    {
+        tune_ = t;
+        split_worlds();
+        return 0;
+    }
+    Tunables tunables() const override { return tune_; }
 
     int kill_world(const int *slots, int n, int world) override
     {
@@ -645,10 +674,15 @@ private:
     T *clusters_ = nullptr;
     size_t clusters_cap_ = 0;
     cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
-    static constexpr int kSmallWorld = 512;
     static constexpr size_t kMaxSolveSmem = 160 * 1024;
+    Tunables tune_{};
     int big_worlds_ = 0;
     int big_cache_ = 0;
+    std::vector<int> order_, nlocal_;
+    std::vector<int> grid_worlds_;             // worlds solved by the cooperative grid solver
+    static constexpr int kGridWorld = 16384;   // local indices above which a world leaves the CTA solver
+    GridScratch *grid_scratch_ = nullptr;
+    int grid_blocks_ = 1;
     bool timing_ = false;
     bool capturing_ = false;
     uint8_t *mask_dev_ = nullptr;
@@ -715,7 +749,7 @@ private:
                       d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
-                      shape_rmax_, clusters_, mask_dev_};
+                      shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
             if (p) cudaFree(p);
         for (cudaEvent_t e : events_) cudaEventDestroy(e);
@@ -736,7 +770,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 15 + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 15 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -752,7 +786,7 @@ private:
         k_zero_ints<<<gb, 256, 0, st_>>>(d.refit_flag, N);
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
         PK_CUDA(mark(3));
-        k_traverse<T><<<(N + 127) / 128, 128, 0, st_>>>(d, sval);
+        k_traverse<T><<<(N + tune_.traverse_threads - 1) / tune_.traverse_threads, tune_.traverse_threads, 0, st_>>>(d, sval);
         k_carry_pairs<T><<<gp, 256, 0, st_>>>(d);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
         PK_CUDA(mark(4));
@@ -763,16 +797,27 @@ private:
         last_sval_ = const_cast<uint64_t *>(pv);
         PK_CUDA(mark(5));
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
-        k_narrow_gjk<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
-        k_narrow_epa<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
+        k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
+        k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         PK_CUDA(mark(7));
+        for (int gw : grid_worlds_)
+        {
+            // one cooperative launch per world too large for a CTA
+            int wid = gw;
+            GridScratch *gs = grid_scratch_;
+            void *args[] = {&d, const_cast<uint64_t **>(&pv), &wid, &gs};
+            PK_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_solve_grid<T>), dim3(grid_blocks_), dim3(256),
+                                                args, 0, st_));
+        }
         if (big_worlds_ > 0)
-            k_solve_world<T><<<big_worlds_, 256, sizeof(Vel<T>) * size_t(big_cache_), st_>>>(d, pv, 0, big_cache_);
+            k_solve_world<T><<<big_worlds_, tune_.solve_threads, sizeof(Vel<T>) * size_t(big_cache_), st_>>>(
+                d, pv, 0, big_cache_, kGridWorld);
         if (cfg_.max_worlds > big_worlds_)
-            k_solve_world<T><<<cfg_.max_worlds - big_worlds_, 256, sizeof(Vel<T>) * kSmallWorld, st_>>>(
-                d, pv, big_worlds_, kSmallWorld);
+            k_solve_world<T><<<cfg_.max_worlds - big_worlds_, tune_.solve_threads,
+                               sizeof(Vel<T>) * size_t(tune_.small_world), st_>>>(d, pv, big_worlds_, tune_.small_world,
+                                                                                   kGridWorld);
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk, pv);

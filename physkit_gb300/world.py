@@ -53,6 +53,12 @@ class StepInfoC(C.Structure):
                 ("gjk_iterations", C.c_int64), ("epa_iterations", C.c_int64), ("epa_iterations_large_mesh", C.c_int64)]
 
 
+class TuneResultC(C.Structure):
+    _fields_ = [("solve_threads", C.c_int32), ("small_world", C.c_int32), ("narrow_grid", C.c_int32),
+                ("traverse_threads", C.c_int32), ("step_ms_before", C.c_double), ("step_ms_after", C.c_double),
+                ("steps_used", C.c_int32), ("reserved", C.c_int32)]
+
+
 class CollideShapeC(C.Structure):
     _fields_ = [("kind", C.c_int32), ("shape", C.c_int32), ("p", C.c_double * 10)]
 
@@ -100,6 +106,7 @@ def lib():
             "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_collide_noalloc": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_world_set_timing": (C.c_int, [vp, C.c_int32]),
+            "pk_world_autotune": (C.c_int, [vp, C.c_double, C.c_int32, P(TuneResultC)]),
             "pk_world_read_stage_times": (C.c_int, [vp, dp, i32p, C.c_int32, i32p]),
             "pk_stage_name": (C.c_char_p, [C.c_int32]),
             "pk_last_cuda_error": (C.c_int, []),
@@ -381,6 +388,12 @@ class World:
 
     def stream(self):
         return self.L.pk_world_stream(self.h)
+
+    def autotune(self, dt, steps_per_candidate=2):
+        """Pick launch shapes by timing real steps (which advance the world); returns the choice."""
+        r = TuneResultC()
+        _check(self.L.pk_world_autotune(self.h, float(dt), int(steps_per_candidate), C.byref(r)), "pk_world_autotune")
+        return {f: getattr(r, f) for f, _ in TuneResultC._fields_ if f != "reserved"}
 
     def set_timing(self, enable=True):
         _check(self.L.pk_world_set_timing(self.h, int(bool(enable))), "pk_world_set_timing")

@@ -152,3 +152,35 @@ def test_fp32_error_against_fp64_oracle():
     rel = np.linalg.norm(g[dyn, 0:3] - o[dyn, 0:3], axis=1) / np.maximum(np.linalg.norm(o[dyn, 0:3], axis=1), 1.0)
     assert rel.max() < 1e-4, rel.max()
     world.close()
+
+
+def test_fp64_grid_solver_large_world_bit_identical():
+    # 17,000 boxes: above the CTA solver's 16,384-index limit, so the cooperative grid solver runs
+    scene = scenes.config1(n=17000, seed=77)
+    scene.bodies["pos"][1:, 1] = 0.3 + (scene.bodies["pos"][1:, 1] % 2.0)  # start near the ground
+    scene.bodies["pos"][1:, 0] *= 2.5
+    scene.bodies["pos"][1:, 2] *= 2.5
+    world, ow, _ = run_pair(scene, 0)
+    for step in range(40):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        assert np.array_equal(world.pairs(), ow.pairs()), f"pair set differs at step {step}"
+    compare_step(world, ow, 40)
+    k, col, nc = world.colours()
+    assert len(k) > 100 and nc > 1  # contacts were solved
+    world.close()
+
+
+def test_autotune_keeps_results():
+    scene = scenes.small_pile(n=60, seed=13)
+    a, _ = scenes.make_world(scene, precision="f64")
+    b, _ = scenes.make_world(scene, precision="f64")
+    r = b.autotune(scene.dt, 1)
+    for _ in range(r["steps_used"]):
+        a.step(scene.dt)
+    for _ in range(20):
+        a.step(scene.dt)
+        b.step(scene.dt)
+    assert np.array_equal(a.bodies(), b.bodies())
+    a.close()
+    b.close()
