@@ -219,13 +219,24 @@ def run_ours(a, rank, world_size, local_rank):
         dist = dist_mod
 
     scene = scenes.config3(nworlds=a.worlds, nmin=a.nmin, nmax=a.nmax, seed=scenes.SEED_BASE + 3 + rank)
-    world, _ = scenes.make_world(scene, precision=a.precision, pair_factor=6)
-    nb = scene.n_dynamic
     dt = scene.dt
+    tuned = None
+    if not a.no_tune:
+        # autotune on a scratch copy of the batch from the same step on, so the timed window below
+        # covers the same simulated steps as an untuned run
+        scratch, _ = scenes.make_world(scene, precision=a.precision, pair_factor=6)
+        for _ in range(a.warmup):
+            scratch.step_async(dt)
+        scratch.synchronize()
+        tuned = scratch.autotune(dt, 2)
+        scratch.close()
+    world, _ = scenes.make_world(scene, precision=a.precision, pair_factor=6)
+    if tuned:
+        world.set_tuning(tuned)
+    nb = scene.n_dynamic
     for _ in range(a.warmup):
         world.step_async(dt)
     world.synchronize()
-    tuned = world.autotune(dt, 2) if not a.no_tune else None
 
     stream = torch.cuda.ExternalStream(world.stream())
     world.set_timing(True)

@@ -171,6 +171,8 @@ typedef struct pk_tune_result
     int32_t reserved;
 } pk_tune_result;
 int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tune_result *out);
+/* Apply launch shapes found by pk_world_autotune (e.g. on a scratch copy of the same scene). */
+int pk_world_set_tuning(pk_world *w, const pk_tune_result *t);
 
 /* Per slot: pos3 quat4 vel3 ang_vel3 alive = 14 doubles (particle.h:135-149). */
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);

@@ -872,6 +872,22 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
     return PK_OK;
 }
 
+int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
+{
+    if (!w || !t) return PK_ERR_INVALID;
+    if (t->solve_threads < 32 || t->solve_threads > 256 || (t->solve_threads & 31) || t->small_world < 1 ||
+        t->narrow_grid < 1 || t->narrow_grid > 16 || t->traverse_threads < 32 || t->traverse_threads > 1024 ||
+        (t->traverse_threads & 31))
+        return PK_ERR_INVALID;
+    pk::Tunables tu;
+    tu.solve_threads = t->solve_threads;
+    tu.small_world = t->small_world;
+    tu.narrow_grid = t->narrow_grid;
+    tu.traverse_threads = t->traverse_threads;
+    w->eng->set_tunables(tu);
+    return PK_OK;
+}
+
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap, int32_t *n)
 {
     if (!w) return PK_ERR_INVALID;

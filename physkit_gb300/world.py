@@ -107,6 +107,7 @@ def lib():
             "pk_collide_noalloc": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_world_set_timing": (C.c_int, [vp, C.c_int32]),
             "pk_world_autotune": (C.c_int, [vp, C.c_double, C.c_int32, P(TuneResultC)]),
+            "pk_world_set_tuning": (C.c_int, [vp, P(TuneResultC)]),
             "pk_world_read_stage_times": (C.c_int, [vp, dp, i32p, C.c_int32, i32p]),
             "pk_stage_name": (C.c_char_p, [C.c_int32]),
             "pk_last_cuda_error": (C.c_int, []),
@@ -394,6 +395,13 @@ class World:
         r = TuneResultC()
         _check(self.L.pk_world_autotune(self.h, float(dt), int(steps_per_candidate), C.byref(r)), "pk_world_autotune")
         return {f: getattr(r, f) for f, _ in TuneResultC._fields_ if f != "reserved"}
+
+    def set_tuning(self, tuned):
+        r = TuneResultC()
+        for f, _ in TuneResultC._fields_:
+            if f in tuned:
+                setattr(r, f, tuned[f])
+        _check(self.L.pk_world_set_tuning(self.h, C.byref(r)), "pk_world_set_tuning")
 
     def set_timing(self, enable=True):
         _check(self.L.pk_world_set_timing(self.h, int(bool(enable))), "pk_world_set_timing")

@@ -157,12 +157,13 @@ def test_fp32_error_against_fp64_oracle():
 def test_fp64_grid_solver_large_world_bit_identical():
     # 17,000 boxes: above the CTA solver's 16,384-index limit, so the cooperative grid solver runs
     scene = scenes.config1(n=17000, seed=77)
-    scene.bodies["pos"][1:, 1] = 0.3 + (scene.bodies["pos"][1:, 1] % 2.0)  # start near the ground
-    scene.bodies["pos"][1:, 0] *= 2.5
-    scene.bodies["pos"][1:, 2] *= 2.5
+    scene.bodies["pos"][1:, 1] = 0.6 + (scene.bodies["pos"][1:, 1] % 6.0)  # start near the ground
+    scene.bodies["pos"][1:, 0] *= 3.0
+    scene.bodies["pos"][1:, 2] *= 3.0
     world, ow, _ = run_pair(scene, 0)
     for step in range(40):
-        world.step(scene.dt)
+        world.step(scene.dt, check=False)
+        assert not world.synchronize()["flags"], world.last_info
         ow.step(scene.dt)
         assert np.array_equal(world.pairs(), ow.pairs()), f"pair set differs at step {step}"
     compare_step(world, ow, 40)
