@@ -23,6 +23,7 @@
 
 #include <cooperative_groups.h>
 #include <cstdint>
+#include <type_traits>
 #include <cstdio>
 #include <cuda_runtime.h>
 #include <vector>
@@ -148,6 +149,11 @@ template <class T> struct Dev
     Manifold<T> *man_old;
     uint64_t *key_old;
     uint64_t *val_old;     // slot pairs of last step's sorted pairs
+    int *mstart_old;       // last step's pair range of each world
+    int *mend_old;
+    int *nstart;           // active world: its range in the sorted list of new pairs;
+    int *nend;             // idle world: 0 and the number of its kept pairs
+    int *nnew;             // pairs found by this step's traversal
     int *npairs_old;
     Manifold<T> *man_new;
     uint8_t *event;
@@ -171,6 +177,7 @@ template <class T> struct Dev
     uint32_t *order;
     int *ncolours;
     const int *world_order; // solver CTA -> world, largest worlds first
+    uint4 *srec;            // solve records of the active manifolds, colour-ordered per world
     const int *world_nlocal; // local indices in use per world (bounds the shared-memory cache)
     // control
     int *status;
@@ -213,6 +220,18 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v)
     return v;
 }
 
+// Slot in a compacted list for every active lane of the warp: one atomic per warp.
+__device__ __forceinline__ int warp_push(int *counter)
+{
+    unsigned m = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
 #define PK_GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += blockDim.x * gridDim.x)
 
 // ------------------------------------------------------------------------------------------------
@@ -227,6 +246,8 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         d.wroot[w] = -1;
         d.mstart[w] = 0;
         d.mend[w] = 0;
+        d.nstart[w] = 0;
+        d.nend[w] = 0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
@@ -324,14 +345,14 @@ template <class T> __global__ void k_integrate_vel(Dev<T> d, T dt)
 // ------------------------------------------------------------------------------------------------
 // LBVH: Morton keys (world id above 30 Morton bits), Karras build, bottom-up refit
 // ------------------------------------------------------------------------------------------------
+// Keys of the bodies of active worlds only, compacted (one atomic per warp); the sort and the
+// LBVH then cover just those bodies.
 template <class T> __global__ void k_morton(Dev<T> d)
 {
     const int n = *d.nslots;
-    const uint64_t dead = (uint64_t(d.max_worlds) << 30) | 0x3FFFFFFFull;
     PK_GRID_STRIDE(i, n)
     {
         Meta m = d.meta[i];
-        uint64_t key = dead;
         if ((m.flags & BODY_ALIVE) && d.wp[m.world].active)
         {
             Aabb<T> tb = d.tbox[i];
@@ -349,11 +370,10 @@ template <class T> __global__ void k_morton(Dev<T> d)
                 uint32_t q = min(1023u, uint32_t(u * 1024.f));
                 code |= spread10(q) << (2 - a);
             }
-            key = (uint64_t(m.world) << 30) | code;
-            atomicAdd(d.nleaf, 1);
+            int slot = warp_push(d.nleaf);
+            d.mkey[slot] = (uint64_t(m.world) << 30) | code;
+            d.mval[slot] = uint64_t(i);
         }
-        d.mkey[i] = key;
-        d.mval[i] = uint64_t(i);
     }
 }
 
@@ -530,6 +550,7 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
 template <class T> __global__ void k_clamp_pairs(Dev<T> d)
 {
     if (*d.npairs > d.pair_cap) *d.npairs = d.pair_cap;
+    *d.nnew = *d.npairs;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -605,17 +626,6 @@ template <class T> __device__ __forceinline__ void add_contact(Manifold<T> &m, c
     m.n = 4;
 }
 
-// Slot in a compacted list for every active lane of the warp: one atomic per warp.
-__device__ __forceinline__ int warp_push(int *counter)
-{
-    unsigned m = __activemask();
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(counter, __popc(m));
-    base = __shfl_sync(m, base, leader);
-    return base + __popc(m & ((1u << lane) - 1u));
-}
 
 // The manifold update of narrow_phase::calculate for one pair given its new contact (if any):
 // warm-start transfer, re-projection of old contacts, reduction to four and begin/end events
@@ -732,8 +742,13 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         int world = int(key >> (2 * d.lbits));
-        if (p == 0 || (skey[p - 1] >> (2 * d.lbits)) != uint64_t(world)) d.mstart[world] = p;
-        if (p == np - 1 || (skey[p + 1] >> (2 * d.lbits)) != uint64_t(world)) d.mend[world] = p + 1;
+        if (!d.wp[world].active)
+        {
+            // kept pair of a world that sits out this step: unchanged, no event
+            d.man_new[p] = d.man_old[d.old_idx[p]];
+            d.event[p] = 0;
+            continue;
+        }
         int lo = 0, hi = nold;
         while (lo < hi)
         {
@@ -742,16 +757,6 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
         }
         int old_idx = (lo < nold && d.key_old[lo] == key) ? lo : -1;
         d.old_idx[p] = old_idx;
-        if (!d.wp[world].active)
-        {
-            // carried pair of a world that sits out this step: unchanged, no event
-            if (old_idx >= 0)
-                d.man_new[p] = d.man_old[old_idx];
-            else
-                d.man_new[p].n = 0;
-            d.event[p] = 0;
-            continue;
-        }
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         V3<T> dc = B.pos - A.pos;
         T rs = A.rmax + B.rmax;
@@ -984,8 +989,60 @@ template <class T> __device__ __forceinline__ void warm_contact(SBody<T> &A, SBo
     if (r.acc[2] != 0.0) apply_reg(A, B, ld3(r.t2), ld3(r.wa_t2), ld3(r.wb_t2), T(r.acc[2]));
 }
 
+// FP32 form of one contact: the accumulated impulses stay FP64 (one add per row, the clamp at zero
+// and the difference that is applied), the rest is FP32, including the friction-cone rescale
+// (sqrt and divide), so the dependent chain holds a handful of FP64 operations instead of a
+// software FP64 square root and divide per contact.
+__device__ __forceinline__ void solve_contact_f32(SBody<float> &A, SBody<float> &B, Row<float> &r)
+{
+    {
+        float Jv = jv_reg(r.n, r.wa_n, r.wb_n, A, B);
+        float lambda = -(Jv + r.bias) * r.meff_n;
+        double old = r.acc[0];
+        double v = old + double(lambda);
+        double acc = v < 0.0 ? 0.0 : v;
+        r.acc[0] = acc;
+        apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), float(acc - old));
+    }
+    float maxf = r.mu * float(r.acc[0]);
+    float b1 = jv_reg(r.t1, r.wa_t1, r.wb_t1, A, B);
+    float b2 = jv_reg(r.t2, r.wa_t2, r.wb_t2, A, B);
+    float l1 = -(r.inv11 * b1 + r.inv12 * b2);
+    float l2 = -(r.inv12 * b1 + r.inv22 * b2);
+    double o1 = r.acc[1], o2 = r.acc[2];
+    double n1 = o1 + double(l1), n2 = o2 + double(l2);
+    float f1 = float(n1), f2 = float(n2);
+    float mag2 = f1 * f1 + f2 * f2;
+    if (mag2 > maxf * maxf)
+    {
+        float sc = maxf / sqrtf(mag2);
+        n1 = n1 * double(sc);
+        n2 = n2 * double(sc);
+    }
+    r.acc[1] = n1;
+    r.acc[2] = n2;
+    float a1 = float(n1 - o1), a2 = float(n2 - o2);
+    if (!A.is_static)
+    {
+        V3<float> imp = ld3(r.t1) * a1 + ld3(r.t2) * a2;
+        A.v = A.v + imp * A.inv_mass;
+        A.w = A.w + matvec(A.I, ld3(r.wa_t1) * a1 + ld3(r.wa_t2) * a2);
+    }
+    if (!B.is_static)
+    {
+        V3<float> imp = (-ld3(r.t1)) * a1 - ld3(r.t2) * a2;
+        B.v = B.v + imp * B.inv_mass;
+        B.w = B.w + matvec(B.I, ld3(r.wb_t1) * a1 + ld3(r.wb_t2) * a2);
+    }
+}
+
 template <class T> __device__ __forceinline__ void solve_contact(SBody<T> &A, SBody<T> &B, Row<T> &r)
 {
+    if constexpr (std::is_same<T, float>::value)
+    {
+        solve_contact_f32(A, B, r);
+        return;
+    }
     // normal row: jacobian_row::apply (constraint.h:49-71), gamma = 0
     {
         T Jv = jv_reg(r.n, r.wa_n, r.wb_n, A, B);
@@ -1091,6 +1148,74 @@ __device__ __forceinline__ void solve_manifold(const Dev<T> &d, int p, uint64_t 
     }
     store_sbody(d, sa, cache, A);
     store_sbody(d, sb, cache, B);
+}
+
+// Solve record of an active manifold, written once per step by the colouring: the pair index, both
+// slots with the static flag in bit 31, and both world-local indices (16 bits each; read only when
+// the world's velocities are cached in shared memory, whose size keeps them below 2^16). One load
+// replaces the chain pair index -> slot pair -> body meta on every sweep.
+template <class T> __device__ __forceinline__ uint4 make_solve_rec(const Dev<T> &d, int p, uint64_t sv)
+{
+    int a = int(sv >> 32), b = int(sv & 0xFFFFFFFFu);
+    const Meta ma = d.meta[a], mb = d.meta[b];
+    uint4 r;
+    r.x = uint32_t(p);
+    r.y = uint32_t(a) | ((ma.flags & BODY_STATIC) ? 0x80000000u : 0u);
+    r.z = uint32_t(b) | ((mb.flags & BODY_STATIC) ? 0x80000000u : 0u);
+    r.w = (uint32_t(ma.local) & 0xFFFFu) | (uint32_t(mb.local) << 16);
+    return r;
+}
+
+template <class T>
+__device__ __forceinline__ void load_rec_body(const Dev<T> &d, uint32_t sw, int local, const Vel<T> *cache, SBody<T> &b)
+{
+    const int s = int(sw & 0x7FFFFFFFu);
+    b.is_static = (sw >> 31) != 0;
+    const Vel<T> ve = (cache && !b.is_static) ? cache[local] : d.vel[s];
+    b.v = ld3(ve.v);
+    b.w = ld3(ve.w);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) b.I[k] = d.iwinv[9 * s + k];
+    b.inv_mass = d.prm[s].inv_mass;
+}
+
+template <class T>
+__device__ __forceinline__ void store_rec_body(const Dev<T> &d, uint32_t sw, int local, Vel<T> *cache, const SBody<T> &b)
+{
+    if (b.is_static) return;
+    Vel<T> ve;
+    st3(ve.v, b.v);
+    st3(ve.w, b.w);
+    if (cache)
+        cache[local] = ve;
+    else
+        d.vel[int(sw & 0x7FFFFFFFu)] = ve;
+}
+
+template <class T> __device__ __forceinline__ void solve_manifold_rec(const Dev<T> &d, uint4 rec, Vel<T> *cache, bool warm)
+{
+    const int p = int(rec.x);
+    const int la = int(rec.w & 0xFFFFu), lb = int(rec.w >> 16);
+    SBody<T> A, B;
+    load_rec_body(d, rec.y, la, cache, A);
+    load_rec_body(d, rec.z, lb, cache, B);
+    const uint8_t mask = d.rowmask[p];
+    for (int q = 0; q < 4; ++q)
+    {
+        if (!(mask & (1u << q))) continue;
+        Row<T> r = d.rows[4 * p + q];
+        if (warm)
+            warm_contact(A, B, r);
+        else
+        {
+            solve_contact(A, B, r);
+            d.rows[4 * p + q].acc[0] = r.acc[0];
+            d.rows[4 * p + q].acc[1] = r.acc[1];
+            d.rows[4 * p + q].acc[2] = r.acc[2];
+        }
+    }
+    store_rec_body(d, rec.y, la, cache, A);
+    store_rec_body(d, rec.z, lb, cache, B);
 }
 
 template <class T>
@@ -1223,7 +1348,11 @@ __global__ void __launch_bounds__(256)
     for (int k = tid; k < na; k += nt)
     {
         int c = colour[k];
-        if (c >= 0 && c < kMaxColours) d.order[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = uint32_t(act[k]);
+        if (c >= 0 && c < kMaxColours)
+        {
+            const int p = act[k];
+            d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = make_solve_rec(d, p, sval[p]);
+        }
     }
     __syncthreads();
     // per-pair colour for read-back (-2: no contact rows)
@@ -1249,8 +1378,7 @@ __global__ void __launch_bounds__(256)
             const int cs = ms + cstart[c], cn = ccount[c];
             for (int k = tid; k < cn; k += nt)
             {
-                int p = int(d.order[cs + k]);
-                solve_manifold(d, p, sval[p], cache, it < 0);
+                solve_manifold_rec(d, d.srec[cs + k], cache, it < 0);
             }
             __syncthreads();
         }
@@ -1476,27 +1604,133 @@ template <class T> __global__ void k_integrate_pos(Dev<T> d, T dt)
     }
 }
 
-// Worlds that sit out this step keep last step's pairs (and, through them, their manifolds and
-// warm-start impulses), so a world's trajectory does not depend on which steps it skipped.
-template <class T> __global__ void k_carry_pairs(Dev<T> d)
+// Pair assembly. The sorted new pairs cover the active worlds only; each world that sits out the
+// step keeps last step's pair segment (and, through it, its manifolds and warm-start impulses), so
+// its trajectory does not depend on which steps it skipped. Pair keys are world-major, so the step's
+// full sorted list is the concatenation, world by world, of one of the two segments.
+template <class T> __global__ void k_pair_bounds(Dev<T> d, const uint64_t *__restrict__ skey)
 {
-    const int nold = *d.npairs_old;
-    PK_GRID_STRIDE(p, nold)
+    const int n = *d.nnew;
+    PK_GRID_STRIDE(p, n)
     {
-        uint64_t key = d.key_old[p];
-        int world = int(key >> (2 * d.lbits));
-        if (d.wp[world].active) continue;
-        uint64_t val = d.val_old[p];
-        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
-        if (!(d.meta[sa].flags & BODY_ALIVE) || !(d.meta[sb].flags & BODY_ALIVE)) continue;
-        int slot = atomicAdd(d.npairs, 1);
-        if (slot < d.pair_cap)
+        int w = int(skey[p] >> (2 * d.lbits));
+        if (p == 0 || int(skey[p - 1] >> (2 * d.lbits)) != w) d.nstart[w] = p;
+        if (p == n - 1 || int(skey[p + 1] >> (2 * d.lbits)) != w) d.nend[w] = p + 1;
+    }
+}
+
+// Kept pairs of an idle world: last step's segment minus pairs of bodies removed since (their
+// manifolds were already emptied by the removal). One CTA per world.
+template <class T> __device__ __forceinline__ bool kept_pair(const Dev<T> &d, int p)
+{
+    uint64_t v = d.val_old[p];
+    return (d.meta[int(v >> 32)].flags & BODY_ALIVE) && (d.meta[int(v & 0xFFFFFFFFu)].flags & BODY_ALIVE);
+}
+
+template <class T> __global__ void __launch_bounds__(256) k_kept_count(Dev<T> d)
+{
+    __shared__ int warp_sum[8];
+    const int w = blockIdx.x;
+    if (d.wp[w].active) return;
+    const int a = d.mstart_old[w], b = d.mend_old[w];
+    if (a >= b) return;
+    int c = 0;
+    for (int p = a + threadIdx.x; p < b; p += blockDim.x) c += kept_pair(d, p);
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        int t = 0;
+        for (int k = 0; k < int(blockDim.x >> 5); ++k) t += warp_sum[k];
+        d.nend[w] = t;
+    }
+}
+
+// One CTA: segment length of every world, exclusive scan -> the world's range in the assembled list.
+template <class T> __global__ void __launch_bounds__(1024) k_pair_segments(Dev<T> d)
+{
+    __shared__ int part[1024];
+    const int W = d.max_worlds;
+    const int per = (W + 1023) / 1024;
+    const int lo = min(W, int(threadIdx.x) * per), hi = min(W, lo + per);
+    int s = 0;
+    for (int w = lo; w < hi; ++w) s += d.nend[w] - d.nstart[w];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1)
+    {
+        int v = int(threadIdx.x) >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+    for (int w = lo; w < hi; ++w)
+    {
+        int len = d.nend[w] - d.nstart[w];
+        d.mstart[w] = min(run, d.pair_cap);
+        d.mend[w] = min(run + len, d.pair_cap);
+        run += len;
+    }
+    if (threadIdx.x == 1023)
+    {
+        if (run > d.pair_cap) atomicOr(d.status, ST_PAIR_OVERFLOW);
+        *d.npairs = min(run, d.pair_cap);
+    }
+}
+
+template <class T>
+__global__ void k_assemble_new(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval,
+                               uint64_t *__restrict__ akey, uint64_t *__restrict__ aval)
+{
+    const int n = *d.nnew;
+    PK_GRID_STRIDE(p, n)
+    {
+        uint64_t key = skey[p];
+        int w = int(key >> (2 * d.lbits));
+        int q = d.mstart[w] + (p - d.nstart[w]);
+        if (q < d.mend[w])
         {
-            d.pkey[slot] = key;
-            d.pval[slot] = val;
+            akey[q] = key;
+            aval[q] = sval[p];
         }
-        else
-            atomicOr(d.status, ST_PAIR_OVERFLOW);
+    }
+}
+
+// Order-preserving compaction of each idle world's kept pairs into its assembled range.
+template <class T> __global__ void __launch_bounds__(256) k_assemble_kept(Dev<T> d, uint64_t *__restrict__ akey,
+                                                                        uint64_t *__restrict__ aval)
+{
+    __shared__ int warp_cnt[8];
+    const int w = blockIdx.x;
+    if (d.wp[w].active) return;
+    const int a = d.mstart_old[w], b = d.mend_old[w];
+    const int out0 = d.mstart[w], out1 = d.mend[w];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int base = out0;
+    for (int c = a; c < b; c += blockDim.x)
+    {
+        int p = c + threadIdx.x;
+        bool keep = p < b && kept_pair(d, p);
+        unsigned m = __ballot_sync(0xFFFFFFFFu, keep);
+        if (lane == 0) warp_cnt[wid] = __popc(m);
+        __syncthreads();
+        int off = 0, tot = 0;
+        for (int k = 0; k < nw; ++k)
+        {
+            off += k < wid ? warp_cnt[k] : 0;
+            tot += warp_cnt[k];
+        }
+        int q = base + off + __popc(m & ((1u << lane) - 1u));
+        if (keep && q < out1)
+        {
+            akey[q] = d.key_old[p];
+            aval[q] = d.val_old[p];
+            d.old_idx[q] = p;
+        }
+        base += tot;
+        __syncthreads();
     }
 }
 
@@ -1508,6 +1742,7 @@ template <class T> __global__ void k_purge_world(Dev<T> d, uint32_t world)
     {
         if (uint32_t(d.key_old[p] >> (2 * d.lbits)) == world) d.man_old[p].n = 0;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.mend_old[world] = d.mstart_old[world]; // nothing to keep
 }
 
 template <class T> __global__ void k_kill_bodies(Dev<T> d, const int *slots, int n)
@@ -1527,6 +1762,11 @@ template <class T> __global__ void k_finish(Dev<T> d, const uint64_t *__restrict
     {
         d.key_old[p] = skey[p];
         d.val_old[p] = sval[p];
+    }
+    PK_GRID_STRIDE(w, d.max_worlds)
+    {
+        d.mstart_old[w] = d.mstart[w];
+        d.mend_old[w] = d.mend[w];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *d.npairs_old = np;
 }

@@ -106,8 +106,8 @@ public:
         PK_CUDA(alloc(&d.tbox, N));
         PK_CUDA(alloc(&d.meta, N));
         PK_CUDA(cudaMemset(d.meta, 0, sizeof(Meta) * N));
-        PK_CUDA(alloc(&counters_, 16));
-        PK_CUDA(cudaMemset(counters_, 0, sizeof(int) * 16));
+        PK_CUDA(alloc(&counters_, 32));
+        PK_CUDA(cudaMemset(counters_, 0, sizeof(int) * 32));
         d.nslots = counters_ + 0;
         d.nleaf = counters_ + 1;
         d.npairs = counters_ + 2;
@@ -119,6 +119,7 @@ public:
         d.gjk_count_heavy = counters_ + 8;
         d.epa_count_heavy = counters_ + 9;
         d.np_iters = reinterpret_cast<unsigned long long *>(counters_ + 10); // counters 10..15
+        d.nnew = counters_ + 16;
         int minus1 = -1;
         PK_CUDA(cudaMemcpy(d.epoch, &minus1, sizeof(int), cudaMemcpyHostToDevice));
         PK_CUDA(alloc(&d.wp, W));
@@ -127,6 +128,12 @@ public:
         PK_CUDA(alloc(&d.wroot, W));
         PK_CUDA(alloc(&d.mstart, W));
         PK_CUDA(alloc(&d.mend, W));
+        PK_CUDA(alloc(&d.mstart_old, W));
+        PK_CUDA(alloc(&d.mend_old, W));
+        PK_CUDA(alloc(&d.nstart, W));
+        PK_CUDA(alloc(&d.nend, W));
+        PK_CUDA(cudaMemset(d.mstart_old, 0, sizeof(int) * W));
+        PK_CUDA(cudaMemset(d.mend_old, 0, sizeof(int) * W));
         PK_CUDA(alloc(&d.ncolours, W));
         PK_CUDA(cudaMemset(d.ncolours, 0, sizeof(int) * W));
         {
@@ -173,6 +180,7 @@ public:
         PK_CUDA(alloc(&d.colour_tmp, P));
         PK_CUDA(alloc(&d.pair_colour, P));
         PK_CUDA(alloc(&d.order, P));
+        PK_CUDA(alloc(&d.srec, P));
         PK_CUDA(alloc(&d.owner, N));
         int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
         PK_CUDA(alloc(&hist_, size_t(kSortRadix) * hb));
@@ -743,11 +751,11 @@ private:
         for (int k = 0; k < 2; ++k)
             if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
         void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
-                      d_.wroot, d_.mstart, d_.mend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
+                      d_.wroot, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list,
                       d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
-                      d_.order, d_.owner, const_cast<int *>(d_.world_order),
+                      d_.order, d_.srec, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
@@ -770,14 +778,14 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 15 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 19 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
         PK_CUDA(mark(1));
         k_morton<T><<<gb, 256, 0, st_>>>(d);
-        // sort all slots by (world, Morton); dead slots sort to the end
-        bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nslots, cfg_.wbits + 30,
+        // sort the bodies of active worlds by (world, Morton)
+        bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nleaf, cfg_.wbits + 30,
                                         cfg_.sort_blocks_bodies, hist_, st_);
         const uint64_t *skey = in1 ? mkey_[1] : mkey_[0];
         const uint64_t *sval = in1 ? mval_[1] : mval_[0];
@@ -787,14 +795,24 @@ private:
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
         PK_CUDA(mark(3));
         k_traverse<T><<<(N + tune_.traverse_threads - 1) / tune_.traverse_threads, tune_.traverse_threads, 0, st_>>>(d, sval);
-        k_carry_pairs<T><<<gp, 256, 0, st_>>>(d);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
+        k_kept_count<T><<<cfg_.max_worlds, 256, 0, st_>>>(d);
         PK_CUDA(mark(4));
+        // sort the new pairs, then assemble every world's segment (new pairs of active worlds,
+        // kept pairs of idle ones) in world order into the sort's other buffer
         bool p1 = radix_sort<uint64_t>(pkey_[0], pval_[0], pkey_[1], pval_[1], d.npairs,
                                        cfg_.wbits + 2 * cfg_.lbits, cfg_.sort_blocks_pairs, hist_, st_);
-        const uint64_t *pk = p1 ? pkey_[1] : pkey_[0];
-        const uint64_t *pv = p1 ? pval_[1] : pval_[0];
-        last_sval_ = const_cast<uint64_t *>(pv);
+        const uint64_t *nk = p1 ? pkey_[1] : pkey_[0];
+        const uint64_t *nv = p1 ? pval_[1] : pval_[0];
+        uint64_t *ak = p1 ? pkey_[0] : pkey_[1];
+        uint64_t *av = p1 ? pval_[0] : pval_[1];
+        k_pair_bounds<T><<<gp, 256, 0, st_>>>(d, nk);
+        k_pair_segments<T><<<1, 1024, 0, st_>>>(d);
+        k_assemble_new<T><<<gp, 256, 0, st_>>>(d, nk, nv, ak, av);
+        k_assemble_kept<T><<<cfg_.max_worlds, 256, 0, st_>>>(d, ak, av);
+        const uint64_t *pk = ak;
+        const uint64_t *pv = av;
+        last_sval_ = av;
         PK_CUDA(mark(5));
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);

@@ -2,7 +2,7 @@
 // device memory, so the launches can be captured in a CUDA graph once and replayed every step.
 //
 // One pass per 8-bit digit, three kernels per pass:
-//   hist    : each CTA counts the digits of its contiguous chunk           -> hist[digit][cta]
+//   hist    : each CTA in use counts the digits of its contiguous chunk    -> hist[digit][cta]
 //   scan    : one CTA turns the digit-major table into exclusive offsets
 //   scatter : each CTA walks its chunk in 256-element tiles, ranks equal digits inside a warp with
 //             __match_any_sync, combines warps through shared-memory counters, and writes each
@@ -19,10 +19,27 @@ namespace pk
 constexpr int kSortThreads = 256;
 constexpr int kSortRadix = 256;
 
-__device__ __forceinline__ void sort_chunk(int n, int nblocks, int b, int &lo, int &hi)
+// Chunking of [0, n) over at most `nblocks` CTAs, at least kSortMinChunk elements per CTA, so
+// a short list touches one CTA and a short digit table (the cost of a pass follows n, not the
+// capacity the launches were sized for). CTAs at or past `used` have no chunk.
+constexpr int kSortMinChunk = 4096;
+
+__device__ __forceinline__ int sort_per(int n, int nblocks)
 {
     int per = (n + nblocks - 1) / nblocks;
-    per = (per + kSortThreads - 1) / kSortThreads * kSortThreads;
+    per = per > kSortMinChunk ? per : kSortMinChunk;
+    return (per + kSortThreads - 1) / kSortThreads * kSortThreads;
+}
+
+__device__ __forceinline__ int sort_used(int n, int nblocks)
+{
+    int per = sort_per(n, nblocks);
+    return (n + per - 1) / per;
+}
+
+__device__ __forceinline__ void sort_chunk(int n, int nblocks, int b, int &lo, int &hi)
+{
+    int per = sort_per(n, nblocks);
     lo = min(n, b * per);
     hi = min(n, lo + per);
 }
@@ -31,20 +48,24 @@ static __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint64_
                                                             int shift, uint32_t *__restrict__ hist)
 {
     __shared__ uint32_t h[kSortRadix];
+    const int n = *n_ptr;
+    const int used = sort_used(n, gridDim.x);
+    if (int(blockIdx.x) >= used) return;
     h[threadIdx.x] = 0;
     __syncthreads();
     int lo, hi;
-    sort_chunk(*n_ptr, gridDim.x, blockIdx.x, lo, hi);
+    sort_chunk(n, gridDim.x, blockIdx.x, lo, hi);
     for (int i = lo + threadIdx.x; i < hi; i += kSortThreads)
         atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
     __syncthreads();
-    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+    hist[threadIdx.x * used + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of `count` entries with one CTA of 1024 threads.
-static __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist, int count)
+// Exclusive scan of the digit table (256 x CTAs in use) with one CTA of 1024 threads.
+static __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist, const int *n_ptr, int nblocks)
 {
     __shared__ uint32_t part[1024];
+    const int count = kSortRadix * sort_used(*n_ptr, nblocks);
     int per = (count + 1023) / 1024;
     int lo = threadIdx.x * per, hi = min(count, lo + per);
     uint32_t s = 0;
@@ -101,10 +122,13 @@ __global__ void __launch_bounds__(kSortThreads)
     __shared__ uint32_t wcnt[W][kSortRadix + 1];
     __shared__ uint32_t tile_total[kSortRadix];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    base[t] = hist[t * gridDim.x + blockIdx.x];
+    const int n = *n_ptr;
+    const int used = sort_used(n, gridDim.x);
+    if (int(blockIdx.x) >= used) return;
+    base[t] = hist[t * used + blockIdx.x];
     running[t] = 0;
     int lo, hi;
-    sort_chunk(*n_ptr, gridDim.x, blockIdx.x, lo, hi);
+    sort_chunk(n, gridDim.x, blockIdx.x, lo, hi);
     const unsigned lt_mask = (1u << lane) - 1u;
     for (int tile = lo; tile < hi; tile += kSortThreads)
     {
@@ -158,7 +182,7 @@ inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_de
     {
         int shift = 8 * p;
         k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n_dev, shift, hist);
-        k_sort_scan<<<1, 1024, 0, st>>>(hist, kSortRadix * nblocks);
+        k_sort_scan<<<1, 1024, 0, st>>>(hist, n_dev, nblocks);
         k_sort_scatter<V><<<nblocks, kSortThreads, 0, st>>>(ka, va, kb, vb, n_dev, shift, hist);
         uint64_t *tk = ka;
         ka = kb;
