@@ -157,7 +157,8 @@ const char *pk_stage_name(int32_t stage);
 
 /* Autotuner: picks the launch shapes of the step (solver CTA size and the split between the
  * solver's large- and small-world launches, narrowphase grid, traversal block size) by timing
- * each stage over `steps_per_candidate` real steps per candidate. These steps advance the world
+ * each stage over `steps_per_candidate` real steps per candidate; large worlds get their own
+ * solver CTA size. These steps advance the world
  * like pk_world_step; launch shapes do not change results. Call before pk_world_capture. */
 typedef struct pk_tune_result
 {
@@ -168,7 +169,7 @@ typedef struct pk_tune_result
     double step_ms_before; /* summed stage times per step before and after tuning */
     double step_ms_after;
     int32_t steps_used;
-    int32_t reserved;
+    int32_t big_threads; /* solver CTA size of the worlds above small_world (0: solve_threads) */
 } pk_tune_result;
 int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tune_result *out);
 /* Apply launch shapes found by pk_world_autotune (e.g. on a scratch copy of the same scene). */

@@ -816,6 +816,25 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
             }
         best = bc;
     }
+    // CTA size of the large-world launch (its worlds are the solver's critical path)
+    {
+        double bt = 1e300;
+        pk::Tunables bc = best;
+        for (int th : {128, 256, 512})
+        {
+            pk::Tunables t = best;
+            t.big_threads = th;
+            w->eng->set_tunables(t);
+            if ((rc = timed_steps(w, dt, k, st))) return rc;
+            used += k;
+            if (st[S_SOLVE] < bt)
+            {
+                bt = st[S_SOLVE];
+                bc = t;
+            }
+        }
+        best = bc;
+    }
     // narrowphase grid
     {
         double bt = 1e300;
@@ -867,7 +886,7 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
         out->step_ms_before = before;
         out->step_ms_after = total(st);
         out->steps_used = used;
-        out->reserved = 0;
+        out->big_threads = best.big_threads;
     }
     return PK_OK;
 }
@@ -875,15 +894,16 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
 int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
 {
     if (!w || !t) return PK_ERR_INVALID;
-    if (t->solve_threads < 32 || t->solve_threads > 256 || (t->solve_threads & 31) || t->small_world < 1 ||
+    if (t->solve_threads < 32 || t->solve_threads > 512 || (t->solve_threads & 31) || t->small_world < 1 ||
         t->narrow_grid < 1 || t->narrow_grid > 16 || t->traverse_threads < 32 || t->traverse_threads > 1024 ||
-        (t->traverse_threads & 31))
+        (t->traverse_threads & 31) || t->big_threads < 0 || t->big_threads > 512 || (t->big_threads & 31))
         return PK_ERR_INVALID;
     pk::Tunables tu;
     tu.solve_threads = t->solve_threads;
     tu.small_world = t->small_world;
     tu.narrow_grid = t->narrow_grid;
     tu.traverse_threads = t->traverse_threads;
+    tu.big_threads = t->big_threads > 0 ? t->big_threads : t->solve_threads;
     w->eng->set_tunables(tu);
     return PK_OK;
 }

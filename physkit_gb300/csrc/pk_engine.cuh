@@ -23,6 +23,7 @@
 
 #include <cooperative_groups.h>
 #include <cstdint>
+#include <cstring>
 #include <type_traits>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -48,6 +49,8 @@ enum : int
 };
 
 constexpr int kMaxColours = 512;
+constexpr int kSolveMaxThreads = 512; // largest solver CTA (FP32 form; the FP64 form's register need caps it at 256)
+template <class T> constexpr int solve_max_threads() { return sizeof(T) == 4 ? kSolveMaxThreads : 256; }
 constexpr uint32_t kLeafBit = 0x80000000u;
 
 template <class T> struct Pose
@@ -91,8 +94,31 @@ template <class T> struct Row
     T t2[3], wa_t2[3], wb_t2[3];
     T meff_t2;
     T inv11, inv12, inv22, mu;
-    double acc[3];
+    T pad; // 36 values: whole 16-byte vectors
 };
+static_assert(sizeof(Row<float>) == 144 && sizeof(Row<double>) == 288, "Row is loaded as 16-byte vectors");
+// FP32 form's row: besides the Jacobian (direction, angular parts wa/wb) it stores the velocity
+// change per unit impulse of each body's rotation, ka = I_a^-1 wa and kb = I_b^-1 wb (computed
+// anyway for the effective masses), so applying an impulse is three multiply-adds per body and
+// the sweep reads no inertia tensors.
+struct RowF
+{
+    float n[3], wa_n[3], wb_n[3], ka_n[3], kb_n[3];
+    float t1[3], wa_t1[3], wb_t1[3], ka_t1[3], kb_t1[3];
+    float t2[3], wa_t2[3], wb_t2[3], ka_t2[3], kb_t2[3];
+    float meff_n, bias, inv11, inv12, inv22, mu;
+    float pad;
+};
+static_assert(sizeof(RowF) == 208, "RowF is loaded as 16-byte vectors");
+template <class T> struct RowSel
+{
+    using type = Row<T>;
+};
+template <> struct RowSel<float>
+{
+    using type = RowF;
+};
+template <class T> using RowT = typename RowSel<T>::type;
 template <class T> struct WorldParams
 {
     T g[3];
@@ -168,7 +194,10 @@ template <class T> struct Dev
     int *epa_count;
     int *epa_count_heavy;
     unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
-    Row<T> *rows;
+    RowT<T> *rows;         // 4 per pair, read-only while the solver sweeps
+    double *racc;          // 12 per pair: accumulated impulses (normal, t1, t2) of the 4 rows
+    float *raccf;          // FP32 form: running totals in FP32 (clamp decisions, warm start)
+    float *rdel;           // FP32 form: this step's change, added to racc once after the sweeps
     uint8_t *rowmask;
     int *colour;      // solver scratch: compacted active manifolds of each world
     int *colour_tmp;  // solver scratch: colour of each compacted manifold
@@ -178,6 +207,7 @@ template <class T> struct Dev
     int *ncolours;
     const int *world_order; // solver CTA -> world, largest worlds first
     uint4 *srec;            // solve records of the active manifolds, colour-ordered per world
+    uint4 *crec;            // the same records in pair order (colouring input)
     const int *world_nlocal; // local indices in use per world (bounds the shared-memory cache)
     // control
     int *status;
@@ -936,10 +966,44 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
                 row.inv22 = row.meff_t2;
                 row.inv12 = T(0);
             }
-            row.acc[0] = c.imp[0];
-            row.acc[1] = c.imp[1];
-            row.acc[2] = c.imp[2];
-            d.rows[4 * p + k] = row;
+            row.pad = T(0);
+            if constexpr (std::is_same<T, float>::value)
+            {
+                RowF rf;
+                st3(rf.n, n);
+                st3(rf.wa_n, wa);
+                st3(rf.wb_n, wb);
+                st3(rf.ka_n, ka);
+                st3(rf.kb_n, kb);
+                st3(rf.t1, t1);
+                st3(rf.wa_t1, wa1);
+                st3(rf.wb_t1, wb1);
+                st3(rf.ka_t1, ka1);
+                st3(rf.kb_t1, kb1);
+                st3(rf.t2, t2);
+                st3(rf.wa_t2, wa2);
+                st3(rf.wb_t2, wb2);
+                st3(rf.ka_t2, ka2);
+                st3(rf.kb_t2, kb2);
+                rf.meff_n = row.meff_n;
+                rf.bias = row.bias;
+                rf.inv11 = row.inv11;
+                rf.inv12 = row.inv12;
+                rf.inv22 = row.inv22;
+                rf.mu = row.mu;
+                rf.pad = 0.0f;
+                d.rows[4 * p + k] = rf;
+                for (int j = 0; j < 3; ++j)
+                {
+                    d.raccf[12 * size_t(p) + 3 * k + j] = float(c.imp[j]);
+                    d.rdel[12 * size_t(p) + 3 * k + j] = 0.0f;
+                }
+            }
+            else
+                d.rows[4 * p + k] = row;
+            d.racc[12 * size_t(p) + 3 * k + 0] = c.imp[0];
+            d.racc[12 * size_t(p) + 3 * k + 1] = c.imp[1];
+            d.racc[12 * size_t(p) + 3 * k + 2] = c.imp[2];
             mask |= uint8_t(1u << k);
         }
         d.rowmask[p] = mask;
@@ -981,88 +1045,118 @@ template <class T> __device__ __forceinline__ void apply_reg(SBody<T> &a, SBody<
     }
 }
 
-template <class T> __device__ __forceinline__ void warm_contact(SBody<T> &A, SBody<T> &B, const Row<T> &r)
+template <class T> __device__ __forceinline__ void warm_contact(SBody<T> &A, SBody<T> &B, const Row<T> &r, const double *acc)
 {
     // jacobian_row::warm_start for the three rows (constraint.h:73-87, 1125-1130)
-    if (r.acc[0] != 0.0) apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), T(r.acc[0]));
-    if (r.acc[1] != 0.0) apply_reg(A, B, ld3(r.t1), ld3(r.wa_t1), ld3(r.wb_t1), T(r.acc[1]));
-    if (r.acc[2] != 0.0) apply_reg(A, B, ld3(r.t2), ld3(r.wa_t2), ld3(r.wb_t2), T(r.acc[2]));
+    if (acc[0] != 0.0) apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), T(acc[0]));
+    if (acc[1] != 0.0) apply_reg(A, B, ld3(r.t1), ld3(r.wa_t1), ld3(r.wb_t1), T(acc[1]));
+    if (acc[2] != 0.0) apply_reg(A, B, ld3(r.t2), ld3(r.wa_t2), ld3(r.wb_t2), T(acc[2]));
 }
 
-// FP32 form of one contact: the accumulated impulses stay FP64 (one add per row, the clamp at zero
-// and the difference that is applied), the rest is FP32, including the friction-cone rescale
-// (sqrt and divide), so the dependent chain holds a handful of FP64 operations instead of a
-// software FP64 square root and divide per contact.
-__device__ __forceinline__ void solve_contact_f32(SBody<float> &A, SBody<float> &B, Row<float> &r)
+// FP32 form: apply an impulse along one direction (J, with the rotation responses ka and kb).
+__device__ __forceinline__ void apply_f32(SBody<float> &A, SBody<float> &B, const float *J, const float *ka, const float *kb,
+                                          float lam)
+{
+    if (!A.is_static)
+    {
+        A.v = A.v + ld3(J) * (lam * A.inv_mass);
+        A.w = A.w + ld3(ka) * lam;
+    }
+    if (!B.is_static)
+    {
+        B.v = B.v - ld3(J) * (lam * B.inv_mass);
+        B.w = B.w + ld3(kb) * lam;
+    }
+}
+
+// FP32 form of one contact (constraint.h:49-71 and 1138-1187 in FP32). The accumulated impulses
+// are FP64 across steps; within a step, the running total is carried in FP32 (tot: clamp
+// decisions) and the change in FP32 (del), which is added to the FP64 accumulator (base) once
+// after the sweeps. Clamping the normal impulse at zero sets the FP64 accumulator to exactly zero.
+// FP64 issues at a small fraction of the FP32 rate here, so the sweeps hold no FP64 arithmetic.
+__device__ __forceinline__ void solve_contact_f32(SBody<float> &A, SBody<float> &B, const RowF &r, float *tot, float *del,
+                                                  double *base)
 {
     {
         float Jv = jv_reg(r.n, r.wa_n, r.wb_n, A, B);
         float lambda = -(Jv + r.bias) * r.meff_n;
-        double old = r.acc[0];
-        double v = old + double(lambda);
-        double acc = v < 0.0 ? 0.0 : v;
-        r.acc[0] = acc;
-        apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), float(acc - old));
+        float nf = tot[0] + lambda;
+        float dl;
+        if (nf < 0.0f)
+        {
+            dl = -tot[0];
+            tot[0] = 0.0f;
+            del[0] = 0.0f;
+            *base = 0.0;
+        }
+        else
+        {
+            dl = lambda;
+            tot[0] = nf;
+            del[0] = del[0] + lambda;
+        }
+        apply_f32(A, B, r.n, r.ka_n, r.kb_n, dl);
     }
-    float maxf = r.mu * float(r.acc[0]);
+    float maxf = r.mu * tot[0];
     float b1 = jv_reg(r.t1, r.wa_t1, r.wb_t1, A, B);
     float b2 = jv_reg(r.t2, r.wa_t2, r.wb_t2, A, B);
     float l1 = -(r.inv11 * b1 + r.inv12 * b2);
     float l2 = -(r.inv12 * b1 + r.inv22 * b2);
-    double o1 = r.acc[1], o2 = r.acc[2];
-    double n1 = o1 + double(l1), n2 = o2 + double(l2);
-    float f1 = float(n1), f2 = float(n2);
-    float mag2 = f1 * f1 + f2 * f2;
+    float o1 = tot[1], o2 = tot[2];
+    float n1 = o1 + l1, n2 = o2 + l2;
+    float mag2 = n1 * n1 + n2 * n2;
     if (mag2 > maxf * maxf)
     {
-        float sc = maxf / sqrtf(mag2);
-        n1 = n1 * double(sc);
-        n2 = n2 * double(sc);
+        float sc = maxf * rsqrtf(mag2);
+        n1 = n1 * sc;
+        n2 = n2 * sc;
     }
-    r.acc[1] = n1;
-    r.acc[2] = n2;
-    float a1 = float(n1 - o1), a2 = float(n2 - o2);
+    float a1 = n1 - o1, a2 = n2 - o2;
+    tot[1] = n1;
+    tot[2] = n2;
+    del[1] = del[1] + a1;
+    del[2] = del[2] + a2;
     if (!A.is_static)
     {
-        V3<float> imp = ld3(r.t1) * a1 + ld3(r.t2) * a2;
-        A.v = A.v + imp * A.inv_mass;
-        A.w = A.w + matvec(A.I, ld3(r.wa_t1) * a1 + ld3(r.wa_t2) * a2);
+        A.v = A.v + (ld3(r.t1) * a1 + ld3(r.t2) * a2) * A.inv_mass;
+        A.w = A.w + ld3(r.ka_t1) * a1 + ld3(r.ka_t2) * a2;
     }
     if (!B.is_static)
     {
-        V3<float> imp = (-ld3(r.t1)) * a1 - ld3(r.t2) * a2;
-        B.v = B.v + imp * B.inv_mass;
-        B.w = B.w + matvec(B.I, ld3(r.wb_t1) * a1 + ld3(r.wb_t2) * a2);
+        B.v = B.v - (ld3(r.t1) * a1 + ld3(r.t2) * a2) * B.inv_mass;
+        B.w = B.w + ld3(r.kb_t1) * a1 + ld3(r.kb_t2) * a2;
     }
 }
 
-template <class T> __device__ __forceinline__ void solve_contact(SBody<T> &A, SBody<T> &B, Row<T> &r)
+__device__ __forceinline__ void warm_contact_f32(SBody<float> &A, SBody<float> &B, const RowF &r, const float *tot)
 {
-    if constexpr (std::is_same<T, float>::value)
-    {
-        solve_contact_f32(A, B, r);
-        return;
-    }
+    if (tot[0] != 0.0f) apply_f32(A, B, r.n, r.ka_n, r.kb_n, tot[0]);
+    if (tot[1] != 0.0f) apply_f32(A, B, r.t1, r.ka_t1, r.kb_t1, tot[1]);
+    if (tot[2] != 0.0f) apply_f32(A, B, r.t2, r.ka_t2, r.kb_t2, tot[2]);
+}
+
+template <class T> __device__ __forceinline__ void solve_contact(SBody<T> &A, SBody<T> &B, const Row<T> &r, double *acc_)
+{
     // normal row: jacobian_row::apply (constraint.h:49-71), gamma = 0
     {
         T Jv = jv_reg(r.n, r.wa_n, r.wb_n, A, B);
-        T cfp = T(0) * T(r.acc[0]);
+        T cfp = T(0) * T(acc_[0]);
         T lambda = -(Jv + r.bias + cfp) * r.meff_n;
-        double old = r.acc[0];
+        double old = acc_[0];
         double v = old + double(lambda);
         double lo = 0.0, hi = 1.7976931348623157e308;
         double acc = (v < lo) ? lo : ((hi < v) ? hi : v);
-        r.acc[0] = acc;
+        acc_[0] = acc;
         apply_reg(A, B, ld3(r.n), ld3(r.wa_n), ld3(r.wb_n), T(acc - old));
     }
     // coupled 2D friction with circular cone clamp (constraint.h:1138-1187)
-    T maxf = r.mu * T(r.acc[0]);
+    T maxf = r.mu * T(acc_[0]);
     T Jv1 = jv_reg(r.t1, r.wa_t1, r.wb_t1, A, B);
     T Jv2 = jv_reg(r.t2, r.wa_t2, r.wb_t2, A, B);
     T b1 = Jv1 + T(0), b2 = Jv2 + T(0);
     T l1 = -(r.inv11 * b1 + r.inv12 * b2);
     T l2 = -(r.inv12 * b1 + r.inv22 * b2);
-    double o1 = r.acc[1], o2 = r.acc[2];
+    double o1 = acc_[1], o2 = acc_[2];
     double n1 = o1 + double(l1), n2 = o2 + double(l2);
     double mag = pk_sqrt(n1 * n1 + n2 * n2);
     if (mag > double(maxf))
@@ -1070,8 +1164,8 @@ template <class T> __device__ __forceinline__ void solve_contact(SBody<T> &A, SB
         n1 = n1 * (double(maxf) / mag);
         n2 = n2 * (double(maxf) / mag);
     }
-    r.acc[1] = n1;
-    r.acc[2] = n2;
+    acc_[1] = n1;
+    acc_[2] = n2;
     T a1 = T(n1 - o1), a2 = T(n2 - o2);
     if (!A.is_static)
     {
@@ -1122,7 +1216,112 @@ template <class T> __device__ __forceinline__ void store_sbody(const Dev<T> &d, 
         d.vel[s] = ve;
 }
 
-// One manifold: warm start (warm = true) or one Gauss-Seidel pass over its contacts in order.
+// Rows do not change while the solver sweeps: read-only vector loads, which the compiler may issue
+// for all of a manifold's rows before the first contact is solved.
+template <class R> __device__ __forceinline__ R ldg_row(const R *src)
+{
+    constexpr int nv = int(sizeof(R) / 16);
+    float4 v[nv];
+    const float4 *s = reinterpret_cast<const float4 *>(src);
+#pragma unroll
+    for (int i = 0; i < nv; ++i) v[i] = __ldg(s + i);
+    R r;
+    memcpy(&r, v, sizeof(r));
+    return r;
+}
+
+// The contact rows of one manifold: warm start (warm = true) or one Gauss-Seidel pass in order.
+__device__ __forceinline__ void solve_rows(const Dev<float> &d, int p, SBody<float> &A, SBody<float> &B, bool warm)
+{
+    const uint8_t mask = d.rowmask[p];
+    float tot[12];
+    float4 *tp = reinterpret_cast<float4 *>(d.raccf + 12 * size_t(p));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        float4 v = tp[i];
+        tot[4 * i] = v.x;
+        tot[4 * i + 1] = v.y;
+        tot[4 * i + 2] = v.z;
+        tot[4 * i + 3] = v.w;
+    }
+    const RowF *rp = d.rows + 4 * size_t(p);
+    if (warm)
+    {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (mask & (1u << q)) warm_contact_f32(A, B, ldg_row(rp + q), tot + 3 * q);
+        return;
+    }
+    float del[12];
+    float4 *dp = reinterpret_cast<float4 *>(d.rdel + 12 * size_t(p));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        float4 v = dp[i];
+        del[4 * i] = v.x;
+        del[4 * i + 1] = v.y;
+        del[4 * i + 2] = v.z;
+        del[4 * i + 3] = v.w;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (mask & (1u << q)) solve_contact_f32(A, B, ldg_row(rp + q), tot + 3 * q, del + 3 * q, d.racc + 12 * size_t(p) + 3 * q);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        tp[i] = make_float4(tot[4 * i], tot[4 * i + 1], tot[4 * i + 2], tot[4 * i + 3]);
+        dp[i] = make_float4(del[4 * i], del[4 * i + 1], del[4 * i + 2], del[4 * i + 3]);
+    }
+}
+
+__device__ __forceinline__ void solve_rows(const Dev<double> &d, int p, SBody<double> &A, SBody<double> &B, bool warm)
+{
+    const uint8_t mask = d.rowmask[p];
+    double acc[12];
+    double2 *ap = reinterpret_cast<double2 *>(d.racc + 12 * size_t(p));
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+    {
+        double2 v = ap[i];
+        acc[2 * i] = v.x;
+        acc[2 * i + 1] = v.y;
+    }
+    const Row<double> *rp = d.rows + 4 * size_t(p);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+    {
+        if (!(mask & (1u << q))) continue;
+        const Row<double> r = ldg_row(rp + q);
+        if (warm)
+            warm_contact(A, B, r, acc + 3 * q);
+        else
+            solve_contact(A, B, r, acc + 3 * q);
+    }
+    if (!warm)
+    {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) ap[i] = make_double2(acc[2 * i], acc[2 * i + 1]);
+    }
+}
+
+// Accumulated impulses of row q of pair p into the manifold cache (the FP32 form adds this
+// step's change to the FP64 accumulator here, once).
+template <class T> __device__ __forceinline__ void store_impulses(const Dev<T> &d, int p, int q)
+{
+    const size_t o = 12 * size_t(p) + 3 * q;
+    Contact<T> &c = d.man_new[p].c[q];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+    {
+        if constexpr (std::is_same<T, float>::value)
+            c.imp[j] = d.racc[o + j] + double(d.rdel[o + j]);
+        else
+            c.imp[j] = d.racc[o + j];
+    }
+}
+
+// One manifold by pair index (the grid-wide solver).
 template <class T>
 __device__ __forceinline__ void solve_manifold(const Dev<T> &d, int p, uint64_t sv, Vel<T> *cache, bool warm,
                                                bool coherent = false)
@@ -1131,21 +1330,7 @@ __device__ __forceinline__ void solve_manifold(const Dev<T> &d, int p, uint64_t 
     SBody<T> A, B;
     load_sbody(d, sa, cache, A, coherent);
     load_sbody(d, sb, cache, B, coherent);
-    const uint8_t mask = d.rowmask[p];
-    for (int q = 0; q < 4; ++q)
-    {
-        if (!(mask & (1u << q))) continue;
-        Row<T> r = d.rows[4 * p + q];
-        if (warm)
-            warm_contact(A, B, r);
-        else
-        {
-            solve_contact(A, B, r);
-            d.rows[4 * p + q].acc[0] = r.acc[0];
-            d.rows[4 * p + q].acc[1] = r.acc[1];
-            d.rows[4 * p + q].acc[2] = r.acc[2];
-        }
-    }
+    solve_rows(d, p, A, B, warm);
     store_sbody(d, sa, cache, A);
     store_sbody(d, sb, cache, B);
 }
@@ -1167,19 +1352,6 @@ template <class T> __device__ __forceinline__ uint4 make_solve_rec(const Dev<T> 
 }
 
 template <class T>
-__device__ __forceinline__ void load_rec_body(const Dev<T> &d, uint32_t sw, int local, const Vel<T> *cache, SBody<T> &b)
-{
-    const int s = int(sw & 0x7FFFFFFFu);
-    b.is_static = (sw >> 31) != 0;
-    const Vel<T> ve = (cache && !b.is_static) ? cache[local] : d.vel[s];
-    b.v = ld3(ve.v);
-    b.w = ld3(ve.w);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) b.I[k] = d.iwinv[9 * s + k];
-    b.inv_mass = d.prm[s].inv_mass;
-}
-
-template <class T>
 __device__ __forceinline__ void store_rec_body(const Dev<T> &d, uint32_t sw, int local, Vel<T> *cache, const SBody<T> &b)
 {
     if (b.is_static) return;
@@ -1192,41 +1364,44 @@ __device__ __forceinline__ void store_rec_body(const Dev<T> &d, uint32_t sw, int
         d.vel[int(sw & 0x7FFFFFFFu)] = ve;
 }
 
+template <class T>
+__device__ __forceinline__ void load_rec_body(const Dev<T> &d, uint32_t sw, int local, const Vel<T> *cache, SBody<T> &b)
+{
+    const int s = int(sw & 0x7FFFFFFFu);
+    b.is_static = (sw >> 31) != 0;
+    const Vel<T> ve = (cache && !b.is_static) ? cache[local] : d.vel[s];
+    b.v = ld3(ve.v);
+    b.w = ld3(ve.w);
+    if constexpr (!std::is_same<T, float>::value) // the FP32 rows carry I^-1 J
+    {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) b.I[k] = d.iwinv[9 * s + k];
+    }
+    b.inv_mass = d.prm[s].inv_mass;
+}
+
 template <class T> __device__ __forceinline__ void solve_manifold_rec(const Dev<T> &d, uint4 rec, Vel<T> *cache, bool warm)
 {
-    const int p = int(rec.x);
     const int la = int(rec.w & 0xFFFFu), lb = int(rec.w >> 16);
     SBody<T> A, B;
     load_rec_body(d, rec.y, la, cache, A);
     load_rec_body(d, rec.z, lb, cache, B);
-    const uint8_t mask = d.rowmask[p];
-    for (int q = 0; q < 4; ++q)
-    {
-        if (!(mask & (1u << q))) continue;
-        Row<T> r = d.rows[4 * p + q];
-        if (warm)
-            warm_contact(A, B, r);
-        else
-        {
-            solve_contact(A, B, r);
-            d.rows[4 * p + q].acc[0] = r.acc[0];
-            d.rows[4 * p + q].acc[1] = r.acc[1];
-            d.rows[4 * p + q].acc[2] = r.acc[2];
-        }
-    }
+    solve_rows(d, int(rec.x), A, B, warm);
     store_rec_body(d, rec.y, la, cache, A);
     store_rec_body(d, rec.z, lb, cache, B);
 }
 
-template <class T>
-__global__ void __launch_bounds__(256)
+// MAXT: the largest CTA the instance is compiled for (256, or 512 for the FP32 form's large worlds;
+// the 512 instance gives up registers for threads).
+template <class T, int MAXT>
+__global__ void __launch_bounds__(MAXT)
     k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies, int grid_world)
 {
     extern __shared__ __align__(16) unsigned char solve_smem[];
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
-    __shared__ int wsum[8];
+    __shared__ int wsum[MAXT / 32];
     __shared__ int remaining;
     __shared__ int nactive;
     const int blk = first_block + int(blockIdx.x);
@@ -1243,28 +1418,42 @@ __global__ void __launch_bounds__(256)
     const bool fits = d.world_nlocal[w] <= cache_bodies;
     Vel<T> *cache = fits ? reinterpret_cast<Vel<T> *>(solve_smem) : nullptr;
     uint32_t *sowner = fits ? reinterpret_cast<uint32_t *>(solve_smem) : nullptr; // during colouring only
-    int *act = d.colour + ms; // compacted active manifolds of this world, ascending p
+    uint4 *rec = d.crec + ms; // solve records of the active manifolds, ascending pair index
 
-    // 1. compact the manifolds that have contact rows (stable: ascending pair index)
-    if (tid == 0) nactive = 0;
-    __syncthreads();
-    for (int base = ms; base < me; base += nt)
+    // 1. compact the manifolds that have contact rows (stable: ascending pair index). Each thread
+    //    takes a contiguous run of pairs, counts, and after one block scan writes its records.
     {
-        int p = base + tid;
-        bool a = p < me && d.rowmask[p] != 0;
-        unsigned bal = __ballot_sync(0xFFFFFFFFu, a);
-        if (lane == 0) wsum[warp] = __popc(bal);
-        __syncthreads();
-        int off = nactive;
-        for (int k = 0; k < warp; ++k) off += wsum[k];
-        if (a) act[off + __popc(bal & ((1u << lane) - 1u))] = p;
+        const int per = (me - ms + nt - 1) / nt;
+        const int lo = min(me, ms + tid * per), hi = min(me, lo + per);
+        int cnt = 0;
+        for (int p = lo; p < hi; ++p) cnt += d.rowmask[p] != 0;
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) wsum[warp] = incl;
         __syncthreads();
         if (tid == 0)
-            for (int k = 0; k < nt / 32; ++k) nactive += wsum[k];
+        {
+            int run = 0;
+            for (int k = 0; k < nt / 32; ++k)
+            {
+                int v = wsum[k];
+                wsum[k] = run;
+                run += v;
+            }
+            nactive = run;
+        }
         __syncthreads();
+        int off = wsum[warp] + incl - cnt;
+        for (int p = lo; p < hi; ++p)
+            if (d.rowmask[p] != 0) rec[off++] = make_solve_rec(d, p, sval[p]);
     }
+    __syncthreads();
     const int na = nactive;
-    int *colour = d.colour_tmp + ms; // colour of act[k]
+    int *colour = d.colour_tmp + ms; // colour of rec[k]
     for (int k = tid; k < na; k += nt) colour[k] = -1;
     for (int c = tid; c < kMaxColours; c += nt)
     {
@@ -1275,7 +1464,8 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
 
     // 2. colouring: each uncoloured manifold claims its dynamic bodies with its index; the winners
-    //    of all their bodies take the round number
+    //    of all their bodies take the round number. Bodies are keyed by world-local index when the
+    //    owner table fits in shared memory, else by slot.
     int round = 0;
     while (remaining > 0)
     {
@@ -1283,36 +1473,27 @@ __global__ void __launch_bounds__(256)
         for (int k = tid; k < na; k += nt)
         {
             if (colour[k] != -1) continue;
-            int p = act[k];
-            uint64_t v = sval[p];
-            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            const Meta ma = d.meta[a], mb = d.meta[b];
-            if (!(ma.flags & BODY_STATIC)) { if (sowner) sowner[ma.local] = 0xFFFFFFFFu; else d.owner[a] = 0xFFFFFFFFu; }
-            if (!(mb.flags & BODY_STATIC)) { if (sowner) sowner[mb.local] = 0xFFFFFFFFu; else d.owner[b] = 0xFFFFFFFFu; }
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) { if (sowner) sowner[r.w & 0xFFFFu] = 0xFFFFFFFFu; else d.owner[r.y] = 0xFFFFFFFFu; }
+            if (!(r.z >> 31)) { if (sowner) sowner[r.w >> 16] = 0xFFFFFFFFu; else d.owner[r.z] = 0xFFFFFFFFu; }
         }
         if (tid == 0) remaining = 0;
         __syncthreads();
         for (int k = tid; k < na; k += nt)
         {
             if (colour[k] != -1) continue;
-            int p = act[k];
-            uint64_t v = sval[p];
-            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            const Meta ma = d.meta[a], mb = d.meta[b];
-            if (!(ma.flags & BODY_STATIC)) { if (sowner) atomicMin(sowner + ma.local, uint32_t(k)); else atomicMin(d.owner + a, uint32_t(k)); }
-            if (!(mb.flags & BODY_STATIC)) { if (sowner) atomicMin(sowner + mb.local, uint32_t(k)); else atomicMin(d.owner + b, uint32_t(k)); }
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) { if (sowner) atomicMin(sowner + (r.w & 0xFFFFu), uint32_t(k)); else atomicMin(d.owner + r.y, uint32_t(k)); }
+            if (!(r.z >> 31)) { if (sowner) atomicMin(sowner + (r.w >> 16), uint32_t(k)); else atomicMin(d.owner + r.z, uint32_t(k)); }
         }
         __syncthreads();
         int left = 0;
         for (int k = tid; k < na; k += nt)
         {
             if (colour[k] != -1) continue;
-            int p = act[k];
-            uint64_t v = sval[p];
-            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            const Meta ma = d.meta[a], mb = d.meta[b];
-            bool oka = (ma.flags & BODY_STATIC) || (sowner ? sowner[ma.local] : d.owner[a]) == uint32_t(k);
-            bool okb = (mb.flags & BODY_STATIC) || (sowner ? sowner[mb.local] : d.owner[b]) == uint32_t(k);
+            const uint4 r = rec[k];
+            bool oka = (r.y >> 31) || (sowner ? sowner[r.w & 0xFFFFu] : d.owner[r.y]) == uint32_t(k);
+            bool okb = (r.z >> 31) || (sowner ? sowner[r.w >> 16] : d.owner[r.z]) == uint32_t(k);
             if (oka && okb)
                 colour[k] = round;
             else
@@ -1348,24 +1529,19 @@ __global__ void __launch_bounds__(256)
     for (int k = tid; k < na; k += nt)
     {
         int c = colour[k];
-        if (c >= 0 && c < kMaxColours)
-        {
-            const int p = act[k];
-            d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = make_solve_rec(d, p, sval[p]);
-        }
+        const uint4 r = rec[k];
+        if (c >= 0 && c < kMaxColours) d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = r;
+        d.pair_colour[r.x] = c; // per-pair colour for read-back (-2: no contact rows)
     }
     __syncthreads();
-    // per-pair colour for read-back (-2: no contact rows)
-    for (int k = tid; k < na; k += nt) d.pair_colour[act[k]] = colour[k];
     if (cache)
     {
         // the owner table is done; the shared memory now caches body velocities
         for (int k = tid; k < na; k += nt)
         {
-            uint64_t v = sval[act[k]];
-            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            if (!(d.meta[a].flags & BODY_STATIC)) cache[d.meta[a].local] = d.vel[a];
-            if (!(d.meta[b].flags & BODY_STATIC)) cache[d.meta[b].local] = d.vel[b];
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) cache[r.w & 0xFFFFu] = d.vel[r.y];
+            if (!(r.z >> 31)) cache[r.w >> 16] = d.vel[r.z];
         }
     }
     __syncthreads();
@@ -1376,10 +1552,7 @@ __global__ void __launch_bounds__(256)
         for (int c = 0; c < ncol; ++c)
         {
             const int cs = ms + cstart[c], cn = ccount[c];
-            for (int k = tid; k < cn; k += nt)
-            {
-                solve_manifold_rec(d, d.srec[cs + k], cache, it < 0);
-            }
+            for (int k = tid; k < cn; k += nt) solve_manifold_rec(d, d.srec[cs + k], cache, it < 0);
             __syncthreads();
         }
     }
@@ -1387,25 +1560,20 @@ __global__ void __launch_bounds__(256)
     {
         for (int k = tid; k < na; k += nt)
         {
-            uint64_t v = sval[act[k]];
-            int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            if (!(d.meta[a].flags & BODY_STATIC)) d.vel[a] = cache[d.meta[a].local];
-            if (!(d.meta[b].flags & BODY_STATIC)) d.vel[b] = cache[d.meta[b].local];
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) d.vel[r.y] = cache[r.w & 0xFFFFu];
+            if (!(r.z >> 31)) d.vel[r.z] = cache[r.w >> 16];
         }
     }
     // 4. write the accumulated impulses back into the manifold cache
     for (int k = tid; k < na; k += nt)
     {
-        int p = act[k];
-        uint8_t mask = d.rowmask[p];
+        const int p = int(rec[k].x);
+        const uint8_t mask = d.rowmask[p];
         for (int q = 0; q < 4; ++q)
         {
             if (!(mask & (1u << q))) continue;
-            const Row<T> &r = d.rows[4 * p + q];
-            Contact<T> &c = d.man_new[p].c[q];
-            c.imp[0] = r.acc[0];
-            c.imp[1] = r.acc[1];
-            c.imp[2] = r.acc[2];
+            store_impulses(d, p, q);
         }
     }
 }
@@ -1539,11 +1707,7 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         for (int q = 0; q < 4; ++q)
         {
             if (!(mask & (1u << q))) continue;
-            const Row<T> &r = d.rows[4 * p + q];
-            Contact<T> &c = d.man_new[p].c[q];
-            c.imp[0] = r.acc[0];
-            c.imp[1] = r.acc[1];
-            c.imp[2] = r.acc[2];
+            store_impulses(d, p, q);
         }
     }
 }

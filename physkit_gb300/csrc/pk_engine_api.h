@@ -39,6 +39,7 @@ struct Tunables
     int small_world = 512;     // worlds up to this many local indices share the small solver launch
     int narrow_grid = 2;       // GJK/EPA grid = narrow_grid x the default grid
     int traverse_threads = 128;
+    int big_threads = 256;     // threads per solver CTA of the worlds above small_world
 };
 
 struct StepCounters

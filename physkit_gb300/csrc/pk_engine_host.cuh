@@ -147,8 +147,10 @@ public:
             d.world_order = wo;
             d.world_nlocal = wn;
         }
-        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, solve_max_threads<T>()>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
         {
             int per_sm = 0;
             PK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_grid<T>, 256, 0));
@@ -175,12 +177,16 @@ public:
         PK_CUDA(alloc(&d.epa_list, P));
         PK_CUDA(alloc(&d.epa_simplex, P));
         PK_CUDA(alloc(&d.rows, 4 * P));
+        PK_CUDA(alloc(&d.racc, 12 * P));
+        if (sizeof(T) == 4) PK_CUDA(alloc(&d.raccf, 12 * P));
+        if (sizeof(T) == 4) PK_CUDA(alloc(&d.rdel, 12 * P));
         PK_CUDA(alloc(&d.rowmask, P));
         PK_CUDA(alloc(&d.colour, P));
         PK_CUDA(alloc(&d.colour_tmp, P));
         PK_CUDA(alloc(&d.pair_colour, P));
         PK_CUDA(alloc(&d.order, P));
         PK_CUDA(alloc(&d.srec, P));
+        PK_CUDA(alloc(&d.crec, P));
         PK_CUDA(alloc(&d.owner, N));
         int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
         PK_CUDA(alloc(&hist_, size_t(kSortRadix) * hb));
@@ -739,6 +745,15 @@ private:
         if (n == 0) n = 1;
         return cudaMalloc(const_cast<void **>(reinterpret_cast<const void **>(p)), sizeof(U) * n);
     }
+    static int solve_threads(int t) { return t < solve_max_threads<T>() ? t : solve_max_threads<T>(); }
+    void launch_solve(int blocks, int threads, size_t smem, const Dev<T> &d, const uint64_t *pv, int first, int cache)
+    {
+        threads = solve_threads(threads);
+        if (threads > 256)
+            k_solve_world<T, solve_max_threads<T>()><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+        else
+            k_solve_world<T, 256><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+    }
     int grid(int n) const
     {
         int g = (n + 255) / 256;
@@ -754,8 +769,8 @@ private:
                       d_.wroot, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list,
-                      d_.epa_list, d_.epa_simplex, d_.rows, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
-                      d_.order, d_.srec, d_.owner, const_cast<int *>(d_.world_order),
+                      d_.epa_list, d_.epa_simplex, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
+                      d_.order, d_.srec, d_.crec, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
@@ -830,12 +845,11 @@ private:
                                                 args, 0, st_));
         }
         if (big_worlds_ > 0)
-            k_solve_world<T><<<big_worlds_, tune_.solve_threads, sizeof(Vel<T>) * size_t(big_cache_), st_>>>(
-                d, pv, 0, big_cache_, kGridWorld);
+            launch_solve(big_worlds_, tune_.big_threads > 0 ? tune_.big_threads : tune_.solve_threads,
+                         sizeof(Vel<T>) * size_t(big_cache_), d, pv, 0, big_cache_);
         if (cfg_.max_worlds > big_worlds_)
-            k_solve_world<T><<<cfg_.max_worlds - big_worlds_, tune_.solve_threads,
-                               sizeof(Vel<T>) * size_t(tune_.small_world), st_>>>(d, pv, big_worlds_, tune_.small_world,
-                                                                                   kGridWorld);
+            launch_solve(cfg_.max_worlds - big_worlds_, tune_.solve_threads, sizeof(Vel<T>) * size_t(tune_.small_world),
+                         d, pv, big_worlds_, tune_.small_world);
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk, pv);

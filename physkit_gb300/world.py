@@ -56,7 +56,7 @@ class StepInfoC(C.Structure):
 class TuneResultC(C.Structure):
     _fields_ = [("solve_threads", C.c_int32), ("small_world", C.c_int32), ("narrow_grid", C.c_int32),
                 ("traverse_threads", C.c_int32), ("step_ms_before", C.c_double), ("step_ms_after", C.c_double),
-                ("steps_used", C.c_int32), ("reserved", C.c_int32)]
+                ("steps_used", C.c_int32), ("big_threads", C.c_int32)]
 
 
 class CollideShapeC(C.Structure):
@@ -394,7 +394,7 @@ class World:
         """Pick launch shapes by timing real steps (which advance the world); returns the choice."""
         r = TuneResultC()
         _check(self.L.pk_world_autotune(self.h, float(dt), int(steps_per_candidate), C.byref(r)), "pk_world_autotune")
-        return {f: getattr(r, f) for f, _ in TuneResultC._fields_ if f != "reserved"}
+        return {f: getattr(r, f) for f, _ in TuneResultC._fields_}
 
     def set_tuning(self, tuned):
         r = TuneResultC()
