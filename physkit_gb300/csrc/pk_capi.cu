@@ -285,7 +285,9 @@ void pk_world_destroy(pk_world *w)
     delete w;
 }
 
-static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
+// uv_stacks/uv_sectors: the layout of a UV sphere from pk_shape_sphere (0: any other vertex list);
+// the device's support search then looks only near the query direction.
+static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out, int uv_stacks = 0, int uv_sectors = 0)
 {
     size_t nv = v.size() / 3;
     if (nv == 0) return PK_ERR_INVALID;
@@ -354,8 +356,8 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out)
     w->ranges.push_back(ncl);
     w->ranges.push_back(gstart);
     w->ranges.push_back(ngr);
-    w->ranges.push_back(0);
-    w->ranges.push_back(0);
+    w->ranges.push_back(uv_stacks);
+    w->ranges.push_back(uv_sectors);
     w->rmax.push_back(rm);
     w->verts.insert(w->verts.end(), v.begin(), v.end());
     for (int k = 0; k < 3; ++k) w->boxes.push_back(mn[k]);
@@ -442,7 +444,9 @@ int pk_shape_sphere(pk_world *w, double r, int32_t stacks, int32_t sectors, int3
     v.push_back(0.0);
     v.push_back(-r);
     v.push_back(0.0);
-    return add_shape(w, v, out);
+    // the neighbourhood search is proven for these layouts (pk_narrow.cuh, argmax_uv)
+    const bool uv = stacks >= 8 && stacks <= 64 && sectors >= 8 && sectors <= 64;
+    return add_shape(w, v, out, uv ? stacks : 0, uv ? sectors : 0);
 }
 
 int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)

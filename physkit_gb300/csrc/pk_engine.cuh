@@ -131,7 +131,7 @@ template <class T> struct WorldParams
 // 8 clusters, the latter two in one array of (centre xyz, radius) records.
 struct ShapeRange
 {
-    int vstart, nverts, cstart, ncl, gstart, ngr, pad0, pad1;
+    int vstart, nverts, cstart, ncl, gstart, ngr, uv_stacks, uv_sectors; // uv: 0 unless a UV sphere
 };
 
 template <class T> struct Dev
@@ -599,6 +599,8 @@ template <class T> __device__ __forceinline__ ShapeRef<T> body_shape(const Dev<T
     s.ngr = r.ngr;
     s.gr = d.clusters + 4 * r.gstart;
     s.rmax = d.shape_rmax[m.shape];
+    s.uv_stacks = r.uv_stacks;
+    s.uv_sectors = r.uv_sectors;
     const Pose<T> &p = d.pose[slot];
     s.pos = ld3(p.p);
     s.q = ldq(p.q);
@@ -706,6 +708,14 @@ __device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const Shape
             st3(oc.n, normal);
             add_contact(nm, oc);
         }
+    }
+    if constexpr (sizeof(T) == 4)
+    {
+        // FP32 form: a contact that did not come out finite is not kept (the FP64 form follows the
+        // reference exactly, whatever it computes)
+        if (hit && !(isfinite(nc.depth) && isfinite(nc.n[0] + nc.n[1] + nc.n[2]) && isfinite(nc.la[0] + nc.la[1] + nc.la[2]) &&
+                     isfinite(nc.lb[0] + nc.lb[1] + nc.lb[2])))
+            hit = false;
     }
     if (hit) add_contact(nm, nc);
     bool was = old.n != 0, is = nm.n != 0;
@@ -1107,7 +1117,9 @@ __device__ __forceinline__ void solve_contact_f32(SBody<float> &A, SBody<float> 
     float mag2 = n1 * n1 + n2 * n2;
     if (mag2 > maxf * maxf)
     {
-        float sc = maxf * rsqrtf(mag2);
+        // IEEE square root and divide: with a tiny normal impulse maxf^2 underflows and mag2 can be
+        // subnormal, where an approximate reciprocal square root would return infinity
+        float sc = maxf / sqrtf(mag2);
         n1 = n1 * sc;
         n2 = n2 * sc;
     }
@@ -1546,14 +1558,21 @@ __global__ void __launch_bounds__(MAXT)
     }
     __syncthreads();
 
-    // 3. warm start, then the iterations, colour by colour
+    // 3. warm start, then the iterations, colour by colour. Each thread reads its first record of
+    //    the next colour before it solves the current one, taking that load off the sweep's path.
+    uint4 cur = make_uint4(0u, 0u, 0u, 0u);
+    if (ncol > 0 && tid < ccount[0]) cur = d.srec[ms + cstart[0] + tid];
     for (int it = -1; it < d.iterations; ++it)
     {
         for (int c = 0; c < ncol; ++c)
         {
             const int cs = ms + cstart[c], cn = ccount[c];
-            for (int k = tid; k < cn; k += nt) solve_manifold_rec(d, d.srec[cs + k], cache, it < 0);
+            const int nc = c + 1 < ncol ? c + 1 : 0;
+            uint4 nxt = make_uint4(0u, 0u, 0u, 0u);
+            if ((c + 1 < ncol || it + 1 < d.iterations) && tid < ccount[nc]) nxt = d.srec[ms + cstart[nc] + tid];
+            for (int k = tid; k < cn; k += nt) solve_manifold_rec(d, k == tid ? cur : d.srec[cs + k], cache, it < 0);
             __syncthreads();
+            cur = nxt;
         }
     }
     if (cache)
@@ -1976,6 +1995,7 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
             r.ngr = 0;
             r.gr = nullptr;
             r.rmax = T(0);
+            r.uv_stacks = r.uv_sectors = 0;
             r.q = Qt<T>{T(1), T(0), T(0), T(0)};
             r.pos = r.a = r.b = V3<T>{T(0), T(0), T(0)};
             if (q.kind == SHAPE_AABB)
@@ -2001,6 +2021,8 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
                 r.ngr = rg.ngr;
                 r.gr = clusters + 4 * rg.gstart;
                 r.rmax = rmax[q.shape];
+                r.uv_stacks = rg.uv_stacks;
+                r.uv_sectors = rg.uv_sectors;
             }
         }
         EpaState<T> es;

@@ -7,6 +7,8 @@
 // exactly as written.
 #pragma once
 
+#include <cmath>
+
 #include <cstdint>
 
 #if defined(__CUDACC__)
@@ -59,6 +61,13 @@ PK_HD float pk_sqrt(float x)
     return __builtin_sqrtf(x);
 #endif
 }
+
+// Inverse trigonometric functions of the platform's math library (they only pick a search
+// neighbourhood; results never depend on their last bits).
+PK_HD double pk_acos(double x) { return acos(x); }
+PK_HD float pk_acos(float x) { return acosf(x); }
+PK_HD double pk_atan2(double y, double x) { return atan2(y, x); }
+PK_HD float pk_atan2(float y, float x) { return atan2f(y, x); }
 
 template <class T> PK_HD T norm(V3<T> a) { return pk_sqrt(sqnorm(a)); }
 template <class T> PK_HD V3<T> normalized(V3<T> a)

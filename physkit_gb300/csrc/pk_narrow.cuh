@@ -13,6 +13,8 @@
 
 #include "pk_math.cuh"
 
+#include <cmath>
+
 namespace pk
 {
 
@@ -62,6 +64,8 @@ template <class T> struct ShapeRef
     int ngr;       // groups of kClusterSize consecutive clusters (64 vertices), same layout
     const T *gr;
     T rmax;
+    int uv_stacks;  // > 0: the vertex list is a UV sphere of this layout (pk_shape_sphere)
+    int uv_sectors;
 
     // First strictly maximal vertex of v.ld over the vertex list, in index order.
     PK_HD int argmax_linear(V3<T> ld, int lo, int hi, int best, T &bd) const
@@ -133,6 +137,73 @@ template <class T> struct ShapeRef
         return best;
     }
 
+    // Same result as argmax_linear over a UV sphere (north pole, stacks-1 rings of `sectors`
+    // vertices at polar angles pi*i/stacks and azimuths 2*pi*j/sectors, south pole). The maximum
+    // of v.ld is the vertex nearest to ld in angle; it and every vertex whose value comes within
+    // rounding of it lie in the 4 rings x 4 sectors around ld's polar and azimuth angles: any
+    // other vertex trails the best one by at least (cos(d_theta/2) - cos(2 d_theta)) * sin(phi) *
+    // sin(pi/stacks) * |ld| * r, which is above 1e-5 |ld| r for the layouts this path accepts
+    // (8 <= stacks, sectors <= 64) and directions further than asin(0.2) from the poles; closer to
+    // a pole the rings around it are scanned whole. Candidates are compared by value, then by
+    // lower index, so ties resolve as in the linear scan.
+    PK_HD int argmax_uv(V3<T> ld) const
+    {
+        const int S = uv_stacks, K = uv_sectors, last = nverts - 1;
+        int best = -1;
+        T bd = T(0);
+        auto take = [&](int i) {
+            T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
+            if (best < 0 || v > bd || (v == bd && i < best))
+            {
+                bd = v;
+                best = i;
+            }
+        };
+        T dn = norm(ld);
+        if (!(dn > T(0))) return 0; // every value is zero: the first vertex
+        T cy = ld.y / dn;
+        cy = cy > T(1) ? T(1) : (cy < T(-1) ? T(-1) : cy);
+        const T pi = T(3.14159265358979323846);
+        T f = pk_acos(cy) * T(S) / pi; // fractional ring index, 0 at the north pole
+        int i0 = int(f);
+        i0 = i0 < 0 ? 0 : (i0 > S ? S : i0);
+        int ilo = i0 - 1, ihi = i0 + 2;
+        T sphi2 = T(1) - cy * cy;
+        if (sphi2 < T(0.04))
+        {
+            // within asin(0.2) of a pole: the pole and whole rings
+            if (ilo <= 0) take(0);
+            if (ihi >= S) take(last);
+            int a = ilo < 1 ? 1 : ilo, b = ihi > S - 1 ? S - 1 : ihi;
+            for (int i = a; i <= b; ++i)
+                for (int j = 0; j < K; ++j) take(1 + (i - 1) * K + j);
+            return best;
+        }
+        T th = pk_atan2(ld.z, ld.x);
+        if (th < T(0)) th = th + T(2) * pi;
+        int j0 = int(th * T(K) / (T(2) * pi));
+        for (int i = ilo; i <= ihi; ++i)
+        {
+            if (i <= 0)
+            {
+                take(0);
+                continue;
+            }
+            if (i >= S)
+            {
+                take(last);
+                continue;
+            }
+            for (int jj = j0 - 1; jj <= j0 + 2; ++jj)
+            {
+                int j = jj % K;
+                j = j < 0 ? j + K : j;
+                take(1 + (i - 1) * K + j);
+            }
+        }
+        return best;
+    }
+
     PK_HD V3<T> support(V3<T> d) const
     {
         if (kind == SHAPE_AABB)
@@ -151,7 +222,9 @@ template <class T> struct ShapeRef
         // (mesh.cpp:341-358, 442-448)
         V3<T> ld = rotate(conj(q), d);
         int best;
-        if (ncl > 0)
+        if (uv_stacks > 0)
+            best = argmax_uv(ld);
+        else if (ncl > 0)
             best = argmax_clustered(ld);
         else
         {
@@ -463,8 +536,84 @@ template <class T> struct EpaState
         a.adj[e1] = uint16_t(f2);
         b.adj[e2] = uint16_t(f1);
     }
+    // FP32 form: the termination face's plane and the contact in FP64, from its three support
+    // points (normal oriented like the FP32 one; centroid weights if the face is degenerate even
+    // in FP64, where the FP32 projection would divide 0 by 0).
+    struct PlaneHP
+    {
+        double n[3], d;
+    };
+    PK_HD PlaneHP plane_hp(const EpaFace<T> &f) const
+    {
+        const V3<T> &a = poly[f.v[0]].p, &b = poly[f.v[1]].p, &c = poly[f.v[2]].p;
+        double ax = a.x, ay = a.y, az = a.z;
+        double ux = double(b.x) - ax, uy = double(b.y) - ay, uz = double(b.z) - az;
+        double vx = double(c.x) - ax, vy = double(c.y) - ay, vz = double(c.z) - az;
+        double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+        double nn = nx * nx + ny * ny + nz * nz;
+        PlaneHP h;
+        if (nn > 0.0)
+        {
+            double inv = 1.0 / pk_sqrt(nn);
+            nx *= inv;
+            ny *= inv;
+            nz *= inv;
+            if (nx * double(f.n.x) + ny * double(f.n.y) + nz * double(f.n.z) < 0.0)
+            {
+                nx = -nx;
+                ny = -ny;
+                nz = -nz;
+            }
+        }
+        else
+        {
+            nx = f.n.x;
+            ny = f.n.y;
+            nz = f.n.z;
+        }
+        h.n[0] = nx;
+        h.n[1] = ny;
+        h.n[2] = nz;
+        h.d = nx * ax + ny * ay + nz * az;
+        return h;
+    }
+    PK_HD Collision<T> barycentric_hp(const EpaFace<T> &f) const
+    {
+        const SupPt<T> &q0 = poly[f.v[0]], &q1 = poly[f.v[1]], &q2 = poly[f.v[2]];
+        PlaneHP h = plane_hp(f);
+        double a[3] = {q0.p.x, q0.p.y, q0.p.z}, b[3] = {q1.p.x, q1.p.y, q1.p.z}, c[3] = {q2.p.x, q2.p.y, q2.p.z};
+        double v0[3], v1[3], v2[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            v0[k] = b[k] - a[k];
+            v1[k] = c[k] - a[k];
+            v2[k] = h.n[k] * h.d - a[k];
+        }
+        double d00 = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
+        double d01 = v0[0] * v1[0] + v0[1] * v1[1] + v0[2] * v1[2];
+        double d11 = v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2];
+        double d20 = v2[0] * v0[0] + v2[1] * v0[1] + v2[2] * v0[2];
+        double d21 = v2[0] * v1[0] + v2[1] * v1[1] + v2[2] * v1[2];
+        double den = d00 * d11 - d01 * d01;
+        double v = 1.0 / 3.0, w = 1.0 / 3.0;
+        if (den > 0.0)
+        {
+            v = (d11 * d20 - d01 * d21) / den;
+            w = (d00 * d21 - d01 * d20) / den;
+        }
+        double u = 1.0 - v - w;
+        Collision<T> col;
+        col.normal = V3<T>{T(-h.n[0]), T(-h.n[1]), T(-h.n[2])};
+        col.world_a = V3<T>{T(u * q0.pa.x + v * q1.pa.x + w * q2.pa.x), T(u * q0.pa.y + v * q1.pa.y + w * q2.pa.y),
+                            T(u * q0.pa.z + v * q1.pa.z + w * q2.pa.z)};
+        col.world_b = V3<T>{T(u * q0.pb.x + v * q1.pb.x + w * q2.pb.x), T(u * q0.pb.y + v * q1.pb.y + w * q2.pb.y),
+                            T(u * q0.pb.z + v * q1.pb.z + w * q2.pb.z)};
+        col.depth = T(h.d);
+        return col;
+    }
     PK_HD Collision<T> barycentric(const EpaFace<T> &f) const
     {
+        if constexpr (sizeof(T) == 4) return barycentric_hp(f);
         const SupPt<T> &p0 = poly[f.v[0]], &p1 = poly[f.v[1]], &p2 = poly[f.v[2]];
         V3<T> pm = f.n * f.d;
         V3<T> v0 = p1.p - p0.p, v1 = p2.p - p0.p, v2 = pm - p0.p;
@@ -534,7 +683,17 @@ PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaSta
         const EpaFace<T> minf = e.faces[mf];
         SupPt<T> p = minkowski(A, B, minf.n);
         T pd = dot(minf.n, p.p);
-        if (pd - minf.d < tol)
+        bool done = pd - minf.d < tol;
+        if constexpr (sizeof(T) == 4)
+        {
+            // FP32 form: near termination the face's plane distance is re-evaluated in FP64
+            if (pd - minf.d < T(8) * tol)
+            {
+                auto h = e.plane_hp(minf);
+                done = h.n[0] * double(p.p.x) + h.n[1] * double(p.p.y) + h.n[2] * double(p.p.z) - h.d < double(tol);
+            }
+        }
+        if (done)
         {
             out = e.barycentric(minf);
             return true;

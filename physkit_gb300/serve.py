@@ -92,6 +92,9 @@ class StepServer:
              .with_capacity(max_bodies=max_bodies, max_pairs=pair_factor * max_bodies, max_worlds=max_worlds,
                             max_bodies_per_world=max_bodies_per_world, max_shape_vertices=4096, max_shapes=256))
         self.world = World(d)
+        # latency first: the largest worlds set a step's length, so they get the widest solver CTA
+        self.world.set_tuning({"solve_threads": 128, "small_world": 1024, "narrow_grid": 2, "traverse_threads": 128,
+                               "big_threads": 512})
         self.dt = dt
         self.templates = BoxPileTemplates(self.world, seed)
         self.rng = np.random.Generator(np.random.PCG64(seed))

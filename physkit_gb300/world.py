@@ -360,10 +360,13 @@ class World:
 
     # stepping ----------------------------------------------------------------------------------
     def step(self, dt, check=True):
+        """One synchronous step. With check=False a raised device status bit (pair overflow, caps,
+        non-finite state) is returned as True instead of raising."""
         rc = self.L.pk_world_step(self.h, float(dt))
         if rc == PK_ERR_DEVICE_STATUS and not check:
-            return
+            return True
         _check(rc, "pk_world_step")
+        return False
 
     def step_async(self, dt):
         _check(self.L.pk_world_step_async(self.h, float(dt)), "pk_world_step_async")

@@ -2,7 +2,9 @@
 //  1. the EPA face heap pops faces in exactly the order std::push_heap/std::pop_heap would
 //     (the reference's heap, collision.cpp:390-408), including ties;
 //  2. the clustered support search returns the same vertex as the linear first-strict-max scan
-//     (mesh.cpp:341-358) for UV spheres and random hulls, in FP64 and FP32.
+//     (mesh.cpp:341-358) for UV spheres and random hulls, in FP64 and FP32;
+//  3. so does the UV-sphere neighbourhood search, for every layout it accepts (8..64 stacks and
+//     sectors), including directions at and near the poles, on ring planes and between sectors.
 #include "../../physkit_gb300/csrc/pk_narrow.cuh"
 
 #include <algorithm>
@@ -116,6 +118,63 @@ template <class T> static int check_support(const std::vector<double> &vd, std::
     return bad;
 }
 
+template <class T> static int check_uv(const std::vector<double> &vd, int stacks, int sectors, std::mt19937_64 &rng, int ndirs)
+{
+    std::vector<T> v(vd.begin(), vd.end());
+    ShapeRef<T> s{};
+    s.kind = SHAPE_MESH;
+    s.nverts = int(v.size() / 3);
+    s.verts = v.data();
+    s.uv_stacks = stacks;
+    s.uv_sectors = sectors;
+    std::normal_distribution<double> nd(0.0, 1.0);
+    std::uniform_real_distribution<double> ud(-1.0, 1.0);
+    int bad = 0;
+    for (int k = 0; k < ndirs; ++k)
+    {
+        V3<double> d;
+        int mode = k % 6;
+        if (mode == 0)
+            d = V3<double>{nd(rng), nd(rng), nd(rng)};
+        else if (mode == 1)
+        { // near a pole
+            double e = std::pow(10.0, -6.0 * std::fabs(ud(rng)));
+            d = V3<double>{e * ud(rng), (ud(rng) < 0 ? -1.0 : 1.0), e * ud(rng)};
+        }
+        else if (mode == 2)
+        { // exactly on a vertex direction (ties between neighbours are common)
+            int i = int(rng() % uint64_t(s.nverts));
+            d = V3<double>{vd[3 * i], vd[3 * i + 1], vd[3 * i + 2]};
+        }
+        else if (mode == 3)
+        { // half way between two sectors of a ring
+            int i = 1 + int(rng() % uint64_t(stacks - 1));
+            double phi = M_PI * i / stacks, th = 2.0 * M_PI * (double(rng() % uint64_t(sectors)) + 0.5) / sectors;
+            d = V3<double>{std::sin(phi) * std::cos(th), std::cos(phi), std::sin(phi) * std::sin(th)};
+        }
+        else if (mode == 4)
+        { // half way between two rings
+            int i = int(rng() % uint64_t(stacks));
+            double phi = M_PI * (i + 0.5) / stacks, th = 2.0 * M_PI * double(rng() % uint64_t(sectors)) / sectors;
+            d = V3<double>{std::sin(phi) * std::cos(th), std::cos(phi), std::sin(phi) * std::sin(th)};
+        }
+        else
+        { // axes and diagonals
+            int a = int(rng() % 26);
+            int x = a % 3 - 1, y = (a / 3) % 3 - 1, z = a / 9 - 1;
+            if (x == 0 && y == 0 && z == 0) x = 1;
+            d = V3<double>{double(x), double(y), double(z)};
+        }
+        double sc = std::pow(10.0, 3.0 * ud(rng));
+        V3<T> dt{T(d.x * sc), T(d.y * sc), T(d.z * sc)};
+        T bd;
+        int lin = s.argmax_linear(dt, 0, s.nverts, -1, bd);
+        int uv = s.argmax_uv(dt);
+        if (lin != uv) ++bad;
+    }
+    return bad;
+}
+
 static std::vector<double> uv_sphere(double r, int stacks, int sectors)
 {
     std::vector<double> v = {0.0, r, 0.0};
@@ -157,6 +216,16 @@ int main()
         bad64 += check_support<double>(v, rng, 500);
         bad32 += check_support<float>(v, rng, 500);
     }
-    std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d\n", bad_heap, bad64, bad32);
-    return (bad_heap || bad64 || bad32) ? 1 : 0;
+    int baduv64 = 0, baduv32 = 0;
+    for (int S : {8, 9, 12, 16, 24, 31, 48, 64})
+        for (int K : {8, 11, 16, 32, 33, 64})
+            for (double r : {0.05, 1.0, 7.5})
+            {
+                auto v = uv_sphere(r, S, K);
+                baduv64 += check_uv<double>(v, S, K, rng, 3000);
+                baduv32 += check_uv<float>(v, S, K, rng, 3000);
+            }
+    std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d uv_mismatch_f64=%d uv_mismatch_f32=%d\n",
+                bad_heap, bad64, bad32, baduv64, baduv32);
+    return (bad_heap || bad64 || bad32 || baduv64 || baduv32) ? 1 : 0;
 }
