@@ -7,6 +7,7 @@
 // device memory a world lives.
 #include "../../include/physkit_gb300.h"
 #include "pk_engine_api.h"
+#include "pk_narrow.cuh"
 #include "pk_math.cuh"
 
 #include <algorithm>
@@ -445,7 +446,7 @@ int pk_shape_sphere(pk_world *w, double r, int32_t stacks, int32_t sectors, int3
     v.push_back(-r);
     v.push_back(0.0);
     // the neighbourhood search is proven for these layouts (pk_narrow.cuh, argmax_uv)
-    const bool uv = stacks >= 8 && stacks <= 64 && sectors >= 8 && sectors <= 64;
+    const bool uv = pk::uv_layout_ok(stacks, sectors);
     return add_shape(w, v, out, uv ? stacks : 0, uv ? sectors : 0);
 }
 

@@ -775,7 +775,6 @@ template <class T>
 __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
 {
     const int np = *d.npairs;
-    const int nold = *d.npairs_old;
     PK_GRID_STRIDE(p, np)
     {
         uint64_t key = skey[p];
@@ -789,13 +788,15 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
             d.event[p] = 0;
             continue;
         }
-        int lo = 0, hi = nold;
+        // last step's pairs of this world are the segment [mstart_old, mend_old) of the sorted list
+        int lo = d.mstart_old[world], hi = d.mend_old[world];
+        const int end = hi;
         while (lo < hi)
         {
             int mid = (lo + hi) >> 1;
             if (d.key_old[mid] < key) lo = mid + 1; else hi = mid;
         }
-        int old_idx = (lo < nold && d.key_old[lo] == key) ? lo : -1;
+        int old_idx = (lo < end && d.key_old[lo] == key) ? lo : -1;
         d.old_idx[p] = old_idx;
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         V3<T> dc = B.pos - A.pos;

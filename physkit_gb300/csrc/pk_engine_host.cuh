@@ -189,7 +189,7 @@ public:
         PK_CUDA(alloc(&d.crec, P));
         PK_CUDA(alloc(&d.owner, N));
         int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
-        PK_CUDA(alloc(&hist_, size_t(kSortRadix) * hb));
+        PK_CUDA(alloc(&hist_, size_t(kSortRadix) * (hb + 1))); // digit table + one row of digit totals
         PK_CUDA(alloc(&d.verts, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
         PK_CUDA(alloc(&shape_range_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
         PK_CUDA(alloc(&shape_box_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));

@@ -49,6 +49,15 @@ template <> struct EpsOf<float>
 
 constexpr int kClusterSize = 8;
 
+// UV-sphere layouts whose support search by neighbourhood (ShapeRef::argmax_uv) is proven exact:
+// 8..64 stacks and sectors, and a ring-to-ring value gap of at least 1e-3 (relative).
+PK_HD bool uv_layout_ok(int S, int K)
+{
+    if (S < 8 || S > 64 || K < 8 || K > 64) return false;
+    const double pi = 3.14159265358979323846;
+    return cos(0.5 * pi / S) - (1.0 - cos(pi / K)) - cos(2.0 * pi / S) >= 1e-3;
+}
+
 // A posed convex shape: aabb (a=min, b=max), obb (pos=center, q, b=half) or mesh instance
 // (pos, q, vertex list). Large meshes carry clusters of kClusterSize consecutive vertices with a
 // bounding sphere each (cx, cy, cz, radius) and the shape's bounding radius `rmax`.
@@ -138,14 +147,19 @@ template <class T> struct ShapeRef
     }
 
     // Same result as argmax_linear over a UV sphere (north pole, stacks-1 rings of `sectors`
-    // vertices at polar angles pi*i/stacks and azimuths 2*pi*j/sectors, south pole). The maximum
-    // of v.ld is the vertex nearest to ld in angle; it and every vertex whose value comes within
-    // rounding of it lie in the 4 rings x 4 sectors around ld's polar and azimuth angles: any
-    // other vertex trails the best one by at least (cos(d_theta/2) - cos(2 d_theta)) * sin(phi) *
-    // sin(pi/stacks) * |ld| * r, which is above 1e-5 |ld| r for the layouts this path accepts
-    // (8 <= stacks, sectors <= 64) and directions further than asin(0.2) from the poles; closer to
-    // a pole the rings around it are scanned whole. Candidates are compared by value, then by
-    // lower index, so ties resolve as in the linear scan.
+    // vertices at polar angles pi*i/S and azimuths 2*pi*j/K, south pole), for the layouts that
+    // uv_layout_ok accepts. With phi, theta the angles of ld, the rings i0-1..i0+2 around
+    // phi (i0 = floor(phi S / pi)) and the sectors j0-1..j0+2 around theta hold the maximum of v.ld
+    // and every vertex within rounding of it:
+    //  - a vertex of any other ring is at least 2 pi/S from ld in polar angle and trails the
+    //    nearest in-ring candidate by cos(pi/2S) - (1 - cos(pi/K)) - cos(2 pi/S), which the layout
+    //    check keeps >= 1e-3 (times |ld| r);
+    //  - another sector of an included ring i trails that ring's nearest sector by
+    //    sin(phi) sin(phi_i) (cos(pi/K) - cos(4 pi/K)) >= 1e-4 once sin(phi) is above the
+    //    threshold computed below (phi_i >= pi/S); nearer a pole the candidate rings are scanned
+    //    whole.
+    // Rounding of any vertex value is below 1e-6 |ld| r in FP32 (below 1e-15 in FP64). Candidates
+    // are compared by value, then by lower index, so ties resolve as in the linear scan.
     PK_HD int argmax_uv(V3<T> ld) const
     {
         const int S = uv_stacks, K = uv_sectors, last = nverts - 1;
@@ -169,7 +183,12 @@ template <class T> struct ShapeRef
         i0 = i0 < 0 ? 0 : (i0 > S ? S : i0);
         int ilo = i0 - 1, ihi = i0 + 2;
         T sphi2 = T(1) - cy * cy;
-        if (sphi2 < T(0.04))
+        // sin(phi) below which the sector gap could fall under 1e-4: 1e-4 / (sin(pi/S) *
+        // (cos(pi/K) - cos(4 pi/K))), with x - x^3/6 <= sin x making it an over-estimate
+        const T dp = pi / T(S), a1 = T(2.5) * pi / T(K), a2 = T(1.5) * pi / T(K);
+        const T lb = (dp - dp * dp * dp / T(6)) * T(2) * (a1 - a1 * a1 * a1 / T(6)) * (a2 - a2 * a2 * a2 / T(6));
+        const T thr = T(1e-4) / lb;
+        if (sphi2 < thr * thr)
         {
             // within asin(0.2) of a pole: the pole and whole rings
             if (ilo <= 0) take(0);
@@ -182,6 +201,7 @@ template <class T> struct ShapeRef
         T th = pk_atan2(ld.z, ld.x);
         if (th < T(0)) th = th + T(2) * pi;
         int j0 = int(th * T(K) / (T(2) * pi));
+        j0 = j0 > K - 1 ? K - 1 : j0;
         for (int i = ilo; i <= ihi; ++i)
         {
             if (i <= 0)
@@ -196,8 +216,7 @@ template <class T> struct ShapeRef
             }
             for (int jj = j0 - 1; jj <= j0 + 2; ++jj)
             {
-                int j = jj % K;
-                j = j < 0 ? j + K : j;
+                int j = jj < 0 ? jj + K : (jj >= K ? jj - K : jj); // jj in [-1, K + 1]
                 take(1 + (i - 1) * K + j);
             }
         }

@@ -3,10 +3,11 @@
 //
 // One pass per 8-bit digit, three kernels per pass:
 //   hist    : each CTA in use counts the digits of its contiguous chunk    -> hist[digit][cta]
-//   scan    : one CTA turns the digit-major table into exclusive offsets
-//   scatter : each CTA walks its chunk in 256-element tiles, ranks equal digits inside a warp with
-//             __match_any_sync, combines warps through shared-memory counters, and writes each
-//             element to offset + running count + rank (stable).
+//   scan    : one CTA per digit turns its row into exclusive offsets and records the row total
+//   scatter : each CTA scans the 256 digit totals into digit bases, then walks its chunk in
+//             256-element tiles, ranks equal digits inside a warp with __match_any_sync, combines
+//             warps through shared-memory counters, and writes each element to digit base + row
+//             offset + running count + rank (stable).
 // Traffic per pass and element: read key+value twice (hist reads keys only), write key+value once.
 #pragma once
 
@@ -61,60 +62,55 @@ static __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint64_
     hist[threadIdx.x * used + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of the digit table (256 x CTAs in use) with one CTA of 1024 threads.
-static __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist, const int *n_ptr, int nblocks)
+// Block-wide exclusive scan of one value per thread (kSortThreads threads); returns the total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &excl)
 {
-    __shared__ uint32_t part[1024];
-    const int count = kSortRadix * sort_used(*n_ptr, nblocks);
-    int per = (count + 1023) / 1024;
-    int lo = threadIdx.x * per, hi = min(count, lo + per);
-    uint32_t s = 0;
-    int i = lo;
-    // eight independent loads in flight per thread instead of a chain of dependent ones
-    for (; i + 8 <= hi; i += 8)
+    __shared__ uint32_t wtot[kSortThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1)
     {
-        uint32_t v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = hist[i + k];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) s += v[k];
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
     }
-    for (; i < hi; ++i) s += hist[i];
-    part[threadIdx.x] = s;
+    if (lane == 31) wtot[warp] = incl;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1)
+    uint32_t before = 0, total = 0;
+    for (int k = 0; k < kSortThreads / 32; ++k)
     {
-        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+        uint32_t t = wtot[k];
+        before += k < warp ? t : 0u;
+        total += t;
     }
-    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-    i = lo;
-    for (; i + 8 <= hi; i += 8)
+    __syncthreads();
+    excl = before + incl - v;
+    return total;
+}
+
+// Row `blockIdx.x` (one digit) of the digit table: exclusive offsets across the CTAs in use, and
+// the row total into tot[digit].
+static __global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__restrict__ hist, const int *n_ptr,
+                                                                   int nblocks, uint32_t *__restrict__ tot)
+{
+    const int used = sort_used(*n_ptr, nblocks);
+    uint32_t *row = hist + size_t(blockIdx.x) * used;
+    uint32_t run = 0;
+    for (int base = 0; base < used; base += kSortThreads)
     {
-        uint32_t v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = hist[i + k];
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-        {
-            hist[i + k] = run;
-            run += v[k];
-        }
+        const int i = base + int(threadIdx.x);
+        uint32_t v = i < used ? row[i] : 0u, ex;
+        uint32_t t = block_exclusive_scan(v, ex);
+        if (i < used) row[i] = run + ex;
+        run += t;
     }
-    for (; i < hi; ++i)
-    {
-        uint32_t v = hist[i];
-        hist[i] = run;
-        run += v;
-    }
+    if (threadIdx.x == 0) tot[blockIdx.x] = run;
 }
 
 template <class V>
 __global__ void __launch_bounds__(kSortThreads)
     k_sort_scatter(const uint64_t *__restrict__ kin, const V *__restrict__ vin, uint64_t *__restrict__ kout,
-                   V *__restrict__ vout, const int *n_ptr, int shift, const uint32_t *__restrict__ hist)
+                   V *__restrict__ vout, const int *n_ptr, int shift, const uint32_t *__restrict__ hist,
+                   const uint32_t *__restrict__ tot)
 {
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t base[kSortRadix];
@@ -125,7 +121,9 @@ __global__ void __launch_bounds__(kSortThreads)
     const int n = *n_ptr;
     const int used = sort_used(n, gridDim.x);
     if (int(blockIdx.x) >= used) return;
-    base[t] = hist[t * used + blockIdx.x];
+    uint32_t digit_base;
+    block_exclusive_scan(tot[t], digit_base);
+    base[t] = digit_base + hist[t * used + blockIdx.x];
     running[t] = 0;
     int lo, hi;
     sort_chunk(n, gridDim.x, blockIdx.x, lo, hi);
@@ -169,7 +167,8 @@ __global__ void __launch_bounds__(kSortThreads)
 }
 
 // Host-side launcher. Sorts [0, *n_dev) of (k0, v0) by the low `bits` bits of the key; ping-pongs
-// with (k1, v1). Returns true when the result ends in (k1, v1).
+// with (k1, v1); `hist` holds kSortRadix * (nblocks + 1) counters. Returns true when the result
+// ends in (k1, v1).
 template <class V>
 inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_dev, int bits, int nblocks,
                        uint32_t *hist, cudaStream_t st)
@@ -182,8 +181,9 @@ inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_de
     {
         int shift = 8 * p;
         k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n_dev, shift, hist);
-        k_sort_scan<<<1, 1024, 0, st>>>(hist, n_dev, nblocks);
-        k_sort_scatter<V><<<nblocks, kSortThreads, 0, st>>>(ka, va, kb, vb, n_dev, shift, hist);
+        k_sort_scan<<<kSortRadix, kSortThreads, 0, st>>>(hist, n_dev, nblocks, hist + size_t(kSortRadix) * nblocks);
+        k_sort_scatter<V><<<nblocks, kSortThreads, 0, st>>>(ka, va, kb, vb, n_dev, shift, hist,
+                                                           hist + size_t(kSortRadix) * nblocks);
         uint64_t *tk = ka;
         ka = kb;
         kb = tk;

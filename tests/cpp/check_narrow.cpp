@@ -3,8 +3,8 @@
 //     (the reference's heap, collision.cpp:390-408), including ties;
 //  2. the clustered support search returns the same vertex as the linear first-strict-max scan
 //     (mesh.cpp:341-358) for UV spheres and random hulls, in FP64 and FP32;
-//  3. so does the UV-sphere neighbourhood search, for every layout it accepts (8..64 stacks and
-//     sectors), including directions at and near the poles, on ring planes and between sectors.
+//  3. so does the UV-sphere neighbourhood search, for every layout it accepts (uv_layout_ok),
+//     including directions at and near the poles, on ring planes and between sectors.
 #include "../../physkit_gb300/csrc/pk_narrow.cuh"
 
 #include <algorithm>
@@ -217,15 +217,18 @@ int main()
         bad32 += check_support<float>(v, rng, 500);
     }
     int baduv64 = 0, baduv32 = 0;
+    int layouts = 0;
     for (int S : {8, 9, 12, 16, 24, 31, 48, 64})
         for (int K : {8, 11, 16, 32, 33, 64})
             for (double r : {0.05, 1.0, 7.5})
             {
+                if (!uv_layout_ok(S, K)) continue;
+                ++layouts;
                 auto v = uv_sphere(r, S, K);
                 baduv64 += check_uv<double>(v, S, K, rng, 3000);
                 baduv32 += check_uv<float>(v, S, K, rng, 3000);
             }
-    std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d uv_mismatch_f64=%d uv_mismatch_f32=%d\n",
-                bad_heap, bad64, bad32, baduv64, baduv32);
-    return (bad_heap || bad64 || bad32 || baduv64 || baduv32) ? 1 : 0;
+    std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d uv_mismatch_f64=%d uv_mismatch_f32=%d "
+                "uv_layouts=%d\n", bad_heap, bad64, bad32, baduv64, baduv32, layouts);
+    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || !uv_layout_ok(16, 32) || layouts < 60) ? 1 : 0;
 }
