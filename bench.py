@@ -218,7 +218,9 @@ def run_ours(a, rank, world_size, local_rank):
         dist_mod.init_process_group("nccl")
         dist = dist_mod
 
-    scene = scenes.config3(nworlds=a.worlds, nmin=a.nmin, nmax=a.nmax, seed=scenes.SEED_BASE + 3 + rank)
+    from physkit_gb300 import replicas
+
+    scene = scenes.config3(nworlds=a.worlds, nmin=a.nmin, nmax=a.nmax, seed=replicas.rank_seed(scenes.SEED_BASE + 3, rank))
     dt = scene.dt
     tuned = None
     if not a.no_tune:
@@ -258,12 +260,10 @@ def run_ours(a, rank, world_size, local_rank):
     ms = ev0.elapsed_time(ev1)
     stages = world.stage_times()
     world.set_timing(False)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, dist, device="cuda")
+    nb_all = replicas.sum_over_ranks(nb, dist, device="cuda")
     ms_per_step = ms / a.steps
-    value = nb * world_size * a.steps / (ms / 1e3)
+    value = replicas.job_throughput(nb_all, a.steps, ms)
 
     # counts for the roofline model (last step)
     keys, counts, _ = world.manifolds()
@@ -295,7 +295,8 @@ def run_ours(a, rank, world_size, local_rank):
         host[:] = world.bodies()
     e2e_s = time.perf_counter() - t0
     bpb = 28 + 24 + 24 if a.precision == "f32" else 56 + 48 + 24
-    e2e = {"value": nb * world_size * n_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+    e2e_s = replicas.max_over_ranks(e2e_s, dist, device="cuda")
+    e2e = {"value": nb_all * n_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
            "d2h_bytes_per_step": len(scene.bodies) * bpb,
            "note": "pk_world_step (synchronous) + pk_world_read_bodies into host memory every step; "
                    "dt is the only per-step input (a kernel argument)",
@@ -345,32 +346,68 @@ def run_ours(a, rank, world_size, local_rank):
 
 
 def precision_report(steps=240, n=1000):
-    """FP32 precision form against FP64 on config 1 (1,000 boxes), 240 steps. The FP64 run is the
-    device FP64 form, which is bit-identical to the FP64 oracle (tests/test_gpu_world_parity.py)."""
+    """FP32 precision form against FP64 on config 1 (1,000 boxes), 240 steps, per quantity. The FP64
+    run is the device FP64 form, which is bit-identical to the FP64 oracle
+    (tests/test_gpu_world_parity.py). Control: the FP64 form again with one body moved by 1e-12 m,
+    which shows how far the pile's own dynamics amplify a perturbation of that size."""
+    import copy
+
     import numpy as np
     from physkit_gb300 import scenes
 
     scene = scenes.config1(n=n)
+    dyn = scene.bodies["type"] == 0
+    pert = copy.deepcopy(scene)
+    k0 = int(np.nonzero(dyn)[0][0])
+    pert.bodies["pos"][k0, 0] += 1e-12
     w32, _ = scenes.make_world(scene, precision="f32")
     w64, _ = scenes.make_world(scene, precision="f64")
-    dyn = scene.bodies["type"] == 0
+    wpp, _ = scenes.make_world(pert, precision="f64")
+
+    def body_err(a, b):
+        dpos = np.linalg.norm(a[:, 0:3] - b[:, 0:3], axis=1)
+        scale = np.maximum(np.linalg.norm(b[:, 0:3], axis=1), 1.0)
+        return {"pos_rel_max": float((dpos / scale).max()), "pos_rel_p50": float(np.median(dpos / scale)),
+                "pos_abs_max_m": float(dpos.max()),
+                "quat_1mdot_max": float((1.0 - np.abs(np.sum(a[:, 3:7] * b[:, 3:7], axis=1))).max()),
+                "vel_abs_max_mps": float(np.linalg.norm(a[:, 7:10] - b[:, 7:10], axis=1).max())}
+
+    def contact_err(wa, wb):
+        ka, ca, ta = wa.manifolds()
+        kb, cb, tb = wb.manifolds()
+        ib = {int(k): i for i, k in enumerate(kb)}
+        dd, dn, same = [], [], 0
+        for i, k in enumerate(ka):
+            j = ib.get(int(k))
+            if j is None or ca[i] != cb[j] or ca[i] == 0:
+                continue
+            same += 1
+            for c in range(ca[i]):
+                dd.append(abs(ta[i, c, 9] - tb[j, c, 9]))
+                dn.append(np.linalg.norm(ta[i, c, 0:3] - tb[j, c, 0:3]))
+        return {"manifolds_compared": same, "depth_abs_max_m": float(max(dd)) if dd else 0.0,
+                "normal_abs_max": float(max(dn)) if dn else 0.0}
+
     rep = {}
+    pairs_equal = 0
     for s in range(1, steps + 1):
         w32.step(scene.dt, check=False)
         w64.step(scene.dt, check=False)
+        wpp.step(scene.dt, check=False)
+        p32, p64 = w32.pairs(), w64.pairs()
+        pairs_equal += int(len(p32) == len(p64) and bool(np.array_equal(np.sort(p32), np.sort(p64))))
         if s in (60, 120, 240):
-            a, b = w32.bodies()[dyn], w64.bodies()[dyn]
-            dpos = np.linalg.norm(a[:, 0:3] - b[:, 0:3], axis=1)
-            scale = np.maximum(np.linalg.norm(b[:, 0:3], axis=1), 1.0)
-            dq = 1.0 - np.abs(np.sum(a[:, 3:7] * b[:, 3:7], axis=1))
-            dv = np.linalg.norm(a[:, 7:10] - b[:, 7:10], axis=1)
-            rep[f"step{s}"] = {"pos_rel_max": float((dpos / scale).max()), "pos_rel_p50": float(np.median(dpos / scale)),
-                               "pos_abs_max_m": float(dpos.max()), "quat_1mdot_max": float(dq.max()),
-                               "vel_abs_max_mps": float(dv.max()),
-                               "pairs_f32_vs_f64": [int(len(w32.pairs())), int(len(w64.pairs()))]}
-    w32.close()
-    w64.close()
-    rep["workload"] = f"config1: {n} boxes + ground, dt=1/120; FP32 form vs FP64 form"
+            a, b, c = w32.bodies()[dyn], w64.bodies()[dyn], wpp.bodies()[dyn]
+            r = body_err(a, b)
+            r.update(contact_err(w32, w64))
+            r["pairs_f32_vs_f64"] = [int(len(p32)), int(len(p64))]
+            r["steps_with_equal_pair_set"] = pairs_equal
+            r["control_fp64_1e-12m"] = body_err(c, b)
+            rep[f"step{s}"] = r
+    for w in (w32, w64, wpp):
+        w.close()
+    rep["workload"] = (f"config1: {n} boxes + ground, dt=1/120; FP32 form vs FP64 form; control: FP64 form with "
+                       f"one body moved 1e-12 m vs FP64 form")
     return rep
 
 
