@@ -480,13 +480,15 @@ template <class T> __global__ void k_lbvh_refit(Dev<T> d, const uint64_t *__rest
         float mx[3] = {up_f(b.mx.x), up_f(b.mx.y), up_f(b.mx.z)};
         int p = d.leaf_parent[j];
         uint32_t me = uint32_t(j) | kLeafBit;
+        // .w of a child's max box: (last leaf position in the child << 1) | (child holds a static body)
+        uint32_t span = (uint32_t(j) << 1) | ((d.meta[slot].flags & BODY_STATIC) ? 1u : 0u);
         while (true)
         {
             int c = (__float_as_uint(d.nodes[4 * p].w) == me) ? 0 : 1;
             float4 *slotp = d.nodes + 4 * p + 2 * c;
             float wv = slotp[0].w;
             __stcg(slotp + 0, make_float4(mn[0], mn[1], mn[2], wv));
-            __stcg(slotp + 1, make_float4(mx[0], mx[1], mx[2], 0.f));
+            __stcg(slotp + 1, make_float4(mx[0], mx[1], mx[2], __uint_as_float(span)));
             __threadfence();
             if (atomicAdd(d.refit_flag + p, 1) == 0) break;
             __threadfence();
@@ -498,6 +500,8 @@ template <class T> __global__ void k_lbvh_refit(Dev<T> d, const uint64_t *__rest
             mx[0] = fmaxf(a1.x, b1.x);
             mx[1] = fmaxf(a1.y, b1.y);
             mx[2] = fmaxf(a1.z, b1.z);
+            // the right child ends the node's leaf range; statics in either child
+            span = (__float_as_uint(b1.w) & ~1u) | ((__float_as_uint(a1.w) | __float_as_uint(b1.w)) & 1u);
             int pp = d.parent[p];
             if (pp < 0) break;
             me = uint32_t(p);
@@ -517,7 +521,9 @@ template <class T> __device__ __forceinline__ bool pair_allowed(const Meta &a, c
 }
 
 // Threads take bodies in Morton (leaf) order, so a warp's queries are spatially close and walk
-// similar paths through the tree.
+// similar paths through the tree. A pair of dynamic bodies is emitted by the one earlier in that
+// order, so a query skips every subtree that ends at or before its own leaf and holds no static
+// body (static bodies do not query; their pairs come from the dynamic side).
 template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int n = *d.nleaf;
@@ -542,24 +548,29 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
             for (int c = 0; c < 2; ++c)
             {
                 float4 bmn = nd[2 * c], bmx = nd[2 * c + 1];
+                const uint32_t span = __float_as_uint(bmx.w);
+                if (int(span >> 1) <= leaf && !(span & 1u)) continue; // only earlier dynamic leaves
                 if (!(bmn.x <= qmx[0] && bmx.x >= qmn[0] && bmn.y <= qmx[1] && bmx.y >= qmn[1] &&
                       bmn.z <= qmx[2] && bmx.z >= qmn[2]))
                     continue;
                 uint32_t ch = __float_as_uint(bmn.w);
                 if (ch & kLeafBit)
                 {
-                    int sj = int(sval[ch & ~kLeafBit]);
+                    const int pos = int(ch & ~kLeafBit);
+                    int sj = int(sval[pos]);
                     if (sj == i) continue;
                     Meta mj = d.meta[sj];
                     bool sj_static = (mj.flags & BODY_STATIC) != 0;
-                    if (!sj_static && mj.local < mi.local) continue; // dynamic pairs once, from the lower index
-                    if (!aabb_intersects(qb, d.tbox[sj])) continue;
+                    if (!sj_static && pos < leaf) continue; // dynamic pairs once, from the earlier leaf
+                    // FP32 form: the node boxes are the exact fat boxes, so the node test was the exact test
+                    if constexpr (!std::is_same<T, float>::value)
+                        if (!aabb_intersects(qb, d.tbox[sj])) continue;
                     if (!pair_allowed<T>(mi, mj)) continue;
                     uint32_t lo = min(mi.local, mj.local), hi = max(mi.local, mj.local);
                     uint32_t slo = (mi.local < mj.local) ? uint32_t(i) : uint32_t(sj);
                     uint32_t shi = (mi.local < mj.local) ? uint32_t(sj) : uint32_t(i);
                     uint64_t key = (uint64_t(mi.world) << (2 * d.lbits)) | (uint64_t(lo) << d.lbits) | uint64_t(hi);
-                    int slot = atomicAdd(d.npairs, 1);
+                    int slot = warp_push(d.npairs); // one atomic per group of lanes emitting together
                     if (slot < d.pair_cap)
                     {
                         d.pkey[slot] = key;
