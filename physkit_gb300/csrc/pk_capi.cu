@@ -233,7 +233,7 @@ int pk_world_create(const pk_world_desc *desc, pk_world **out)
     int per_world = desc->max_bodies_per_world > 0 ? desc->max_bodies_per_world : desc->max_bodies;
     c.lbits = bits_for(per_world);
     c.wbits = bits_for((long long)desc->max_worlds + 1);
-    if (c.wbits + 2 * c.lbits > 64 || c.wbits + 30 > 64)
+    if (c.wbits + 2 * c.lbits > 64 || c.wbits + 31 > 64)
     {
         delete w;
         return PK_ERR_INVALID;

@@ -401,7 +401,9 @@ template <class T> __global__ void k_morton(Dev<T> d)
                 code |= spread10(q) << (2 - a);
             }
             int slot = warp_push(d.nleaf);
-            d.mkey[slot] = (uint64_t(m.world) << 30) | code;
+            // world | static | Morton: a world's static bodies form their own subtree (the reference
+            // keeps them in a separate tree too), so queries prune dynamic subtrees by position alone
+            d.mkey[slot] = (uint64_t(m.world) << 31) | (uint64_t((m.flags & BODY_STATIC) ? 1 : 0) << 30) | code;
             d.mval[slot] = uint64_t(i);
         }
     }
@@ -455,15 +457,15 @@ template <class T> __global__ void k_lbvh_build(Dev<T> d, const uint64_t *__rest
             d.parent[gamma + 1] = i;
         if (i == 0) d.parent[0] = -1;
         // the node spanning exactly one world's leaves is that world's root
-        uint64_t wf = skey[first] >> 30, wl = skey[last] >> 30;
-        if (wf == wl && (first == 0 || (skey[first - 1] >> 30) != wf) && (last == n - 1 || (skey[last + 1] >> 30) != wl))
+        uint64_t wf = skey[first] >> 31, wl = skey[last] >> 31;
+        if (wf == wl && (first == 0 || (skey[first - 1] >> 31) != wf) && (last == n - 1 || (skey[last + 1] >> 31) != wl))
             d.wroot[wf] = i;
     }
     // single-leaf worlds
     PK_GRID_STRIDE(j, n)
     {
-        uint64_t w = skey[j] >> 30;
-        if ((j == 0 || (skey[j - 1] >> 30) != w) && (j == n - 1 || (skey[j + 1] >> 30) != w))
+        uint64_t w = skey[j] >> 31;
+        if ((j == 0 || (skey[j - 1] >> 31) != w) && (j == n - 1 || (skey[j + 1] >> 31) != w))
             d.wroot[w] = int(uint32_t(j) | kLeafBit);
     }
 }

@@ -792,15 +792,15 @@ private:
         const int N = cfg_.body_cap;
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
-        const int mpasses = (cfg_.wbits + 30 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
+        const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
         launches_ = 19 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
         PK_CUDA(mark(1));
         k_morton<T><<<gb, 256, 0, st_>>>(d);
-        // sort the bodies of active worlds by (world, Morton)
-        bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nleaf, cfg_.wbits + 30,
+        // sort the bodies of active worlds by (world, static, Morton)
+        bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nleaf, cfg_.wbits + 31,
                                         cfg_.sort_blocks_bodies, hist_, st_);
         const uint64_t *skey = in1 ? mkey_[1] : mkey_[0];
         const uint64_t *sval = in1 ? mval_[1] : mval_[0];
