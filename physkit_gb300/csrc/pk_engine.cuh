@@ -680,9 +680,15 @@ __device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const Shape
                                 bool hit, const Collision<T> &col)
 {
     const T d2eps = T(0.005 * 0.005), breaking = T(0.05), drift2_eps = T(0.06);
+    // only the contacts in use are read and written: most pairs have an empty manifold
     Manifold<T> old;
     old.n = 0;
-    if (old_idx >= 0) old = d.man_old[old_idx];
+    if (old_idx >= 0)
+    {
+        const Manifold<T> *src = d.man_old + old_idx;
+        old.n = src->n;
+        for (int k = 0; k < old.n; ++k) old.c[k] = src->c[k];
+    }
     Contact<T> nc;
     if (hit)
     {
@@ -733,7 +739,10 @@ __device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const Shape
     if (hit) add_contact(nm, nc);
     bool was = old.n != 0, is = nm.n != 0;
     d.event[p] = (!was && is) ? 1 : ((was && !is) ? 2 : 0);
-    d.man_new[p] = nm;
+    Manifold<T> *dst = d.man_new + p;
+    dst->n = nm.n;
+    dst->pad = 0;
+    for (int k = 0; k < nm.n; ++k) dst->c[k] = nm.c[k];
 }
 
 // Separating-axis test of the two bodies' oriented local AABBs (15 axes). True only when some axis
