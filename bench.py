@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-raycast", action="store_true")
     ap.add_argument("--served-rates", default="1000,5000,20000",
                     help="Poisson request rates (req/s) for the served form; empty to skip")
     ap.add_argument("--served-seconds", type=float, default=2.0)
@@ -301,6 +302,22 @@ def run_ours(a, rank, world_size, local_rank):
            "note": "pk_world_step (synchronous) + pk_world_read_bodies into host memory every step; "
                    "dt is the only per-step input (a kernel argument)",
            "steps_with_device_status": flagged}
+    raycast = None
+    if not a.no_raycast:
+        # world raycasts through the C ABI on the batch after the steps: 1 M rays spread over the
+        # worlds' bins, the call rebuilds the LBVH over every body and returns each ray's 16 nearest
+        rr = np.random.default_rng(7 + rank)
+        nr = 1_000_000
+        org = np.column_stack([rr.uniform(-2.5, 2.5, nr), rr.uniform(0.0, 6.0, nr), rr.uniform(-2.5, 2.5, nr)])
+        drc = rr.normal(size=(nr, 3))
+        wid = rr.integers(0, a.worlds, nr).astype(np.int32)
+        world.raycast_arrays(org[:1000], drc[:1000], 10.0, wid[:1000], cap=16)  # warm
+        t0 = time.perf_counter()
+        _, _, cnt = world.raycast_arrays(org, drc, 10.0, wid, cap=16)
+        rs = time.perf_counter() - t0
+        raycast = {"rays": nr, "ms": rs * 1e3, "rays_per_s": nr / rs, "hits_per_ray": float(cnt.mean()),
+                   "note": "pk_world_raycast with host arrays: LBVH rebuild over all bodies + one thread per ray, "
+                           "16 nearest hits kept per ray"}
     world.close()
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": a.steps,
@@ -319,6 +336,8 @@ def run_ours(a, rank, world_size, local_rank):
                       "gjk_iterations": info["gjk_iterations"], "epa_iterations": info["epa_iterations"],
                       "epa_iterations_large_mesh": info["epa_iterations_large_mesh"],
                       "status": info["flags"]}}
+    if raycast:
+        out["raycast"] = raycast
 
     if rank == 0 and not a.no_plain:
         out["plain_single_world"] = plain_world(a)

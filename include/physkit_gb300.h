@@ -188,6 +188,23 @@ int pk_world_read_manifolds(pk_world *w, uint64_t *keys, int32_t *worlds, int32_
                             int32_t cap, int32_t *n);
 /* Begin (1) / end (2) collision events of the last step (collision_phases.h:309-318). */
 int pk_world_read_events(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *kinds, int32_t cap, int32_t *n);
+/* World raycast, replaces world_base::raycast (world.h:260-319), which walks the static and the
+ * dynamic tree (bvh.h:402-450) and yields every body whose broadphase box the ray enters within
+ * max_distance, with the entry distance (0 when the origin is inside; ray::intersect_distance,
+ * bvh.h:62-93; the direction is normalised, bvh.h:47-50). The hit set is the reference's; the order
+ * here is ascending (distance, handle) instead of its trees' depth-first order. For ray i,
+ * handles/distances[i * cap + k] hold the min(counts[i], cap) nearest hits. Uses the body state after
+ * the last step (or after any later add/remove): the tree is rebuilt over all worlds per call. */
+typedef struct pk_ray
+{
+    double origin[3];
+    double direction[3];
+    double max_distance;
+    int32_t world;
+    int32_t reserved;
+} pk_ray;
+int pk_world_raycast(pk_world *w, const pk_ray *rays, int32_t n, int32_t cap, uint64_t *handles, double *distances,
+                     int32_t *counts);
 /* Solver colour of each manifold with contact rows in the last step (key order). */
 int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t cap, int32_t *n,
                           int32_t *ncolours_world0);

@@ -246,6 +246,37 @@ struct Aabb
         return {sx > 0 ? max.x : min.x, sy > 0 ? max.y : min.y, sz > 0 ? max.z : min.z};
     }
 };
+
+// ray (bvh.h:38-93): the direction is normalised at construction; slab test with safe_inv
+// (1/x, +-inf at zero, bvh.h:24-35) and NaN limits (an axis the ray is parallel to is unconstrained
+// when the origin lies between its slabs, empty otherwise).
+struct Ray
+{
+    V3 o, d;
+    Ray(V3 origin, V3 dir) : o(origin), d(normalized(dir)) {}
+    static double safe_inv(double x) { return 1.0 / x; }
+    bool intersect_distance(const Aabb &b, double max_d, double &out) const
+    {
+        auto slab = [](double lo, double hi, double &a, double &c) {
+            if (std::isnan(lo)) lo = -std::numeric_limits<double>::infinity();
+            if (std::isnan(hi)) hi = std::numeric_limits<double>::infinity();
+            a = std::fmin(lo, hi);
+            c = std::fmax(lo, hi);
+        };
+        double tminx, tmaxx, tminy, tmaxy, tminz, tmaxz;
+        slab((b.min.x - o.x) * safe_inv(d.x), (b.max.x - o.x) * safe_inv(d.x), tminx, tmaxx);
+        slab((b.min.y - o.y) * safe_inv(d.y), (b.max.y - o.y) * safe_inv(d.y), tminy, tmaxy);
+        slab((b.min.z - o.z) * safe_inv(d.z), (b.max.z - o.z) * safe_inv(d.z), tminz, tmaxz);
+        double tmin = std::max({tminx, tminy, tminz});
+        double tmax = std::min({tmaxx, tmaxy, tmaxz});
+        if (tmax >= 0.0 && tmin <= tmax && tmin <= max_d)
+        {
+            out = std::max(0.0, tmin);
+            return true;
+        }
+        return false;
+    }
+};
 inline Aabb aabb_union(const Aabb &a, const Aabb &b)
 {
     return {{dmin(a.min.x, b.min.x), dmin(a.min.y, b.min.y), dmin(a.min.z, b.min.z)},
@@ -1035,6 +1066,47 @@ struct DynTree
         refit_and_rotate(nodes[leaf].parent);
         return true;
     }
+    // dynamic_bvh::raycast (bvh.h:402-450): depth first, the nearer child first
+    template <class F> void raycast(const Ray &r, double max_d, F &&cb) const
+    {
+        if (root == null) return;
+        std::array<uint32_t, 64> stack{};
+        int sp = 0;
+        stack[sp++] = root;
+        while (sp > 0)
+        {
+            uint32_t ni = stack[--sp];
+            const Node &nd = nodes[ni];
+            double dn;
+            if (!r.intersect_distance(nd.bounds, max_d, dn)) continue;
+            if (nd.is_leaf())
+            {
+                cb(nd.data, dn);
+                continue;
+            }
+            assert(sp + 1 < 64);
+            double dl, dr;
+            bool hl = r.intersect_distance(nodes[nd.left].bounds, max_d, dl);
+            bool hr = r.intersect_distance(nodes[nd.right].bounds, max_d, dr);
+            if (hl && hr)
+            {
+                if (dl > dr)
+                {
+                    stack[sp++] = nd.left;
+                    stack[sp++] = nd.right;
+                }
+                else
+                {
+                    stack[sp++] = nd.right;
+                    stack[sp++] = nd.left;
+                }
+            }
+            else if (hl)
+                stack[sp++] = nd.left;
+            else if (hr)
+                stack[sp++] = nd.right;
+        }
+    }
     template <class F> void query(const Aabb &box, F &&cb) const
     {
         if (root == null) return;
@@ -1425,6 +1497,34 @@ struct World
             gen = slots[idx].gen;
         }
         return static_cast<uint64_t>(idx) | (static_cast<uint64_t>(gen) << 32);
+    }
+    // world_base::raycast (world.h:260-319): both trees' hits, merged by their current distance
+    // (static first on a tie), as (handle, distance)
+    std::vector<std::pair<uint64_t, double>> raycast(V3 origin, V3 dir, double max_d) const
+    {
+        Ray r(origin, dir);
+        std::vector<std::pair<uint32_t, double>> sh, dh;
+        static_tree.raycast(r, max_d, [&](uint32_t id, double t) { sh.push_back({id, t}); });
+        dynamic_tree.raycast(r, max_d, [&](uint32_t id, double t) { dh.push_back({id, t}); });
+        auto handle = [&](uint32_t idx) { return static_cast<uint64_t>(idx) | (static_cast<uint64_t>(slots[idx].gen) << 32); };
+        std::vector<std::pair<uint64_t, double>> out;
+        size_t i = 0, j = 0;
+        while (i < sh.size() && j < dh.size())
+        {
+            if (sh[i].second <= dh[j].second)
+            {
+                out.push_back({handle(sh[i].first), sh[i].second});
+                ++i;
+            }
+            else
+            {
+                out.push_back({handle(dh[j].first), dh[j].second});
+                ++j;
+            }
+        }
+        for (; i < sh.size(); ++i) out.push_back({handle(sh[i].first), sh[i].second});
+        for (; j < dh.size(); ++j) out.push_back({handle(dh[j].first), dh[j].second});
+        return out;
     }
     // world_base::remove_rigid (world.h:209-218) -> broad_phase::remove (collision_phases.h:350-369)
     bool remove(uint64_t h)
@@ -1945,6 +2045,19 @@ int pko_gjk_epa(pko_world *w, int ka, const double *pa, int sa, int kb, const do
                     r->world_a.z, r->world_b.x, r->world_b.y, r->world_b.z, r->depth};
     std::copy(v, v + 10, out);
     return 1;
+}
+
+int pko_world_raycast(pko_world *w, const double *origin, const double *dir, double max_dist, uint64_t *handles,
+                      double *dist, int cap)
+{
+    auto hits = w->w.raycast({origin[0], origin[1], origin[2]}, {dir[0], dir[1], dir[2]}, max_dist);
+    int n = static_cast<int>(hits.size());
+    for (int i = 0; i < n && i < cap; ++i)
+    {
+        if (handles) handles[i] = hits[static_cast<size_t>(i)].first;
+        if (dist) dist[i] = hits[static_cast<size_t>(i)].second;
+    }
+    return n;
 }
 
 pko_tree *pko_tree_create(void) { return new pko_tree; }

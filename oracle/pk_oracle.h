@@ -65,6 +65,9 @@ int pko_read_pairs(pko_world *w, uint64_t *keys, int cap);
 int pko_read_manifolds(pko_world *w, uint64_t *keys, int *counts, double *contacts, int cap);
 /* Events of the last step in narrowphase order: key and kind (1 begin, 2 end). */
 int pko_read_events(pko_world *w, uint64_t *keys, int *kinds, int cap);
+/* world_base::raycast (world.h:260-319): hits in the reference's order; returns the hit count */
+int pko_world_raycast(pko_world *w, const double *origin, const double *dir, double max_dist, uint64_t *handles,
+                      double *dist, int cap);
 /* Colour of each active manifold of the last step (key order) and the colour count. */
 int pko_read_colours(pko_world *w, uint64_t *keys, int *colours, int cap, int *ncolours);
 /* Number of reinsertions (moved leaves) of the last step. */

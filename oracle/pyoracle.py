@@ -47,6 +47,7 @@ def lib():
             "pko_read_pairs": (C.c_int, [C.c_void_p, up, C.c_int]),
             "pko_read_manifolds": (C.c_int, [C.c_void_p, up, ip, dp, C.c_int]),
             "pko_read_events": (C.c_int, [C.c_void_p, up, ip, C.c_int]),
+            "pko_world_raycast": (C.c_int, [C.c_void_p, dp, dp, C.c_double, up, dp, C.c_int]),
             "pko_read_colours": (C.c_int, [C.c_void_p, up, ip, C.c_int, ip]),
             "pko_last_moved": (C.c_int, [C.c_void_p]),
             "pko_gjk_epa": (C.c_int, [C.c_void_p, C.c_int, dp, C.c_int, C.c_int, dp, C.c_int, dp]),
@@ -189,6 +190,17 @@ class OracleWorld:
 
     def last_moved(self):
         return self.L.pko_last_moved(self.h)
+
+    def raycast(self, origin, direction, max_dist):
+        """world_base::raycast (world.h:260-319): [(handle, distance)] in the reference's order."""
+        o, op = _dp(origin)
+        dv, dp_ = _dp(direction)
+        n = self.L.pko_world_raycast(self.h, op, dp_, float(max_dist), None, None, 0)
+        hs = np.zeros(max(n, 1), dtype=np.uint64)
+        ds = np.zeros(max(n, 1))
+        self.L.pko_world_raycast(self.h, op, dp_, float(max_dist), hs.ctypes.data_as(P(C.c_uint64)),
+                                 ds.ctypes.data_as(P(C.c_double)), n)
+        return list(zip(hs[:n].tolist(), ds[:n].tolist()))
 
     # narrowphase on primitive shapes ---------------------------------------------------------
     def shape_params(self, spec):

@@ -1010,6 +1010,57 @@ int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t
     return PK_OK;
 }
 
+int pk_world_raycast(pk_world *w, const pk_ray *rays, int32_t n, int32_t cap, uint64_t *handles, double *distances,
+                     int32_t *counts)
+{
+    if (!w || n < 0 || (n > 0 && (!rays || !counts || cap < 1 || !handles || !distances))) return PK_ERR_INVALID;
+    if (n == 0) return PK_OK;
+    for (int i = 0; i < n; ++i)
+        if (rays[i].world < 0 || rays[i].world >= w->cfg.max_worlds || !(rays[i].max_distance >= 0.0))
+            return PK_ERR_INVALID;
+    if (int rc = flush_shapes(w)) return rc;
+    std::vector<double> r(size_t(n) * 8);
+    for (int i = 0; i < n; ++i)
+    {
+        double *o = r.data() + size_t(i) * 8;
+        for (int k = 0; k < 3; ++k)
+        {
+            o[k] = rays[i].origin[k];
+            o[3 + k] = rays[i].direction[k];
+        }
+        o[6] = rays[i].max_distance;
+        o[7] = double(rays[i].world);
+    }
+    const size_t m = size_t(n) * size_t(cap);
+    std::vector<int> slots(m);
+    std::vector<double> dist(m);
+    if (w->eng->raycast(r.data(), n, cap, counts, slots.data(), dist.data()))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    // device slots -> handles, then (distance, handle) order within each ray
+    std::vector<std::pair<double, uint64_t>> hit;
+    for (int i = 0; i < n; ++i)
+    {
+        const int k = counts[i] < cap ? counts[i] : cap;
+        hit.clear();
+        for (int j = 0; j < k; ++j)
+        {
+            const size_t q = size_t(i) * size_t(cap) + size_t(j);
+            const int s = slots[q];
+            hit.push_back({dist[q], uint64_t(uint32_t(s)) | (uint64_t(w->slots[size_t(s)].gen) << 32)});
+        }
+        std::sort(hit.begin(), hit.end());
+        for (int j = 0; j < k; ++j)
+        {
+            handles[size_t(i) * size_t(cap) + size_t(j)] = hit[size_t(j)].second;
+            distances[size_t(i) * size_t(cap) + size_t(j)] = hit[size_t(j)].first;
+        }
+    }
+    return PK_OK;
+}
+
 int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out, int32_t *hit)
 {
     if (!w || n < 0 || (n > 0 && (!a || !b || !out || !hit))) return PK_ERR_INVALID;

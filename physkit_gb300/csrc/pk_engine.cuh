@@ -24,6 +24,7 @@
 #include <cooperative_groups.h>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <type_traits>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -377,13 +378,13 @@ template <class T> __global__ void k_integrate_vel(Dev<T> d, T dt)
 // ------------------------------------------------------------------------------------------------
 // Keys of the bodies of active worlds only, compacted (one atomic per warp); the sort and the
 // LBVH then cover just those bodies.
-template <class T> __global__ void k_morton(Dev<T> d)
+template <class T> __global__ void k_morton(Dev<T> d, bool all_worlds = false)
 {
     const int n = *d.nslots;
     PK_GRID_STRIDE(i, n)
     {
         Meta m = d.meta[i];
-        if ((m.flags & BODY_ALIVE) && d.wp[m.world].active)
+        if ((m.flags & BODY_ALIVE) && (all_worlds || d.wp[m.world].active))
         {
             Aabb<T> tb = d.tbox[i];
             const unsigned *wb = d.wbounds + 6 * m.world;
@@ -587,6 +588,112 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
                     atomicOr(d.status, ST_TRAVERSAL_STACK);
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// world raycast (world.h:260-319): every body whose broadphase box the ray enters within the
+// distance limit, with the entry distance, on the LBVH of the ray's world
+// ------------------------------------------------------------------------------------------------
+template <class T> __global__ void k_tree_reset(Dev<T> d)
+{
+    PK_GRID_STRIDE(w, d.max_worlds) d.wroot[w] = -1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d.nleaf = 0;
+}
+
+// ray::intersect_distance (bvh.h:62-93): slab test with 1/x (+-inf at zero) and the reference's
+// NaN limits, in the engine's precision.
+template <class T>
+__device__ __forceinline__ bool ray_box(V3<T> o, V3<T> inv, T maxd, V3<T> mn, V3<T> mx, T &out)
+{
+    const T inf = std::numeric_limits<T>::infinity();
+    auto slab = [&](T lo, T hi, T &a, T &c) {
+        if (lo != lo) lo = -inf;
+        if (hi != hi) hi = inf;
+        a = fmin(lo, hi);
+        c = fmax(lo, hi);
+    };
+    T tminx, tmaxx, tminy, tmaxy, tminz, tmaxz;
+    slab((mn.x - o.x) * inv.x, (mx.x - o.x) * inv.x, tminx, tmaxx);
+    slab((mn.y - o.y) * inv.y, (mx.y - o.y) * inv.y, tminy, tmaxy);
+    slab((mn.z - o.z) * inv.z, (mx.z - o.z) * inv.z, tminz, tmaxz);
+    const T t0 = tmax(tmax(tminx, tminy), tminz); // std::max / std::min over the three axes
+    const T t1 = tmin(tmin(tmaxx, tmaxy), tmaxz);
+    if (t1 >= T(0) && t0 <= t1 && t0 <= maxd)
+    {
+        out = tmax(T(0), t0);
+        return true;
+    }
+    return false;
+}
+
+// One thread per ray (8 doubles: origin, direction, distance limit, world). Keeps the `cap`
+// nearest hits ordered by (distance, slot) and counts all of them.
+template <class T>
+__global__ void k_raycast(Dev<T> d, const uint64_t *__restrict__ sval, const double *__restrict__ rays, int n, int cap,
+                          int *__restrict__ counts, int *__restrict__ hit_slot, T *__restrict__ hit_t)
+{
+    PK_GRID_STRIDE(r, n)
+    {
+        const double *ry = rays + 8 * size_t(r);
+        const V3<T> o{T(ry[0]), T(ry[1]), T(ry[2])};
+        const V3<T> dir = normalized(V3<T>{T(ry[3]), T(ry[4]), T(ry[5])});
+        const V3<T> inv{T(1) / dir.x, T(1) / dir.y, T(1) / dir.z};
+        const T maxd = T(ry[6]);
+        const int world = int(ry[7]);
+        int *os = hit_slot + size_t(r) * cap;
+        T *ot = hit_t + size_t(r) * cap;
+        int cnt = 0;
+        auto emit = [&](int slot, T t) {
+            int k = cnt < cap ? cnt : cap;
+            ++cnt;
+            if (k == cap && !(t < ot[cap - 1] || (t == ot[cap - 1] && slot < os[cap - 1]))) return;
+            int pos = k == cap ? cap - 1 : k;
+            while (pos > 0 && (t < ot[pos - 1] || (t == ot[pos - 1] && slot < os[pos - 1])))
+            {
+                os[pos] = os[pos - 1];
+                ot[pos] = ot[pos - 1];
+                --pos;
+            }
+            os[pos] = slot;
+            ot[pos] = t;
+        };
+        auto leaf_test = [&](int pos) {
+            const int slot = int(sval[pos]);
+            const Aabb<T> b = d.tbox[slot];
+            T t;
+            if (ray_box(o, inv, maxd, b.mn, b.mx, t)) emit(slot, t);
+        };
+        const int root = (world >= 0 && world < d.max_worlds) ? d.wroot[world] : -1;
+        if (root >= 0 && (uint32_t(root) & kLeafBit))
+            leaf_test(int(uint32_t(root) & ~kLeafBit));
+        else if (root >= 0)
+        {
+            int stack[96];
+            int sp = 0;
+            stack[sp++] = root;
+            while (sp > 0)
+            {
+                const float4 *nd = d.nodes + 4 * stack[--sp];
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+                {
+                    const float4 bmn = nd[2 * c], bmx = nd[2 * c + 1];
+                    T t;
+                    // node boxes enclose their leaves' boxes, and the slab test only widens with the box
+                    if (!ray_box(o, inv, maxd, V3<T>{T(bmn.x), T(bmn.y), T(bmn.z)}, V3<T>{T(bmx.x), T(bmx.y), T(bmx.z)}, t))
+                        continue;
+                    const uint32_t ch = __float_as_uint(bmn.w);
+                    if (ch & kLeafBit)
+                        leaf_test(int(ch & ~kLeafBit));
+                    else if (sp < 96)
+                        stack[sp++] = int(ch);
+                    else
+                        atomicOr(d.status, ST_TRAVERSAL_STACK);
+                }
+            }
+        }
+        counts[r] = cnt;
     }
 }
 
@@ -917,16 +1024,22 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
     const int np = *d.npairs;
     PK_GRID_STRIDE(p, np)
     {
+        d.pair_colour[p] = -2;
+        const Manifold<T> &m = d.man_new[p];
+        const int mn = m.n;
+        if (mn == 0) // most pairs: nothing else to read
+        {
+            d.rowmask[p] = 0;
+            continue;
+        }
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         int world = int(skey[p] >> (2 * d.lbits));
-        d.pair_colour[p] = -2;
         if (!d.wp[world].active)
         {
             d.rowmask[p] = 0;
             continue;
         }
-        const Manifold<T> &m = d.man_new[p];
         const Pose<T> &PA = d.pose[sa];
         const Pose<T> &PB = d.pose[sb];
         const Params<T> &ra = d.prm[sa];
@@ -939,7 +1052,7 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
         V3<T> xa = ld3(PA.p), xb = ld3(PB.p);
         const T rthr = T(2) * d.wp[world].gnorm * dt;
         uint8_t mask = 0;
-        for (int k = 0; k < m.n; ++k)
+        for (int k = 0; k < mn; ++k)
         {
             const Contact<T> &c = m.c[k];
             V3<T> nn = normalized(ld3(c.n));

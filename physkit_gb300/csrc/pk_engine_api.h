@@ -84,6 +84,9 @@ public:
     virtual int read_colours(uint64_t *keys, int *colours, int cap, int *ncolours_world0) = 0;
     virtual int collide(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) = 0;
     // Same narrowphase launch on device buffers the caller provides; allocates nothing.
+    // rays: 8 doubles each (origin, direction, distance limit, world); per ray up to `cap` nearest
+    // hits (device slot, distance) ordered by (distance, slot), and the total hit count
+    virtual int raycast(const double *rays, int n, int cap, int *counts, int *slots, double *dists) = 0;
     virtual int collide_device(const void *specs_a_dev, const void *specs_b_dev, int n, double *out_dev,
                                int *hit_dev, int *status_dev) = 0;
     virtual int capture_graph(double dt) = 0;        // record the step as CUDA graphs

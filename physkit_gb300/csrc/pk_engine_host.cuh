@@ -658,6 +658,49 @@ public:
         return 0;
     }
 
+    // World raycast: rebuild the LBVH over every alive body of every world (the step's tree covers
+    // only the worlds that stepped, and bodies may have changed since), then one thread per ray.
+    int raycast(const double *rays, int n, int cap, int *counts, int *slots, double *dists) override
+    {
+        if (n <= 0) return 0;
+        Dev<T> d = d_;
+        d.mkey = mkey_[0];
+        d.mval = mval_[0];
+        const int N = cfg_.body_cap;
+        const int gb = grid(N);
+        k_tree_reset<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
+        k_morton<T><<<gb, 256, 0, st_>>>(d, true);
+        bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nleaf, cfg_.wbits + 31,
+                                        cfg_.sort_blocks_bodies, hist_, st_);
+        const uint64_t *skey = in1 ? mkey_[1] : mkey_[0];
+        const uint64_t *sval = in1 ? mval_[1] : mval_[0];
+        k_lbvh_build<T><<<gb, 256, 0, st_>>>(d, skey);
+        k_zero_ints<<<gb, 256, 0, st_>>>(d.refit_flag, N);
+        k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
+        double *drays = nullptr;
+        int *dcnt = nullptr, *dslot = nullptr;
+        T *dt = nullptr;
+        const size_t m = size_t(n) * size_t(cap);
+        PK_CUDA(cudaMalloc(&drays, sizeof(double) * 8 * size_t(n)));
+        PK_CUDA(cudaMalloc(&dcnt, sizeof(int) * size_t(n)));
+        PK_CUDA(cudaMalloc(&dslot, sizeof(int) * m));
+        PK_CUDA(cudaMalloc(&dt, sizeof(T) * m));
+        PK_CUDA(cudaMemcpyAsync(drays, rays, sizeof(double) * 8 * size_t(n), cudaMemcpyHostToDevice, st_));
+        k_raycast<T><<<(n + 127) / 128, 128, 0, st_>>>(d, sval, drays, n, cap, dcnt, dslot, dt);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaStreamSynchronize(st_));
+        std::vector<T> ht(m);
+        PK_CUDA(cudaMemcpy(counts, dcnt, sizeof(int) * size_t(n), cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(slots, dslot, sizeof(int) * m, cudaMemcpyDeviceToHost));
+        PK_CUDA(cudaMemcpy(ht.data(), dt, sizeof(T) * m, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < m; ++i) dists[i] = double(ht[i]);
+        cudaFree(drays);
+        cudaFree(dcnt);
+        cudaFree(dslot);
+        cudaFree(dt);
+        return 0;
+    }
+
     int collide_device(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) override
     {
         if (n <= 0) return 0;
@@ -798,7 +841,7 @@ private:
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
         PK_CUDA(mark(1));
-        k_morton<T><<<gb, 256, 0, st_>>>(d);
+        k_morton<T><<<gb, 256, 0, st_>>>(d, false);
         // sort the bodies of active worlds by (world, static, Morton)
         bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nleaf, cfg_.wbits + 31,
                                         cfg_.sort_blocks_bodies, hist_, st_);

@@ -59,6 +59,11 @@ class TuneResultC(C.Structure):
                 ("steps_used", C.c_int32), ("big_threads", C.c_int32)]
 
 
+class RayC(C.Structure):
+    _fields_ = [("origin", C.c_double * 3), ("direction", C.c_double * 3), ("max_distance", C.c_double),
+                ("world", C.c_int32), ("reserved", C.c_int32)]
+
+
 class CollideShapeC(C.Structure):
     _fields_ = [("kind", C.c_int32), ("shape", C.c_int32), ("p", C.c_double * 10)]
 
@@ -103,6 +108,7 @@ def lib():
             "pk_world_read_manifolds": (C.c_int, [vp, u64p, i32p, i32p, dp, C.c_int32, i32p]),
             "pk_world_read_events": (C.c_int, [vp, u64p, i32p, i32p, C.c_int32, i32p]),
             "pk_world_read_colours": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p, i32p]),
+            "pk_world_raycast": (C.c_int, [vp, P(RayC), C.c_int32, C.c_int32, u64p, dp, i32p]),
             "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_collide_noalloc": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_world_set_timing": (C.c_int, [vp, C.c_int32]),
@@ -439,6 +445,35 @@ class World:
         s = np.ascontiguousarray(state13, dtype=np.float64)
         _check(self.L.pk_world_write_body(self.h, C.c_uint64(int(handle)), _ptr(s, C.c_double)),
                "pk_world_write_body")
+
+    RAY_DTYPE = np.dtype([("origin", np.float64, 3), ("direction", np.float64, 3), ("max_distance", np.float64),
+                          ("world", np.int32), ("reserved", np.int32)])
+
+    def raycast_arrays(self, origins, directions, max_distance, worlds=0, cap=64):
+        """World raycast (world.h:260-319) for n rays: handles (n, cap), distances (n, cap) nearest
+        first (the first min(count, cap) of each row are valid) and total hit counts (n,)."""
+        o = np.atleast_2d(np.asarray(origins, dtype=np.float64))
+        n = len(o)
+        rays = np.zeros(n, dtype=self.RAY_DTYPE)
+        rays["origin"] = o
+        rays["direction"] = np.atleast_2d(np.asarray(directions, dtype=np.float64))
+        rays["max_distance"] = np.broadcast_to(np.asarray(max_distance, dtype=np.float64), (n,))
+        rays["world"] = np.broadcast_to(np.asarray(worlds, dtype=np.int32), (n,))
+        hs = np.zeros((max(n, 1), cap), dtype=np.uint64)
+        ds = np.zeros((max(n, 1), cap))
+        cnt = np.zeros(max(n, 1), dtype=np.int32)
+        _check(self.L.pk_world_raycast(self.h, rays.ctypes.data_as(C.POINTER(RayC)), n, cap, _ptr(hs, C.c_uint64),
+                                       _ptr(ds, C.c_double), _ptr(cnt, C.c_int32)), "pk_world_raycast")
+        return hs[:n], ds[:n], cnt[:n]
+
+    def raycast(self, origins, directions, max_distance, worlds=0, cap=64):
+        """As raycast_arrays, as a list of [(handle, distance)] per ray, and the counts."""
+        hs, ds, cnt = self.raycast_arrays(origins, directions, max_distance, worlds, cap)
+        out = []
+        for i in range(len(cnt)):
+            k = min(int(cnt[i]), cap)
+            out.append(list(zip(hs[i, :k].tolist(), ds[i, :k].tolist())))
+        return out, cnt.copy()
 
     def pairs(self, with_worlds=False):
         n = C.c_int32()

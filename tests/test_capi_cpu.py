@@ -37,6 +37,7 @@ def test_descriptor_layouts_match_header():
     assert world.BODY_DTYPE.itemsize == 216
     assert C.sizeof(world.WorldDescC) == 56
     assert C.sizeof(world.CollideShapeC) == 88
+    assert C.sizeof(world.RayC) == 64
 
 
 def test_no_device_is_an_error_not_a_fallback():

@@ -133,3 +133,56 @@ def test_box_comes_to_rest_on_ground():
     assert abs(st[1] - 0.5) < 0.02
     assert np.linalg.norm(st[7:10]) < 0.05
     w.close()
+
+
+def _slab_hit(box, o, d, maxd):
+    """ray::intersect_distance (bvh.h:62-93) restated in numpy float64 for the brute-force check."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = np.float64(1.0) / d
+        lo = (box[:3] - o) * inv
+        hi = (box[3:] - o) * inv
+    lo = np.where(np.isnan(lo), -np.inf, lo)
+    hi = np.where(np.isnan(hi), np.inf, hi)
+    tmin = np.max(np.minimum(lo, hi))
+    tmax = np.min(np.maximum(lo, hi))
+    if tmax >= 0.0 and tmin <= tmax and tmin <= maxd:
+        return max(0.0, tmin)
+    return None
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_world_raycast_bruteforce_and_merge_order(seed):
+    """world_base::raycast (world.h:260-319): the hit set equals a brute-force slab test over every
+    body's broadphase box (exact boxes before the first step), distances bit-identical, each body
+    once."""
+    rng = np.random.default_rng(seed)
+    ow = pyoracle.OracleWorld(gravity=(0, 0, 0))
+    boxes, handles = [], []
+    for k in range(60):
+        he = rng.uniform(0.1, 0.6, 3)
+        sh = ow.box(*he)
+        pos = rng.uniform(-6, 6, 3)
+        static = k % 7 == 0
+        handles.append(ow.add(sh, tuple(pos), static=static))
+        boxes.append(np.concatenate([pos - he, pos + he]))
+    boxes = np.array(boxes)
+    for r in range(200):
+        o = rng.uniform(-8, 8, 3)
+        dv = rng.normal(size=3)
+        if r % 5 == 0:
+            dv[r % 3] = 0.0  # parallel to a slab pair: the NaN limits
+        if r % 11 == 0:
+            o = boxes[r % len(boxes)][:3] + 0.01  # origin inside a box: distance 0
+        maxd = float(rng.uniform(1, 20))
+        got = ow.raycast(o, dv, maxd)
+        n2 = float(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2])
+        dn = dv / math.sqrt(n2)
+        want = {}
+        for i, b in enumerate(boxes):
+            t = _slab_hit(b, o, dn, maxd)
+            if t is not None:
+                want[int(handles[i])] = t
+        assert {h for h, _ in got} == set(want)
+        for h, t in got:
+            assert t == want[h]
+        assert len(got) == len(want)  # no body twice
