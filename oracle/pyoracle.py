@@ -294,6 +294,8 @@ def load_scene(ow: "OracleWorld", scene):
             ids.append(ow.box(*s[1:4]))
         elif s[0] == "sphere":
             ids.append(ow.sphere(s[1], s[2], s[3]))
+        elif s[0] == "pyramid":
+            ids.append(ow.pyramid(s[1], s[2]))
         else:
             ids.append(ow.mesh(s[1], s[2]))
     handles = []

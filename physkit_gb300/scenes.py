@@ -32,7 +32,8 @@ SEED_BASE = 0x50484B0000000000
 @dataclasses.dataclass
 class Scene:
     name: str
-    shapes: list            # ("box", hx, hy, hz) | ("sphere", r, stacks, sectors) | ("mesh", verts, tris)
+    shapes: list            # ("box", hx, hy, hz) | ("sphere", r, stacks, sectors) | ("pyramid", base_half, height)
+                            # | ("mesh", verts, tris)
     bodies: np.ndarray      # BODY_DTYPE records; "shape" indexes `shapes`
     nworlds: int = 1
     gravity: tuple = (0.0, -9.81, 0.0)
@@ -51,6 +52,8 @@ class Scene:
                 n += 8
             elif s[0] == "sphere":
                 n += 2 + (s[2] - 1) * s[3]
+            elif s[0] == "pyramid":
+                n += 5
             else:
                 n += len(s[1])
         return n
@@ -308,6 +311,8 @@ def load(world, scene: Scene, shape_offset_map=None):
             ids.append(world.mesh_box(*s[1:4]))
         elif s[0] == "sphere":
             ids.append(world.mesh_sphere(s[1], s[2], s[3]))
+        elif s[0] == "pyramid":
+            ids.append(world.mesh_pyramid(s[1], s[2]))
         else:
             ids.append(world.mesh_make(s[1], s[2]))
     rec = scene.bodies.copy()
@@ -330,3 +335,61 @@ def make_world(scene: Scene, precision="f64", pair_factor=8, iterations=None, ma
     w = World(d)
     handles = load(w, scene)
     return w, handles
+
+
+def load_json(path_or_text, name=None) -> Scene:
+    """A scene in the reference's demo JSON format (tests/helper/src/graphics.cpp:20-140):
+    {"gravity": [3], "solver_iterations": n, "objects": [{"pos": [3], "vel": [3],
+    "orientation": [w, x, y, z], "angular_velocity": [3], "inertia_tensor": [Ixx, Iyy, Izz],
+    "type": "dynam" | "stat", "mesh": {...}, "mass": m, "restitution": e, "friction": mu}]}, with
+    the reference's defaults (vel, angular velocity 0, orientation identity, inertia (1, 1, 1),
+    dynamic, box half extents 0.5, restitution 0.5, friction 0.5, sphere 16 stacks x 32 sectors).
+    Mesh fields are single precision in the reference (graphics.cpp:24-41), so they are rounded to
+    float32 here too. A pyramid gets `height` as its base half size and `base_size` as its height,
+    the order in which the reference's loader passes them to mesh::pyramid(base_half, height)
+    (graphics.cpp:101-102, mesh.h:236). Camera and window fields are ignored (no rendering).
+    Identical meshes are shared, as the reference keys them by their JSON text."""
+    import json
+    import os
+
+    if isinstance(path_or_text, str) and os.path.exists(path_or_text):
+        with open(path_or_text) as f:
+            cfg = json.load(f)
+        name = name or os.path.basename(path_or_text)
+    else:
+        cfg = json.loads(path_or_text)
+    f32 = lambda x: float(np.float32(x))
+    gravity = tuple(float(v) for v in cfg.get("gravity", (0.0, -9.81, 0.0)))
+    iterations = int(cfg.get("solver_iterations", 10))
+    shapes, keys, recs = [], {}, []
+    for o in cfg.get("objects", []):
+        mesh = o.get("mesh", {"name": "box", "half_extents": [0.5, 0.5, 0.5]})
+        kind = mesh.get("name")
+        if kind is None:  # a variant is also recognised by its fields
+            kind = "box" if "half_extents" in mesh else ("pyramid" if "height" in mesh else "sphere")
+        if kind == "box":
+            shape = ("box",) + tuple(f32(v) for v in mesh["half_extents"])
+        elif kind == "pyramid":
+            shape = ("pyramid", f32(mesh["height"]), f32(mesh["base_size"]))
+        elif kind == "sphere":
+            shape = ("sphere", f32(mesh["radius"]), int(mesh.get("stacks", 16)), int(mesh.get("sectors", 32)))
+        else:
+            raise ValueError(f"unknown mesh kind {kind!r}")
+        if shape not in keys:
+            keys[shape] = len(shapes)
+            shapes.append(shape)
+        r = np.zeros((), dtype=BODY_DTYPE)
+        r["type"] = 1 if o.get("type", "dynam") == "stat" else 0
+        r["shape"] = keys[shape]
+        r["pos"] = o["pos"]
+        r["vel"] = o.get("vel", (0.0, 0.0, 0.0))
+        r["quat"] = o.get("orientation", (1.0, 0.0, 0.0, 0.0))
+        r["ang_vel"] = o.get("angular_velocity", (0.0, 0.0, 0.0))
+        it = o.get("inertia_tensor", (1.0, 1.0, 1.0))
+        r["inertia"] = (it[0], 0, 0, 0, it[1], 0, 0, 0, it[2])
+        r["mass"] = float(o["mass"])
+        r["restitution"] = float(o.get("restitution", 0.5))
+        r["friction"] = float(o.get("friction", 0.5))
+        recs.append(r)
+    bodies = np.array(recs, dtype=BODY_DTYPE) if recs else np.zeros(0, dtype=BODY_DTYPE)
+    return Scene(name or "json scene", shapes, bodies, 1, gravity, iterations=iterations)

@@ -185,3 +185,17 @@ def test_autotune_keeps_results():
     assert np.array_equal(a.bodies(), b.bodies())
     a.close()
     b.close()
+
+
+def test_fp64_json_scene_bit_identical():
+    # a scene in the reference's demo JSON format (boxes, UV spheres of two layouts, a pyramid)
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scene_mixed_stack.json")
+    scene = scenes.load_json(path)
+    world, ow, _ = run_pair(scene, 0)
+    for step in range(180):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        compare_step(world, ow, step)
+    world.close()
