@@ -205,6 +205,35 @@ typedef struct pk_ray
 } pk_ray;
 int pk_world_raycast(pk_world *w, const pk_ray *rays, int32_t n, int32_t cap, uint64_t *handles, double *distances,
                      int32_t *counts);
+/* Waiting on collision events: the part of the reference's task handler that consumes them
+ * (wait_for_collision / wait_for_separation / wait_until_destroyed, core/awaitables.h:136-300;
+ * task_handler::on_collision, on_collision_exit, on_destruction, core/co.h:495-595). A waiter watches
+ * one object for a begin (PK_WAIT_COLLISION) or end (PK_WAIT_SEPARATION) event with `with` or with
+ * any object (PK_HANDLE_ANY), or for its removal (PK_WAIT_DESTROYED). pk_world_dispatch offers the
+ * last step's events in pair-key order (each event to the first object's waiters, then the
+ * second's; every matching waiter fires once and is removed) and returns the fired waiters; call it
+ * after each step, before bodies are added or removed. Removing an object fails its collision and
+ * separation waiters and those that name it as `with` (failed = 1) and fires its destruction
+ * waiters. pk_world_wait returns PK_ERR_STALE_HANDLE for an object that is not alive (the
+ * reference's await_ready resumes at once). */
+#define PK_HANDLE_ANY UINT64_MAX
+enum
+{
+    PK_WAIT_COLLISION = 1,
+    PK_WAIT_SEPARATION = 2,
+    PK_WAIT_DESTROYED = 3
+};
+typedef struct pk_wake
+{
+    uint64_t waiter;
+    uint64_t object;
+    uint64_t other; /* PK_HANDLE_ANY for destruction and failures */
+    int32_t kind;
+    int32_t failed;
+} pk_wake;
+int pk_world_wait(pk_world *w, int32_t kind, uint64_t object, uint64_t with, uint64_t *waiter);
+int pk_world_cancel_wait(pk_world *w, uint64_t waiter);
+int pk_world_dispatch(pk_world *w, pk_wake *out, int32_t cap, int32_t *n);
 /* Solver colour of each manifold with contact rows in the last step (key order). */
 int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t cap, int32_t *n,
                           int32_t *ncolours_world0);

@@ -7,6 +7,7 @@
 // device memory a world lives.
 #include "../../include/physkit_gb300.h"
 #include "pk_engine_api.h"
+#include "pk_events.h"
 #include "pk_narrow.cuh"
 #include "pk_math.cuh"
 
@@ -77,6 +78,10 @@ struct pk_world
     int steps = 0;
     bool shapes_dirty = false;
     bool order_dirty = false; // solver schedule needs recomputing (bodies added or removed)
+    pk::EventDispatcher waiters; // collision / separation / destruction waiters (pk_world_wait)
+    std::vector<pk::Wake> wakes; // fired, not yet returned by pk_world_dispatch
+    size_t wake_head = 0;
+    int dispatched_step = 0;     // host step whose events were last offered to the waiters
 };
 
 // Allocation-free narrowphase (pk_collide_noalloc). Its device staging lives in this file-scope
@@ -575,6 +580,7 @@ static int kill_slot(pk_world *w, int slot)
 {
     SlotInfo &si = w->slots[size_t(slot)];
     SubWorld &sw = w->worlds[size_t(si.world)];
+    w->waiters.destroyed(uint64_t(uint32_t(slot)) | (uint64_t(si.gen) << 32), w->wakes);
     si.alive = false;
     sw.local_alive[size_t(si.local)] = 0;
     sw.local_gen[size_t(si.local)]++;
@@ -606,7 +612,11 @@ int pk_world_clear(pk_world *w, int32_t world)
     {
         int slot = sw.local_slot[l];
         if (slot < 0) continue;
-        if (w->slots[size_t(slot)].alive) dead.push_back(slot);
+        if (w->slots[size_t(slot)].alive)
+        {
+            dead.push_back(slot);
+            w->waiters.destroyed(uint64_t(uint32_t(slot)) | (uint64_t(w->slots[size_t(slot)].gen) << 32), w->wakes);
+        }
         w->slots[size_t(slot)] = SlotInfo{};
         w->free_slots.push_back(slot);
     }
@@ -986,6 +996,65 @@ int pk_world_read_events(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *
         split_key(w, raw[size_t(i)], keys ? keys + i : nullptr, worlds ? worlds + i : nullptr);
         if (kinds) kinds[i] = kd[size_t(i)];
     }
+    return PK_OK;
+}
+
+int pk_world_wait(pk_world *w, int32_t kind, uint64_t object, uint64_t with, uint64_t *waiter)
+{
+    if (!w || kind < PK_WAIT_COLLISION || kind > PK_WAIT_DESTROYED || !waiter) return PK_ERR_INVALID;
+    int slot;
+    if (!resolve(w, object, &slot)) return PK_ERR_STALE_HANDLE; // await_ready: nothing to wait for
+    *waiter = w->waiters.add(kind, object, with);
+    return PK_OK;
+}
+
+int pk_world_cancel_wait(pk_world *w, uint64_t waiter)
+{
+    if (!w) return PK_ERR_INVALID;
+    return w->waiters.cancel(waiter) ? PK_OK : PK_ERR_INVALID;
+}
+
+int pk_world_dispatch(pk_world *w, pk_wake *out, int32_t cap, int32_t *n)
+{
+    if (!w || cap < 0 || (cap > 0 && !out)) return PK_ERR_INVALID;
+    if (w->dispatched_step != w->steps)
+    {
+        // the last step's begin/end events, in pair-key order, as (handle, handle) pairs
+        int ne = w->eng->read_events(nullptr, nullptr, 0);
+        if (ne < 0) return PK_ERR_CUDA;
+        std::vector<uint64_t> raw(static_cast<size_t>(ne));
+        std::vector<int> kd(static_cast<size_t>(ne));
+        if (ne > 0 && w->eng->read_events(raw.data(), kd.data(), ne) < 0) return PK_ERR_CUDA;
+        for (int i = 0; i < ne; ++i)
+        {
+            uint64_t ref;
+            int32_t wid;
+            split_key(w, raw[size_t(i)], &ref, &wid);
+            const SubWorld &sw = w->worlds[size_t(wid)];
+            uint64_t h[2];
+            const uint32_t loc[2] = {uint32_t(ref >> 32), uint32_t(ref & 0xFFFFFFFFu)};
+            for (int k = 0; k < 2; ++k)
+            {
+                const int slot = loc[k] < sw.local_slot.size() ? sw.local_slot[loc[k]] : -1;
+                h[k] = slot < 0 ? pk::EventDispatcher::kAny
+                                : uint64_t(uint32_t(slot)) | (uint64_t(sw.local_gen[loc[k]]) << 32);
+            }
+            w->waiters.event(kd[size_t(i)], h[0], h[1], w->wakes);
+        }
+        w->dispatched_step = w->steps;
+    }
+    int m = 0;
+    while (m < cap && w->wake_head < w->wakes.size())
+    {
+        const pk::Wake &k = w->wakes[w->wake_head++];
+        out[m++] = pk_wake{k.waiter, k.object, k.other, k.kind, k.failed};
+    }
+    if (w->wake_head == w->wakes.size())
+    {
+        w->wakes.clear();
+        w->wake_head = 0;
+    }
+    if (n) *n = m;
     return PK_OK;
 }
 

@@ -64,6 +64,15 @@ class RayC(C.Structure):
                 ("world", C.c_int32), ("reserved", C.c_int32)]
 
 
+class WakeC(C.Structure):
+    _fields_ = [("waiter", C.c_uint64), ("object", C.c_uint64), ("other", C.c_uint64), ("kind", C.c_int32),
+                ("failed", C.c_int32)]
+
+
+HANDLE_ANY = 0xFFFFFFFFFFFFFFFF
+WAIT_COLLISION, WAIT_SEPARATION, WAIT_DESTROYED = 1, 2, 3
+
+
 class CollideShapeC(C.Structure):
     _fields_ = [("kind", C.c_int32), ("shape", C.c_int32), ("p", C.c_double * 10)]
 
@@ -109,6 +118,9 @@ def lib():
             "pk_world_read_events": (C.c_int, [vp, u64p, i32p, i32p, C.c_int32, i32p]),
             "pk_world_read_colours": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p, i32p]),
             "pk_world_raycast": (C.c_int, [vp, P(RayC), C.c_int32, C.c_int32, u64p, dp, i32p]),
+            "pk_world_wait": (C.c_int, [vp, C.c_int32, C.c_uint64, C.c_uint64, u64p]),
+            "pk_world_cancel_wait": (C.c_int, [vp, C.c_uint64]),
+            "pk_world_dispatch": (C.c_int, [vp, P(WakeC), C.c_int32, i32p]),
             "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_collide_noalloc": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
             "pk_world_set_timing": (C.c_int, [vp, C.c_int32]),
@@ -445,6 +457,34 @@ class World:
         s = np.ascontiguousarray(state13, dtype=np.float64)
         _check(self.L.pk_world_write_body(self.h, C.c_uint64(int(handle)), _ptr(s, C.c_double)),
                "pk_world_write_body")
+
+    # waiting on collision events ---------------------------------------------------------------
+    def wait(self, kind, obj, with_=None):
+        """Register a waiter (WAIT_COLLISION / WAIT_SEPARATION with an object or any, or
+        WAIT_DESTROYED); returns its id, or None when `obj` is not alive (nothing to wait for)."""
+        out = C.c_uint64()
+        rc = self.L.pk_world_wait(self.h, int(kind), int(obj), HANDLE_ANY if with_ is None else int(with_),
+                                  C.byref(out))
+        if rc == PK_ERR_STALE_HANDLE:
+            return None
+        _check(rc, "pk_world_wait")
+        return out.value
+
+    def cancel_wait(self, waiter):
+        _check(self.L.pk_world_cancel_wait(self.h, int(waiter)), "pk_world_cancel_wait")
+
+    def dispatch(self, cap=1024):
+        """Offer the last step's events to the waiters; returns the fired ones as
+        (waiter, object, other or None, kind, failed)."""
+        out, res = (WakeC * cap)(), []
+        while True:
+            n = C.c_int32()
+            _check(self.L.pk_world_dispatch(self.h, out, cap, C.byref(n)), "pk_world_dispatch")
+            for i in range(n.value):
+                k = out[i]
+                res.append((k.waiter, k.object, None if k.other == HANDLE_ANY else k.other, k.kind, bool(k.failed)))
+            if n.value < cap:
+                return res
 
     RAY_DTYPE = np.dtype([("origin", np.float64, 3), ("direction", np.float64, 3), ("max_distance", np.float64),
                           ("world", np.int32), ("reserved", np.int32)])

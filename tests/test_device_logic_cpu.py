@@ -1,4 +1,5 @@
-"""Device code checked on the CPU: pk_narrow.cuh compiled with g++ (no GPU needed)."""
+"""Code of the library checked on the CPU with g++ (no GPU needed): pk_narrow.cuh (device code
+compiled for the host) and pk_events.h (the host-side event dispatcher)."""
 import os
 import subprocess
 
@@ -11,4 +12,13 @@ def test_heap_order_and_clustered_support(tmp_path):
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", src, "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "heap_mismatch=0 support_mismatch_f64=0 support_mismatch_f32=0" in r.stdout
+    assert "heap_mismatch=0 support_mismatch_f64=0 support_mismatch_f32=0 uv_mismatch_f64=0 uv_mismatch_f32=0" in r.stdout
+
+
+def test_event_dispatcher_rules(tmp_path):
+    exe = tmp_path / "check_events"
+    src = os.path.join(ROOT, "tests", "cpp", "check_events.cpp")
+    subprocess.run(["g++", "-O2", "-std=c++17", src, "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "event_check_failures=0" in r.stdout
