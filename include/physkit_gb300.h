@@ -205,6 +205,41 @@ typedef struct pk_ray
 } pk_ray;
 int pk_world_raycast(pk_world *w, const pk_ray *rays, int32_t n, int32_t cap, uint64_t *handles, double *distances,
                      int32_t *counts);
+/* Joints, replacing constraint_solver::add_constraint / remove_constraint (constraint.h:1036-1049)
+ * and the joint types of constraint.h:139-865, added through the world's command queue
+ * (world.h:155-175). type: 0 distance (local_a, local_b, distance), 1 ball_socket (anchor, world
+ * space), 2 hinge (local_a, local_b, axis_a, axis_b: local anchors and axes), 3 slider (anchor and
+ * axis_a in world space), 4 weld (anchor, world space), 5 spring (local_a, local_b, distance,
+ * stiffness, damping). Anchors given in world space are projected into both bodies at the call,
+ * from their current poses, as the reference's constructors do. Joint rows are solved before the
+ * contacts in every iteration, in the reference's order (per world: types in order, then arena
+ * slots). Removing a body removes its joints (the reference leaves that to the caller). A step
+ * graph captured before joints are added must be captured again. */
+enum
+{
+    PK_JOINT_DISTANCE = 0,
+    PK_JOINT_BALL_SOCKET = 1,
+    PK_JOINT_HINGE = 2,
+    PK_JOINT_SLIDER = 3,
+    PK_JOINT_WELD = 4,
+    PK_JOINT_SPRING = 5
+};
+typedef struct pk_joint_desc
+{
+    int32_t type;
+    int32_t reserved;
+    uint64_t a, b; /* body handles, same world */
+    double anchor[3];
+    double local_a[3], local_b[3];
+    double axis_a[3], axis_b[3];
+    double distance, stiffness, damping;
+} pk_joint_desc;
+void pk_joint_desc_init(pk_joint_desc *d);
+int pk_joint_add(pk_world *w, const pk_joint_desc *d, uint64_t *out_handle);
+int pk_joint_remove(pk_world *w, uint64_t handle);
+/* Accumulated impulses of the joint's rows (up to 6) after the last step; nrows = its row count. */
+int pk_joint_read_impulses(pk_world *w, uint64_t handle, double *out6, int32_t *nrows);
+
 /* Waiting on collision events: the part of the reference's task handler that consumes them
  * (wait_for_collision / wait_for_separation / wait_until_destroyed, core/awaitables.h:136-300;
  * task_handler::on_collision, on_collision_exit, on_destruction, core/co.h:495-595). A waiter watches

@@ -1345,6 +1345,171 @@ struct ContactRows
     int manifold = 0; // index of the owning manifold in the step's active list
 };
 
+// ---------------------------------------------------------------------------------------------
+// joints (collision/constraint.h:139-865): per-world arenas per type, built into rows every step
+// ---------------------------------------------------------------------------------------------
+enum JointType
+{
+    J_DISTANCE = 0, // constraint_type order (constraint.h:15-24), which is also the arenas' order
+    J_BALL_SOCKET,
+    J_HINGE,
+    J_SLIDER,
+    J_WELD,
+    J_SPRING,
+    J_COUNT
+};
+constexpr int kJointRows[J_COUNT] = {1, 3, 5, 5, 6, 1}; // jacobian_dimension of each type
+
+struct Joint
+{
+    int type = J_DISTANCE;
+    uint32_t a = 0, b = 0; // body arena indices
+    V3 la, lb;             // local anchors
+    V3 axa, axb;           // hinge: local axes (normalised); slider: local axis of a
+    V3 va, wa;             // hinge: orthonormal basis of axa; slider: local tangents of a
+    Qt qrel;               // slider, weld: conj(q_a) q_b at creation
+    double distance = 0, stiffness = 0, damping = 0;
+    double acc[6] = {0, 0, 0, 0, 0, 0}; // accumulated impulses, kept for warm starting
+};
+struct JointSlot
+{
+    std::optional<Joint> value;
+    uint32_t gen = 0;
+};
+struct JointRow
+{
+    Row row;
+    double *dst; // the joint's accumulated impulse this row writes back
+};
+
+// The rows of one joint in the reference's build order (build_jacobian_impl of each type).
+inline void build_joint_rows(Joint &j, Body &a, Body &b, double dt, std::vector<JointRow> &out)
+{
+    const V3 r_a = rotate(a.q, j.la), r_b = rotate(b.q, j.lb);
+    auto linear = [&](V3 n, V3 arm_a, double bias_factor, V3 delta, double *acc, bool slider) {
+        Row r;
+        r.J_v = n;
+        r.J_w_a = cross(arm_a, n);
+        r.J_w_b = -cross(r_b, n);
+        r.acc = *acc;
+        r.a = &a;
+        r.b = &b;
+        V3 k_a = matvec(a.I_w_inv, r.J_w_a), k_b = matvec(b.I_w_inv, r.J_w_b);
+        if (slider)
+        {
+            double lin = a.inv_mass + b.inv_mass;
+            double ang = dot(r.J_w_a, k_a) + dot(r.J_w_b, k_b);
+            double reg = 0.01 * ang;
+            r.gamma = reg;
+            r.M_eff = 1.0 / (lin + ang + reg);
+            double e = dot(delta, n);
+            e = (e < -0.2) ? -0.2 : ((0.2 < e) ? 0.2 : e); // std::clamp to +-0.2 m
+            r.bias = (bias_factor / dt) * e;
+        }
+        else
+        {
+            r.M_eff = 1.0 / (a.inv_mass + b.inv_mass + dot(r.J_w_a, k_a) + dot(r.J_w_b, k_b));
+            r.bias = (bias_factor / dt) * dot(delta, n);
+        }
+        out.push_back({r, acc});
+    };
+    auto angular = [&](V3 n, double bias_factor, V3 err, double *acc) {
+        Row r;
+        r.J_v = V3{0.0, 0.0, 0.0};
+        r.J_w_a = n;
+        r.J_w_b = -n;
+        r.acc = *acc;
+        r.a = &a;
+        r.b = &b;
+        V3 k_a = matvec(a.I_w_inv, r.J_w_a), k_b = matvec(b.I_w_inv, r.J_w_b);
+        r.M_eff = 1.0 / (dot(r.J_w_a, k_a) + dot(r.J_w_b, k_b));
+        r.bias = (bias_factor / dt) * dot(err, n);
+        out.push_back({r, acc});
+    };
+    const V3 axes[3] = {V3{1.0, 0.0, 0.0}, V3{0.0, 1.0, 0.0}, V3{0.0, 0.0, 1.0}};
+    switch (j.type)
+    {
+    case J_DISTANCE:
+    case J_SPRING: {
+        // distance_constraint / spring_constraint::build_jacobian_impl (constraint.h:187-231, 309-352)
+        V3 delta = (a.pos + r_a) - (b.pos + r_b);
+        double cur = norm(delta);
+        if (cur < 1e-6) return;
+        V3 u = delta / cur;
+        Row r;
+        r.J_v = u;
+        r.J_w_a = cross(r_a, u);
+        r.J_w_b = -cross(r_b, u);
+        r.acc = j.acc[0];
+        r.a = &a;
+        r.b = &b;
+        V3 k_a = matvec(a.I_w_inv, r.J_w_a), k_b = matvec(b.I_w_inv, r.J_w_b);
+        if (j.type == J_DISTANCE)
+        {
+            r.M_eff = 1.0 / (a.inv_mass + b.inv_mass + dot(r.J_w_a, k_a) + dot(r.J_w_b, k_b));
+            r.bias = (0.1 / dt) * (cur - j.distance);
+        }
+        else
+        {
+            double mc = a.inv_mass + b.inv_mass + dot(r.J_w_a, k_a) + dot(r.J_w_b, k_b);
+            double gamma = 1.0 / (dt * (j.damping + dt * j.stiffness));
+            double beta = dt * j.stiffness / (j.damping + dt * j.stiffness);
+            r.M_eff = 1.0 / (mc + gamma);
+            r.bias = (beta / dt) * (cur - j.distance);
+            r.gamma = gamma;
+        }
+        out.push_back({r, &j.acc[0]});
+        return;
+    }
+    case J_BALL_SOCKET: {
+        // ball_socket_constraint::build_jacobian_impl (constraint.h:407-446)
+        V3 delta = (a.pos + r_a) - (b.pos + r_b);
+        for (int k = 0; k < 3; ++k) linear(axes[k], r_a, 0.1, delta, &j.acc[k], false);
+        return;
+    }
+    case J_HINGE: {
+        // hinge_constraint::build_jacobian_impl (constraint.h:512-580)
+        V3 delta = (a.pos + r_a) - (b.pos + r_b);
+        for (int k = 0; k < 3; ++k) linear(axes[k], r_a, 0.2, delta, &j.acc[k], false);
+        V3 u_a = rotate(a.q, j.axa), u_b = rotate(b.q, j.axb);
+        V3 err = -cross(u_a, u_b);
+        angular(rotate(a.q, j.va), 0.2, err, &j.acc[3]);
+        angular(rotate(a.q, j.wa), 0.2, err, &j.acc[4]);
+        return;
+    }
+    case J_SLIDER: {
+        // slider_constraint::build_jacobian_impl (constraint.h:654-738)
+        V3 delta = (a.pos + r_a) - (b.pos + r_b);
+        V3 axis_a = rotate(a.q, j.axa);
+        V3 t1 = rotate(a.q, j.va), t2 = rotate(a.q, j.wa);
+        V3 lever = r_a - delta;
+        linear(t1, lever, 0.1, delta, &j.acc[0], true);
+        linear(t2, lever, 0.1, delta, &j.acc[1], true);
+        Qt cur = qmul(conj(a.q), b.q);
+        Qt e = qmul(j.qrel, conj(cur));
+        if (e.w < 0) e = Qt{-e.w, -e.x, -e.y, -e.z};
+        V3 err = rotate(a.q, V3{e.x, e.y, e.z} * 2.0);
+        angular(axis_a, 0.1, err, &j.acc[2]);
+        angular(t1, 0.1, err, &j.acc[3]);
+        angular(t2, 0.1, err, &j.acc[4]);
+        return;
+    }
+    case J_WELD: {
+        // weld_constraint::build_jacobian_impl (constraint.h:789-855)
+        V3 delta = (a.pos + r_a) - (b.pos + r_b);
+        for (int k = 0; k < 3; ++k) linear(axes[k], r_a, 0.1, delta, &j.acc[k], false);
+        Qt cur = qmul(conj(a.q), b.q);
+        Qt e = qmul(j.qrel, conj(cur));
+        if (e.w < 0) e = Qt{-e.w, -e.x, -e.y, -e.z};
+        V3 err = rotate(a.q, V3{e.x, e.y, e.z} * 2.0);
+        for (int k = 0; k < 3; ++k) angular(axes[k], 0.1, err, &j.acc[3 + k]);
+        return;
+    }
+    default:
+        return;
+    }
+}
+
 // build_contact_jacobian (constraint.h:874-953)
 std::optional<ContactRows> build_contact(Body &a, Body &b, V3 la, V3 lb, V3 wn, double dt, double rthr)
 {
@@ -1457,6 +1622,8 @@ struct World
     std::vector<uint32_t> free_stack;
 
     DynTree static_tree, dynamic_tree;
+    std::array<std::vector<JointSlot>, J_COUNT> joints;
+    std::array<std::vector<uint32_t>, J_COUNT> joint_free;
     std::vector<uint32_t> moved;
     std::unordered_set<uint64_t> pairs;
     std::map<uint64_t, Manifold> manifolds; // narrow_phase store, iterated in key order
@@ -1498,6 +1665,100 @@ struct World
         }
         return static_cast<uint64_t>(idx) | (static_cast<uint64_t>(gen) << 32);
     }
+    // constraint_solver::add_constraint via the world's command (world.h:155-166): the joint is
+    // built from the bodies' current poses (constructors, constraint.h:183-187, 386-392, 494-500,
+    // 635-652, 779-785)
+    uint64_t add_joint(int type, uint64_t ha, uint64_t hb, V3 anchor, V3 la, V3 lb, V3 axis_a, V3 axis_b,
+                       double distance, double stiffness, double damping)
+    {
+        uint32_t ia = static_cast<uint32_t>(ha & 0xFFFFFFFFu), ib = static_cast<uint32_t>(hb & 0xFFFFFFFFu);
+        Body &a = *get(ia);
+        Body &b = *get(ib);
+        Joint j;
+        j.type = type;
+        j.a = ia;
+        j.b = ib;
+        j.distance = distance;
+        j.stiffness = stiffness;
+        j.damping = damping;
+        switch (type)
+        {
+        case J_DISTANCE:
+        case J_SPRING:
+            j.la = la;
+            j.lb = lb;
+            break;
+        case J_BALL_SOCKET:
+        case J_WELD:
+            j.la = a.to_local(anchor);
+            j.lb = b.to_local(anchor);
+            j.qrel = qmul(conj(a.q), b.q);
+            break;
+        case J_HINGE: {
+            j.la = la;
+            j.lb = lb;
+            j.axa = normalized(axis_a);
+            j.axb = normalized(axis_b);
+            auto t = orthonormal_basis(j.axa);
+            j.va = t.first;
+            j.wa = t.second;
+            break;
+        }
+        case J_SLIDER: {
+            j.la = a.to_local(anchor);
+            j.lb = b.to_local(anchor);
+            V3 n = normalized(axis_a);
+            j.axa = rotate(conj(a.q), n);
+            auto t = orthonormal_basis(n);
+            j.va = rotate(conj(a.q), t.first);
+            j.wa = rotate(conj(a.q), t.second);
+            j.qrel = qmul(conj(a.q), b.q);
+            break;
+        }
+        default:
+            return ~uint64_t(0);
+        }
+        auto &ar = joints[static_cast<size_t>(type)];
+        auto &fr = joint_free[static_cast<size_t>(type)];
+        uint32_t idx, gen;
+        if (fr.empty())
+        {
+            idx = static_cast<uint32_t>(ar.size());
+            ar.push_back({});
+            ar.back().value.emplace(j);
+            gen = 0;
+        }
+        else
+        {
+            idx = fr.back();
+            fr.pop_back();
+            ar[idx].value.emplace(j);
+            gen = ar[idx].gen;
+        }
+        return static_cast<uint64_t>(idx) | (static_cast<uint64_t>(gen & 0xFFFFFFu) << 32) |
+               (static_cast<uint64_t>(type) << 56);
+    }
+    bool remove_joint(uint64_t h)
+    {
+        int type = static_cast<int>(h >> 56);
+        uint32_t idx = static_cast<uint32_t>(h & 0xFFFFFFFFu), gen = static_cast<uint32_t>((h >> 32) & 0xFFFFFFu);
+        if (type < 0 || type >= J_COUNT) return false;
+        auto &ar = joints[static_cast<size_t>(type)];
+        if (idx >= ar.size() || !ar[idx].value || (ar[idx].gen & 0xFFFFFFu) != gen) return false;
+        ar[idx].value.reset();
+        ar[idx].gen++;
+        joint_free[static_cast<size_t>(type)].push_back(idx);
+        return true;
+    }
+    const Joint *joint(uint64_t h) const
+    {
+        int type = static_cast<int>(h >> 56);
+        uint32_t idx = static_cast<uint32_t>(h & 0xFFFFFFFFu);
+        if (type < 0 || type >= J_COUNT || idx >= joints[static_cast<size_t>(type)].size()) return nullptr;
+        const auto &s = joints[static_cast<size_t>(type)][idx];
+        return s.value ? &*s.value : nullptr;
+    }
+
     // world_base::raycast (world.h:260-319): both trees' hits, merged by their current distance
     // (static first on a tie), as (handle, distance)
     std::vector<std::pair<uint64_t, double>> raycast(V3 origin, V3 dir, double max_d) const
@@ -1731,6 +1992,13 @@ struct World
             ncolours = active_keys.empty() ? 0 : 1;
         }
 
+        // joint rows: every arena in type order, slots in index order (constraint.h:1109-1119)
+        std::vector<JointRow> jrows;
+        for (int t = 0; t < J_COUNT; ++t)
+            for (auto &js : joints[static_cast<size_t>(t)])
+                if (js.value) build_joint_rows(*js.value, *get(js.value->a), *get(js.value->b), dt, jrows);
+
+        for (auto &jr : jrows) jr.row.warm_start();
         for (size_t oi : order)
         {
             rows[oi].normal.warm_start();
@@ -1739,6 +2007,7 @@ struct World
         }
         for (int it = 0; it < iterations; ++it)
         {
+            for (auto &jr : jrows) jr.row.apply();
             for (size_t oi : order)
             {
                 ContactRows &pt = rows[oi];
@@ -1782,6 +2051,7 @@ struct World
             pt.cache->tangent_impulse[0] = pt.t1.acc;
             pt.cache->tangent_impulse[1] = pt.t2.acc;
         }
+        for (auto &jr : jrows) *jr.dst = jr.row.acc;
     }
 
     // world::step_impl (src/world.cpp:20-56)
@@ -2058,6 +2328,22 @@ int pko_world_raycast(pko_world *w, const double *origin, const double *dir, dou
         if (dist) dist[i] = hits[static_cast<size_t>(i)].second;
     }
     return n;
+}
+
+uint64_t pko_joint_add(pko_world *w, int type, uint64_t a, uint64_t b, const double *p16)
+{
+    // p16: anchor3, local_a3, local_b3, axis_a3, axis_b3, distance (stiffness, damping: p16[16..17])
+    const double *p = p16;
+    return w->w.add_joint(type, a, b, {p[0], p[1], p[2]}, {p[3], p[4], p[5]}, {p[6], p[7], p[8]}, {p[9], p[10], p[11]},
+                          {p[12], p[13], p[14]}, p[15], p[16], p[17]);
+}
+int pko_joint_remove(pko_world *w, uint64_t h) { return w->w.remove_joint(h) ? 1 : 0; }
+int pko_joint_impulses(pko_world *w, uint64_t h, double *out6)
+{
+    const Joint *j = w->w.joint(h);
+    if (!j) return -1;
+    for (int k = 0; k < 6; ++k) out6[k] = j->acc[k];
+    return kJointRows[j->type];
 }
 
 pko_tree *pko_tree_create(void) { return new pko_tree; }

@@ -65,6 +65,12 @@ int pko_read_pairs(pko_world *w, uint64_t *keys, int cap);
 int pko_read_manifolds(pko_world *w, uint64_t *keys, int *counts, double *contacts, int cap);
 /* Events of the last step in narrowphase order: key and kind (1 begin, 2 end). */
 int pko_read_events(pko_world *w, uint64_t *keys, int *kinds, int cap);
+/* Joints (constraint.h:139-865), type 0 distance 1 ball_socket 2 hinge 3 slider 4 weld 5 spring.
+ * p18: anchor3 local_a3 local_b3 axis_a3 axis_b3 distance stiffness damping. Returns the handle
+ * (slot | gen << 32 | type << 56). pko_joint_impulses: the accumulated impulses, returns the row count. */
+uint64_t pko_joint_add(pko_world *w, int type, uint64_t a, uint64_t b, const double *p18);
+int pko_joint_remove(pko_world *w, uint64_t handle);
+int pko_joint_impulses(pko_world *w, uint64_t handle, double *out6);
 /* world_base::raycast (world.h:260-319): hits in the reference's order; returns the hit count */
 int pko_world_raycast(pko_world *w, const double *origin, const double *dir, double max_dist, uint64_t *handles,
                       double *dist, int cap);

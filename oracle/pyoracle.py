@@ -48,6 +48,9 @@ def lib():
             "pko_read_manifolds": (C.c_int, [C.c_void_p, up, ip, dp, C.c_int]),
             "pko_read_events": (C.c_int, [C.c_void_p, up, ip, C.c_int]),
             "pko_world_raycast": (C.c_int, [C.c_void_p, dp, dp, C.c_double, up, dp, C.c_int]),
+            "pko_joint_add": (C.c_uint64, [C.c_void_p, C.c_int, C.c_uint64, C.c_uint64, dp]),
+            "pko_joint_remove": (C.c_int, [C.c_void_p, C.c_uint64]),
+            "pko_joint_impulses": (C.c_int, [C.c_void_p, C.c_uint64, dp]),
             "pko_read_colours": (C.c_int, [C.c_void_p, up, ip, C.c_int, ip]),
             "pko_last_moved": (C.c_int, [C.c_void_p]),
             "pko_gjk_epa": (C.c_int, [C.c_void_p, C.c_int, dp, C.c_int, C.c_int, dp, C.c_int, dp]),
@@ -190,6 +193,23 @@ class OracleWorld:
 
     def last_moved(self):
         return self.L.pko_last_moved(self.h)
+
+    JOINT_TYPES = {"distance": 0, "ball_socket": 1, "hinge": 2, "slider": 3, "weld": 4, "spring": 5}
+
+    def add_joint(self, kind, a, b, anchor=(0, 0, 0), local_a=(0, 0, 0), local_b=(0, 0, 0), axis_a=(0, 0, 0),
+                  axis_b=(0, 0, 0), distance=0.0, stiffness=0.0, damping=0.0):
+        """constraint_solver::add_constraint (constraint.h:1036-1041); returns the joint handle."""
+        p, pp = _dp(list(anchor) + list(local_a) + list(local_b) + list(axis_a) + list(axis_b) +
+                    [distance, stiffness, damping])
+        return self.L.pko_joint_add(self.h, self.JOINT_TYPES[kind], int(a), int(b), pp)
+
+    def remove_joint(self, handle):
+        return bool(self.L.pko_joint_remove(self.h, int(handle)))
+
+    def joint_impulses(self, handle):
+        out, op = _dp(np.zeros(6))
+        n = self.L.pko_joint_impulses(self.h, int(handle), op)
+        return out[:max(n, 0)]
 
     def raycast(self, origin, direction, max_dist):
         """world_base::raycast (world.h:260-319): [(handle, distance)] in the reference's order."""

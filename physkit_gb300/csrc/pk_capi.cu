@@ -51,6 +51,19 @@ struct SubWorld
     std::vector<char> local_alive;
     double gravity[3] = {0.0, -9.81, 0.0};
     int active = 1;
+    // joint arenas, one per constraint type (constraint.h:969-1020): slot -> joint index or -1
+    std::vector<int> jslot[6];
+    std::vector<uint32_t> jgen[6];
+    std::vector<int> jfree[6];
+};
+
+struct JointHost
+{
+    int type = 0, world = 0, arena = 0;
+    int slot_a = 0, slot_b = 0, local_a = 0, local_b = 0;
+    double p[25] = {}; // la3 lb3 axa3 axb3 va3 wa3 qrel4 distance stiffness damping
+    double acc[6] = {};
+    bool alive = false;
 };
 
 int bits_for(long long v)
@@ -78,6 +91,9 @@ struct pk_world
     int steps = 0;
     bool shapes_dirty = false;
     bool order_dirty = false; // solver schedule needs recomputing (bodies added or removed)
+    std::vector<JointHost> joints; // every joint ever added (dead ones keep their index)
+    std::vector<int> joint_order;  // joints as last uploaded, in (world, type, arena slot) order
+    bool joints_dirty = false;
     pk::EventDispatcher waiters; // collision / separation / destruction waiters (pk_world_wait)
     std::vector<pk::Wake> wakes; // fired, not yet returned by pk_world_dispatch
     size_t wake_head = 0;
@@ -402,6 +418,63 @@ static int flush_order(pk_world *w)
     return PK_OK;
 }
 
+// Joints go to the device in the reference's solve order: per world, constraint types in order,
+// arena slots in order (constraint.h:1109-1119). Accumulated impulses carry over.
+static int flush_joints(pk_world *w)
+{
+    if (!w->joints_dirty) return PK_OK;
+    const size_t nup = w->joint_order.size();
+    if (nup > 0)
+    {
+        std::vector<double> acc(nup * 6);
+        if (w->eng->read_joint_acc(acc.data(), int(nup))) return PK_ERR_CUDA;
+        for (size_t i = 0; i < nup; ++i)
+            for (int k = 0; k < 6; ++k) w->joints[size_t(w->joint_order[i])].acc[k] = acc[i * 6 + size_t(k)];
+    }
+    const int nw = w->cfg.max_worlds;
+    std::vector<int> order, js(size_t(nw), 0), je(size_t(nw), 0);
+    for (int wi = 0; wi < nw; ++wi)
+    {
+        const SubWorld &sw = w->worlds[size_t(wi)];
+        js[size_t(wi)] = int(order.size());
+        for (int t = 0; t < 6; ++t)
+            for (int j : sw.jslot[t])
+                if (j >= 0 && w->joints[size_t(j)].alive) order.push_back(j);
+        je[size_t(wi)] = int(order.size());
+    }
+    const size_t n = order.size();
+    std::vector<int> ints(n * 5);
+    std::vector<double> params(n * 25), acc(n * 6);
+    for (size_t i = 0; i < n; ++i)
+    {
+        const JointHost &j = w->joints[size_t(order[i])];
+        const int v[5] = {j.type, j.slot_a, j.slot_b, j.local_a, j.local_b};
+        for (int k = 0; k < 5; ++k) ints[i * 5 + size_t(k)] = v[k];
+        for (int k = 0; k < 25; ++k) params[i * 25 + size_t(k)] = j.p[k];
+        for (int k = 0; k < 6; ++k) acc[i * 6 + size_t(k)] = j.acc[k];
+    }
+    if (w->eng->set_joints(ints.data(), params.data(), acc.data(), int(n), js.data(), je.data()))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    w->joint_order = order;
+    w->joints_dirty = false;
+    return PK_OK;
+}
+
+static void drop_joint(pk_world *w, int j)
+{
+    JointHost &jh = w->joints[size_t(j)];
+    if (!jh.alive) return;
+    SubWorld &sw = w->worlds[size_t(jh.world)];
+    jh.alive = false;
+    sw.jslot[jh.type][size_t(jh.arena)] = -1;
+    sw.jgen[jh.type][size_t(jh.arena)]++;
+    sw.jfree[jh.type].push_back(jh.arena);
+    w->joints_dirty = true;
+}
+
 static int flush_shapes(pk_world *w)
 {
     if (!w->shapes_dirty) return PK_OK;
@@ -581,6 +654,8 @@ static int kill_slot(pk_world *w, int slot)
     SlotInfo &si = w->slots[size_t(slot)];
     SubWorld &sw = w->worlds[size_t(si.world)];
     w->waiters.destroyed(uint64_t(uint32_t(slot)) | (uint64_t(si.gen) << 32), w->wakes);
+    for (size_t j = 0; j < w->joints.size(); ++j) // joints cannot outlive their bodies
+        if (w->joints[j].alive && (w->joints[j].slot_a == slot || w->joints[j].slot_b == slot)) drop_joint(w, int(j));
     si.alive = false;
     sw.local_alive[size_t(si.local)] = 0;
     sw.local_gen[size_t(si.local)]++;
@@ -619,6 +694,14 @@ int pk_world_clear(pk_world *w, int32_t world)
         }
         w->slots[size_t(slot)] = SlotInfo{};
         w->free_slots.push_back(slot);
+    }
+    for (size_t j = 0; j < w->joints.size(); ++j)
+        if (w->joints[j].alive && w->joints[j].world == world) drop_joint(w, int(j));
+    for (int t = 0; t < 6; ++t)
+    {
+        sw.jslot[t].clear();
+        sw.jgen[t].clear();
+        sw.jfree[t].clear();
     }
     // one kernel kills the bodies, one empties every cached manifold of the world
     if (w->eng->kill_world(dead.data(), int(dead.size()), world))
@@ -672,6 +755,7 @@ int pk_world_step_async(pk_world *w, double dt)
     if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
     if (int frc = flush_shapes(w)) return frc;
     if (int orc = flush_order(w)) return orc;
+    if (int jrc = flush_joints(w)) return jrc;
     int rc = w->eng->step(dt);
     if (rc)
     {
@@ -720,6 +804,7 @@ int pk_world_capture(pk_world *w, double dt)
     if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
     if (int rc = flush_shapes(w)) return rc;
     if (int orc = flush_order(w)) return orc;
+    if (int jrc = flush_joints(w)) return jrc;
     if (w->eng->capture_graph(dt))
     {
         g_last_cuda = w->eng->last_error();
@@ -795,6 +880,7 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
     if (!w || !(dt > 0.0) || steps_per_candidate < 1) return PK_ERR_INVALID;
     if (int rc = flush_shapes(w)) return rc;
     if (int rc = flush_order(w)) return rc;
+    if (int jrc = flush_joints(w)) return jrc;
     const int k = steps_per_candidate;
     int used = 0;
     double st[pk::kStages];
@@ -996,6 +1082,158 @@ int pk_world_read_events(pk_world *w, uint64_t *keys, int32_t *worlds, int32_t *
         split_key(w, raw[size_t(i)], keys ? keys + i : nullptr, worlds ? worlds + i : nullptr);
         if (kinds) kinds[i] = kd[size_t(i)];
     }
+    return PK_OK;
+}
+
+void pk_joint_desc_init(pk_joint_desc *d)
+{
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+}
+
+// The constructors of the joint types (constraint.h:183-187, 298-305, 386-392, 494-500, 635-652,
+// 779-785), from the bodies' current poses.
+int pk_joint_add(pk_world *w, const pk_joint_desc *d, uint64_t *out)
+{
+    using V = pk::V3<double>;
+    using Q = pk::Qt<double>;
+    if (!w || !d || d->type < PK_JOINT_DISTANCE || d->type > PK_JOINT_SPRING) return PK_ERR_INVALID;
+    int sa, sb;
+    SlotInfo *ia = resolve(w, d->a, &sa), *ib = resolve(w, d->b, &sb);
+    if (!ia || !ib) return PK_ERR_STALE_HANDLE;
+    if (ia->world != ib->world || sa == sb) return PK_ERR_INVALID;
+    double pa[7], pb[7];
+    if (w->eng->read_pose(sa, pa) || w->eng->read_pose(sb, pb)) return PK_ERR_CUDA;
+    const V xa{pa[0], pa[1], pa[2]}, xb{pb[0], pb[1], pb[2]};
+    const Q qa{pa[3], pa[4], pa[5], pa[6]}, qb{pb[3], pb[4], pb[5], pb[6]};
+    auto vec = [](const double *v) { return V{v[0], v[1], v[2]}; };
+    auto basis = [](V n, V &t1, V &t2) { // build_orthonormal_basis (constraint.h:104-113)
+        double sign = std::copysign(1.0, n.z);
+        double a = -1.0 / (sign + n.z);
+        double b = n.x * n.y * a;
+        t1 = V{1.0 + sign * n.x * n.x * a, sign * b, -sign * n.x};
+        t2 = V{b, sign + n.y * n.y * a, -n.y};
+    };
+    JointHost j;
+    j.type = d->type;
+    j.world = ia->world;
+    j.slot_a = sa;
+    j.slot_b = sb;
+    j.local_a = ia->local;
+    j.local_b = ib->local;
+    j.alive = true;
+    V la{0, 0, 0}, lb{0, 0, 0}, axa{0, 0, 0}, axb{0, 0, 0}, va{0, 0, 0}, wa{0, 0, 0};
+    Q qrel{1, 0, 0, 0};
+    const V anchor = vec(d->anchor);
+    switch (d->type)
+    {
+    case PK_JOINT_DISTANCE:
+    case PK_JOINT_SPRING:
+        la = vec(d->local_a);
+        lb = vec(d->local_b);
+        break;
+    case PK_JOINT_BALL_SOCKET:
+    case PK_JOINT_WELD:
+        la = pk::rotate(pk::conj(qa), anchor - xa); // project_to_local (particle.h:107-108)
+        lb = pk::rotate(pk::conj(qb), anchor - xb);
+        qrel = pk::qmul(pk::conj(qa), qb);
+        break;
+    case PK_JOINT_HINGE:
+        la = vec(d->local_a);
+        lb = vec(d->local_b);
+        axa = pk::normalized(vec(d->axis_a));
+        axb = pk::normalized(vec(d->axis_b));
+        basis(axa, va, wa);
+        break;
+    case PK_JOINT_SLIDER: {
+        la = pk::rotate(pk::conj(qa), anchor - xa);
+        lb = pk::rotate(pk::conj(qb), anchor - xb);
+        V n = pk::normalized(vec(d->axis_a));
+        axa = pk::rotate(pk::conj(qa), n);
+        V t1, t2;
+        basis(n, t1, t2);
+        va = pk::rotate(pk::conj(qa), t1);
+        wa = pk::rotate(pk::conj(qa), t2);
+        qrel = pk::qmul(pk::conj(qa), qb);
+        break;
+    }
+    default:
+        return PK_ERR_INVALID;
+    }
+    const V vs[6] = {la, lb, axa, axb, va, wa};
+    for (int k = 0; k < 6; ++k)
+    {
+        j.p[3 * k + 0] = vs[k].x;
+        j.p[3 * k + 1] = vs[k].y;
+        j.p[3 * k + 2] = vs[k].z;
+    }
+    j.p[18] = qrel.w;
+    j.p[19] = qrel.x;
+    j.p[20] = qrel.y;
+    j.p[21] = qrel.z;
+    j.p[22] = d->distance;
+    j.p[23] = d->stiffness;
+    j.p[24] = d->damping;
+    SubWorld &sw = w->worlds[size_t(j.world)];
+    const int t = d->type;
+    int idx;
+    if (sw.jfree[t].empty())
+    {
+        idx = int(sw.jslot[t].size());
+        sw.jslot[t].push_back(-1);
+        sw.jgen[t].push_back(0);
+    }
+    else
+    {
+        idx = sw.jfree[t].back();
+        sw.jfree[t].pop_back();
+    }
+    j.arena = idx;
+    sw.jslot[t][size_t(idx)] = int(w->joints.size());
+    w->joints.push_back(j);
+    w->joints_dirty = true;
+    if (out)
+        *out = uint64_t(uint32_t(idx) & 0xFFFFFFu) | (uint64_t(sw.jgen[t][size_t(idx)] & 0xFFFFu) << 24) |
+               (uint64_t(uint32_t(j.world) & 0xFFFFFu) << 40) | (uint64_t(t) << 60);
+    return PK_OK;
+}
+
+static int resolve_joint(pk_world *w, uint64_t h)
+{
+    const int t = int(h >> 60), world = int((h >> 40) & 0xFFFFFu), idx = int(h & 0xFFFFFFu);
+    const uint32_t gen = uint32_t((h >> 24) & 0xFFFFu);
+    if (t > PK_JOINT_SPRING || world >= w->cfg.max_worlds) return -1;
+    const SubWorld &sw = w->worlds[size_t(world)];
+    if (size_t(idx) >= sw.jslot[t].size() || (sw.jgen[t][size_t(idx)] & 0xFFFFu) != gen) return -1;
+    return sw.jslot[t][size_t(idx)];
+}
+
+int pk_joint_remove(pk_world *w, uint64_t h)
+{
+    if (!w) return PK_ERR_INVALID;
+    const int j = resolve_joint(w, h);
+    if (j < 0) return PK_ERR_STALE_HANDLE;
+    if (int rc = flush_joints(w)) return rc; // keep the other joints' impulses
+    drop_joint(w, j);
+    return PK_OK;
+}
+
+int pk_joint_read_impulses(pk_world *w, uint64_t h, double *out6, int32_t *nrows)
+{
+    if (!w || !out6) return PK_ERR_INVALID;
+    const int j = resolve_joint(w, h);
+    if (j < 0) return PK_ERR_STALE_HANDLE;
+    static const int rows[6] = {1, 3, 5, 5, 6, 1};
+    const JointHost &jh = w->joints[size_t(j)];
+    for (int k = 0; k < 6; ++k) out6[k] = jh.acc[k];
+    for (size_t i = 0; i < w->joint_order.size(); ++i)
+        if (w->joint_order[i] == j && !w->joints_dirty)
+        {
+            std::vector<double> acc(w->joint_order.size() * 6);
+            if (w->eng->read_joint_acc(acc.data(), int(w->joint_order.size()))) return PK_ERR_CUDA;
+            for (int k = 0; k < 6; ++k) out6[k] = acc[i * 6 + size_t(k)];
+        }
+    if (nrows) *nrows = rows[jh.type];
     return PK_OK;
 }
 

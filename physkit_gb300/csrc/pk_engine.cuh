@@ -120,6 +120,26 @@ template <> struct RowSel<float>
     using type = RowF;
 };
 template <class T> using RowT = typename RowSel<T>::type;
+
+// Joints (constraint.h:139-865): type as constraint_type (0 distance, 1 ball_socket, 2 hinge,
+// 3 slider, 4 weld, 5 spring); bodies as device slots and world-local indices; the parameters
+// fixed at creation.
+template <class T> struct JointDev
+{
+    int type, a, b, local_a, local_b, pad[3];
+    T la[3], lb[3]; // local anchors
+    T axa[3], axb[3]; // hinge: local axes; slider: local axis of a
+    T va[3], wa[3];   // hinge: basis of axa; slider: local tangents of a
+    T qrel[4];        // slider, weld: conj(q_a) q_b at creation
+    T distance, stiffness, damping;
+};
+// One joint row (jacobian_row, constraint.h:29-88); the clamp bounds are -+DBL_MAX for all joints.
+template <class T> struct JRow
+{
+    T Jv[3], Jwa[3], Jwb[3];
+    T meff, bias, gamma;
+};
+constexpr int kJointMaxRows = 6;
 template <class T> struct WorldParams
 {
     T g[3];
@@ -199,6 +219,13 @@ template <class T> struct Dev
     double *racc;          // 12 per pair: accumulated impulses (normal, t1, t2) of the 4 rows
     float *raccf;          // FP32 form: running totals in FP32 (clamp decisions, warm start)
     float *rdel;           // FP32 form: this step's change, added to racc once after the sweeps
+    const JointDev<T> *joints; // ordered by (world, type, arena slot)
+    JRow<T> *jrows;        // kJointMaxRows per joint, built every step
+    int *jnrows;           // rows built for each joint this step
+    double *jacc;          // kJointMaxRows accumulated impulses per joint (kept across steps)
+    int *jstart;           // each world's joint range
+    int *jend;
+    const int *njoints;
     uint8_t *rowmask;
     int *colour;      // solver scratch: compacted active manifolds of each world
     int *colour_tmp;  // solver scratch: colour of each compacted manifold
@@ -1199,6 +1226,218 @@ template <class T> __device__ __forceinline__ void warm_contact(SBody<T> &A, SBo
     if (acc[2] != 0.0) apply_reg(A, B, ld3(r.t2), ld3(r.wa_t2), ld3(r.wb_t2), T(acc[2]));
 }
 
+// Rows of every joint from the bodies' current poses (build_jacobian_impl of each type,
+// constraint.h:187-231, 309-352, 407-446, 512-580, 654-738, 789-855), in the oracle's order of
+// operations.
+template <class T> __global__ void k_joint_setup(Dev<T> d, T dt)
+{
+    const int nj = *d.njoints;
+    PK_GRID_STRIDE(j, nj)
+    {
+        const JointDev<T> jd = d.joints[j];
+        const int sa = jd.a, sb = jd.b;
+        const Pose<T> &PA = d.pose[sa];
+        const Pose<T> &PB = d.pose[sb];
+        const Qt<T> qa = ldq(PA.q), qb = ldq(PB.q);
+        const V3<T> xa = ld3(PA.p), xb = ld3(PB.p);
+        const T *Ia = d.iwinv + 9 * sa;
+        const T *Ib = d.iwinv + 9 * sb;
+        const T ima = d.prm[sa].inv_mass, imb = d.prm[sb].inv_mass;
+        const V3<T> r_a = rotate(qa, ld3(jd.la)), r_b = rotate(qb, ld3(jd.lb));
+        const V3<T> delta = (xa + r_a) - (xb + r_b);
+        JRow<T> *out = d.jrows + size_t(j) * kJointMaxRows;
+        int nr = 0;
+        auto linear = [&](V3<T> n, V3<T> arm_a, T bias_factor, bool slider) {
+            JRow<T> r;
+            V3<T> Jwa = cross(arm_a, n), Jwb = -cross(r_b, n);
+            V3<T> ka = matvec(Ia, Jwa), kb = matvec(Ib, Jwb);
+            r.gamma = T(0);
+            if (slider)
+            {
+                T lin = ima + imb;
+                T ang = dot(Jwa, ka) + dot(Jwb, kb);
+                T reg = T(0.01) * ang;
+                r.gamma = reg;
+                r.meff = T(1) / (lin + ang + reg);
+                T e = dot(delta, n);
+                e = (e < T(-0.2)) ? T(-0.2) : ((T(0.2) < e) ? T(0.2) : e);
+                r.bias = (bias_factor / dt) * e;
+            }
+            else
+            {
+                r.meff = T(1) / (ima + imb + dot(Jwa, ka) + dot(Jwb, kb));
+                r.bias = (bias_factor / dt) * dot(delta, n);
+            }
+            st3(r.Jv, n);
+            st3(r.Jwa, Jwa);
+            st3(r.Jwb, Jwb);
+            out[nr++] = r;
+        };
+        auto angular = [&](V3<T> n, T bias_factor, V3<T> err) {
+            JRow<T> r;
+            V3<T> Jwa = n, Jwb = -n;
+            V3<T> ka = matvec(Ia, Jwa), kb = matvec(Ib, Jwb);
+            r.meff = T(1) / (dot(Jwa, ka) + dot(Jwb, kb));
+            r.bias = (bias_factor / dt) * dot(err, n);
+            r.gamma = T(0);
+            st3(r.Jv, V3<T>{T(0), T(0), T(0)});
+            st3(r.Jwa, Jwa);
+            st3(r.Jwb, Jwb);
+            out[nr++] = r;
+        };
+        auto rel_error = [&]() {
+            Qt<T> cur = qmul(conj(qa), qb);
+            Qt<T> e = qmul(ldq(jd.qrel), conj(cur));
+            if (e.w < T(0)) e = Qt<T>{-e.w, -e.x, -e.y, -e.z};
+            return rotate(qa, V3<T>{e.x, e.y, e.z} * T(2));
+        };
+        const V3<T> ex{T(1), T(0), T(0)}, ey{T(0), T(1), T(0)}, ez{T(0), T(0), T(1)};
+        switch (jd.type)
+        {
+        case 0:
+        case 5: {
+            T cur = norm(delta);
+            if (cur < T(1e-6)) break;
+            V3<T> u = delta / cur;
+            JRow<T> r;
+            V3<T> Jwa = cross(r_a, u), Jwb = -cross(r_b, u);
+            V3<T> ka = matvec(Ia, Jwa), kb = matvec(Ib, Jwb);
+            if (jd.type == 0)
+            {
+                r.meff = T(1) / (ima + imb + dot(Jwa, ka) + dot(Jwb, kb));
+                r.bias = (T(0.1) / dt) * (cur - jd.distance);
+                r.gamma = T(0);
+            }
+            else
+            {
+                T mc = ima + imb + dot(Jwa, ka) + dot(Jwb, kb);
+                T gamma = T(1) / (dt * (jd.damping + dt * jd.stiffness));
+                T beta = dt * jd.stiffness / (jd.damping + dt * jd.stiffness);
+                r.meff = T(1) / (mc + gamma);
+                r.bias = (beta / dt) * (cur - jd.distance);
+                r.gamma = gamma;
+            }
+            st3(r.Jv, u);
+            st3(r.Jwa, Jwa);
+            st3(r.Jwb, Jwb);
+            out[nr++] = r;
+            break;
+        }
+        case 1:
+            linear(ex, r_a, T(0.1), false);
+            linear(ey, r_a, T(0.1), false);
+            linear(ez, r_a, T(0.1), false);
+            break;
+        case 2: {
+            linear(ex, r_a, T(0.2), false);
+            linear(ey, r_a, T(0.2), false);
+            linear(ez, r_a, T(0.2), false);
+            V3<T> u_a = rotate(qa, ld3(jd.axa)), u_b = rotate(qb, ld3(jd.axb));
+            V3<T> err = -cross(u_a, u_b);
+            angular(rotate(qa, ld3(jd.va)), T(0.2), err);
+            angular(rotate(qa, ld3(jd.wa)), T(0.2), err);
+            break;
+        }
+        case 3: {
+            V3<T> axis_a = rotate(qa, ld3(jd.axa));
+            V3<T> t1 = rotate(qa, ld3(jd.va)), t2 = rotate(qa, ld3(jd.wa));
+            V3<T> lever = r_a - delta;
+            linear(t1, lever, T(0.1), true);
+            linear(t2, lever, T(0.1), true);
+            V3<T> err = rel_error();
+            angular(axis_a, T(0.1), err);
+            angular(t1, T(0.1), err);
+            angular(t2, T(0.1), err);
+            break;
+        }
+        case 4: {
+            linear(ex, r_a, T(0.1), false);
+            linear(ey, r_a, T(0.1), false);
+            linear(ez, r_a, T(0.1), false);
+            V3<T> err = rel_error();
+            angular(ex, T(0.1), err);
+            angular(ey, T(0.1), err);
+            angular(ez, T(0.1), err);
+            break;
+        }
+        default:
+            break;
+        }
+        d.jnrows[j] = nr;
+    }
+}
+
+// The joints [js, je) of one world, in order, by one thread: warm start, or one pass of
+// jacobian_row::apply (constraint.h:49-71) over their rows. Solved before the contacts of the same
+// pass, as the reference does (constraint.h:1121-1137).
+template <class T>
+__device__ __noinline__ void solve_joints(const Dev<T> &d, int js, int je, Vel<T> *cache, bool warm, bool coherent)
+{
+    for (int j = js; j < je; ++j)
+    {
+        const JointDev<T> &jd = d.joints[j];
+        const int nr = d.jnrows[j];
+        if (nr == 0) continue;
+        SBody<T> A, B;
+        const int sl[2] = {jd.a, jd.b}, lc[2] = {jd.local_a, jd.local_b};
+        SBody<T> *bs[2] = {&A, &B};
+        for (int k = 0; k < 2; ++k)
+        {
+            SBody<T> &bb = *bs[k];
+            const int s = sl[k];
+            bb.is_static = (d.meta[s].flags & BODY_STATIC) != 0;
+            Vel<T> ve;
+            if (cache && !bb.is_static)
+                ve = cache[lc[k]];
+            else if (coherent)
+            {
+                const T *src = reinterpret_cast<const T *>(d.vel + s);
+                for (int q = 0; q < 3; ++q)
+                {
+                    ve.v[q] = __ldcg(src + q);
+                    ve.w[q] = __ldcg(src + 3 + q);
+                }
+            }
+            else
+                ve = d.vel[s];
+            bb.v = ld3(ve.v);
+            bb.w = ld3(ve.w);
+            for (int q = 0; q < 9; ++q) bb.I[q] = d.iwinv[9 * s + q];
+            bb.inv_mass = d.prm[s].inv_mass;
+        }
+        for (int r = 0; r < nr; ++r)
+        {
+            const JRow<T> row = d.jrows[size_t(j) * kJointMaxRows + r];
+            double &acc = d.jacc[size_t(j) * kJointMaxRows + r];
+            if (warm)
+            {
+                if (acc != 0.0) apply_reg(A, B, ld3(row.Jv), ld3(row.Jwa), ld3(row.Jwb), T(acc));
+                continue;
+            }
+            T Jv = jv_reg(row.Jv, row.Jwa, row.Jwb, A, B);
+            T cfp = row.gamma * T(acc);
+            T lambda = -(Jv + row.bias + cfp) * row.meff;
+            double old = acc;
+            double v = old + double(lambda);
+            const double lo = -1.7976931348623157e308, hi = 1.7976931348623157e308;
+            acc = (v < lo) ? lo : ((hi < v) ? hi : v);
+            apply_reg(A, B, ld3(row.Jv), ld3(row.Jwa), ld3(row.Jwb), T(acc - old));
+        }
+        for (int k = 0; k < 2; ++k)
+        {
+            const SBody<T> &bb = *bs[k];
+            if (bb.is_static) continue;
+            Vel<T> ve;
+            st3(ve.v, bb.v);
+            st3(ve.w, bb.w);
+            if (cache)
+                cache[lc[k]] = ve;
+            else
+                d.vel[sl[k]] = ve;
+        }
+    }
+}
+
 // FP32 form: apply an impulse along one direction (J, with the rotation responses ka and kb).
 __device__ __forceinline__ void apply_f32(SBody<float> &A, SBody<float> &B, const float *J, const float *ka, const float *kb,
                                           float lam)
@@ -1557,8 +1796,9 @@ __global__ void __launch_bounds__(MAXT)
     const int w = d.world_order[blk];
     if (!d.wp[w].active || d.world_nlocal[w] > grid_world) return; // large worlds: k_solve_grid
     const int ms = d.mstart[w], me = d.mend[w];
+    const int js = d.jstart[w], je = d.jend[w];
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
-    if (me <= ms)
+    if (me <= ms && je <= js)
     {
         if (tid == 0) d.ncolours[w] = 0;
         return;
@@ -1691,6 +1931,12 @@ __global__ void __launch_bounds__(MAXT)
             if (!(r.y >> 31)) cache[r.w & 0xFFFFu] = d.vel[r.y];
             if (!(r.z >> 31)) cache[r.w >> 16] = d.vel[r.z];
         }
+        for (int j = js + tid; j < je; j += nt) // bodies of the world's joints
+        {
+            const JointDev<T> &jd = d.joints[j];
+            if (!(d.meta[jd.a].flags & BODY_STATIC)) cache[jd.local_a] = d.vel[jd.a];
+            if (!(d.meta[jd.b].flags & BODY_STATIC)) cache[jd.local_b] = d.vel[jd.b];
+        }
     }
     __syncthreads();
 
@@ -1700,6 +1946,11 @@ __global__ void __launch_bounds__(MAXT)
     if (ncol > 0 && tid < ccount[0]) cur = d.srec[ms + cstart[0] + tid];
     for (int it = -1; it < d.iterations; ++it)
     {
+        if (je > js)
+        {
+            if (tid == 0) solve_joints(d, js, je, cache, it < 0, false);
+            __syncthreads();
+        }
         for (int c = 0; c < ncol; ++c)
         {
             const int cs = ms + cstart[c], cn = ccount[c];
@@ -1718,6 +1969,12 @@ __global__ void __launch_bounds__(MAXT)
             const uint4 r = rec[k];
             if (!(r.y >> 31)) d.vel[r.y] = cache[r.w & 0xFFFFu];
             if (!(r.z >> 31)) d.vel[r.z] = cache[r.w >> 16];
+        }
+        for (int j = js + tid; j < je; j += nt)
+        {
+            const JointDev<T> &jd = d.joints[j];
+            if (!(d.meta[jd.a].flags & BODY_STATIC)) d.vel[jd.a] = cache[jd.local_a];
+            if (!(d.meta[jd.b].flags & BODY_STATIC)) d.vel[jd.b] = cache[jd.local_b];
         }
     }
     // 4. write the accumulated impulses back into the manifold cache
@@ -1753,8 +2010,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
     cg::grid_group grid = cg::this_grid();
     if (!d.wp[w].active) return;
     const int ms = d.mstart[w], me = d.mend[w];
+    const int js = d.jstart[w], je = d.jend[w];
     const int gtid = int(grid.thread_rank()), gn = int(grid.size());
-    if (me <= ms)
+    if (me <= ms && je <= js)
     {
         if (gtid == 0) d.ncolours[w] = 0;
         return;
@@ -1845,6 +2103,11 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
     grid.sync();
     for (int it = -1; it < d.iterations; ++it)
     {
+        if (je > js)
+        {
+            if (gtid == 0) solve_joints(d, js, je, (Vel<T> *)nullptr, it < 0, true);
+            grid.sync();
+        }
         for (int c = 0; c < ncol; ++c)
         {
             const int cs = ms + __ldcg(&g->cstart[c]), cn = __ldcg(&g->ccount[c]);

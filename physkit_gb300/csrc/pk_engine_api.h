@@ -84,6 +84,10 @@ public:
     virtual int read_colours(uint64_t *keys, int *colours, int cap, int *ncolours_world0) = 0;
     virtual int collide(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) = 0;
     // Same narrowphase launch on device buffers the caller provides; allocates nothing.
+    virtual int set_joints(const int *ints, const double *params, const double *acc, int n, const int *jstart,
+                           const int *jend) = 0;
+    virtual int read_joint_acc(double *acc, int n) = 0;
+    virtual int read_pose(int slot, double *out7) = 0;
     // rays: 8 doubles each (origin, direction, distance limit, world); per ray up to `cap` nearest
     // hits (device slot, distance) ordered by (distance, slot), and the total hit count
     virtual int raycast(const double *rays, int n, int cap, int *counts, int *slots, double *dists) = 0;

@@ -120,6 +120,11 @@ public:
         d.epa_count_heavy = counters_ + 9;
         d.np_iters = reinterpret_cast<unsigned long long *>(counters_ + 10); // counters 10..15
         d.nnew = counters_ + 16;
+        d.njoints = counters_ + 17; // zero until joints are set
+        PK_CUDA(alloc(&d.jstart, W));
+        PK_CUDA(alloc(&d.jend, W));
+        PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
+        PK_CUDA(cudaMemset(d.jend, 0, sizeof(int) * W));
         int minus1 = -1;
         PK_CUDA(cudaMemcpy(d.epoch, &minus1, sizeof(int), cudaMemcpyHostToDevice));
         PK_CUDA(alloc(&d.wp, W));
@@ -701,6 +706,90 @@ public:
         return 0;
     }
 
+    // Joints, ordered by (world, type, arena slot): 5 ints (type, slot a, slot b, local a, local b)
+    // and 25 doubles (la3 lb3 axa3 axb3 va3 wa3 qrel4 distance stiffness damping) each, their
+    // accumulated impulses (6 each) and every world's range. Growing the buffers drops a captured
+    // step graph (its kernels hold the old pointers).
+    int set_joints(const int *ints, const double *params, const double *acc, int n, const int *jstart,
+                   const int *jend) override
+    {
+        PK_CUDA(cudaStreamSynchronize(st_));
+        if (n > joint_cap_)
+        {
+            int cap = n < 64 ? 64 : n;
+            void *old[] = {const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc};
+            for (void *p : old)
+                if (p) cudaFree(p);
+            JointDev<T> *jd;
+            PK_CUDA(alloc(&jd, size_t(cap)));
+            d_.joints = jd;
+            PK_CUDA(alloc(&d_.jrows, size_t(cap) * kJointMaxRows));
+            PK_CUDA(alloc(&d_.jnrows, size_t(cap)));
+            PK_CUDA(alloc(&d_.jacc, size_t(cap) * kJointMaxRows));
+            PK_CUDA(cudaMemset(d_.jnrows, 0, sizeof(int) * size_t(cap)));
+            joint_cap_ = cap;
+            for (int k = 0; k < 2; ++k)
+            {
+                if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
+                graph_exec_[k] = nullptr;
+            }
+        }
+        std::vector<JointDev<T>> h(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i)
+        {
+            JointDev<T> &j = h[size_t(i)];
+            const int *ii = ints + 5 * size_t(i);
+            const double *p = params + 25 * size_t(i);
+            j.type = ii[0];
+            j.a = ii[1];
+            j.b = ii[2];
+            j.local_a = ii[3];
+            j.local_b = ii[4];
+            j.pad[0] = j.pad[1] = j.pad[2] = 0;
+            for (int k = 0; k < 3; ++k)
+            {
+                j.la[k] = T(p[k]);
+                j.lb[k] = T(p[3 + k]);
+                j.axa[k] = T(p[6 + k]);
+                j.axb[k] = T(p[9 + k]);
+                j.va[k] = T(p[12 + k]);
+                j.wa[k] = T(p[15 + k]);
+            }
+            for (int k = 0; k < 4; ++k) j.qrel[k] = T(p[18 + k]);
+            j.distance = T(p[22]);
+            j.stiffness = T(p[23]);
+            j.damping = T(p[24]);
+        }
+        if (n > 0)
+        {
+            PK_CUDA(cudaMemcpy(const_cast<JointDev<T> *>(d_.joints), h.data(), sizeof(JointDev<T>) * size_t(n),
+                               cudaMemcpyHostToDevice));
+            PK_CUDA(cudaMemcpy(d_.jacc, acc, sizeof(double) * kJointMaxRows * size_t(n), cudaMemcpyHostToDevice));
+        }
+        PK_CUDA(cudaMemcpy(d_.jstart, jstart, sizeof(int) * cfg_.max_worlds, cudaMemcpyHostToDevice));
+        PK_CUDA(cudaMemcpy(d_.jend, jend, sizeof(int) * cfg_.max_worlds, cudaMemcpyHostToDevice));
+        PK_CUDA(cudaMemcpy(counters_ + 17, &n, sizeof(int), cudaMemcpyHostToDevice));
+        njoints_ = n;
+        return 0;
+    }
+
+    int read_joint_acc(double *acc, int n) override
+    {
+        PK_CUDA(cudaStreamSynchronize(st_));
+        if (n > 0) PK_CUDA(cudaMemcpy(acc, d_.jacc, sizeof(double) * kJointMaxRows * size_t(n), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+
+    int read_pose(int slot, double *out7) override
+    {
+        Pose<T> p;
+        PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaMemcpy(&p, d_.pose + slot, sizeof(p), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 3; ++k) out7[k] = double(p.p[k]);
+        for (int k = 0; k < 4; ++k) out7[3 + k] = double(p.q[k]);
+        return 0;
+    }
+
     int collide_device(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) override
     {
         if (n <= 0) return 0;
@@ -731,6 +820,7 @@ private:
     T *clusters_ = nullptr;
     size_t clusters_cap_ = 0;
     cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+    int joint_cap_ = 0, njoints_ = 0;
     static constexpr size_t kMaxSolveSmem = 160 * 1024;
     Tunables tune_{};
     int big_worlds_ = 0;
@@ -809,7 +899,8 @@ private:
         for (int k = 0; k < 2; ++k)
             if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
         void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
-                      d_.wroot, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
+                      d_.wroot, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
+                      const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list,
                       d_.epa_list, d_.epa_simplex, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
@@ -877,6 +968,7 @@ private:
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
+        if (joint_cap_ > 0) k_joint_setup<T><<<grid(joint_cap_), 128, 0, st_>>>(d, dt);
         PK_CUDA(mark(7));
         for (int gw : grid_worlds_)
         {

@@ -64,6 +64,16 @@ class RayC(C.Structure):
                 ("world", C.c_int32), ("reserved", C.c_int32)]
 
 
+class JointDescC(C.Structure):
+    _fields_ = [("type", C.c_int32), ("reserved", C.c_int32), ("a", C.c_uint64), ("b", C.c_uint64),
+                ("anchor", C.c_double * 3), ("local_a", C.c_double * 3), ("local_b", C.c_double * 3),
+                ("axis_a", C.c_double * 3), ("axis_b", C.c_double * 3), ("distance", C.c_double),
+                ("stiffness", C.c_double), ("damping", C.c_double)]
+
+
+JOINT_TYPES = {"distance": 0, "ball_socket": 1, "hinge": 2, "slider": 3, "weld": 4, "spring": 5}
+
+
 class WakeC(C.Structure):
     _fields_ = [("waiter", C.c_uint64), ("object", C.c_uint64), ("other", C.c_uint64), ("kind", C.c_int32),
                 ("failed", C.c_int32)]
@@ -119,6 +129,9 @@ def lib():
             "pk_world_read_colours": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p, i32p]),
             "pk_world_raycast": (C.c_int, [vp, P(RayC), C.c_int32, C.c_int32, u64p, dp, i32p]),
             "pk_world_wait": (C.c_int, [vp, C.c_int32, C.c_uint64, C.c_uint64, u64p]),
+            "pk_joint_add": (C.c_int, [vp, P(JointDescC), u64p]),
+            "pk_joint_remove": (C.c_int, [vp, C.c_uint64]),
+            "pk_joint_read_impulses": (C.c_int, [vp, C.c_uint64, dp, i32p]),
             "pk_world_cancel_wait": (C.c_int, [vp, C.c_uint64]),
             "pk_world_dispatch": (C.c_int, [vp, P(WakeC), C.c_int32, i32p]),
             "pk_collide": (C.c_int, [vp, P(CollideShapeC), P(CollideShapeC), C.c_int32, dp, i32p]),
@@ -457,6 +470,33 @@ class World:
         s = np.ascontiguousarray(state13, dtype=np.float64)
         _check(self.L.pk_world_write_body(self.h, C.c_uint64(int(handle)), _ptr(s, C.c_double)),
                "pk_world_write_body")
+
+    # joints ------------------------------------------------------------------------------------
+    def add_joint(self, kind, a, b, anchor=(0, 0, 0), local_a=(0, 0, 0), local_b=(0, 0, 0), axis_a=(0, 0, 0),
+                  axis_b=(0, 0, 0), distance=0.0, stiffness=0.0, damping=0.0):
+        """A joint between bodies a and b (constraint.h:139-865); returns its handle."""
+        d = JointDescC()
+        d.type = JOINT_TYPES[kind]
+        d.a, d.b = int(a), int(b)
+        d.anchor[:] = list(map(float, anchor))
+        d.local_a[:] = list(map(float, local_a))
+        d.local_b[:] = list(map(float, local_b))
+        d.axis_a[:] = list(map(float, axis_a))
+        d.axis_b[:] = list(map(float, axis_b))
+        d.distance, d.stiffness, d.damping = float(distance), float(stiffness), float(damping)
+        out = C.c_uint64()
+        _check(self.L.pk_joint_add(self.h, C.byref(d), C.byref(out)), "pk_joint_add")
+        return out.value
+
+    def remove_joint(self, handle):
+        _check(self.L.pk_joint_remove(self.h, int(handle)), "pk_joint_remove")
+
+    def joint_impulses(self, handle):
+        out = np.zeros(6)
+        n = C.c_int32()
+        _check(self.L.pk_joint_read_impulses(self.h, int(handle), _ptr(out, C.c_double), C.byref(n)),
+               "pk_joint_read_impulses")
+        return out[:n.value]
 
     # waiting on collision events ---------------------------------------------------------------
     def wait(self, kind, obj, with_=None):

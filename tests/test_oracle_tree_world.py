@@ -186,3 +186,43 @@ def test_world_raycast_bruteforce_and_merge_order(seed):
         for h, t in got:
             assert t == want[h]
         assert len(got) == len(want)  # no body twice
+
+
+def _joint_world():
+    ow = pyoracle.OracleWorld(gravity=(0, -9.81, 0))
+    box = ow.box(0.2, 0.2, 0.2)
+    anchor = ow.add(box, (0, 5, 0), static=True)
+    return ow, box, anchor
+
+
+def test_oracle_ball_socket_pendulum_keeps_the_anchor():
+    # ball_socket_constraint (constraint.h:368-453): the shared anchor point stays together
+    ow, box, anchor = _joint_world()
+    bob = ow.add(box, (1.0, 5.0, 0.0), mass=1.0, inertia=(0.03, 0.03, 0.03))
+    h = ow.add_joint("ball_socket", anchor, bob, anchor=(0.0, 5.0, 0.0))
+    for _ in range(240):
+        ow.step(1 / 120)
+    st = ow.bodies()[int(bob) & 0xFFFFFFFF]
+    assert st[1] < 5.0  # it swung down
+    assert abs(np.linalg.norm(st[0:3] - np.array([0.0, 5.0, 0.0])) - 1.0) < 0.05  # ~1 m from the anchor
+    assert len(ow.joint_impulses(h)) == 3 and np.any(ow.joint_impulses(h) != 0)
+
+
+def test_oracle_joint_types_stay_finite_and_hold():
+    ow, box, anchor = _joint_world()
+    bodies = [ow.add(box, (x, 5.0 - 0.6, 0.0), mass=1.0, inertia=(0.03, 0.03, 0.03)) for x in (-3, -1.5, 0, 1.5, 3, 4.5)]
+    hs = [ow.add_joint("distance", anchor, bodies[0], local_a=(0, 0, 0), local_b=(0, 0.2, 0), distance=1.0),
+          ow.add_joint("hinge", anchor, bodies[1], local_a=(0, 0, 0), local_b=(0, 0.6, 0), axis_a=(0, 0, 1), axis_b=(0, 0, 1)),
+          ow.add_joint("slider", anchor, bodies[2], anchor=(0, 4.4, 0), axis_a=(0, 1, 0)),
+          ow.add_joint("weld", anchor, bodies[3], anchor=(1.5, 5.0, 0)),
+          ow.add_joint("spring", anchor, bodies[4], local_b=(0, 0.2, 0), distance=1.0, stiffness=50.0, damping=1.0),
+          ow.add_joint("ball_socket", bodies[4], bodies[5], anchor=(3.75, 4.4, 0))]
+    for _ in range(120):
+        ow.step(1 / 120)
+    st = ow.bodies()
+    assert np.isfinite(st[:, :13]).all()
+    w = st[int(bodies[3]) & 0xFFFFFFFF]
+    assert np.linalg.norm(w[0:3] - np.array([1.5, 4.4, 0.0])) < 0.05  # the weld holds the box in place
+    assert [len(ow.joint_impulses(h)) for h in hs] == [1, 5, 5, 6, 1, 3]
+    assert ow.remove_joint(hs[0]) and not ow.remove_joint(hs[0])
+    ow.step(1 / 120)
