@@ -1780,7 +1780,7 @@ template <class T> __device__ __forceinline__ void solve_manifold_rec(const Dev<
 
 // MAXT: the largest CTA the instance is compiled for (256, or 512 for the FP32 form's large worlds;
 // the 512 instance gives up registers for threads).
-template <class T, int MAXT>
+template <class T, int MAXT, bool JOINTS>
 __global__ void __launch_bounds__(MAXT)
     k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies, int grid_world)
 {
@@ -1796,7 +1796,7 @@ __global__ void __launch_bounds__(MAXT)
     const int w = d.world_order[blk];
     if (!d.wp[w].active || d.world_nlocal[w] > grid_world) return; // large worlds: k_solve_grid
     const int ms = d.mstart[w], me = d.mend[w];
-    const int js = d.jstart[w], je = d.jend[w];
+    const int js = JOINTS ? d.jstart[w] : 0, je = JOINTS ? d.jend[w] : 0; // instance without joints
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     if (me <= ms && je <= js)
     {
@@ -1931,7 +1931,7 @@ __global__ void __launch_bounds__(MAXT)
             if (!(r.y >> 31)) cache[r.w & 0xFFFFu] = d.vel[r.y];
             if (!(r.z >> 31)) cache[r.w >> 16] = d.vel[r.z];
         }
-        for (int j = js + tid; j < je; j += nt) // bodies of the world's joints
+        for (int j = js + tid; JOINTS && j < je; j += nt) // bodies of the world's joints
         {
             const JointDev<T> &jd = d.joints[j];
             if (!(d.meta[jd.a].flags & BODY_STATIC)) cache[jd.local_a] = d.vel[jd.a];
@@ -1946,7 +1946,7 @@ __global__ void __launch_bounds__(MAXT)
     if (ncol > 0 && tid < ccount[0]) cur = d.srec[ms + cstart[0] + tid];
     for (int it = -1; it < d.iterations; ++it)
     {
-        if (je > js)
+        if (JOINTS && je > js)
         {
             if (tid == 0) solve_joints(d, js, je, cache, it < 0, false);
             __syncthreads();
@@ -1970,7 +1970,7 @@ __global__ void __launch_bounds__(MAXT)
             if (!(r.y >> 31)) d.vel[r.y] = cache[r.w & 0xFFFFu];
             if (!(r.z >> 31)) d.vel[r.z] = cache[r.w >> 16];
         }
-        for (int j = js + tid; j < je; j += nt)
+        for (int j = js + tid; JOINTS && j < je; j += nt)
         {
             const JointDev<T> &jd = d.joints[j];
             if (!(d.meta[jd.a].flags & BODY_STATIC)) d.vel[jd.a] = cache[jd.local_a];

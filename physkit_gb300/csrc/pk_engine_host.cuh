@@ -152,9 +152,13 @@ public:
             d.world_order = wo;
             d.world_nlocal = wn;
         }
-        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
-        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, solve_max_threads<T>()>,
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(kMaxSolveSmem)));
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, solve_max_threads<T>(), false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
+        PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, solve_max_threads<T>(), true>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
         {
             int per_sm = 0;
@@ -879,13 +883,19 @@ private:
         return cudaMalloc(const_cast<void **>(reinterpret_cast<const void **>(p)), sizeof(U) * n);
     }
     static int solve_threads(int t) { return t < solve_max_threads<T>() ? t : solve_max_threads<T>(); }
+    // The joint-free instances serve batches that never had joints (buffers unallocated).
     void launch_solve(int blocks, int threads, size_t smem, const Dev<T> &d, const uint64_t *pv, int first, int cache)
     {
         threads = solve_threads(threads);
-        if (threads > 256)
-            k_solve_world<T, solve_max_threads<T>()><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+        const bool joints = joint_cap_ > 0;
+        if (threads > 256 && joints)
+            k_solve_world<T, solve_max_threads<T>(), true><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+        else if (threads > 256)
+            k_solve_world<T, solve_max_threads<T>(), false><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+        else if (joints)
+            k_solve_world<T, 256, true><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
         else
-            k_solve_world<T, 256><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+            k_solve_world<T, 256, false><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
     }
     int grid(int n) const
     {
