@@ -80,10 +80,11 @@ template <class T> struct Contact
     T n[3], la[3], lb[3], depth;
     double imp[3];
 };
-template <class T> struct Manifold
+template <class T> struct alignas(32) Manifold // header in one 32-byte sector
 {
     int n;
     int pad;
+    T sep[3]; // a direction that separated the pair when it was last found apart (zero: none)
     Contact<T> c[4];
 };
 template <class T> struct Row
@@ -210,11 +211,16 @@ template <class T> struct Dev
     int *gjk_list;
     int *gjk_count;        // light items
     int *gjk_count_heavy;
+    int *gjk_list2;        // the items the separating-direction check left for GJK, same two classes
+    int *gjk2_count;
+    int *gjk2_count_heavy;
     int *epa_list;
     Simplex<T> *epa_simplex;
     int *epa_count;
     int *epa_count_heavy;
     unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
+    int *clist;            // pairs of active worlds whose new manifold holds contacts (any order)
+    int *ccount;
     RowT<T> *rows;         // 4 per pair, read-only while the solver sweeps
     double *racc;          // 12 per pair: accumulated impulses (normal, t1, t2) of the 4 rows
     float *raccf;          // FP32 form: running totals in FP32 (clamp decisions, warm start)
@@ -315,6 +321,9 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.epa_count = 0;
         *d.gjk_count_heavy = 0;
         *d.epa_count_heavy = 0;
+        *d.gjk2_count = 0;
+        *d.gjk2_count_heavy = 0;
+        *d.ccount = 0;
         d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
         *d.epoch += 1;
     }
@@ -567,13 +576,15 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
         Aabb<T> qb = d.tbox[i];
         float qmn[3] = {down_f(qb.mn.x), down_f(qb.mn.y), down_f(qb.mn.z)};
         float qmx[3] = {up_f(qb.mx.x), up_f(qb.mx.y), up_f(qb.mx.z)};
+        // the node being visited stays in a register: a visit descends into one child it overlaps
+        // and pushes the other, and pops only when neither child is an internal node to visit
         int stack[96];
         int sp = 0;
-        stack[sp++] = root;
-        while (sp > 0)
+        int node = root;
+        while (node >= 0)
         {
-            int node = stack[--sp];
             const float4 *nd = d.nodes + 4 * node;
+            int next = -1;
 #pragma unroll
             for (int c = 0; c < 2; ++c)
             {
@@ -609,11 +620,14 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
                     else
                         atomicOr(d.status, ST_PAIR_OVERFLOW);
                 }
+                else if (next < 0)
+                    next = int(ch);
                 else if (sp < 96)
                     stack[sp++] = int(ch);
                 else
                     atomicOr(d.status, ST_TRAVERSAL_STACK);
             }
+            node = next >= 0 ? next : (sp > 0 ? stack[--sp] : -1);
         }
     }
 }
@@ -811,7 +825,7 @@ template <class T> __device__ __forceinline__ void add_contact(Manifold<T> &m, c
 // (collision_phases.h:261-318).
 template <class T>
 __device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const ShapeRef<T> &A, const ShapeRef<T> &B,
-                                bool hit, const Collision<T> &col)
+                                bool hit, const Collision<T> &col, V3<T> sep = V3<T>{T(0), T(0), T(0)})
 {
     const T d2eps = T(0.005 * 0.005), breaking = T(0.05), drift2_eps = T(0.06);
     // only the contacts in use are read and written: most pairs have an empty manifold
@@ -876,7 +890,9 @@ __device__ void manifold_update(const Dev<T> &d, int p, int old_idx, const Shape
     Manifold<T> *dst = d.man_new + p;
     dst->n = nm.n;
     dst->pad = 0;
+    st3(dst->sep, sep);
     for (int k = 0; k < nm.n; ++k) dst->c[k] = nm.c[k];
+    if (nm.n > 0) d.clist[warp_push(d.ccount)] = p; // contact rows are built for these pairs only
 }
 
 // Separating-axis test of the two bodies' oriented local AABBs (15 axes). True only when some axis
@@ -928,7 +944,7 @@ __device__ __forceinline__ bool obb_separated(const Aabb<T> &la, Qt<T> qa, V3<T>
 // their oriented local boxes are apart by more than a rounding margin: the shapes are then
 // disjoint, and the reference's GJK returns no collision for them (collision.cpp:181-182).
 template <class T>
-__global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
+__global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t *__restrict__ skey, const uint64_t *__restrict__ sval)
 {
     const int np = *d.npairs;
     PK_GRID_STRIDE(p, np)
@@ -937,10 +953,16 @@ __global__ void __launch_bounds__(256) k_narrow_pre(Dev<T> d, const uint64_t *__
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         int world = int(key >> (2 * d.lbits));
+        d.rowmask[p] = 0; // no contact rows unless the contact setup builds some
         if (!d.wp[world].active)
         {
             // kept pair of a world that sits out this step: unchanged, no event
-            d.man_new[p] = d.man_old[d.old_idx[p]];
+            const Manifold<T> &src = d.man_old[d.old_idx[p]];
+            Manifold<T> &dst = d.man_new[p];
+            dst.n = src.n;
+            dst.pad = 0;
+            for (int k = 0; k < 3; ++k) dst.sep[k] = src.sep[k];
+            for (int k = 0; k < src.n; ++k) dst.c[k] = src.c[k];
             d.event[p] = 0;
             continue;
         }
@@ -986,19 +1008,65 @@ __device__ __forceinline__ int list_slot(int i, int nheavy, int cap)
 #define PK_EPA_MIN_BLOCKS 4
 #endif
 
+// Narrowphase pass 2a: last step's separating direction. If A - B still lies short of the origin
+// along it by more than a rounding margin, the shapes are disjoint and GJK returns no collision
+// (collision.cpp:181-182), so the pair is settled with one support query per shape; the others go
+// on to GJK. A separate pass keeps the GJK warps on pairs that all run the full iteration.
 template <class T>
-__global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
+__global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.gjk_count_heavy;
     const int n = nh + *d.gjk_count;
     PK_GRID_STRIDE(i, n)
     {
-        int p = d.gjk_list[list_slot(i, nh, d.pair_cap)];
+        const int p = d.gjk_list[list_slot(i, nh, d.pair_cap)];
+        const int oi = d.old_idx[p];
+        bool settled = false;
+        if (oi >= 0)
+        {
+            const V3<T> ax = ld3(d.man_old[oi].sep);
+            if (sqnorm(ax) > T(0))
+            {
+                const uint64_t val = sval[p];
+                const int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+                const ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+                const T rs = A.rmax + B.rmax;
+                const T margin = (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6) + T(1e-5) * rs;
+                const SupPt<T> sp = minkowski(A, B, ax);
+                if (dot(sp.p, ax) < -margin)
+                {
+                    Collision<T> none;
+                    manifold_update(d, p, oi, A, B, false, none, ax);
+                    settled = true;
+                }
+            }
+        }
+        if (!settled)
+        {
+            if (i < nh)
+                d.gjk_list2[d.pair_cap - 1 - warp_push(d.gjk2_count_heavy)] = p;
+            else
+                d.gjk_list2[warp_push(d.gjk2_count)] = p;
+        }
+    }
+}
+
+// Narrowphase pass 2b: GJK (collision.cpp:165-189) over the remaining pairs; enclosing simplices are
+// queued for EPA, the rest are settled without a new contact and keep GJK's separating direction.
+template <class T>
+__global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int nh = *d.gjk2_count_heavy;
+    const int n = nh + *d.gjk2_count;
+    PK_GRID_STRIDE(i, n)
+    {
+        int p = d.gjk_list2[list_slot(i, nh, d.pair_cap)];
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         Simplex<T> s;
-        bool enclosed = gjk(A, B, s);
+        V3<T> sep{T(0), T(0), T(0)};
+        bool enclosed = gjk(A, B, s, &sep);
         atomicAdd(d.np_iters, (unsigned long long)s.iters);
         if (enclosed)
         {
@@ -1013,7 +1081,7 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
         else
         {
             Collision<T> none;
-            manifold_update(d, p, d.old_idx[p], A, B, false, none);
+            manifold_update(d, p, d.old_idx[p], A, B, false, none, sep);
         }
     }
 }
@@ -1048,25 +1116,17 @@ __global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa(Dev<T> d,
 template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__restrict__ skey,
                                                    const uint64_t *__restrict__ sval, T dt)
 {
-    const int np = *d.npairs;
-    PK_GRID_STRIDE(p, np)
+    // the pairs of active worlds with contacts, queued by the manifold update; every other pair
+    // was given no rows (rowmask 0, colour -2) by the narrowphase pre-pass
+    const int nc = *d.ccount;
+    PK_GRID_STRIDE(ci, nc)
     {
-        d.pair_colour[p] = -2;
+        const int p = d.clist[ci];
         const Manifold<T> &m = d.man_new[p];
         const int mn = m.n;
-        if (mn == 0) // most pairs: nothing else to read
-        {
-            d.rowmask[p] = 0;
-            continue;
-        }
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         int world = int(skey[p] >> (2 * d.lbits));
-        if (!d.wp[world].active)
-        {
-            d.rowmask[p] = 0;
-            continue;
-        }
         const Pose<T> &PA = d.pose[sa];
         const Pose<T> &PB = d.pose[sb];
         const Params<T> &ra = d.prm[sa];

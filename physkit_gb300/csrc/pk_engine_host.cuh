@@ -121,6 +121,9 @@ public:
         d.np_iters = reinterpret_cast<unsigned long long *>(counters_ + 10); // counters 10..15
         d.nnew = counters_ + 16;
         d.njoints = counters_ + 17; // zero until joints are set
+        d.ccount = counters_ + 18;
+        d.gjk2_count = counters_ + 19;
+        d.gjk2_count_heavy = counters_ + 20;
         PK_CUDA(alloc(&d.jstart, W));
         PK_CUDA(alloc(&d.jend, W));
         PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
@@ -152,6 +155,7 @@ public:
             d.world_order = wo;
             d.world_nlocal = wn;
         }
+        PK_CUDA(radix_sort_prepare<uint64_t>());
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -183,6 +187,8 @@ public:
         PK_CUDA(alloc(&d.event, P));
         PK_CUDA(alloc(&d.old_idx, P));
         PK_CUDA(alloc(&d.gjk_list, P));
+        PK_CUDA(alloc(&d.clist, P));
+        PK_CUDA(alloc(&d.gjk_list2, P));
         PK_CUDA(alloc(&d.epa_list, P));
         PK_CUDA(alloc(&d.epa_simplex, P));
         PK_CUDA(alloc(&d.rows, 4 * P));
@@ -622,6 +628,11 @@ public:
         {
             PK_CUDA(cudaMemcpy(col.data(), d_.pair_colour, sizeof(int) * np, cudaMemcpyDeviceToHost));
             PK_CUDA(cudaMemcpy(k.data(), d_.key_old, sizeof(uint64_t) * np, cudaMemcpyDeviceToHost));
+            // the solver colours only pairs with contact rows; the others read -2
+            std::vector<uint8_t> mask(static_cast<size_t>(np));
+            PK_CUDA(cudaMemcpy(mask.data(), d_.rowmask, size_t(np), cudaMemcpyDeviceToHost));
+            for (int i = 0; i < np; ++i)
+                if (!mask[i]) col[i] = -2;
         }
         if (nc0) PK_CUDA(cudaMemcpy(nc0, d_.ncolours, sizeof(int), cudaMemcpyDeviceToHost));
         int cnt = 0;
@@ -912,7 +923,7 @@ private:
                       d_.wroot, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
-                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list,
+                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
                       d_.epa_list, d_.epa_simplex, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.srec, d_.crec, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
@@ -937,7 +948,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 19 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 20 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -974,6 +985,7 @@ private:
         last_sval_ = av;
         PK_CUDA(mark(5));
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
+        k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));

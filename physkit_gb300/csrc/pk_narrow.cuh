@@ -395,8 +395,10 @@ template <class T> PK_HD bool gjk_simplex(Simplex<T> &s, V3<T> &dir)
     return false;
 }
 
-// gjk_collision (collision.cpp:165-189). Returns true with the enclosing simplex.
-template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s)
+// gjk_collision (collision.cpp:165-189). Returns true with the enclosing simplex. On the exit
+// where the support in the search direction does not pass the origin, that direction (unit
+// length) goes to *sep: no point of A - B lies beyond the origin along it.
+template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, V3<T> *sep = nullptr)
 {
     s.n = 0;
     s.iters = 0;
@@ -409,7 +411,11 @@ template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Si
     {
         s.iters = iter + 1;
         SupPt<T> np = minkowski(A, B, dir);
-        if (dot(np.p, dir) <= T(0)) return false;
+        if (dot(np.p, dir) <= T(0))
+        {
+            if (sep) *sep = dir;
+            return false;
+        }
         s.push(np);
         if (gjk_simplex(s, dir)) return true;
     }

@@ -4,10 +4,12 @@
 // One pass per 8-bit digit, three kernels per pass:
 //   hist    : each CTA in use counts the digits of its contiguous chunk    -> hist[digit][cta]
 //   scan    : one CTA per digit turns its row into exclusive offsets and records the row total
-//   scatter : each CTA scans the 256 digit totals into digit bases, then walks its chunk in
-//             256-element tiles, ranks equal digits inside a warp with __match_any_sync, combines
-//             warps through shared-memory counters, and writes each element to digit base + row
-//             offset + running count + rank (stable).
+//   scatter : each CTA scans the 256 digit totals into digit bases, then walks its chunk in tiles
+//             of kSortTile elements: every warp ranks its contiguous sub-tile (equal digits inside a
+//             warp through ballots of the digit bits, across its rounds through per-warp counters),
+//             the CTA combines the warps, sorts the tile by digit in shared memory and writes each
+//             digit's run out contiguously (stable). Runs of ~16 elements per digit per tile keep
+//             the writes of the low, near-random digits in whole sectors.
 // Traffic per pass and element: read key+value twice (hist reads keys only), write key+value once.
 #pragma once
 
@@ -19,6 +21,9 @@ namespace pk
 
 constexpr int kSortThreads = 256;
 constexpr int kSortRadix = 256;
+constexpr int kSortItems = 16;                        // elements per thread and tile
+constexpr int kSortTile = kSortThreads * kSortItems; // elements per tile
+constexpr size_t kSortSmem = size_t(kSortTile) * 16; // tile keys + values in dynamic shared memory
 
 // Chunking of [0, n) over at most `nblocks` CTAs, at least kSortMinChunk elements per CTA, so
 // a short list touches one CTA and a short digit table (the cost of a pass follows n, not the
@@ -60,6 +65,21 @@ static __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint64_
         atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1u);
     __syncthreads();
     hist[threadIdx.x * used + blockIdx.x] = h[threadIdx.x];
+}
+
+// Lanes of the warp holding the same 8-bit digit as this lane (d = kSortRadix marks an empty lane,
+// which matches only other empty lanes): one ballot per digit bit plus one for emptiness.
+__device__ __forceinline__ unsigned digit_peers(int d)
+{
+    unsigned m = __ballot_sync(0xFFFFFFFFu, d == kSortRadix);
+    if (d != kSortRadix) m = ~m;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+    {
+        const unsigned v = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1);
+        m &= ((d >> b) & 1) ? v : ~v;
+    }
+    return m;
 }
 
 // Block-wide exclusive scan of one value per thread (kSortThreads threads); returns the total.
@@ -107,16 +127,19 @@ static __global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__r
 }
 
 template <class V>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, 2)
     k_sort_scatter(const uint64_t *__restrict__ kin, const V *__restrict__ vin, uint64_t *__restrict__ kout,
                    V *__restrict__ vout, const int *n_ptr, int shift, const uint32_t *__restrict__ hist,
                    const uint32_t *__restrict__ tot)
 {
+    static_assert(sizeof(V) == 8, "tile staging holds 8-byte values");
     constexpr int W = kSortThreads / 32;
-    __shared__ uint32_t base[kSortRadix];
-    __shared__ uint32_t running[kSortRadix];
-    __shared__ uint32_t wcnt[W][kSortRadix + 1];
-    __shared__ uint32_t tile_total[kSortRadix];
+    extern __shared__ uint64_t sort_tile[];
+    uint64_t *skey = sort_tile;
+    V *sval = reinterpret_cast<V *>(sort_tile + kSortTile);
+    __shared__ uint32_t base[kSortRadix];    // output position of this CTA's next element of each digit
+    __shared__ uint32_t tstart[kSortRadix];  // first tile position of each digit
+    __shared__ uint32_t wcnt[W][kSortRadix]; // per-warp digit counts, then offsets across warps
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int n = *n_ptr;
     const int used = sort_used(n, gridDim.x);
@@ -124,46 +147,82 @@ __global__ void __launch_bounds__(kSortThreads)
     uint32_t digit_base;
     block_exclusive_scan(tot[t], digit_base);
     base[t] = digit_base + hist[t * used + blockIdx.x];
-    running[t] = 0;
     int lo, hi;
     sort_chunk(n, gridDim.x, blockIdx.x, lo, hi);
     const unsigned lt_mask = (1u << lane) - 1u;
-    for (int tile = lo; tile < hi; tile += kSortThreads)
+    for (int tile = lo; tile < hi; tile += kSortTile)
     {
         for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
-        if (t == 0)
-            for (int w = 0; w < W; ++w) wcnt[w][kSortRadix] = 0;
         __syncthreads();
-        int i = tile + t;
-        bool valid = i < hi;
-        uint64_t k = valid ? kin[i] : 0;
-        V v = valid ? vin[i] : V(0);
-        int d = valid ? int((k >> shift) & 0xFF) : kSortRadix;
-        unsigned same = __match_any_sync(0xFFFFFFFFu, d);
-        int rank = __popc(same & lt_mask);
-        if (rank == 0) wcnt[warp][d] = __popc(same);
-        __syncthreads();
+        // warp `warp` owns elements [wb, wb + 32 * kSortItems) of the tile, round r holding
+        // wb + 32 r + lane, so (round, lane) order is element order
+        const int wb = tile + warp * 32 * kSortItems;
+        uint64_t k[kSortItems];
+        V v[kSortItems];
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r)
         {
-            uint32_t s = 0;
-            for (int w = 0; w < W; ++w)
+            const int i = wb + 32 * r + lane;
+            k[r] = i < hi ? kin[i] : 0;
+            v[r] = i < hi ? vin[i] : V(0);
+        }
+        uint32_t rk[kSortItems];
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r)
+        {
+            const int i = wb + 32 * r + lane;
+            const int d = i < hi ? int((k[r] >> shift) & 0xFF) : kSortRadix;
+            const unsigned same = digit_peers(d);
+            const uint32_t before = d < kSortRadix ? wcnt[warp][d] : 0u;
+            __syncwarp();
+            if (d < kSortRadix && (same & lt_mask) == 0) wcnt[warp][d] = before + uint32_t(__popc(same));
+            __syncwarp();
+            rk[r] = before + uint32_t(__popc(same & lt_mask));
+        }
+        __syncthreads();
+        uint32_t cnt = 0; // this tile's count of digit t
+        for (int w = 0; w < W; ++w)
+        {
+            const uint32_t c = wcnt[w][t];
+            wcnt[w][t] = cnt;
+            cnt += c;
+        }
+        uint32_t ts;
+        block_exclusive_scan(cnt, ts);
+        tstart[t] = ts;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r)
+        {
+            const int i = wb + 32 * r + lane;
+            if (i < hi)
             {
-                uint32_t c = wcnt[w][t];
-                wcnt[w][t] = s;
-                s += c;
+                const int d = int((k[r] >> shift) & 0xFF);
+                const uint32_t pos = tstart[d] + wcnt[warp][d] + rk[r];
+                skey[pos] = k[r];
+                sval[pos] = v[r];
             }
-            tile_total[t] = s;
         }
         __syncthreads();
-        if (valid)
+        const int tn = min(kSortTile, hi - tile);
+        for (int j = t; j < tn; j += kSortThreads)
         {
-            uint32_t dst = base[d] + running[d] + wcnt[warp][d] + uint32_t(rank);
-            kout[dst] = k;
-            vout[dst] = v;
+            const uint64_t kk = skey[j];
+            const int d = int((kk >> shift) & 0xFF);
+            const uint32_t dst = base[d] + uint32_t(j) - tstart[d];
+            kout[dst] = kk;
+            vout[dst] = sval[j];
         }
         __syncthreads();
-        running[t] += tile_total[t];
-        __syncthreads();
+        base[t] += cnt;
     }
+}
+
+// The scatter's tile staging exceeds the default dynamic shared-memory limit; call once per device
+// before the first sort.
+template <class V> inline cudaError_t radix_sort_prepare()
+{
+    return cudaFuncSetAttribute(k_sort_scatter<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSortSmem));
 }
 
 // Host-side launcher. Sorts [0, *n_dev) of (k0, v0) by the low `bits` bits of the key; ping-pongs
@@ -182,7 +241,7 @@ inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_de
         int shift = 8 * p;
         k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n_dev, shift, hist);
         k_sort_scan<<<kSortRadix, kSortThreads, 0, st>>>(hist, n_dev, nblocks, hist + size_t(kSortRadix) * nblocks);
-        k_sort_scatter<V><<<nblocks, kSortThreads, 0, st>>>(ka, va, kb, vb, n_dev, shift, hist,
+        k_sort_scatter<V><<<nblocks, kSortThreads, kSortSmem, st>>>(ka, va, kb, vb, n_dev, shift, hist,
                                                            hist + size_t(kSortRadix) * nblocks);
         uint64_t *tk = ka;
         ka = kb;
