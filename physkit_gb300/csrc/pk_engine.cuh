@@ -53,6 +53,9 @@ constexpr int kMaxColours = 512;
 constexpr int kSolveMaxThreads = 512; // largest solver CTA (FP32 form; the FP64 form's register need caps it at 256)
 template <class T> constexpr int solve_max_threads() { return sizeof(T) == 4 ? kSolveMaxThreads : 256; }
 constexpr uint32_t kLeafBit = 0x80000000u;
+// Worlds with at most this many leaves find their pairs by testing all pairs in shared memory
+// (k_broad_small); larger worlds traverse their LBVH.
+constexpr int kBroadMax = 2304;
 
 template <class T> struct Pose
 {
@@ -177,6 +180,8 @@ template <class T> struct Dev
     WorldParams<T> *wp;
     unsigned *wbounds;
     int *wroot;
+    int *wleaf_lo;         // each world's range of leaf positions in the sorted leaf list
+    int *wleaf_hi;
     int *mstart;
     int *mend;
     int max_worlds;
@@ -308,6 +313,8 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         d.wbounds[6 * w + 0] = d.wbounds[6 * w + 1] = d.wbounds[6 * w + 2] = 0xFFFFFFFFu;
         d.wbounds[6 * w + 3] = d.wbounds[6 * w + 4] = d.wbounds[6 * w + 5] = 0u;
         d.wroot[w] = -1;
+        d.wleaf_lo[w] = 0;
+        d.wleaf_hi[w] = 0;
         d.mstart[w] = 0;
         d.mend[w] = 0;
         d.nstart[w] = 0;
@@ -498,22 +505,31 @@ template <class T> __global__ void k_lbvh_build(Dev<T> d, const uint64_t *__rest
         if (wf == wl && (first == 0 || (skey[first - 1] >> 31) != wf) && (last == n - 1 || (skey[last + 1] >> 31) != wl))
             d.wroot[wf] = i;
     }
-    // single-leaf worlds
+    // each world's leaf range; single-leaf worlds
     PK_GRID_STRIDE(j, n)
     {
         uint64_t w = skey[j] >> 31;
-        if ((j == 0 || (skey[j - 1] >> 31) != w) && (j == n - 1 || (skey[j + 1] >> 31) != w))
-            d.wroot[w] = int(uint32_t(j) | kLeafBit);
+        const bool first = j == 0 || (skey[j - 1] >> 31) != w, last = j == n - 1 || (skey[j + 1] >> 31) != w;
+        if (first) d.wleaf_lo[w] = j;
+        if (last) d.wleaf_hi[w] = j + 1;
+        if (first && last) d.wroot[w] = int(uint32_t(j) | kLeafBit);
     }
 }
 
-template <class T> __global__ void k_lbvh_refit(Dev<T> d, const uint64_t *__restrict__ sval)
+// With `skip_small`, the leaves of worlds the all-pairs pass covers are left out: only the larger
+// worlds' subtrees (below their roots) get boxes.
+template <class T> __global__ void k_lbvh_refit(Dev<T> d, const uint64_t *__restrict__ sval, bool skip_small = false)
 {
     const int n = *d.nleaf;
     if (n < 2) return;
     PK_GRID_STRIDE(j, n)
     {
         int slot = int(sval[j]);
+        if (skip_small)
+        {
+            const int w = int(d.meta[slot].world);
+            if (d.wleaf_hi[w] - d.wleaf_lo[w] <= kBroadMax) continue;
+        }
         Aabb<T> b = d.tbox[slot];
         float mn[3] = {down_f(b.mn.x), down_f(b.mn.y), down_f(b.mn.z)};
         float mx[3] = {up_f(b.mx.x), up_f(b.mx.y), up_f(b.mx.z)};
@@ -571,6 +587,7 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
         const int i = int(sval[leaf]);
         Meta mi = d.meta[i];
         if (!(mi.flags & BODY_ALIVE) || (mi.flags & BODY_STATIC) || !d.wp[mi.world].active) continue;
+        if (d.wleaf_hi[mi.world] - d.wleaf_lo[mi.world] <= kBroadMax) continue; // all-pairs pass
         int root = d.wroot[mi.world];
         if (root < 0 || (uint32_t(root) & kLeafBit)) continue;
         Aabb<T> qb = d.tbox[i];
@@ -632,13 +649,233 @@ template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restri
     }
 }
 
+// Writes the pair of leaves ja, jb (positions lo + ja, lo + jb of the sorted leaf list) of world w
+// at `slot`, or at a fresh slot of the pair list (slot < 0; pairs the reference does not pair yet
+// are dropped there).
+template <class T>
+__device__ __forceinline__ void broad_emit(const Dev<T> &d, int w, int lo, const uint64_t *__restrict__ sval, int ja,
+                                           int jb, int slot)
+{
+    const int i = int(sval[lo + ja]), sj = int(sval[lo + jb]);
+    const Meta mi = d.meta[i], mj = d.meta[sj];
+    if (slot < 0)
+    {
+        if (!pair_allowed<T>(mi, mj)) return;
+        slot = atomicAdd(d.npairs, 1);
+    }
+    const uint32_t l0 = min(mi.local, mj.local), l1 = max(mi.local, mj.local);
+    const uint32_t slo = (mi.local < mj.local) ? uint32_t(i) : uint32_t(sj);
+    const uint32_t shi = (mi.local < mj.local) ? uint32_t(sj) : uint32_t(i);
+    if (slot < d.pair_cap)
+    {
+        d.pkey[slot] = (uint64_t(w) << (2 * d.lbits)) | (uint64_t(l0) << d.lbits) | uint64_t(l1);
+        d.pval[slot] = (uint64_t(slo) << 32) | shi;
+    }
+    else
+        atomicOr(d.status, ST_PAIR_OVERFLOW);
+}
+
+// Broadphase of a world with at most kBroadMax leaves, one CTA per world, by sweep and prune in
+// shared memory:
+//  1. sort the leaves by the lower bound of their box along the axis on which the world's box
+//     centres spread most (bitonic sort of (bound, leaf) keys);
+//  2. copy the leaves' boxes into shared memory in that order;
+//  3. one warp per sorted leaf a tests the leaves after it until their lower bound passes a's upper
+//     bound, so every pair overlapping on the axis is met once, from its earlier leaf, and queues
+//     the overlapping pairs in shared memory;
+//  4. the CTA drops queued pairs the reference does not pair yet (pair_allowed), reserves its range
+//     of the pair list with one atomic and writes the pairs there.
+// A world's static leaves sort after its dynamic ones in the leaf list, so "leaf >= first static"
+// marks them and static-static pairs are skipped. The pair test is the traversal's (closed
+// intervals on the exact fat boxes), so the pair set is the same; sweep bounds are rounded outward
+// to FP32, which only widens the window. A world whose overlaps overflow the queue sweeps again and
+// emits straight to the pair list.
+constexpr int kBroadPow2 = 4096;  // sort capacity, a power of two >= kBroadMax, indices in 12 bits
+constexpr int kBroadQueue = 10240; // queued pairs per world (two 12-bit sorted positions each)
+static_assert(kBroadPow2 >= kBroadMax && kBroadPow2 <= 4096, "sort capacity");
+static_assert(kBroadQueue * 4 >= kBroadPow2 * 8, "the sort keys live in the queue's space");
+
+template <class T> constexpr size_t broad_smem_bytes()
+{ return size_t(kBroadQueue) * 4 + (6 * sizeof(T) + 4 + 2) * size_t(kBroadMax); }
+
+template <class T>
+__global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *__restrict__ skey,
+                                                     const uint64_t *__restrict__ sval)
+{
+    extern __shared__ __align__(16) unsigned char broad_smem[];
+    __shared__ int ndyn, fill, cta_base;
+    __shared__ int warp_count[16];
+    const int w = blockIdx.x;
+    const int lo = d.wleaf_lo[w];
+    const int n = d.wleaf_hi[w] - lo;
+    if (n < 2 || n > kBroadMax) return;
+    int P = 2;
+    while (P < n) P <<= 1;
+    uint32_t *queue = reinterpret_cast<uint32_t *>(broad_smem); // kBroadQueue entries
+    uint64_t *srt = reinterpret_cast<uint64_t *>(broad_smem);   // sort keys, before the sweep
+    T *box = reinterpret_cast<T *>(queue + kBroadQueue);         // 6 per sorted position: mn, mx
+    float *lowax = reinterpret_cast<float *>(box + 6 * n);       // lower bound on the sweep axis
+    uint16_t *leaf = reinterpret_cast<uint16_t *>(lowax + n);     // leaf index | 0x8000 if static
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
+    // sweep axis: the widest spread of box centres (world bounds kept for the Morton codes)
+    const unsigned *wb = d.wbounds + 6 * w;
+    int ax = 0;
+    float ext = ord2f(wb[3]) - ord2f(wb[0]);
+    for (int k = 1; k < 3; ++k)
+    {
+        const float e = ord2f(wb[3 + k]) - ord2f(wb[k]);
+        if (e > ext)
+        {
+            ext = e;
+            ax = k;
+        }
+    }
+    if (tid == 0)
+    {
+        ndyn = n;
+        fill = 0;
+    }
+    __syncthreads();
+    for (int j = tid; j < P; j += bs)
+    {
+        if (j >= n)
+        {
+            srt[j] = ~0ull;
+            continue;
+        }
+        const Aabb<T> b = d.tbox[int(sval[lo + j])];
+        const T lower = ax == 0 ? b.mn.x : (ax == 1 ? b.mn.y : b.mn.z);
+        srt[j] = (uint64_t(f2ord(down_f(lower))) << 32) | uint32_t(j);
+        if ((skey[lo + j] >> 30) & 1u) atomicMin(&ndyn, j);
+    }
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1)
+        {
+            for (int t = tid; t < (P >> 1); t += bs)
+            {
+                const int i = 2 * t - (t & (stride - 1));
+                const int j = i + stride;
+                const uint64_t x = srt[i], y = srt[j];
+                if ((x > y) == ((i & size) == 0))
+                {
+                    srt[i] = y;
+                    srt[j] = x;
+                }
+            }
+            __syncthreads();
+        }
+    const int nd = ndyn;
+    for (int r = tid; r < n; r += bs)
+    {
+        const uint64_t e = srt[r];
+        const int j = int(uint32_t(e));
+        const Aabb<T> b = d.tbox[int(sval[lo + j])];
+        T *o = box + 6 * r;
+        o[0] = b.mn.x;
+        o[1] = b.mn.y;
+        o[2] = b.mn.z;
+        o[3] = b.mx.x;
+        o[4] = b.mx.y;
+        o[5] = b.mx.z;
+        lowax[r] = ord2f(uint32_t(e >> 32));
+        leaf[r] = uint16_t(j | (j >= nd ? 0x8000 : 0));
+    }
+    __syncthreads(); // the sort keys are dead from here on; their space holds the queue
+    for (int pass = 0; pass < 2; ++pass)
+    {
+        // pass 0 queues; pass 1 only runs after a queue overflow and emits straight to the list
+        if (pass == 1 && fill <= kBroadQueue) break;
+        for (int r = warp; r < n - 1; r += nw)
+        {
+            const T *qa = box + 6 * r;
+            const T qnx = qa[0], qny = qa[1], qnz = qa[2], qxx = qa[3], qxy = qa[4], qxz = qa[5];
+            const float upa = up_f(ax == 0 ? qxx : (ax == 1 ? qxy : qxz));
+            const bool a_static = (leaf[r] & 0x8000) != 0;
+            for (int base = r + 1; base < n; base += 32)
+            {
+                const int sb = base + lane;
+                bool past = true, hit = false;
+                if (sb < n)
+                {
+                    past = lowax[sb] > upa;
+                    const T *qb = box + 6 * sb;
+                    hit = !past && !(a_static && (leaf[sb] & 0x8000)) && qb[0] <= qxx && qb[3] >= qnx &&
+                          qb[1] <= qxy && qb[4] >= qny && qb[2] <= qxz && qb[5] >= qnz;
+                }
+                const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);
+                if (hits)
+                {
+                    if (pass == 0)
+                    {
+                        int q0 = 0;
+                        if (lane == 0) q0 = atomicAdd(&fill, __popc(hits));
+                        q0 = __shfl_sync(0xFFFFFFFFu, q0, 0) + __popc(hits & ((1u << lane) - 1u));
+                        if (hit && q0 < kBroadQueue) queue[q0] = uint32_t(r) | (uint32_t(sb) << 12);
+                    }
+                    else if (hit)
+                        broad_emit(d, w, lo, sval, int(leaf[r] & 0xFFF), int(leaf[sb] & 0xFFF), -1);
+                }
+                if (__any_sync(0xFFFFFFFFu, past)) break; // sorted: every later leaf is past too
+            }
+        }
+        __syncthreads();
+    }
+    const int nq = fill;
+    if (nq > kBroadQueue) return; // emitted by the second sweep
+    // drop the pairs the reference does not pair yet, then one reservation for the rest
+    int mine = 0;
+    for (int q = tid; q < nq; q += bs)
+    {
+        const uint32_t e = queue[q];
+        const int ja = leaf[e & 0xFFFu] & 0xFFF, jb = leaf[(e >> 12) & 0xFFFu] & 0xFFF;
+        if (pair_allowed<T>(d.meta[int(sval[lo + ja])], d.meta[int(sval[lo + jb])]))
+            ++mine;
+        else
+            queue[q] = e | 0x80000000u;
+    }
+    int before = mine;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, before, o);
+        if (lane >= o) before += y;
+    }
+    if (lane == 31) warp_count[warp] = before;
+    __syncthreads();
+    if (tid == 0)
+    {
+        int t = 0;
+        for (int k = 0; k < nw; ++k)
+        {
+            const int c = warp_count[k];
+            warp_count[k] = t;
+            t += c;
+        }
+        cta_base = t ? atomicAdd(d.npairs, t) : 0;
+    }
+    __syncthreads();
+    int slot = cta_base + warp_count[warp] + before - mine;
+    for (int q = tid; q < nq; q += bs)
+    {
+        const uint32_t e = queue[q];
+        if (e & 0x80000000u) continue;
+        broad_emit(d, w, lo, sval, int(leaf[e & 0xFFFu] & 0xFFF), int(leaf[(e >> 12) & 0xFFFu] & 0xFFF), slot++);
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // world raycast (world.h:260-319): every body whose broadphase box the ray enters within the
 // distance limit, with the entry distance, on the LBVH of the ray's world
 // ------------------------------------------------------------------------------------------------
 template <class T> __global__ void k_tree_reset(Dev<T> d)
 {
-    PK_GRID_STRIDE(w, d.max_worlds) d.wroot[w] = -1;
+    PK_GRID_STRIDE(w, d.max_worlds)
+    {
+        d.wroot[w] = -1;
+        d.wleaf_lo[w] = 0;
+        d.wleaf_hi[w] = 0;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) *d.nleaf = 0;
 }
 

@@ -134,6 +134,8 @@ public:
         PK_CUDA(cudaMemset(d.wp, 0, sizeof(WorldParams<T>) * W));
         PK_CUDA(alloc(&d.wbounds, 6 * W));
         PK_CUDA(alloc(&d.wroot, W));
+        PK_CUDA(alloc(&d.wleaf_lo, W));
+        PK_CUDA(alloc(&d.wleaf_hi, W));
         PK_CUDA(alloc(&d.mstart, W));
         PK_CUDA(alloc(&d.mend, W));
         PK_CUDA(alloc(&d.mstart_old, W));
@@ -156,6 +158,8 @@ public:
             d.world_nlocal = wn;
         }
         PK_CUDA(radix_sort_prepare<uint64_t>());
+        PK_CUDA(cudaFuncSetAttribute(k_broad_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(broad_smem_bytes<T>())));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -920,7 +924,7 @@ private:
         for (int k = 0; k < 2; ++k)
             if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
         void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
-                      d_.wroot, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
+                      d_.wroot, d_.wleaf_lo, d_.wleaf_hi, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
@@ -948,7 +952,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 20 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 21 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -962,9 +966,10 @@ private:
         PK_CUDA(mark(2));
         k_lbvh_build<T><<<gb, 256, 0, st_>>>(d, skey);
         k_zero_ints<<<gb, 256, 0, st_>>>(d.refit_flag, N);
-        k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval);
+        k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval, true);
         PK_CUDA(mark(3));
         k_traverse<T><<<(N + tune_.traverse_threads - 1) / tune_.traverse_threads, tune_.traverse_threads, 0, st_>>>(d, sval);
+        k_broad_small<T><<<cfg_.max_worlds, 512, broad_smem_bytes<T>(), st_>>>(d, skey, sval);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
         k_kept_count<T><<<cfg_.max_worlds, 256, 0, st_>>>(d);
         PK_CUDA(mark(4));

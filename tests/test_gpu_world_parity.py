@@ -137,6 +137,30 @@ def test_batched_worlds_equal_alone_and_oracle():
     batch.close()
 
 
+def test_fp64_all_pairs_and_tree_worlds_in_one_batch():
+    # worlds of at most 2,304 leaves find their pairs by the all-pairs pass in shared memory, larger
+    # ones by their LBVH; in one batch both give every world the oracle's bits
+    scene = scenes.config3(nworlds=3, nmin=1200, nmax=3600, seed=1, kinds=(1,))
+    counts = np.bincount(scene.bodies["world"])
+    assert counts.max() > 2304 and counts.min() < 2304
+    batch, _ = scenes.make_world(scene, precision="f64", max_bodies_per_world=4096)
+    steps = 30
+    for _ in range(steps):
+        batch.step(scene.dt)
+    bb = batch.bodies()
+    for w in range(scene.nworlds):
+        sub = scenes.Scene("world %d" % w, scene.shapes, scene.world_slice(w).copy(), 1)
+        sub.bodies["world"] = 0
+        ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+        pyoracle.load_scene(ow, sub)
+        for _ in range(steps):
+            ow.step(scene.dt)
+        assert len(ow.pairs()) > counts[w]  # the piles are in contact
+        assert np.array_equal(bb[scene.bodies["world"] == w][:, :13], ow.bodies()[:, :13]), f"world {w}"
+        ow.close()
+    batch.close()
+
+
 def test_fp32_error_against_fp64_oracle():
     # precision form: FP32 bulk arithmetic, FP64 accumulated impulses. Free flight + first contacts
     # over 60 steps of config1: positions within 1e-4 relative of the FP64 oracle.
