@@ -182,6 +182,8 @@ template <class T> struct Dev
     int *wroot;
     int *wleaf_lo;         // each world's range of leaf positions in the sorted leaf list
     int *wleaf_hi;
+    int *wlive;            // bodies of each world that take part in this step's broadphase
+    int *all_small;        // 1 while no world of the step has more than kBroadMax such bodies
     int *mstart;
     int *mend;
     int max_worlds;
@@ -315,6 +317,7 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         d.wroot[w] = -1;
         d.wleaf_lo[w] = 0;
         d.wleaf_hi[w] = 0;
+        d.wlive[w] = 0;
         d.mstart[w] = 0;
         d.mend[w] = 0;
         d.nstart[w] = 0;
@@ -331,6 +334,7 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.gjk2_count = 0;
         *d.gjk2_count_heavy = 0;
         *d.ccount = 0;
+        *d.all_small = 1;
         d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
         *d.epoch += 1;
     }
@@ -366,10 +370,10 @@ template <class T> __global__ void k_integrate_vel(Dev<T> d, T dt)
     PK_GRID_STRIDE(i, n)
     {
         Meta m = d.meta[i];
-        if (!(m.flags & BODY_ALIVE)) continue;
-        if (!d.wp[m.world].active) continue;
-        Aabb<T> tb = d.tbox[i];
-        if (!(m.flags & BODY_STATIC))
+        const bool live = (m.flags & BODY_ALIVE) && d.wp[m.world].active;
+        Aabb<T> tb{};
+        if (live) tb = d.tbox[i];
+        if (live && !(m.flags & BODY_STATIC))
         {
             const Params<T> &pr = d.prm[i];
             const WorldParams<T> &wp = d.wp[m.world];
@@ -402,17 +406,30 @@ template <class T> __global__ void k_integrate_vel(Dev<T> d, T dt)
                 d.meta[i].reinserted = epoch;
             }
         }
-        // world bounds of the fat-box centres (for the Morton quantisation only)
-        float cx = float(T(0.5) * (tb.mn.x + tb.mx.x));
-        float cy = float(T(0.5) * (tb.mn.y + tb.mx.y));
-        float cz = float(T(0.5) * (tb.mn.z + tb.mx.z));
-        unsigned *wb = d.wbounds + 6 * m.world;
-        atomicMin(wb + 0, f2ord(cx));
-        atomicMin(wb + 1, f2ord(cy));
-        atomicMin(wb + 2, f2ord(cz));
-        atomicMax(wb + 3, f2ord(cx));
-        atomicMax(wb + 4, f2ord(cy));
-        atomicMax(wb + 5, f2ord(cz));
+        // world bounds of the fat-box centres (Morton quantisation, sweep axis): reduced over the
+        // lanes of the same world first, so a warp of one world does 6 atomics, not 6 per body
+        const unsigned peers = __match_any_sync(__activemask(), live ? int(m.world) : -1);
+        if (live)
+        {
+            const unsigned ox = f2ord(float(T(0.5) * (tb.mn.x + tb.mx.x)));
+            const unsigned oy = f2ord(float(T(0.5) * (tb.mn.y + tb.mx.y)));
+            const unsigned oz = f2ord(float(T(0.5) * (tb.mn.z + tb.mx.z)));
+            const unsigned lx = __reduce_min_sync(peers, ox), ly = __reduce_min_sync(peers, oy),
+                           lz = __reduce_min_sync(peers, oz);
+            const unsigned hx = __reduce_max_sync(peers, ox), hy = __reduce_max_sync(peers, oy),
+                           hz = __reduce_max_sync(peers, oz);
+            if (int(threadIdx.x & 31) == __ffs(peers) - 1)
+            {
+                atomicAdd(d.wlive + m.world, __popc(peers));
+                unsigned *wb = d.wbounds + 6 * m.world;
+                atomicMin(wb + 0, lx);
+                atomicMin(wb + 1, ly);
+                atomicMin(wb + 2, lz);
+                atomicMax(wb + 3, hx);
+                atomicMax(wb + 4, hy);
+                atomicMax(wb + 5, hz);
+            }
+        }
     }
 }
 
@@ -429,6 +446,7 @@ template <class T> __global__ void k_morton(Dev<T> d, bool all_worlds = false)
         Meta m = d.meta[i];
         if ((m.flags & BODY_ALIVE) && (all_worlds || d.wp[m.world].active))
         {
+            if (!all_worlds && d.wlive[m.world] > kBroadMax) *d.all_small = 0; // some world traverses
             Aabb<T> tb = d.tbox[i];
             const unsigned *wb = d.wbounds + 6 * m.world;
             float c[3] = {float(T(0.5) * (tb.mn.x + tb.mx.x)), float(T(0.5) * (tb.mn.y + tb.mx.y)),
@@ -461,10 +479,14 @@ __device__ __forceinline__ int lbvh_delta(const uint64_t *k, int n, int i, int j
     return __clzll(a ^ b);
 }
 
-template <class T> __global__ void k_lbvh_build(Dev<T> d, const uint64_t *__restrict__ skey)
+// With `tree_if_needed`, the internal nodes are built only when some world of the step traverses
+// (all_small == 0): the all-pairs worlds need just their leaf ranges, and their leaves may then be
+// ordered by the world and static bits alone.
+template <class T> __global__ void k_lbvh_build(Dev<T> d, const uint64_t *__restrict__ skey, bool tree_if_needed = false)
 {
     const int n = *d.nleaf;
-    PK_GRID_STRIDE(i, n - 1)
+    const int ninner = (tree_if_needed && *d.all_small) ? 0 : n - 1;
+    PK_GRID_STRIDE(i, ninner)
     {
         int dir = (lbvh_delta(skey, n, i, i + 1) - lbvh_delta(skey, n, i, i - 1)) >= 0 ? 1 : -1;
         int dmin = lbvh_delta(skey, n, i, i - dir);
@@ -521,7 +543,7 @@ template <class T> __global__ void k_lbvh_build(Dev<T> d, const uint64_t *__rest
 template <class T> __global__ void k_lbvh_refit(Dev<T> d, const uint64_t *__restrict__ sval, bool skip_small = false)
 {
     const int n = *d.nleaf;
-    if (n < 2) return;
+    if (n < 2 || (skip_small && *d.all_small)) return;
     PK_GRID_STRIDE(j, n)
     {
         int slot = int(sval[j]);
@@ -581,7 +603,7 @@ template <class T> __device__ __forceinline__ bool pair_allowed(const Meta &a, c
 // body (static bodies do not query; their pairs come from the dynamic side).
 template <class T> __global__ void k_traverse(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    const int n = *d.nleaf;
+    const int n = *d.all_small ? 0 : *d.nleaf; // no world traverses in this step
     PK_GRID_STRIDE(leaf, n)
     {
         const int i = int(sval[leaf]);

@@ -124,6 +124,7 @@ public:
         d.ccount = counters_ + 18;
         d.gjk2_count = counters_ + 19;
         d.gjk2_count_heavy = counters_ + 20;
+        d.all_small = counters_ + 21;
         PK_CUDA(alloc(&d.jstart, W));
         PK_CUDA(alloc(&d.jend, W));
         PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
@@ -136,6 +137,7 @@ public:
         PK_CUDA(alloc(&d.wroot, W));
         PK_CUDA(alloc(&d.wleaf_lo, W));
         PK_CUDA(alloc(&d.wleaf_hi, W));
+        PK_CUDA(alloc(&d.wlive, W));
         PK_CUDA(alloc(&d.mstart, W));
         PK_CUDA(alloc(&d.mend, W));
         PK_CUDA(alloc(&d.mstart_old, W));
@@ -924,7 +926,7 @@ private:
         for (int k = 0; k < 2; ++k)
             if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
         void *ps[] = {d_.pose, d_.vel, d_.iw, d_.iwinv, d_.prm, d_.tbox, d_.meta, counters_, d_.wp, d_.wbounds,
-                      d_.wroot, d_.wleaf_lo, d_.wleaf_hi, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
+                      d_.wroot, d_.wleaf_lo, d_.wleaf_hi, d_.wlive, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
@@ -958,13 +960,14 @@ private:
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
         PK_CUDA(mark(1));
         k_morton<T><<<gb, 256, 0, st_>>>(d, false);
-        // sort the bodies of active worlds by (world, static, Morton)
+        // sort the bodies of active worlds by (world, static, Morton); the two lowest digits, Morton
+        // bits only the LBVH needs, are skipped in steps where no world traverses
         bool in1 = radix_sort<uint64_t>(mkey_[0], mval_[0], mkey_[1], mval_[1], d.nleaf, cfg_.wbits + 31,
-                                        cfg_.sort_blocks_bodies, hist_, st_);
+                                        cfg_.sort_blocks_bodies, hist_, st_, d.all_small, 2);
         const uint64_t *skey = in1 ? mkey_[1] : mkey_[0];
         const uint64_t *sval = in1 ? mval_[1] : mval_[0];
         PK_CUDA(mark(2));
-        k_lbvh_build<T><<<gb, 256, 0, st_>>>(d, skey);
+        k_lbvh_build<T><<<gb, 256, 0, st_>>>(d, skey, true);
         k_zero_ints<<<gb, 256, 0, st_>>>(d.refit_flag, N);
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval, true);
         PK_CUDA(mark(3));

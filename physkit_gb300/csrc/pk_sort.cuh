@@ -51,9 +51,10 @@ __device__ __forceinline__ void sort_chunk(int n, int nblocks, int b, int &lo, i
 }
 
 static __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint64_t *__restrict__ keys, const int *n_ptr,
-                                                            int shift, uint32_t *__restrict__ hist)
+                                                            int shift, uint32_t *__restrict__ hist, const int *skip)
 {
     __shared__ uint32_t h[kSortRadix];
+    if (skip && *skip) return;
     const int n = *n_ptr;
     const int used = sort_used(n, gridDim.x);
     if (int(blockIdx.x) >= used) return;
@@ -110,8 +111,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &e
 // Row `blockIdx.x` (one digit) of the digit table: exclusive offsets across the CTAs in use, and
 // the row total into tot[digit].
 static __global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__restrict__ hist, const int *n_ptr,
-                                                                   int nblocks, uint32_t *__restrict__ tot)
+                                                                   int nblocks, uint32_t *__restrict__ tot, const int *skip)
 {
+    if (skip && *skip) return;
     const int used = sort_used(*n_ptr, nblocks);
     uint32_t *row = hist + size_t(blockIdx.x) * used;
     uint32_t run = 0;
@@ -130,9 +132,10 @@ template <class V>
 __global__ void __launch_bounds__(kSortThreads, 2)
     k_sort_scatter(const uint64_t *__restrict__ kin, const V *__restrict__ vin, uint64_t *__restrict__ kout,
                    V *__restrict__ vout, const int *n_ptr, int shift, const uint32_t *__restrict__ hist,
-                   const uint32_t *__restrict__ tot)
+                   const uint32_t *__restrict__ tot, const int *skip)
 {
     static_assert(sizeof(V) == 8, "tile staging holds 8-byte values");
+    if (skip && *skip) return;
     constexpr int W = kSortThreads / 32;
     extern __shared__ uint64_t sort_tile[];
     uint64_t *skey = sort_tile;
@@ -226,11 +229,13 @@ template <class V> inline cudaError_t radix_sort_prepare()
 }
 
 // Host-side launcher. Sorts [0, *n_dev) of (k0, v0) by the low `bits` bits of the key; ping-pongs
-// with (k1, v1); `hist` holds kSortRadix * (nblocks + 1) counters. Returns true when the result
-// ends in (k1, v1).
+// with (k1, v1); `hist` holds kSortRadix * (nblocks + 1) counters. The first `skip_passes` passes
+// (an even number, so the buffers still alternate as planned) do nothing while *skip is non-zero
+// at run time: the result is then ordered by the higher digits only, stably. Returns true when the
+// result ends in (k1, v1).
 template <class V>
 inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_dev, int bits, int nblocks,
-                       uint32_t *hist, cudaStream_t st)
+                       uint32_t *hist, cudaStream_t st, const int *skip = nullptr, int skip_passes = 0)
 {
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
@@ -239,10 +244,11 @@ inline bool radix_sort(uint64_t *k0, V *v0, uint64_t *k1, V *v1, const int *n_de
     for (int p = 0; p < passes; ++p)
     {
         int shift = 8 * p;
-        k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n_dev, shift, hist);
-        k_sort_scan<<<kSortRadix, kSortThreads, 0, st>>>(hist, n_dev, nblocks, hist + size_t(kSortRadix) * nblocks);
+        const int *sk = (skip && p < (skip_passes & ~1)) ? skip : nullptr;
+        k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n_dev, shift, hist, sk);
+        k_sort_scan<<<kSortRadix, kSortThreads, 0, st>>>(hist, n_dev, nblocks, hist + size_t(kSortRadix) * nblocks, sk);
         k_sort_scatter<V><<<nblocks, kSortThreads, kSortSmem, st>>>(ka, va, kb, vb, n_dev, shift, hist,
-                                                           hist + size_t(kSortRadix) * nblocks);
+                                                                   hist + size_t(kSortRadix) * nblocks, sk);
         uint64_t *tk = ka;
         ka = kb;
         kb = tk;
