@@ -40,6 +40,8 @@ struct Tunables
     int narrow_grid = 2;       // GJK/EPA grid = narrow_grid x the default grid
     int traverse_threads = 128;
     int big_threads = 256;     // threads per solver CTA of the worlds above small_world
+    int tiny_world = 0;        // worlds up to this many local indices get a launch of their own
+    int tiny_threads = 32;     // (many small CTAs resident per SM: one colour sweep per warp)
 };
 
 struct StepCounters

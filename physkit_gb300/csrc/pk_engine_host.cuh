@@ -346,6 +346,7 @@ public:
     void split_worlds()
     {
         big_worlds_ = 0;
+        tiny_worlds_ = 0;
         int maxl = 0;
         grid_worlds_.clear();
         for (size_t i = 0; i < order_.size(); ++i)
@@ -357,6 +358,7 @@ public:
                 continue;
             }
             if (nl > tune_.small_world) ++big_worlds_;
+            else if (tune_.tiny_world > 0 && tune_.tiny_world < tune_.small_world && nl <= tune_.tiny_world) ++tiny_worlds_;
             maxl = nl > maxl ? nl : maxl;
         }
         // worlds handled by the grid solver sort first (largest first): skip them in the CTA launches
@@ -845,6 +847,7 @@ private:
     static constexpr size_t kMaxSolveSmem = 160 * 1024;
     Tunables tune_{};
     int big_worlds_ = 0;
+    int tiny_worlds_ = 0; // the last worlds of the order: their own launch
     int big_cache_ = 0;
     std::vector<int> order_, nlocal_;
     std::vector<int> grid_worlds_;             // worlds solved by the cooperative grid solver
@@ -954,7 +957,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 21 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 21 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1012,9 +1015,12 @@ private:
         if (big_worlds_ > 0)
             launch_solve(big_worlds_, tune_.big_threads > 0 ? tune_.big_threads : tune_.solve_threads,
                          sizeof(Vel<T>) * size_t(big_cache_), d, pv, 0, big_cache_);
-        if (cfg_.max_worlds > big_worlds_)
-            launch_solve(cfg_.max_worlds - big_worlds_, tune_.solve_threads, sizeof(Vel<T>) * size_t(tune_.small_world),
-                         d, pv, big_worlds_, tune_.small_world);
+        if (cfg_.max_worlds > big_worlds_ + tiny_worlds_)
+            launch_solve(cfg_.max_worlds - big_worlds_ - tiny_worlds_, tune_.solve_threads,
+                         sizeof(Vel<T>) * size_t(tune_.small_world), d, pv, big_worlds_, tune_.small_world);
+        if (tiny_worlds_ > 0)
+            launch_solve(tiny_worlds_, tune_.tiny_threads, sizeof(Vel<T>) * size_t(tune_.tiny_world), d, pv,
+                         cfg_.max_worlds - tiny_worlds_, tune_.tiny_world);
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk, pv);
