@@ -1563,15 +1563,41 @@ std::optional<ContactRows> build_contact(Body &a, Body &b, V3 la, V3 lb, V3 wn, 
     return res;
 }
 
-// Deterministic min-index claiming colouring over the step's active manifolds: in each round
-// every uncoloured manifold claims its dynamic bodies with the minimum manifold index, and the
-// manifolds that won all their dynamic bodies take the round number as colour.
+// Deterministic colouring of the step's active manifolds (in key order), as the device solver
+// colours them. A world of at most 4,096 arena slots is coloured first-fit: each manifold takes
+// the lowest colour that no earlier manifold on one of its dynamic bodies has. A larger world is
+// coloured by min-index claiming rounds: in each round every uncoloured manifold claims its
+// dynamic bodies with the minimum manifold index, and the manifolds that won all their dynamic
+// bodies take the round number as colour.
 std::vector<int> colour_manifolds(const std::vector<std::pair<uint32_t, uint32_t>> &bodies,
                                   const std::vector<std::pair<bool, bool>> &stat, size_t nslots,
                                   int *ncolours)
 {
     size_t m = bodies.size();
     std::vector<int> col(m, -1);
+    if (nslots <= 4096)
+    {
+        std::vector<std::vector<bool>> used(nslots);
+        int top = 0;
+        for (size_t i = 0; i < m; ++i)
+        {
+            auto taken = [&](uint32_t b, bool st, int c)
+            { return !st && size_t(c) < used[b].size() && used[b][size_t(c)]; };
+            int c = 0;
+            while (taken(bodies[i].first, stat[i].first, c) || taken(bodies[i].second, stat[i].second, c)) ++c;
+            col[i] = c;
+            for (auto [b, st] : {std::pair<uint32_t, bool>{bodies[i].first, stat[i].first},
+                                 std::pair<uint32_t, bool>{bodies[i].second, stat[i].second}})
+            {
+                if (st) continue;
+                if (used[b].size() <= size_t(c)) used[b].resize(size_t(c) + 1, false);
+                used[b][size_t(c)] = true;
+            }
+            top = std::max(top, c + 1);
+        }
+        *ncolours = top;
+        return col;
+    }
     std::vector<uint32_t> owner(nslots, 0xFFFFFFFFu);
     size_t left = m;
     int round = 0;

@@ -50,6 +50,9 @@ enum : int
 };
 
 constexpr int kMaxColours = 512;
+// Worlds with at most this many local indices are coloured first-fit in pair order (one thread,
+// a 128-bit mask of used colours per body in shared memory); larger worlds by claiming rounds.
+constexpr int kFirstFitMax = 4096;
 constexpr int kSolveMaxThreads = 512; // largest solver CTA (FP32 form; the FP64 form's register need caps it at 256)
 template <class T> constexpr int solve_max_threads() { return sizeof(T) == 4 ? kSolveMaxThreads : 256; }
 constexpr uint32_t kLeafBit = 0x80000000u;
@@ -2170,10 +2173,80 @@ __global__ void __launch_bounds__(MAXT)
     if (tid == 0) remaining = na;
     __syncthreads();
 
-    // 2. colouring: each uncoloured manifold claims its dynamic bodies with its index; the winners
-    //    of all their bodies take the round number. Bodies are keyed by world-local index when the
-    //    owner table fits in shared memory, else by slot.
+    // 2. colouring. Worlds up to kFirstFitMax local indices: first fit in pair order, each manifold
+    //    taking the lowest colour that none of the earlier manifolds on its dynamic bodies has
+    //    (one thread; a 128-bit used-colour mask per body). Larger worlds: each uncoloured manifold
+    //    claims its dynamic bodies with its index; the winners of all their bodies take the round
+    //    number. Bodies are keyed by world-local index when the table fits in shared memory, else
+    //    by slot.
+    __shared__ int ff_ncol;
     int round = 0;
+    if (d.world_nlocal[w] <= kFirstFitMax)
+    {
+        uint64_t *used = reinterpret_cast<uint64_t *>(solve_smem); // 2 words per local index
+        for (int l = tid; l < 2 * d.world_nlocal[w]; l += nt) used[l] = 0ull;
+        __syncthreads();
+        if (tid == 0)
+        {
+            int top = 0;
+            bool capped = false;
+            constexpr int kAhead = 8; // records loaded ahead of the mask chain
+            for (int k0 = 0; k0 < na; k0 += kAhead)
+            {
+                uint4 rr[kAhead];
+#pragma unroll
+                for (int j = 0; j < kAhead; ++j) rr[j] = k0 + j < na ? rec[k0 + j] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (int j = 0; j < kAhead; ++j)
+                {
+                    if (k0 + j >= na) break;
+                    const uint4 r = rr[j];
+                    const bool da = !(r.y >> 31), db = !(r.z >> 31);
+                    const int la = int(r.w & 0xFFFFu), lb = int(r.w >> 16);
+                    uint64_t u0 = 0ull, u1 = 0ull;
+                    if (da)
+                    {
+                        u0 |= used[2 * la];
+                        u1 |= used[2 * la + 1];
+                    }
+                    if (db)
+                    {
+                        u0 |= used[2 * lb];
+                        u1 |= used[2 * lb + 1];
+                    }
+                    int c;
+                    if (~u0)
+                        c = __ffsll(~u0) - 1;
+                    else if (~u1)
+                        c = 64 + __ffsll(~u1) - 1;
+                    else
+                    {
+                        capped = true; // a body with 128 manifolds in one step
+                        c = -1;
+                    }
+                    colour[k0 + j] = c;
+                    if (c < 0) continue;
+                    const uint64_t b0 = c < 64 ? (1ull << c) : 0ull, b1 = c < 64 ? 0ull : (1ull << (c - 64));
+                    if (da)
+                    {
+                        used[2 * la] |= b0;
+                        used[2 * la + 1] |= b1;
+                    }
+                    if (db)
+                    {
+                        used[2 * lb] |= b0;
+                        used[2 * lb + 1] |= b1;
+                    }
+                    top = c + 1 > top ? c + 1 : top;
+                }
+            }
+            if (capped) atomicOr(d.status, ST_COLOUR_CAP);
+            ff_ncol = top;
+        }
+        __syncthreads();
+        round = ff_ncol;
+    }
+    else
     while (remaining > 0)
     {
         __syncthreads();

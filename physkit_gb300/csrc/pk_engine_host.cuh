@@ -90,6 +90,9 @@ public:
         PK_CUDA(cudaGetDevice(&dev));
         PK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
         PK_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        PK_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        PK_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+        PK_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
         const size_t N = size_t(cfg.body_cap), P = size_t(cfg.pair_cap), W = size_t(cfg.max_worlds);
         Dev<T> &d = d_;
         std::memset(&d, 0, sizeof(d));
@@ -365,6 +368,10 @@ public:
         big_worlds_ += int(grid_worlds_.size());
         int limit = int(kMaxSolveSmem / sizeof(Vel<T>));
         big_cache_ = maxl <= limit ? maxl : 0;
+        // first-fit colouring keeps 16 bytes per local index in the same shared memory
+        big_smem_ = sizeof(Vel<T>) * size_t(big_cache_);
+        const size_t ff = 16 * size_t(maxl < kFirstFitMax ? maxl : kFirstFitMax);
+        if (ff > big_smem_) big_smem_ = ff;
     }
 
     int set_tunables(const Tunables &t) override
@@ -827,6 +834,8 @@ private:
     EngineConfig cfg_{};
     Dev<T> d_{};
     cudaStream_t st_ = nullptr;
+    cudaStream_t st2_ = nullptr; // the solver's small-world launches run beside the large-world one
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
     int sms_ = 1;
     int nslots_ = 0;
     int parity_ = 0;
@@ -849,6 +858,7 @@ private:
     int big_worlds_ = 0;
     int tiny_worlds_ = 0; // the last worlds of the order: their own launch
     int big_cache_ = 0;
+    size_t big_smem_ = 0; // dynamic shared memory of the large-world launch
     std::vector<int> order_, nlocal_;
     std::vector<int> grid_worlds_;             // worlds solved by the cooperative grid solver
     static constexpr int kGridWorld = 16384;   // local indices above which a world leaves the CTA solver
@@ -904,18 +914,19 @@ private:
     }
     static int solve_threads(int t) { return t < solve_max_threads<T>() ? t : solve_max_threads<T>(); }
     // The joint-free instances serve batches that never had joints (buffers unallocated).
-    void launch_solve(int blocks, int threads, size_t smem, const Dev<T> &d, const uint64_t *pv, int first, int cache)
+    void launch_solve(int blocks, int threads, size_t smem, const Dev<T> &d, const uint64_t *pv, int first, int cache,
+                      cudaStream_t st)
     {
         threads = solve_threads(threads);
         const bool joints = joint_cap_ > 0;
         if (threads > 256 && joints)
-            k_solve_world<T, solve_max_threads<T>(), true><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+            k_solve_world<T, solve_max_threads<T>(), true><<<blocks, threads, smem, st>>>(d, pv, first, cache, kGridWorld);
         else if (threads > 256)
-            k_solve_world<T, solve_max_threads<T>(), false><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+            k_solve_world<T, solve_max_threads<T>(), false><<<blocks, threads, smem, st>>>(d, pv, first, cache, kGridWorld);
         else if (joints)
-            k_solve_world<T, 256, true><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+            k_solve_world<T, 256, true><<<blocks, threads, smem, st>>>(d, pv, first, cache, kGridWorld);
         else
-            k_solve_world<T, 256, false><<<blocks, threads, smem, st_>>>(d, pv, first, cache, kGridWorld);
+            k_solve_world<T, 256, false><<<blocks, threads, smem, st>>>(d, pv, first, cache, kGridWorld);
     }
     int grid(int n) const
     {
@@ -942,6 +953,11 @@ private:
         for (cudaEvent_t e : events_) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         st_ = nullptr;
+        if (st2_) cudaStreamDestroy(st2_);
+        st2_ = nullptr;
+        if (fork_) cudaEventDestroy(fork_);
+        if (join_) cudaEventDestroy(join_);
+        fork_ = join_ = nullptr;
     }
 
     int enqueue_step(T dt, int parity)
@@ -1012,15 +1028,29 @@ private:
             PK_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_solve_grid<T>), dim3(grid_blocks_), dim3(256),
                                                 args, 0, st_));
         }
+        // the large worlds' launch (the solver's critical path) and the smaller worlds' launches run
+        // side by side: the small worlds fill the SMs the large ones leave idle. Worlds are disjoint.
+        const bool side = big_worlds_ > 0 && cfg_.max_worlds > big_worlds_;
+        cudaStream_t sst = side ? st2_ : st_;
+        if (side)
+        {
+            PK_CUDA(cudaEventRecord(fork_, st_));
+            PK_CUDA(cudaStreamWaitEvent(st2_, fork_, 0));
+        }
         if (big_worlds_ > 0)
-            launch_solve(big_worlds_, tune_.big_threads > 0 ? tune_.big_threads : tune_.solve_threads,
-                         sizeof(Vel<T>) * size_t(big_cache_), d, pv, 0, big_cache_);
+            launch_solve(big_worlds_, tune_.big_threads > 0 ? tune_.big_threads : tune_.solve_threads, big_smem_, d, pv,
+                         0, big_cache_, st_);
         if (cfg_.max_worlds > big_worlds_ + tiny_worlds_)
             launch_solve(cfg_.max_worlds - big_worlds_ - tiny_worlds_, tune_.solve_threads,
-                         sizeof(Vel<T>) * size_t(tune_.small_world), d, pv, big_worlds_, tune_.small_world);
+                         sizeof(Vel<T>) * size_t(tune_.small_world), d, pv, big_worlds_, tune_.small_world, sst);
         if (tiny_worlds_ > 0)
             launch_solve(tiny_worlds_, tune_.tiny_threads, sizeof(Vel<T>) * size_t(tune_.tiny_world), d, pv,
-                         cfg_.max_worlds - tiny_worlds_, tune_.tiny_world);
+                         cfg_.max_worlds - tiny_worlds_, tune_.tiny_world, sst);
+        if (side)
+        {
+            PK_CUDA(cudaEventRecord(join_, st2_));
+            PK_CUDA(cudaStreamWaitEvent(st_, join_, 0));
+        }
         PK_CUDA(mark(8));
         k_integrate_pos<T><<<gb, 256, 0, st_>>>(d, dt);
         k_finish<T><<<gp, 256, 0, st_>>>(d, pk, pv);

@@ -226,3 +226,34 @@ def test_oracle_joint_types_stay_finite_and_hold():
     assert [len(ow.joint_impulses(h)) for h in hs] == [1, 5, 5, 6, 1, 3]
     assert ow.remove_joint(hs[0]) and not ow.remove_joint(hs[0])
     ow.step(1 / 120)
+
+
+def test_colour_order_first_fit_in_key_order():
+    # the colour order the device solver sweeps in, as the oracle restates it: in a world of at
+    # most 4,096 slots every manifold takes the lowest colour no earlier manifold (key order) on one
+    # of its dynamic bodies has; colours are then a proper colouring of the shared dynamic bodies
+    from physkit_gb300 import scenes
+
+    scene = scenes.small_pile(n=80, seed=3, kinds=(0, 1, 2))
+    ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+    pyoracle.load_scene(ow, scene)
+    static = scene.bodies["type"] != 0
+    checked = 0
+    for step in range(90):
+        ow.step(scene.dt)
+        if step % 10:
+            continue
+        keys, cols, nc = ow.colours()
+        used = {}
+        for k, c in zip(keys.tolist(), cols.tolist()):
+            lo, hi = k >> 32, k & 0xFFFFFFFF
+            dyn = [b for b in (lo, hi) if not static[b]]
+            taken = set().union(*(used.get(b, set()) for b in dyn)) if dyn else set()
+            want = next(x for x in range(len(keys) + 1) if x not in taken)
+            assert c == want, (step, k, c, want)
+            for b in dyn:
+                used.setdefault(b, set()).add(c)
+            checked += 1
+        assert nc == (max(cols) + 1 if len(cols) else 0)
+    assert checked > 50
+    ow.close()
