@@ -1201,7 +1201,51 @@ __device__ __forceinline__ bool obb_separated(const Aabb<T> &la, Qt<T> qa, V3<T>
     return false;
 }
 
-// Narrowphase pass 1: per pair, find last step's manifold, then either settle the pair at once or
+// Last step's manifold of each pair of an active world. Last step's pairs of a world are the
+// segment [mstart_old, mend_old) of last step's sorted keys, and this step's pairs are sorted the
+// same way, so each thread takes a run of consecutive pairs: one binary search for the first,
+// then a forward walk (with a binary search again past a long gap) for the rest. Pairs of idle
+// worlds keep the index their assembly gave them.
+constexpr int kOldRun = 8;
+template <class T> __global__ void k_old_index(Dev<T> d, const uint64_t *__restrict__ skey)
+{
+    const int np = *d.npairs;
+    PK_GRID_STRIDE(t, (np + kOldRun - 1) / kOldRun)
+    {
+        const int p0 = t * kOldRun, p1 = min(np, p0 + kOldRun);
+        int cw = -1, lo = 0, end = -1;
+        for (int p = p0; p < p1; ++p)
+        {
+            const uint64_t key = skey[p];
+            const int w = int(key >> (2 * d.lbits));
+            if (w != cw)
+            {
+                cw = w;
+                end = d.wp[w].active ? d.mend_old[w] : -1;
+                lo = d.mstart_old[w];
+            }
+            if (end < 0) continue;
+            int step = 0;
+            while (lo < end && d.key_old[lo] < key && step < 4)
+            {
+                ++lo;
+                ++step;
+            }
+            if (lo < end && d.key_old[lo] < key)
+            {
+                int hi = end;
+                while (lo < hi)
+                {
+                    const int mid = (lo + hi) >> 1;
+                    if (d.key_old[mid] < key) lo = mid + 1; else hi = mid;
+                }
+            }
+            d.old_idx[p] = (lo < end && d.key_old[lo] == key) ? lo : -1;
+        }
+    }
+}
+
+// Narrowphase pass 1: per pair, take last step's manifold, then either settle the pair at once or
 // queue it for GJK. A pair is settled without a new contact when the bodies' bounding spheres or
 // their oriented local boxes are apart by more than a rounding margin: the shapes are then
 // disjoint, and the reference's GJK returns no collision for them (collision.cpp:181-182).
@@ -1228,16 +1272,7 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
             d.event[p] = 0;
             continue;
         }
-        // last step's pairs of this world are the segment [mstart_old, mend_old) of the sorted list
-        int lo = d.mstart_old[world], hi = d.mend_old[world];
-        const int end = hi;
-        while (lo < hi)
-        {
-            int mid = (lo + hi) >> 1;
-            if (d.key_old[mid] < key) lo = mid + 1; else hi = mid;
-        }
-        int old_idx = (lo < end && d.key_old[lo] == key) ? lo : -1;
-        d.old_idx[p] = old_idx;
+        const int old_idx = d.old_idx[p]; // k_old_index
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         V3<T> dc = B.pos - A.pos;
         T rs = A.rmax + B.rmax;

@@ -973,7 +973,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 21 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
+        launches_ = 22 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1011,6 +1011,7 @@ private:
         const uint64_t *pv = av;
         last_sval_ = av;
         PK_CUDA(mark(5));
+        k_old_index<T><<<gp, 256, 0, st_>>>(d, pk);
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
