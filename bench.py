@@ -285,22 +285,25 @@ def run_ours(a, rank, world_size, local_rank):
     if os.path.exists(prof):
         traffic = json.load(open(prof)).get(dom)
 
-    # end to end through the C ABI: step + host read-back of every body's state
-    host = np.zeros((len(scene.bodies), 14))
+    # end to end through the C ABI: step + host read-back of every body's state into a pinned
+    # host array (registered once, outside the timed region)
+    host = np.empty((len(scene.bodies), 14))
+    world.pin(host)
     n_e2e = max(3, min(a.steps, 20))
     flagged = int(world.step(dt, check=False))
-    world.bodies()
+    world.bodies(out=host)
     t0 = time.perf_counter()
     for _ in range(n_e2e):
         flagged += int(world.step(dt, check=False))
-        host[:] = world.bodies()
+        world.bodies(out=host)
     e2e_s = time.perf_counter() - t0
-    bpb = 28 + 24 + 24 if a.precision == "f32" else 56 + 48 + 24
+    world.unpin(host)
     e2e_s = replicas.max_over_ranks(e2e_s, dist, device="cuda")
     e2e = {"value": nb_all * n_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
-           "d2h_bytes_per_step": len(scene.bodies) * bpb,
-           "note": "pk_world_step (synchronous) + pk_world_read_bodies into host memory every step; "
-                   "dt is the only per-step input (a kernel argument)",
+           "d2h_bytes_per_step": int(host.nbytes),
+           "note": "pk_world_step (synchronous) + pk_world_read_bodies (14 doubles per slot, packed on "
+                   "the device) into a pinned host array every step; dt is the only per-step input "
+                   "(a kernel argument)",
            "steps_with_device_status": flagged}
     raycast = None
     if not a.no_raycast:

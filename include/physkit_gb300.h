@@ -179,6 +179,10 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t);
 
 /* Per slot: pos3 quat4 vel3 ang_vel3 alive = 14 doubles (particle.h:135-149). */
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);
+/* Page-lock (pin) a host buffer the caller reads into or writes from every step, so that
+ * pk_world_read_bodies copies straight into it; unregister before freeing it. */
+int pk_host_register(void *ptr, size_t bytes);
+int pk_host_unregister(void *ptr);
 /* Overwrite pos/quat/vel/ang_vel of one body and refresh its cached world inertia. */
 int pk_world_write_body(pk_world *w, uint64_t handle, const double *state13);
 /* Sorted broadphase pairs of the last step. keys use the reference layout

@@ -1046,6 +1046,30 @@ int pk_world_read_bodies(pk_world *w, double *out, int32_t cap, int32_t *n)
     return PK_OK;
 }
 
+int pk_host_register(void *ptr, size_t bytes)
+{
+    if (!ptr || bytes == 0) return PK_ERR_INVALID;
+    cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
+int pk_host_unregister(void *ptr)
+{
+    if (!ptr) return PK_ERR_INVALID;
+    cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
 int pk_world_write_body(pk_world *w, uint64_t handle, const double *s)
 {
     if (!w || !s) return PK_ERR_INVALID;

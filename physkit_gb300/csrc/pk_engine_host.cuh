@@ -69,6 +69,31 @@ template <class T> __global__ void k_refresh_derived(Dev<T> d, int first, int n)
 
 template <class T> __global__ void k_kill_body(Dev<T> d, int slot) { d.meta[slot].flags = 0; }
 
+// Read-back rows (particle.h:135-149): pos3 quat4 vel3 ang_vel3 alive, 14 doubles per slot; an
+// empty slot reads as zeros.
+template <class T> __global__ void k_pack_bodies(Dev<T> d, double *__restrict__ out, int n)
+{
+    PK_GRID_STRIDE(i, n)
+    {
+        double *o = out + 14 * size_t(i);
+        if (!(d.meta[i].flags & BODY_ALIVE))
+        {
+            for (int k = 0; k < 14; ++k) o[k] = 0.0;
+            continue;
+        }
+        const Pose<T> ps = d.pose[i];
+        const Vel<T> ve = d.vel[i];
+        for (int k = 0; k < 3; ++k)
+        {
+            o[k] = double(ps.p[k]);
+            o[7 + k] = double(ve.v[k]);
+            o[10 + k] = double(ve.w[k]);
+        }
+        for (int k = 0; k < 4; ++k) o[3 + k] = double(ps.q[k]);
+        o[13] = 1.0;
+    }
+}
+
 static __global__ void k_zero_ints(int *p, int n)
 {
     PK_GRID_STRIDE(i, n) p[i] = 0;
@@ -508,33 +533,24 @@ public:
         return 0;
     }
 
+    // The state rows are packed on the device (k_pack_bodies) and copied to the caller's buffer in
+    // one transfer; a buffer pinned with pk_host_register takes the direct path.
     int read_bodies(double *out, int n) override
     {
         if (n > nslots_) n = nslots_;
-        std::vector<Pose<T>> pose(n);
-        std::vector<Vel<T>> vel(n);
-        std::vector<Meta> meta(n);
-        PK_CUDA(cudaStreamSynchronize(st_));
-        PK_CUDA(cudaMemcpy(pose.data(), d_.pose, sizeof(Pose<T>) * n, cudaMemcpyDeviceToHost));
-        PK_CUDA(cudaMemcpy(vel.data(), d_.vel, sizeof(Vel<T>) * n, cudaMemcpyDeviceToHost));
-        PK_CUDA(cudaMemcpy(meta.data(), d_.meta, sizeof(Meta) * n, cudaMemcpyDeviceToHost));
-        for (int i = 0; i < n; ++i)
+        if (n <= 0) return 0;
+        if (size_t(n) > pack_cap_)
         {
-            double *o = out + 14 * i;
-            if (!(meta[i].flags & BODY_ALIVE))
-            {
-                for (int k = 0; k < 14; ++k) o[k] = 0.0; // no body in this slot
-                continue;
-            }
-            for (int k = 0; k < 3; ++k)
-            {
-                o[k] = double(pose[i].p[k]);
-                o[7 + k] = double(vel[i].v[k]);
-                o[10 + k] = double(vel[i].w[k]);
-            }
-            for (int k = 0; k < 4; ++k) o[3 + k] = double(pose[i].q[k]);
-            o[13] = (meta[i].flags & BODY_ALIVE) ? 1.0 : 0.0;
+            if (pack_) cudaFree(pack_);
+            pack_ = nullptr;
+            pack_cap_ = 0;
+            PK_CUDA(cudaMalloc(&pack_, sizeof(double) * 14 * size_t(n)));
+            pack_cap_ = size_t(n);
         }
+        k_pack_bodies<T><<<grid(n), 256, 0, st_>>>(d_, pack_, n);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaMemcpyAsync(out, pack_, sizeof(double) * 14 * size_t(n), cudaMemcpyDeviceToHost, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
         return n;
     }
 
@@ -859,6 +875,8 @@ private:
     int tiny_worlds_ = 0; // the last worlds of the order: their own launch
     int big_cache_ = 0;
     size_t big_smem_ = 0; // dynamic shared memory of the large-world launch
+    double *pack_ = nullptr; // read-back staging: 14 doubles per slot
+    size_t pack_cap_ = 0;
     std::vector<int> order_, nlocal_;
     std::vector<int> grid_worlds_;             // worlds solved by the cooperative grid solver
     static constexpr int kGridWorld = 16384;   // local indices above which a world leaves the CTA solver
@@ -950,6 +968,9 @@ private:
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
             if (p) cudaFree(p);
+        if (pack_) cudaFree(pack_);
+        pack_ = nullptr;
+        pack_cap_ = 0;
         for (cudaEvent_t e : events_) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         st_ = nullptr;

@@ -123,6 +123,8 @@ def lib():
             "pk_world_step_graph": (C.c_int, [vp]),
             "pk_world_stream": (C.c_void_p, [vp]),
             "pk_world_read_bodies": (C.c_int, [vp, dp, C.c_int32, i32p]),
+            "pk_host_register": (C.c_int, [vp, C.c_size_t]),
+            "pk_host_unregister": (C.c_int, [vp]),
             "pk_world_write_body": (C.c_int, [vp, C.c_uint64, dp]),
             "pk_world_read_pairs": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p]),
             "pk_world_read_manifolds": (C.c_int, [vp, u64p, i32p, i32p, dp, C.c_int32, i32p]),
@@ -451,13 +453,27 @@ class World:
         return {self.L.pk_stage_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(n.value)}
 
     # reads -------------------------------------------------------------------------------------
-    def bodies(self):
+    def bodies(self, out=None):
+        """State rows of every slot (pos3 quat4 vel3 ang_vel3 alive). With `out` (a C-contiguous
+        float64 array of shape (>= slots, 14), ideally pinned with pin()), the rows are read into it
+        and a view of the filled part is returned."""
         n = C.c_int32()
         self.L.pk_world_read_bodies(self.h, None, 0, C.byref(n))
-        out = np.zeros((max(n.value, 1), 14))
+        if out is None:
+            out = np.empty((max(n.value, 1), 14))
+        elif out.dtype != np.float64 or out.ndim != 2 or out.shape[1] != 14 or not out.flags.c_contiguous \
+                or out.shape[0] < n.value:
+            raise ValueError("out must be a C-contiguous float64 array of shape (>= %d, 14)" % n.value)
         _check(self.L.pk_world_read_bodies(self.h, _ptr(out, C.c_double), n.value, C.byref(n)),
                "pk_world_read_bodies")
         return out[: n.value]
+
+    def pin(self, arr):
+        """Page-lock a host array that is read into (or written from) every step."""
+        _check(self.L.pk_host_register(C.c_void_p(arr.ctypes.data), arr.nbytes), "pk_host_register")
+
+    def unpin(self, arr):
+        _check(self.L.pk_host_unregister(C.c_void_p(arr.ctypes.data)), "pk_host_unregister")
 
     def get_rigid(self, handle):
         """world_base::get_rigid (world.h:220-224): state row, or None for a stale handle."""
