@@ -98,6 +98,31 @@ def test_fp64_remove_and_add_bodies():
     world.close()
 
 
+def test_read_back_into_pinned_array_equals_fresh_read():
+    # pk_world_read_bodies into a caller's page-locked buffer gives the same rows as a fresh read,
+    # FP32 and FP64, with an empty slot reading as zeros
+    for precision in ("f32", "f64"):
+        scene = scenes.small_pile(n=40, seed=9, kinds=(0, 1, 2))
+        world, handles = scenes.make_world(scene, precision=precision)
+        for _ in range(30):
+            world.step(scene.dt)
+        assert world.remove_rigid(int(handles[5]))
+        world.step(scene.dt)
+        host = np.full((len(scene.bodies) + 3, 14), 7.0)
+        world.pin(host)
+        got = world.bodies(out=host)
+        fresh = world.bodies()
+        world.unpin(host)
+        assert got.base is host
+        assert np.array_equal(got, fresh)
+        slot = int(handles[5]) & 0xFFFFFFFF
+        assert np.all(fresh[slot] == 0.0)
+        assert np.all(host[len(fresh):] == 7.0)  # rows past the slots are not touched
+        with pytest.raises(ValueError):
+            world.bodies(out=np.zeros((2, 14)))
+        world.close()
+
+
 def test_fp64_graph_replay_matches_plain_steps():
     scene = scenes.small_pile(n=50, seed=4)
     a, _ = scenes.make_world(scene, precision="f64")
