@@ -1565,8 +1565,8 @@ std::optional<ContactRows> build_contact(Body &a, Body &b, V3 la, V3 lb, V3 wn, 
 
 // Deterministic colouring of the step's active manifolds (in key order), as the device solver
 // colours them. A world of at most 4,096 arena slots is coloured first-fit: each manifold takes
-// the lowest colour that no earlier manifold on one of its dynamic bodies has. A larger world is
-// coloured by min-index claiming rounds: in each round every uncoloured manifold claims its
+// the lowest colour that no earlier manifold on one of its dynamic bodies has, unless that needs a
+// colour above 127. Other worlds are coloured by min-index claiming rounds: in each round every uncoloured manifold claims its
 // dynamic bodies with the minimum manifold index, and the manifolds that won all their dynamic
 // bodies take the round number as colour.
 std::vector<int> colour_manifolds(const std::vector<std::pair<uint32_t, uint32_t>> &bodies,
@@ -1595,8 +1595,12 @@ std::vector<int> colour_manifolds(const std::vector<std::pair<uint32_t, uint32_t
             }
             top = std::max(top, c + 1);
         }
-        *ncolours = top;
-        return col;
+        if (top <= 128)
+        {
+            *ncolours = top;
+            return col;
+        }
+        std::fill(col.begin(), col.end(), -1);
     }
     std::vector<uint32_t> owner(nslots, 0xFFFFFFFFu);
     size_t left = m;

@@ -2210,12 +2210,13 @@ __global__ void __launch_bounds__(MAXT)
 
     // 2. colouring. Worlds up to kFirstFitMax local indices: first fit in pair order, each manifold
     //    taking the lowest colour that none of the earlier manifolds on its dynamic bodies has
-    //    (one thread; a 128-bit used-colour mask per body). Larger worlds: each uncoloured manifold
-    //    claims its dynamic bodies with its index; the winners of all their bodies take the round
-    //    number. Bodies are keyed by world-local index when the table fits in shared memory, else
-    //    by slot.
+    //    (one thread; a 128-bit used-colour mask per body). Larger worlds, and worlds where a body
+    //    would need a first-fit colour above 127: each uncoloured manifold claims its dynamic bodies
+    //    with its index; the winners of all their bodies take the round number. Bodies are keyed by
+    //    world-local index when the table fits in shared memory, else by slot.
     __shared__ int ff_ncol;
     int round = 0;
+    bool coloured = false;
     if (d.world_nlocal[w] <= kFirstFitMax)
     {
         uint64_t *used = reinterpret_cast<uint64_t *>(solve_smem); // 2 words per local index
@@ -2275,14 +2276,21 @@ __global__ void __launch_bounds__(MAXT)
                     top = c + 1 > top ? c + 1 : top;
                 }
             }
-            if (capped) atomicOr(d.status, ST_COLOUR_CAP);
-            ff_ncol = top;
+            ff_ncol = capped ? -1 : top;
         }
         __syncthreads();
-        round = ff_ncol;
+        if (ff_ncol >= 0)
+        {
+            round = ff_ncol;
+            coloured = true;
+        }
+        else
+        {
+            for (int k = tid; k < na; k += nt) colour[k] = -1; // claiming rounds from scratch
+            __syncthreads();
+        }
     }
-    else
-    while (remaining > 0)
+    while (!coloured && remaining > 0)
     {
         __syncthreads();
         for (int k = tid; k < na; k += nt)

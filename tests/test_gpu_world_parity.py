@@ -98,6 +98,30 @@ def test_fp64_remove_and_add_bodies():
     world.close()
 
 
+def test_fp64_dense_cluster_queue_overflow_and_colour_fallback():
+    # 150 boxes crammed into 0.4 m: about 11,000 overlapping pairs, more than the sweep-and-prune
+    # queue holds (10,240), so the world's pairs come from its second sweep; and bodies carry ~150
+    # manifolds, so first-fit colouring (128 colours at most) gives way to claiming rounds. Both
+    # paths must give the oracle's bits.
+    scene = scenes.small_pile(n=150, seed=13, kinds=(1,))
+    rng = np.random.default_rng(0)
+    dyn = scene.bodies["type"] == 0
+    m = int(dyn.sum())
+    scene.bodies["pos"][dyn] = np.stack([rng.uniform(-0.2, 0.2, m), 1.5 + rng.uniform(-0.2, 0.2, m),
+                                         rng.uniform(-0.2, 0.2, m)], 1)
+    world, _ = scenes.make_world(scene, precision="f64", pair_factor=200)
+    ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+    pyoracle.load_scene(ow, scene)
+    for step in range(4):
+        world.step(scene.dt)
+        ow.step(scene.dt)
+        compare_step(world, ow, step)
+    assert len(world.pairs()) > 10240
+    assert world.colours()[2] > 128
+    world.close()
+    ow.close()
+
+
 def test_read_back_into_pinned_array_equals_fresh_read():
     # pk_world_read_bodies into a caller's page-locked buffer gives the same rows as a fresh read,
     # FP32 and FP64, with an empty slot reading as zeros
