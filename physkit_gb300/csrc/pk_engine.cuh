@@ -4,9 +4,13 @@
 //   k_integrate_vel   gravity + semi-implicit velocity update (integrate.h:36-40, particle.h:72-79),
 //                     world AABB of the rotated mesh bounds (mesh.cpp:398, bounds.h:144-158) and the
 //                     fat-box hysteresis of dynamic_bvh::update_leaf (bvh.cpp:475-514)
-//   k_morton + radix sort + k_lbvh_build + k_lbvh_refit      per-step LBVH over the fat boxes
-//   k_traverse + radix sort                                  overlap pairs (collision_phases.h:377-436)
-//   k_narrow          GJK/EPA + manifold update + begin/end events (collision_phases.h:244-320)
+//   k_morton + radix sort       the step's leaves grouped by world (static ones last), Morton order
+//   k_broad_small               overlap pairs of worlds up to kBroadMax leaves: sweep and prune in
+//                               shared memory (collision_phases.h:377-436)
+//   k_lbvh_build + k_lbvh_refit + k_traverse    the same for larger worlds, on a per-step LBVH
+//   pair radix sort + assembly  the step's sorted pair list, world by world
+//   k_old_index, k_narrow_pre, k_narrow_axis, k_narrow_gjk, k_narrow_epa
+//                     GJK/EPA + manifold update + begin/end events (collision_phases.h:244-320)
 //   k_contact_setup   contact Jacobians (constraint.h:874-953, 1052-1104)
 //   k_solve_world     colouring + warm start + sequential impulses, one CTA per world
 //                     (constraint.h:1107-1201)
