@@ -51,3 +51,22 @@ def test_no_device_is_an_error_not_a_fallback():
     with pytest.raises(RuntimeError, match="no CUDA device"):
         World()
     assert L.pk_version().decode().startswith("physkit_gb300")
+
+
+def test_host_register_rejects_invalid_arguments():
+    # argument checks come before any CUDA call, so they hold without a device too
+    from physkit_gb300 import lib
+    from physkit_gb300.world import PK_ERR_INVALID
+
+    L = lib()
+    assert L.pk_host_register(None, 0) == PK_ERR_INVALID
+    assert L.pk_host_unregister(None) == PK_ERR_INVALID
+
+
+def test_tune_result_layout():
+    from physkit_gb300 import world
+
+    # solve_threads, small_world, narrow_grid, traverse_threads, 2 doubles, steps_used, big_threads,
+    # tiny_world, tiny_threads (the doubles start at offset 16)
+    assert C.sizeof(world.TuneResultC) == 48
+    assert world.TuneResultC.step_ms_before.offset == 16
