@@ -1,23 +1,27 @@
 """World-step throughput benchmark (body-steps/s) on the batched-worlds workload.
 
 Workload (headline): 4,096 independent worlds with log-uniform body counts in [8, 2048] (~1.5 M
-dynamic bodies: UV spheres, boxes and 16-point hulls dropped into 5 m walled bins), FP32 bulk
-arithmetic with FP64 accumulated impulses, dt = 1/120, 10 solver iterations. One step = one
-world-step of every world. Inputs are synthetic (seeded generator in physkit_gb300/scenes.py).
+dynamic bodies: UV spheres, boxes and 16-point hulls dropped into 5 m walled bins), dt = 1/120,
+10 solver iterations, in the FP64 parity form: the reference's own precision (it computes in
+double throughout), bit-identical to the FP64 oracle. One step = one world-step of every world.
+Inputs are synthetic (seeded generator in physkit_gb300/scenes.py).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision f64|f32]
 
-value: dynamic bodies x K / device time of K steps (CUDA events on the world's stream, max over
-ranks); e2e: the same metric through the C ABI with a host read-back of every body's state after
-each step (pk_world_step + pk_world_read_bodies, wall clock). The reference arm times the FP64 CPU
-restatement of the reference step (oracle/) on a bounded sample of the same worlds with all host
-cores. Under torchrun each rank steps its own independent batch (weak scaling, no collective).
+Every timed window is the same: W warm-up steps from the initial state, then K timed steps.
+value: dynamic bodies x K / device time of the K steps (CUDA events on the world's stream, no
+stage instrumentation, max over ranks). e2e: the same window on a fresh copy of the batch through
+the C ABI, pk_world_step + pk_world_read_bodies of every body into pinned host memory each step
+(wall clock). stage_ms_per_step and the roofline come from a third copy stepped with per-stage
+CUDA events over the same window. precision_form: the FP32 form on the same window. The
+reference arm times the FP64 CPU restatement of the reference step (oracle/) on the whole batch
+and the same window, with one process per host core. Under torchrun each rank steps its own
+independent batch (weak scaling, no collective).
 """
 from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -47,30 +51,39 @@ BYTES = {
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--worlds", type=int, default=4096)
     ap.add_argument("--nmin", type=int, default=8)
     ap.add_argument("--nmax", type=int, default=2048)
-    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--precision", default="f64", choices=["f32", "f64"])
     ap.add_argument("--cpu-sample-worlds", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-precision-form", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-raycast", action="store_true")
-    ap.add_argument("--served-rates", default="1000,5000,20000",
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-stages", action="store_true")
+    ap.add_argument("--served-rates", default="1000,2000,5000,10000,20000,50000",
                     help="Poisson request rates (req/s) for the served form; empty to skip")
-    ap.add_argument("--served-seconds", type=float, default=2.0)
+    ap.add_argument("--served-seconds", type=float, default=1.5)
     return ap.parse_args()
 
 
-def config_dict(a, scene, world_size):
+def window(a):
+    return f"steps {a.warmup + 1}-{a.warmup + a.steps} after {a.warmup} warm-up steps from the initial state"
+
+
+def config_dict(a, n_dynamic, world_size):
     return {"workload": f"batched worlds: {a.worlds} worlds x log-uniform[{a.nmin},{a.nmax}] bodies "
-                        f"(spheres/boxes/hulls in 5 m bins), {a.precision.upper()} bulk + FP64 impulses, "
+                        f"(spheres/boxes/hulls in 5 m bins), {a.precision.upper()}"
+                        f"{' parity form (bit-identical to the FP64 oracle)' if a.precision == 'f64' else ' bulk + FP64 impulses'}, "
                         f"dt=1/120, 10 iterations",
-            "worlds_per_gpu": a.worlds, "dynamic_bodies_per_gpu": scene.n_dynamic if scene else None,
+            "worlds_per_gpu": a.worlds, "dynamic_bodies_per_gpu": n_dynamic,
+            "window": window(a),
             "parallelism": f"replicas x{world_size} (independent worlds per GPU, no collective)",
             "l2": "inputs larger than L2 (device-resident body state > 129 MB)",
             "seed": "scenes.config3 seed 0x50484B0000000003 + rank"}
@@ -127,19 +140,29 @@ class Clocks:
 
 
 # ------------------------------------------------------------------------------------------------
-# CPU baseline: the FP64 oracle on a bounded sample of the same worlds
+# CPU legs: the FP64 oracle on worlds of the same batch, same window
 # ------------------------------------------------------------------------------------------------
+def world_ranges(scene):
+    """[start, end) of each world's records (config3 keeps every world's records contiguous)."""
+    import numpy as np
+
+    w = scene.bodies["world"]
+    starts = np.searchsorted(w, np.arange(scene.nworlds), side="left")
+    ends = np.searchsorted(w, np.arange(scene.nworlds), side="right")
+    return starts, ends
+
+
 def _cpu_worker(args):
     scene_kw, worlds, steps, warmup, barrier, out_q = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
     import pyoracle
     from physkit_gb300 import scenes
 
     scene = scenes.config3(**scene_kw)
+    starts, ends = world_ranges(scene)
     ows, nb = [], 0
     for w in worlds:
-        sub = scenes.Scene("w", scene.shapes, scene.world_slice(w).copy(), 1)
+        sub = scenes.Scene("w", scene.shapes, scene.bodies[starts[w]:ends[w]].copy(), 1)
         ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="key")
         pyoracle.load_scene(ow, sub)
         ows.append(ow)
@@ -159,11 +182,22 @@ def _cpu_worker(args):
     out_q.put((nb, t1 - t0))
 
 
-def cpu_baseline(scene_kw, worlds, steps, warmup, procs):
+def cpu_baseline(scene_kw, worlds, steps, warmup, procs, sizes=None):
+    """FP64 oracle over `worlds` with `procs` processes (spawned, one world list each, largest
+    worlds dealt first to the least loaded process); returns (body-steps/s, bodies, wall s)."""
     import multiprocessing as mp
 
     ctx = mp.get_context("spawn")
-    shards = [worlds[i::procs] for i in range(procs)]
+    shards = [[] for _ in range(procs)]
+    if sizes is None:
+        for i, w in enumerate(worlds):
+            shards[i % procs].append(w)
+    else:
+        load = [0] * procs
+        for w in sorted(worlds, key=lambda w: -sizes[w]):
+            k = min(range(procs), key=load.__getitem__)
+            shards[k].append(w)
+            load[k] += sizes[w]
     shards = [s for s in shards if s]
     q = ctx.Queue()
     barrier = ctx.Barrier(len(shards) + 1) if len(shards) > 1 else None
@@ -186,23 +220,81 @@ def cpu_baseline(scene_kw, worlds, steps, warmup, procs):
 
 # ------------------------------------------------------------------------------------------------
 def run_reference(a, rank, world_size):
+    """The reference's CPU path (the FP64 oracle restating it; the reference itself does not
+    build here) on the whole batch of this configuration and the same window as our arm."""
     if rank != 0:
         return
+    import numpy as np
+    from physkit_gb300 import scenes
+
     ncpu = os.cpu_count() or 1
-    sample = min(a.worlds, max(4 * ncpu, a.cpu_sample_worlds))
-    steps = max(1, min(a.steps, 10))
     kw = {"nworlds": a.worlds, "nmin": a.nmin, "nmax": a.nmax}
-    value, nb, wall = cpu_baseline(kw, list(range(sample)), steps, min(a.warmup, 3), ncpu)
+    scene = scenes.config3(**kw)
+    starts, ends = world_ranges(scene)
+    sizes = (ends - starts).tolist()
+    value, nb, wall = cpu_baseline(kw, list(range(a.worlds)), a.steps, a.warmup, ncpu, sizes)
+    assert nb == scene.n_dynamic
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(a, None, world_size),
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": wall * 1e3 / a.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(argparse.Namespace(**{**vars(a), "precision": "f64"}),
+                                                       nb, world_size),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncpu, "kind": "port",
-                             "sample": f"FP64 oracle restating the reference step, first {sample} of the "
-                                       f"{a.worlds} worlds ({nb} dynamic bodies), {steps} steps per "
-                                       f"process after warm-up, {ncpu} processes"},
+                             "sample": f"FP64 oracle restating the reference step on all {a.worlds} worlds "
+                                       f"({nb} dynamic bodies), {window(a)}, {ncpu} processes "
+                                       f"(worlds dealt largest first), {wall:.1f} s timed"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _make(scene, precision, tuned):
+    from physkit_gb300 import scenes
+
+    # pair capacity 12 per body: settled piles keep ~6 fat-box pairs per body
+    world, _ = scenes.make_world(scene, precision=precision, pair_factor=12)
+    if tuned:
+        world.set_tuning(tuned)
+    return world
+
+
+def _tune(scene, precision, warmup):
+    """The project's autotuner on a scratch copy of the batch, from the step the timed window starts."""
+    scratch = _make(scene, precision, None)
+    for _ in range(warmup):
+        scratch.step_async(scene.dt)
+    scratch.synchronize()
+    tuned = scratch.autotune(scene.dt, 2)
+    scratch.close()
+    return tuned
+
+
+def _device_window(world, dt, warmup, steps, dist, local_rank, clocks=False):
+    """W untimed steps, then K steps timed by CUDA events on the world's stream between a barrier
+    and synchronisations; returns (max-over-ranks ms, step info, clocks)."""
+    import torch
+    from physkit_gb300 import replicas
+
+    for _ in range(warmup):
+        world.step_async(dt)
+    world.synchronize()
+    stream = torch.cuda.ExternalStream(world.stream())
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = None
+    if clocks:
+        clk = Clocks(local_rank)
+        clk.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        world.step_async(dt)
+    ev1.record(stream)
+    info = world.synchronize()
+    torch.cuda.synchronize()
+    clk = clk.stop() if clk else None
+    ms = replicas.max_over_ranks(ev0.elapsed_time(ev1), dist, device="cuda")
+    return ms, info, clk
 
 
 def run_ours(a, rank, world_size, local_rank):
@@ -210,7 +302,7 @@ def run_ours(a, rank, world_size, local_rank):
     import torch
 
     torch.cuda.set_device(local_rank)
-    from physkit_gb300 import scenes
+    from physkit_gb300 import replicas, scenes
 
     dist = None
     if world_size > 1:
@@ -219,119 +311,85 @@ def run_ours(a, rank, world_size, local_rank):
         dist_mod.init_process_group("nccl")
         dist = dist_mod
 
-    from physkit_gb300 import replicas
-
-    scene = scenes.config3(nworlds=a.worlds, nmin=a.nmin, nmax=a.nmax, seed=replicas.rank_seed(scenes.SEED_BASE + 3, rank))
+    scene = scenes.config3(nworlds=a.worlds, nmin=a.nmin, nmax=a.nmax,
+                           seed=replicas.rank_seed(scenes.SEED_BASE + 3, rank))
     dt = scene.dt
-    tuned = None
-    if not a.no_tune:
-        # autotune on a scratch copy of the batch from the same step on, so the timed window below
-        # covers the same simulated steps as an untuned run
-        scratch, _ = scenes.make_world(scene, precision=a.precision, pair_factor=12)
-        for _ in range(a.warmup):
-            scratch.step_async(dt)
-        scratch.synchronize()
-        tuned = scratch.autotune(dt, 2)
-        scratch.close()
-    # pair capacity 12 per body: settled piles keep ~6 fat-box pairs per body, so long runs stay below it
-    world, _ = scenes.make_world(scene, precision=a.precision, pair_factor=12)
-    if tuned:
-        world.set_tuning(tuned)
     nb = scene.n_dynamic
-    for _ in range(a.warmup):
-        world.step_async(dt)
-    world.synchronize()
-
-    stream = torch.cuda.ExternalStream(world.stream())
-    world.set_timing(True)
-    world.stage_times()  # clear
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks = Clocks(local_rank)
-    clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(a.steps):
-        world.step_async(dt)
-    ev1.record(stream)
-    info = world.synchronize()
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    stages = world.stage_times()
-    world.set_timing(False)
-    ms = replicas.max_over_ranks(ms, dist, device="cuda")
     nb_all = replicas.sum_over_ranks(nb, dist, device="cuda")
-    ms_per_step = ms / a.steps
+    tuned = None if a.no_tune else _tune(scene, a.precision, a.warmup)
+
+    # headline: no stage events inside the timed region
+    world = _make(scene, a.precision, tuned)
+    ms, info, clk = _device_window(world, dt, a.warmup, a.steps, dist, local_rank, clocks=True)
     value = replicas.job_throughput(nb_all, a.steps, ms)
-
-    # counts for the roofline model (last step)
     keys, counts, _ = world.manifolds()
-    P = len(keys)
-    Cn = int(counts.sum())
-    units = {"body": nb, "pair": P, "contact": Cn, "contact_iter": Cn * (scene.iterations + 1)}
-    per_stage = {k: v[0] / max(v[1], 1) for k, v in stages.items()}
-    dom = max(per_stage, key=per_stage.get)
-    unit, bpu = BYTES[dom]
-    achieved = bpu * units[unit] / (per_stage[dom] / 1e3) / 1e9
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
-    else:
-        peak, peak_src = 6800.0, "fallback"
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        traffic = json.load(open(prof)).get(dom)
-
-    # end to end through the C ABI: step + host read-back of every body's state into a pinned
-    # host array (registered once, outside the timed region)
-    host = np.empty((len(scene.bodies), 14))
-    world.pin(host)
-    n_e2e = max(3, min(a.steps, 20))
-    flagged = int(world.step(dt, check=False))
-    world.bodies(out=host)
-    t0 = time.perf_counter()
-    for _ in range(n_e2e):
-        flagged += int(world.step(dt, check=False))
-        world.bodies(out=host)
-    e2e_s = time.perf_counter() - t0
-    world.unpin(host)
-    e2e_s = replicas.max_over_ranks(e2e_s, dist, device="cuda")
-    e2e = {"value": nb_all * n_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
-           "d2h_bytes_per_step": int(host.nbytes),
-           "note": "pk_world_step (synchronous) + pk_world_read_bodies (14 doubles per slot, packed on "
-                   "the device) into a pinned host array every step; dt is the only per-step input "
-                   "(a kernel argument)",
-           "steps_with_device_status": flagged}
-    raycast = None
-    if not a.no_raycast:
-        # world raycasts through the C ABI on the batch after the steps: 1 M rays spread over the
-        # worlds' bins, the call rebuilds the LBVH over every body and returns each ray's 16 nearest
-        rr = np.random.default_rng(7 + rank)
-        nr = 1_000_000
-        org = np.column_stack([rr.uniform(-2.5, 2.5, nr), rr.uniform(0.0, 6.0, nr), rr.uniform(-2.5, 2.5, nr)])
-        drc = rr.normal(size=(nr, 3))
-        wid = rr.integers(0, a.worlds, nr).astype(np.int32)
-        world.raycast_arrays(org[:1000], drc[:1000], 10.0, wid[:1000], cap=16)  # warm
-        t0 = time.perf_counter()
-        _, _, cnt = world.raycast_arrays(org, drc, 10.0, wid, cap=16)
-        rs = time.perf_counter() - t0
-        raycast = {"rays": nr, "ms": rs * 1e3, "rays_per_s": nr / rs, "hits_per_ray": float(cnt.mean()),
-                   "note": "pk_world_raycast with host arrays: LBVH rebuild over all bodies + one thread per ray, "
-                           "16 nearest hits kept per ray"}
+    P, Cn = len(keys), int(counts.sum())
     world.close()
 
+    # end to end through the C ABI, same window on a fresh copy: step + host read-back of every
+    # body's state into a pinned host array (registered once, before the window)
+    e2e = None
+    if not a.no_e2e:
+        world = _make(scene, a.precision, tuned)
+        host = np.empty((len(scene.bodies), 14))
+        world.pin(host)
+        for _ in range(a.warmup):
+            world.step(dt, check=False)
+        if dist:
+            dist.barrier()
+        flagged = 0
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            flagged += int(world.step(dt, check=False))
+            world.bodies(out=host)
+        e2e_s = time.perf_counter() - t0
+        world.unpin(host)
+        world.close()
+        e2e_s = replicas.max_over_ranks(e2e_s, dist, device="cuda")
+        e2e = {"value": nb_all * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": int(host.nbytes), "ms_per_step": e2e_s * 1e3 / a.steps,
+               "note": "fresh copy of the batch, same window: pk_world_step (synchronous) + pk_world_read_bodies "
+                       "(14 doubles per slot, packed on the device) into a pinned host array every step; dt is "
+                       "the only per-step input (a kernel argument)",
+               "steps_with_device_status": flagged}
+
+    # stage split and roofline: a third copy, same window, CUDA events between the stages
+    per_stage, roof = {}, None
+    if not a.no_stages:
+        world = _make(scene, a.precision, tuned)
+        for _ in range(a.warmup):
+            world.step_async(dt)
+        world.synchronize()
+        world.set_timing(True)
+        world.stage_times()  # clear
+        for _ in range(a.steps):
+            world.step_async(dt)
+        world.synchronize()
+        stages = world.stage_times()
+        world.close()
+        per_stage = {k: v[0] / max(v[1], 1) for k, v in stages.items()}
+        units = {"body": nb, "pair": P, "contact": Cn, "contact_iter": Cn * (scene.iterations + 1)}
+        dom = max(per_stage, key=per_stage.get)
+        unit, bpu = BYTES[dom]
+        achieved = bpu * units[unit] / (per_stage[dom] / 1e3) / 1e9
+        peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(peaks_path):
+            peak, peak_src = json.load(open(peaks_path))["hbm_gbs"], "measured"
+        else:
+            peak, peak_src = 6800.0, "fallback"
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(prof):
+            traffic = json.load(open(prof)).get(f"{a.precision}:{dom}")
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "peak_source": peak_src,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "model": f"{bpu:g} B per {unit} x {units[unit]} {unit}s per launch"}
+
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+           "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": a.precision, "data": "synthetic",
-           "config": config_dict(a, scene, world_size), "e2e": e2e,
-           "gpu_launches": info["launches"] * a.steps, "clocks": clk,
-           "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                        "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
-                        "traffic": traffic,
-                        "model": f"{bpu:g} B per {unit} x {units[unit]} {unit}s per launch"},
+           "config": config_dict(a, nb, world_size), "e2e": e2e,
+           "gpu_launches": info["launches"] * a.steps, "clocks": clk, "roofline": roof,
            "stage_ms_per_step": {k: round(v, 4) for k, v in per_stage.items()},
            "autotune": tuned,
            "counts": {"pairs": P, "contacts": Cn, "gjk": info["gjk"], "epa": info["epa"],
@@ -339,9 +397,21 @@ def run_ours(a, rank, world_size, local_rank):
                       "gjk_iterations": info["gjk_iterations"], "epa_iterations": info["epa_iterations"],
                       "epa_iterations_large_mesh": info["epa_iterations_large_mesh"],
                       "status": info["flags"]}}
-    if raycast:
-        out["raycast"] = raycast
 
+    if not a.no_precision_form:
+        # the other precision form on the same window
+        other = "f32" if a.precision == "f64" else "f64"
+        t2 = None if a.no_tune else _tune(scene, other, a.warmup)
+        world = _make(scene, other, t2)
+        ms2, _, _ = _device_window(world, dt, a.warmup, a.steps, dist, local_rank)
+        world.close()
+        v2 = replicas.job_throughput(nb_all, a.steps, ms2)
+        out["precision_form"] = {"dtype": other, "value": v2, "unit": UNIT, "ms_per_step": ms2 / a.steps,
+                                 f"ratio_to_{a.precision}": v2 / value, "autotune": t2,
+                                 "accuracy": "per-quantity error against the FP64 form: precision_f32_vs_f64"}
+
+    if rank == 0 and not a.no_raycast:
+        out["raycast"] = raycast_bench(scene, a, rank)
     if rank == 0 and not a.no_plain:
         out["plain_single_world"] = plain_world(a)
         out["batched_vs_plain"] = value / world_size / out["plain_single_world"]["value"]
@@ -356,35 +426,66 @@ def run_ours(a, rank, world_size, local_rank):
         kw = {"nworlds": a.worlds, "nmin": a.nmin, "nmax": a.nmax}
         sample = list(range(min(a.cpu_sample_worlds, a.worlds)))
         csteps = max(1, min(a.steps, 10))
-        v, cnb, wall = cpu_baseline(kw, sample, csteps, min(a.warmup, 3), 1)
+        v, cnb, wall = cpu_baseline(kw, sample, csteps, a.warmup, 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                                "sample": f"FP64 oracle, worlds 0-{len(sample) - 1} of the batch ({cnb} dynamic "
-                                         f"bodies), {csteps} steps after {min(a.warmup, 3)} warm-up steps, "
-                                         f"1 thread, {wall:.1f} s"}
+                                         f"bodies), steps {a.warmup + 1}-{a.warmup + csteps} after {a.warmup} "
+                                         f"warm-up steps, 1 thread, {wall:.1f} s"}
     if dist:
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
 
 
-def precision_report(steps=240, n=1000):
-    """FP32 precision form against FP64 on config 1 (1,000 boxes), 240 steps, per quantity. The FP64
-    run is the device FP64 form, which is bit-identical to the FP64 oracle
-    (tests/test_gpu_world_parity.py). Control: the FP64 form again with one body moved by 1e-12 m,
-    which shows how far the pile's own dynamics amplify a perturbation of that size."""
+def raycast_bench(scene, a, rank):
+    """World raycasts through the C ABI on the batch after the window's steps: 1 M rays spread over
+    the worlds' bins; the call rebuilds the LBVH over every body and returns each ray's 16 nearest."""
+    import numpy as np
+
+    world = _make(scene, a.precision, None)
+    for _ in range(a.warmup):
+        world.step_async(scene.dt)
+    world.synchronize()
+    rr = np.random.default_rng(7 + rank)
+    nr = 1_000_000
+    org = np.column_stack([rr.uniform(-2.5, 2.5, nr), rr.uniform(0.0, 6.0, nr), rr.uniform(-2.5, 2.5, nr)])
+    drc = rr.normal(size=(nr, 3))
+    wid = rr.integers(0, a.worlds, nr).astype(np.int32)
+    world.raycast_arrays(org[:1000], drc[:1000], 10.0, wid[:1000], cap=16)  # warm
+    t0 = time.perf_counter()
+    _, _, cnt = world.raycast_arrays(org, drc, 10.0, wid, cap=16)
+    rs = time.perf_counter() - t0
+    world.close()
+    return {"rays": nr, "ms": rs * 1e3, "rays_per_s": nr / rs, "hits_per_ray": float(cnt.mean()),
+            "note": "pk_world_raycast with host arrays: LBVH rebuild over all bodies + one thread per ray, "
+                    "16 nearest hits kept per ray"}
+
+
+def _rounded_to_f32(scene):
+    """The scene with every value the FP32 form rounds at upload rounded to float32 (pose,
+    velocities, mass, inertia, box half extents), still stepped in FP64."""
     import copy
 
     import numpy as np
-    from physkit_gb300 import scenes
 
-    scene = scenes.config1(n=n)
-    dyn = scene.bodies["type"] == 0
-    pert = copy.deepcopy(scene)
-    k0 = int(np.nonzero(dyn)[0][0])
-    pert.bodies["pos"][k0, 0] += 1e-12
-    w32, _ = scenes.make_world(scene, precision="f32")
-    w64, _ = scenes.make_world(scene, precision="f64")
-    wpp, _ = scenes.make_world(pert, precision="f64")
+    s = copy.deepcopy(scene)
+    for f in ("pos", "quat", "vel", "ang_vel", "mass", "inertia", "restitution", "friction"):
+        s.bodies[f] = s.bodies[f].astype(np.float32).astype(np.float64)
+    s.shapes = [(sh[0],) + tuple(float(np.float32(x)) for x in sh[1:]) if sh[0] == "box" else sh
+                for sh in s.shapes]
+    return s
+
+
+def precision_report(steps=240):
+    """FP32 precision form against FP64 per quantity, 240 steps, on two scenes. The FP64 run is
+    the device FP64 form, bit-identical to the FP64 oracle (tests/test_gpu_world_parity.py).
+
+    config1 (1,000 boxes falling into a pile): control = the FP64 form started from the initial
+    state rounded to float32 (an FP32-sized perturbation, once) against the FP64 form; it shows how
+    far the pile's own dynamics amplify FP32 rounding, which bounds what any FP32 form can reach.
+    resting stacks (scenes.resting_stacks): separated stacks of aligned boxes, not chaotic."""
+    import numpy as np
+    from physkit_gb300 import scenes
 
     def body_err(a, b):
         dpos = np.linalg.norm(a[:, 0:3] - b[:, 0:3], axis=1)
@@ -410,26 +511,45 @@ def precision_report(steps=240, n=1000):
         return {"manifolds_compared": same, "depth_abs_max_m": float(max(dd)) if dd else 0.0,
                 "normal_abs_max": float(max(dn)) if dn else 0.0}
 
-    rep = {}
-    pairs_equal = 0
-    for s in range(1, steps + 1):
-        w32.step(scene.dt, check=False)
-        w64.step(scene.dt, check=False)
-        wpp.step(scene.dt, check=False)
-        p32, p64 = w32.pairs(), w64.pairs()
-        pairs_equal += int(len(p32) == len(p64) and bool(np.array_equal(np.sort(p32), np.sort(p64))))
-        if s in (60, 120, 240):
-            a, b, c = w32.bodies()[dyn], w64.bodies()[dyn], wpp.bodies()[dyn]
-            r = body_err(a, b)
-            r.update(contact_err(w32, w64))
-            r["pairs_f32_vs_f64"] = [int(len(p32)), int(len(p64))]
-            r["steps_with_equal_pair_set"] = pairs_equal
-            r["control_fp64_1e-12m"] = body_err(c, b)
-            rep[f"step{s}"] = r
-    for w in (w32, w64, wpp):
-        w.close()
-    rep["workload"] = (f"config1: {n} boxes + ground, dt=1/120; FP32 form vs FP64 form; control: FP64 form with "
-                       f"one body moved 1e-12 m vs FP64 form")
+    def same_pairs(wa, wb):
+        p, q = wa.pairs(), wb.pairs()
+        return int(len(p) == len(q) and bool(np.array_equal(np.sort(p), np.sort(q))))
+
+    def run(scene, control, marks):
+        dyn = scene.bodies["type"] == 0
+        w32, _ = scenes.make_world(scene, precision="f32")
+        w64, _ = scenes.make_world(scene, precision="f64")
+        wct = scenes.make_world(control, precision="f64")[0] if control is not None else None
+        rep, eq32, eqct = {}, 0, 0
+        for s in range(1, steps + 1):
+            for w in (w32, w64, wct):
+                if w is not None:
+                    w.step(scene.dt, check=False)
+            eq32 += same_pairs(w32, w64)
+            if wct is not None:
+                eqct += same_pairs(wct, w64)
+            if s in marks:
+                a, b = w32.bodies()[dyn], w64.bodies()[dyn]
+                r = body_err(a, b)
+                r.update(contact_err(w32, w64))
+                r["steps_with_equal_pair_set"] = eq32
+                if wct is not None:
+                    r["control_fp64_from_f32_rounded_start"] = dict(body_err(wct.bodies()[dyn], b),
+                                                                    steps_with_equal_pair_set=eqct)
+                rep[f"step{s}"] = r
+        for w in (w32, w64, wct):
+            if w is not None:
+                w.close()
+        return rep
+
+    c1 = scenes.config1(n=1000)
+    rep = {"config1": run(c1, _rounded_to_f32(c1), (60, 120, 240)),
+           "resting_boxes": run(scenes.resting_stacks(height=1), None, (240,)),
+           "resting_stacks": run(scenes.resting_stacks(height=3), None, (240,))}
+    rep["workload"] = ("config1: 1,000 boxes + ground, dt=1/120, FP32 form vs FP64 form; control: FP64 form from "
+                       "the float32-rounded initial state vs FP64 form. resting_boxes / resting_stacks: "
+                       "10 x 10 separated stacks of 1 / 3 aligned boxes dropped 1 cm onto a ground box, FP32 vs FP64 "
+                       "(the FP64 oracle with its state rounded to float32 after every step reaches 1.1e-6 / 3.4e-5)")
     return rep
 
 
@@ -442,7 +562,7 @@ def plain_world(a):
     scene = scenes.config1()
     world, _ = scenes.make_world(scene, precision=a.precision)
     world.capture(scene.dt)
-    for _ in range(5):
+    for _ in range(a.warmup):
         world.step_graph()
     world.synchronize()
     stream = torch.cuda.ExternalStream(world.stream())
@@ -455,8 +575,9 @@ def plain_world(a):
     world.synchronize()
     ms = ev0.elapsed_time(ev1)
     world.close()
-    return {"workload": "config1: 1,000 boxes + ground, one world, CUDA-graph replay", "value": scene.n_dynamic * n / (ms / 1e3),
-            "unit": UNIT, "ms_per_step": ms / n}
+    return {"workload": f"config1: 1,000 boxes + ground, one world, {a.precision.upper()}, CUDA-graph replay, "
+                        f"steps {a.warmup + 1}-{a.warmup + n}",
+            "value": scene.n_dynamic * n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / n}
 
 
 def main():

@@ -41,6 +41,7 @@ extern "C" {
 #define PK_STATUS_COLOUR_CAP 4      /* more than 512 colouring rounds in one world */
 #define PK_STATUS_TRAVERSAL_STACK 8 /* LBVH traversal stack overflow */
 #define PK_STATUS_NAN 16            /* a non-finite position appeared */
+#define PK_STATUS_CONTACT_OVERFLOW 32 /* more pairs with contacts (or in EPA) than max_contact_pairs */
 
 enum
 {
@@ -66,6 +67,9 @@ typedef struct pk_world_desc
     int32_t max_bodies_per_world; /* 0: max_bodies */
     int32_t max_shape_vertices;   /* 0: 65536 */
     int32_t max_shapes;           /* 0: 1024 */
+    int32_t max_contact_pairs;    /* pairs with contact rows (and pairs in EPA) per step; 0: max_pairs.
+                                     Contact rows take ~1 KB per pair, so a world with many more
+                                     broadphase pairs than touching pairs sets this lower */
 } pk_world_desc;
 
 typedef struct pk_body_desc /* object_desc (object.h:15-109) */
@@ -280,7 +284,10 @@ int pk_world_read_colours(pk_world *w, uint64_t *keys, int32_t *colours, int32_t
                           int32_t *ncolours_world0);
 
 /* Narrowphase (gjk_epa, collision.cpp:512-518) on n primitive shape pairs; out has 10 doubles per
- * pair: normal3 world_a3 world_b3 depth. hit[i] = 1 on collision. */
+ * pair: normal3 world_a3 world_b3 depth. hit[i] = 1 on collision. Returns PK_ERR_DEVICE_STATUS
+ * (with every result written) when a pair's EPA hit a fixed capacity of this implementation (face,
+ * horizon or flood-fill stack): that pair's result is the best face found so far, which can differ
+ * from the reference's. The reference's own 64-expansion limit is not an error. */
 int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
                int32_t *hit);
 
@@ -294,7 +301,10 @@ int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b
  * The first call on a device looks up the array's device address; make that first call before
  * any stream capture. All calls share the one array: calls whose GPU work overlaps (several
  * threads, or several world objects on one device) race and must be serialised by the caller.
- * The world's shapes must already be on the device (after a pk_body_add, a step or a pk_collide). */
+ * The world's shapes must already be on the device (after a pk_body_add, a step or a pk_collide).
+ * Call it with the device current on which the world was created (PK_ERR_INVALID otherwise); a
+ * device reset ends the world and this cache with it. Capacity status as for pk_collide
+ * (PK_ERR_DEVICE_STATUS with every result written). */
 #define PK_COLLIDE_NOALLOC_MAX 4096
 int pk_collide_noalloc(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
                        int32_t *hit);

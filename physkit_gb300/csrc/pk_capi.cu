@@ -98,6 +98,7 @@ struct pk_world
     std::vector<pk::Wake> wakes; // fired, not yet returned by pk_world_dispatch
     size_t wake_head = 0;
     int dispatched_step = 0;     // host step whose events were last offered to the waiters
+    int device = 0;              // CUDA device current at pk_world_create: its stream and buffers live there
 };
 
 // Allocation-free narrowphase (pk_collide_noalloc). Its device staging lives in this file-scope
@@ -110,7 +111,8 @@ constexpr int kNoAllocMax = PK_COLLIDE_NOALLOC_MAX;
 constexpr size_t kNoAllocSpecs = sizeof(pk_collide_shape) * kNoAllocMax; // one side's descriptors
 constexpr size_t kNoAllocOut = sizeof(double) * 10 * kNoAllocMax;
 constexpr size_t kNoAllocInts = sizeof(int32_t) * kNoAllocMax;
-constexpr size_t kNoAllocBytes = 2 * kNoAllocSpecs + kNoAllocOut + 2 * kNoAllocInts;
+// + 256 bytes at the end: the OR of every pair's status bits
+constexpr size_t kNoAllocBytes = 2 * kNoAllocSpecs + kNoAllocOut + 2 * kNoAllocInts + 256;
 } // namespace
 
 static __device__ __align__(256) unsigned char g_collide_scratch[kNoAllocBytes];
@@ -123,7 +125,9 @@ constexpr int kMaxDevices = 64;
 unsigned char *g_scratch_ptr[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
-int scratch_for_current_device(unsigned char **out)
+// The world's stream and shape tables live on the device that was current at pk_world_create, so
+// the call must run with that device current; any other current device is PK_ERR_INVALID.
+int scratch_for_world_device(int world_device, unsigned char **out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -132,7 +136,7 @@ int scratch_for_current_device(unsigned char **out)
         g_last_cuda = int(e);
         return PK_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) return PK_ERR_INVALID;
+    if (dev != world_device || dev < 0 || dev >= kMaxDevices) return PK_ERR_INVALID;
     std::lock_guard<std::mutex> lk(g_scratch_mu);
     if (!g_scratch_ptr[dev])
     {
@@ -194,35 +198,40 @@ int pk_collide_noalloc(pk_world *w, const pk_collide_shape *a, const pk_collide_
     if (n == 0) return PK_OK;
     if (w->shapes_dirty) return PK_ERR_INVALID; // shapes are uploaded by a step, a body add or pk_collide first
     unsigned char *base = nullptr;
-    if (int rc = scratch_for_current_device(&base)) return rc;
+    if (int rc = scratch_for_world_device(w->device, &base)) return rc;
     unsigned char *da = base, *db = base + kNoAllocSpecs;
     double *dout = reinterpret_cast<double *>(base + 2 * kNoAllocSpecs);
     int32_t *dhit = reinterpret_cast<int32_t *>(base + 2 * kNoAllocSpecs + kNoAllocOut);
     int32_t *dst = dhit + kNoAllocMax;
+    int32_t *dany = dst + kNoAllocMax;
     cudaStream_t st = static_cast<cudaStream_t>(w->eng->stream());
     size_t spec_bytes = sizeof(pk_collide_shape) * size_t(n);
+    int32_t any = 0; // copied back into this stack variable: nothing is allocated, on the host either
     cudaError_t e;
     if ((e = cudaMemcpyAsync(da, a, spec_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
         (e = cudaMemcpyAsync(db, b, spec_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-        // the array keeps the previous call's results: misses leave `out` untouched, so clear it
-        (e = cudaMemsetAsync(dout, 0, sizeof(double) * 10 * size_t(n), st)) != cudaSuccess)
+        // the array keeps the previous call's results: misses leave `out` untouched, so clear it,
+        // and the status word must start at zero
+        (e = cudaMemsetAsync(dout, 0, sizeof(double) * 10 * size_t(n), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(dany, 0, sizeof(int32_t), st)) != cudaSuccess)
     {
         g_last_cuda = int(e);
         return PK_ERR_CUDA;
     }
-    if (w->eng->collide_device(da, db, n, dout, dhit, dst))
+    if (w->eng->collide_device(da, db, n, dout, dhit, dst, dany))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
     }
     if ((e = cudaMemcpyAsync(out, dout, sizeof(double) * 10 * size_t(n), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (e = cudaMemcpyAsync(hit, dhit, sizeof(int32_t) * size_t(n), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&any, dany, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
     {
         g_last_cuda = int(e);
         return PK_ERR_CUDA;
     }
-    return PK_OK;
+    return any ? PK_ERR_DEVICE_STATUS : PK_OK;
 }
 
 int pk_last_cuda_error(void) { return g_last_cuda; }
@@ -239,7 +248,8 @@ int pk_world_create(const pk_world_desc *desc, pk_world **out)
         g_last_cuda = int(e);
         return PK_ERR_NO_DEVICE;
     }
-    if (desc->max_bodies <= 0 || desc->max_worlds <= 0 || desc->solver_iterations < 0) return PK_ERR_INVALID;
+    if (desc->max_bodies <= 0 || desc->max_worlds <= 0 || desc->solver_iterations < 0 || desc->max_contact_pairs < 0)
+        return PK_ERR_INVALID;
     if (desc->precision != PK_PRECISION_F64 && desc->precision != PK_PRECISION_F32) return PK_ERR_INVALID;
     auto *w = new (std::nothrow) pk_world;
     if (!w) return PK_ERR_CAPACITY;
@@ -247,6 +257,8 @@ int pk_world_create(const pk_world_desc *desc, pk_world **out)
     pk::EngineConfig &c = w->cfg;
     c.body_cap = desc->max_bodies;
     c.pair_cap = desc->max_pairs > 0 ? desc->max_pairs : 8 * desc->max_bodies;
+    c.contact_cap = desc->max_contact_pairs > 0 && desc->max_contact_pairs < c.pair_cap ? desc->max_contact_pairs
+                                                                                        : c.pair_cap;
     c.max_worlds = desc->max_worlds;
     c.vert_cap = desc->max_shape_vertices > 0 ? desc->max_shape_vertices : 65536;
     c.shape_cap = desc->max_shapes > 0 ? desc->max_shapes : 1024;
@@ -262,6 +274,7 @@ int pk_world_create(const pk_world_desc *desc, pk_world **out)
     int sms = 148;
     int dev = 0;
     cudaGetDevice(&dev);
+    w->device = dev;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     auto blocks_for = [&](long long n)
     {
@@ -1439,6 +1452,8 @@ int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
     }
+    for (int i = 0; i < n; ++i)
+        if (status[size_t(i)]) return PK_ERR_DEVICE_STATUS; // results written; a pair hit a capacity cap
     return PK_OK;
 }
 

@@ -51,6 +51,7 @@ enum : int
     ST_COLOUR_CAP = 1 << 2,
     ST_TRAVERSAL_STACK = 1 << 3,
     ST_NAN = 1 << 4,
+    ST_CONTACT_OVERFLOW = 1 << 5,
 };
 
 constexpr int kMaxColours = 512;
@@ -228,15 +229,20 @@ template <class T> struct Dev
     int *gjk_list2;        // the items the separating-direction check left for GJK, same two classes
     int *gjk2_count;
     int *gjk2_count_heavy;
-    int *epa_list;
+    int *epa_list;         // contact_cap entries: light items from the start, heavy ones from the end
     Simplex<T> *epa_simplex;
     int *epa_count;
     int *epa_count_heavy;
+    int *epa_total;        // items admitted to the EPA list (at most contact_cap)
     unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
     int *clist;            // pairs of active worlds whose new manifold holds contacts (any order)
     int *ccount;
-    RowT<T> *rows;         // 4 per pair, read-only while the solver sweeps
-    double *racc;          // 12 per pair: accumulated impulses (normal, t1, t2) of the 4 rows
+    // Contact rows live at the pair's position in clist (rowidx), so they take memory only for the
+    // pairs that have contacts: at most contact_cap of them per step.
+    int contact_cap;
+    int *rowidx;           // per pair: its row block (valid while rowmask != 0)
+    RowT<T> *rows;         // 4 per row block, read-only while the solver sweeps
+    double *racc;          // 12 per row block: accumulated impulses (normal, t1, t2) of the 4 rows
     float *raccf;          // FP32 form: running totals in FP32 (clamp decisions, warm start)
     float *rdel;           // FP32 form: this step's change, added to racc once after the sweeps
     const JointDev<T> *joints; // ordered by (world, type, arena slot)
@@ -341,6 +347,7 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.gjk2_count = 0;
         *d.gjk2_count_heavy = 0;
         *d.ccount = 0;
+        *d.epa_total = 0;
         *d.all_small = 1;
         d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
         *d.epoch += 1;
@@ -1369,11 +1376,20 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
         V3<T> sep{T(0), T(0), T(0)};
         bool enclosed = gjk(A, B, s, &sep);
         atomicAdd(d.np_iters, (unsigned long long)s.iters);
-        if (enclosed)
+        // admitted first against the list's capacity, so the two ends never meet
+        const bool admit = enclosed && warp_push(d.epa_total) < d.contact_cap;
+        if (enclosed && !admit)
+        {
+            // no room for this pair's EPA: flagged, and the pair keeps last step's contacts
+            atomicOr(d.status, ST_CONTACT_OVERFLOW);
+            Collision<T> none;
+            manifold_update(d, p, d.old_idx[p], A, B, false, none);
+        }
+        else if (admit)
         {
             int j;
             if (A.ncl > 0 || B.ncl > 0)
-                j = d.pair_cap - 1 - warp_push(d.epa_count_heavy);
+                j = d.contact_cap - 1 - warp_push(d.epa_count_heavy);
             else
                 j = warp_push(d.epa_count);
             d.epa_list[j] = p;
@@ -1395,7 +1411,7 @@ __global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa(Dev<T> d,
     const int n = nh + *d.epa_count;
     PK_GRID_STRIDE(i, n)
     {
-        int j = list_slot(i, nh, d.pair_cap);
+        int j = list_slot(i, nh, d.contact_cap);
         int p = d.epa_list[j];
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
@@ -1420,9 +1436,12 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
     // the pairs of active worlds with contacts, queued by the manifold update; every other pair
     // was given no rows (rowmask 0, colour -2) by the narrowphase pre-pass
     const int nc = *d.ccount;
+    if (nc > d.contact_cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(d.status, ST_CONTACT_OVERFLOW);
     PK_GRID_STRIDE(ci, nc)
     {
         const int p = d.clist[ci];
+        if (ci >= d.contact_cap) continue; // no room for rows: the pair is not solved (flagged)
+        d.rowidx[p] = ci;
         const Manifold<T> &m = d.man_new[p];
         const int mn = m.n;
         uint64_t val = sval[p];
@@ -1526,18 +1545,18 @@ template <class T> __global__ void k_contact_setup(Dev<T> d, const uint64_t *__r
                 rf.inv22 = row.inv22;
                 rf.mu = row.mu;
                 rf.pad = 0.0f;
-                d.rows[4 * p + k] = rf;
+                d.rows[4 * size_t(ci) + k] = rf;
                 for (int j = 0; j < 3; ++j)
                 {
-                    d.raccf[12 * size_t(p) + 3 * k + j] = float(c.imp[j]);
-                    d.rdel[12 * size_t(p) + 3 * k + j] = 0.0f;
+                    d.raccf[12 * size_t(ci) + 3 * k + j] = float(c.imp[j]);
+                    d.rdel[12 * size_t(ci) + 3 * k + j] = 0.0f;
                 }
             }
             else
-                d.rows[4 * p + k] = row;
-            d.racc[12 * size_t(p) + 3 * k + 0] = c.imp[0];
-            d.racc[12 * size_t(p) + 3 * k + 1] = c.imp[1];
-            d.racc[12 * size_t(p) + 3 * k + 2] = c.imp[2];
+                d.rows[4 * size_t(ci) + k] = row;
+            d.racc[12 * size_t(ci) + 3 * k + 0] = c.imp[0];
+            d.racc[12 * size_t(ci) + 3 * k + 1] = c.imp[1];
+            d.racc[12 * size_t(ci) + 3 * k + 2] = c.imp[2];
             mask |= uint8_t(1u << k);
         }
         d.rowmask[p] = mask;
@@ -1982,8 +2001,9 @@ template <class R> __device__ __forceinline__ R ldg_row(const R *src)
 __device__ __forceinline__ void solve_rows(const Dev<float> &d, int p, SBody<float> &A, SBody<float> &B, bool warm)
 {
     const uint8_t mask = d.rowmask[p];
+    const size_t ri = size_t(d.rowidx[p]);
     float tot[12];
-    float4 *tp = reinterpret_cast<float4 *>(d.raccf + 12 * size_t(p));
+    float4 *tp = reinterpret_cast<float4 *>(d.raccf + 12 * ri);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
@@ -1993,7 +2013,7 @@ __device__ __forceinline__ void solve_rows(const Dev<float> &d, int p, SBody<flo
         tot[4 * i + 2] = v.z;
         tot[4 * i + 3] = v.w;
     }
-    const RowF *rp = d.rows + 4 * size_t(p);
+    const RowF *rp = d.rows + 4 * ri;
     if (warm)
     {
 #pragma unroll
@@ -2002,7 +2022,7 @@ __device__ __forceinline__ void solve_rows(const Dev<float> &d, int p, SBody<flo
         return;
     }
     float del[12];
-    float4 *dp = reinterpret_cast<float4 *>(d.rdel + 12 * size_t(p));
+    float4 *dp = reinterpret_cast<float4 *>(d.rdel + 12 * ri);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
@@ -2014,7 +2034,7 @@ __device__ __forceinline__ void solve_rows(const Dev<float> &d, int p, SBody<flo
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-        if (mask & (1u << q)) solve_contact_f32(A, B, ldg_row(rp + q), tot + 3 * q, del + 3 * q, d.racc + 12 * size_t(p) + 3 * q);
+        if (mask & (1u << q)) solve_contact_f32(A, B, ldg_row(rp + q), tot + 3 * q, del + 3 * q, d.racc + 12 * ri + 3 * q);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
@@ -2026,8 +2046,9 @@ __device__ __forceinline__ void solve_rows(const Dev<float> &d, int p, SBody<flo
 __device__ __forceinline__ void solve_rows(const Dev<double> &d, int p, SBody<double> &A, SBody<double> &B, bool warm)
 {
     const uint8_t mask = d.rowmask[p];
+    const size_t ri = size_t(d.rowidx[p]);
     double acc[12];
-    double2 *ap = reinterpret_cast<double2 *>(d.racc + 12 * size_t(p));
+    double2 *ap = reinterpret_cast<double2 *>(d.racc + 12 * ri);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
     {
@@ -2035,7 +2056,7 @@ __device__ __forceinline__ void solve_rows(const Dev<double> &d, int p, SBody<do
         acc[2 * i] = v.x;
         acc[2 * i + 1] = v.y;
     }
-    const Row<double> *rp = d.rows + 4 * size_t(p);
+    const Row<double> *rp = d.rows + 4 * ri;
 #pragma unroll
     for (int q = 0; q < 4; ++q)
     {
@@ -2057,7 +2078,7 @@ __device__ __forceinline__ void solve_rows(const Dev<double> &d, int p, SBody<do
 // step's change to the FP64 accumulator here, once).
 template <class T> __device__ __forceinline__ void store_impulses(const Dev<T> &d, int p, int q)
 {
-    const size_t o = 12 * size_t(p) + 3 * q;
+    const size_t o = 12 * size_t(d.rowidx[p]) + 3 * q;
     Contact<T> &c = d.man_new[p].c[q];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -2815,7 +2836,7 @@ struct ShapeSpec
 };
 template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const ShapeSpec *sb, int n, const T *verts,
                                                    const ShapeRange *ranges, const T *clusters, const T *rmax,
-                                                   double *out, int *hit, int *status)
+                                                   double *out, int *hit, int *status, int *status_any)
 {
     PK_GRID_STRIDE(i, n)
     {
@@ -2869,6 +2890,7 @@ template <class T> __global__ void k_collide_batch(const ShapeSpec *sa, const Sh
         bool h = gjk_epa(s[0], s[1], es, c, &st);
         hit[i] = h ? 1 : 0;
         status[i] = st;
+        if (st && status_any) atomicOr(status_any, st); // a capacity of this implementation was hit
         double *o = out + 10 * i;
         if (h)
         {

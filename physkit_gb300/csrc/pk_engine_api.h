@@ -11,6 +11,7 @@ struct EngineConfig
 {
     int body_cap = 0;
     int pair_cap = 0;
+    int contact_cap = 0; // pairs with contact rows per step (0: pair_cap)
     int max_worlds = 1;
     int vert_cap = 0;
     int shape_cap = 0;
@@ -85,7 +86,6 @@ public:
     virtual int read_events(uint64_t *keys, int *kinds, int cap) = 0;
     virtual int read_colours(uint64_t *keys, int *colours, int cap, int *ncolours_world0) = 0;
     virtual int collide(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) = 0;
-    // Same narrowphase launch on device buffers the caller provides; allocates nothing.
     virtual int set_joints(const int *ints, const double *params, const double *acc, int n, const int *jstart,
                            const int *jend) = 0;
     virtual int read_joint_acc(double *acc, int n) = 0;
@@ -93,8 +93,10 @@ public:
     // rays: 8 doubles each (origin, direction, distance limit, world); per ray up to `cap` nearest
     // hits (device slot, distance) ordered by (distance, slot), and the total hit count
     virtual int raycast(const double *rays, int n, int cap, int *counts, int *slots, double *dists) = 0;
+    // The narrowphase launch of collide on device buffers the caller provides; allocates nothing.
+    // status_any_dev (may be null): OR of every pair's status bits
     virtual int collide_device(const void *specs_a_dev, const void *specs_b_dev, int n, double *out_dev,
-                               int *hit_dev, int *status_dev) = 0;
+                               int *hit_dev, int *status_dev, int *status_any_dev) = 0;
     virtual int capture_graph(double dt) = 0;        // record the step as CUDA graphs
     virtual int launch_graph() = 0;                  // replay one captured step
     virtual void *stream() = 0;

@@ -119,10 +119,12 @@ public:
         PK_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
         PK_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
         const size_t N = size_t(cfg.body_cap), P = size_t(cfg.pair_cap), W = size_t(cfg.max_worlds);
+        const size_t CC = size_t(cfg.contact_cap > 0 && cfg.contact_cap < cfg.pair_cap ? cfg.contact_cap : cfg.pair_cap);
         Dev<T> &d = d_;
         std::memset(&d, 0, sizeof(d));
         d.max_worlds = cfg.max_worlds;
         d.pair_cap = cfg.pair_cap;
+        d.contact_cap = int(CC);
         d.lbits = cfg.lbits;
         d.wbits = cfg.wbits;
         d.iterations = cfg.iterations;
@@ -153,6 +155,7 @@ public:
         d.gjk2_count = counters_ + 19;
         d.gjk2_count_heavy = counters_ + 20;
         d.all_small = counters_ + 21;
+        d.epa_total = counters_ + 22;
         PK_CUDA(alloc(&d.jstart, W));
         PK_CUDA(alloc(&d.jend, W));
         PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
@@ -223,12 +226,13 @@ public:
         PK_CUDA(alloc(&d.gjk_list, P));
         PK_CUDA(alloc(&d.clist, P));
         PK_CUDA(alloc(&d.gjk_list2, P));
-        PK_CUDA(alloc(&d.epa_list, P));
-        PK_CUDA(alloc(&d.epa_simplex, P));
-        PK_CUDA(alloc(&d.rows, 4 * P));
-        PK_CUDA(alloc(&d.racc, 12 * P));
-        if (sizeof(T) == 4) PK_CUDA(alloc(&d.raccf, 12 * P));
-        if (sizeof(T) == 4) PK_CUDA(alloc(&d.rdel, 12 * P));
+        PK_CUDA(alloc(&d.epa_list, CC));
+        PK_CUDA(alloc(&d.epa_simplex, CC));
+        PK_CUDA(alloc(&d.rowidx, P));
+        PK_CUDA(alloc(&d.rows, 4 * CC));
+        PK_CUDA(alloc(&d.racc, 12 * CC));
+        if (sizeof(T) == 4) PK_CUDA(alloc(&d.raccf, 12 * CC));
+        if (sizeof(T) == 4) PK_CUDA(alloc(&d.rdel, 12 * CC));
         PK_CUDA(alloc(&d.rowmask, P));
         PK_CUDA(alloc(&d.colour, P));
         PK_CUDA(alloc(&d.colour_tmp, P));
@@ -695,7 +699,7 @@ public:
         PK_CUDA(cudaMemcpy(db, specs_b, sizeof(ShapeSpec) * n, cudaMemcpyHostToDevice));
         PK_CUDA(cudaMemset(dout, 0, sizeof(double) * 10 * n));
         k_collide_batch<T><<<(n + 127) / 128, 128, 0, st_>>>(da, db, n, d_.verts, shape_range_, d_.clusters,
-                                                              shape_rmax_, dout, dhit, dst);
+                                                              shape_rmax_, dout, dhit, dst, nullptr);
         PK_CUDA(cudaGetLastError());
         PK_CUDA(cudaStreamSynchronize(st_));
         PK_CUDA(cudaMemcpy(out, dout, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost));
@@ -836,12 +840,14 @@ public:
         return 0;
     }
 
-    int collide_device(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status) override
+    int collide_device(const void *specs_a, const void *specs_b, int n, double *out, int *hit, int *status,
+                       int *status_any) override
     {
         if (n <= 0) return 0;
         k_collide_batch<T><<<(n + 127) / 128, 128, 0, st_>>>(static_cast<const ShapeSpec *>(specs_a),
                                                               static_cast<const ShapeSpec *>(specs_b), n, d_.verts,
-                                                              shape_range_, d_.clusters, shape_rmax_, out, hit, status);
+                                                              shape_range_, d_.clusters, shape_rmax_, out, hit, status,
+                                                              status_any);
         PK_CUDA(cudaGetLastError());
         return 0;
     }
@@ -962,7 +968,7 @@ private:
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
-                      d_.epa_list, d_.epa_simplex, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
+                      d_.epa_list, d_.epa_simplex, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.srec, d_.crec, d_.owner, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};

@@ -98,10 +98,9 @@ def hull_shape(rng, scale):
     tris = hull.simplices.copy()
     # orient every triangle outward (signed-tetrahedron volume of mesh::volume, mesh.cpp:139-151)
     c = p.mean(axis=0)
-    for t in tris:
-        a, b, d = p[t[0]], p[t[1]], p[t[2]]
-        if np.dot(np.cross(b - a, d - a), a - c) < 0:
-            t[1], t[2] = t[2], t[1]
+    a, b, d = p[tris[:, 0]], p[tris[:, 1]], p[tris[:, 2]]
+    flip = np.einsum("ij,ij->i", np.cross(b - a, d - a), a - c) < 0
+    tris[flip, 1], tris[flip, 2] = tris[flip, 2], tris[flip, 1].copy()
     vol = float(abs(hull.volume))
     lo, hi = p.min(axis=0), p.max(axis=0)
     he = 0.5 * (hi - lo)
@@ -254,11 +253,15 @@ def config3(nworlds=4096, nmin=8, nmax=2048, seed=None, kinds=(0, 1, 2), half=2.
                  shapes, recs, nworlds, dt=1 / 120, steps=240, iterations=10)
 
 
-def config5(n=1_000_000, seed=None, half=10.0, nradii=32):
-    """Spheres poured into a 20 x 20 m open box; radii drawn from a pool of `nradii` lognormal
-    radii so the UV meshes are shared."""
+def config5(n=1_000_000, seed=None, half=10.0, nradii=32, spacing=0.125):
+    """Spheres (r ~ lognormal(ln 0.05, 0.3)) poured into a (2*half) m square open box: they start
+    on a jittered cubic lattice of `spacing` just above the floor, filling the box's footprint layer
+    by layer, and fall into a dense pile in the first ~100 steps (about 6 contacts per body once
+    settled). Radii come from a pool of `nradii` lognormal radii so the UV meshes are shared.
+    config5(n=10_000, half=1.0) is a sub-region replica of the full pile: the same lattice, depth
+    and radii on a 2 x 2 m footprint."""
     rng = rng_for(5, seed)
-    thick, wall_h = 0.25, 10.0
+    thick, wall_h = 0.25, 4.0
     shapes = [("box", half + thick, thick, half + thick), ("box", thick, wall_h, half + 2 * thick),
               ("box", half + 2 * thick, wall_h, thick)]
     radii = np.exp(rng.normal(math.log(0.05), 0.3, nradii))
@@ -267,19 +270,58 @@ def config5(n=1_000_000, seed=None, half=10.0, nradii=32):
     recs = bin_statics(shapes, 0, half, wall_h, thick)
     r = _records(n)
     pick = rng.integers(0, nradii, n)
-    for i in range(n):
-        m, I = sphere_mass(radii[pick[i]])
-        r[i]["shape"] = 3 + pick[i]
-        r[i]["mass"] = m
-        r[i]["inertia"] = np.diag(I).reshape(-1)
-    r["pos"][:, 0] = rng.uniform(-half + 0.2, half - 0.2, n)
-    r["pos"][:, 2] = rng.uniform(-half + 0.2, half - 0.2, n)
-    r["pos"][:, 1] = rng.uniform(0.1, 0.1 + n * 2e-5, n)
+    rad = radii[pick]
+    m = RHO * 4.0 / 3.0 * math.pi * rad ** 3
+    r["shape"] = 3 + pick
+    r["mass"] = m
+    r["inertia"][:, 0] = r["inertia"][:, 4] = r["inertia"][:, 8] = 0.4 * m * rad * rad
+    side = int((2.0 * half - 2.0 * 0.1) // spacing)  # lattice sites per row, 0.1 m clear of the walls
+    k = np.arange(n)
+    layer, cell = k // (side * side), k % (side * side)
+    jit = rng.uniform(-0.01, 0.01, size=(n, 2))
+    r["pos"][:, 0] = -half + 0.1 + (cell % side + 0.5) * spacing + jit[:, 0]
+    r["pos"][:, 2] = -half + 0.1 + (cell // side + 0.5) * spacing + jit[:, 1]
+    r["pos"][:, 1] = 0.5 * spacing + layer * spacing
     r["quat"] = random_quats(rng, n)
     r["restitution"] = 0.0
     recs.append(r)
-    return Scene("config5: %d spheres in a 20x20 m box, dt=1/240, 480 steps, 20 iterations" % n,
-                 shapes, np.concatenate(recs), 1, dt=1 / 240, steps=480, iterations=20)
+    return Scene("config5: %d spheres poured into a %g x %g m box, dt=1/240, 480 steps, 20 iterations"
+                 % (n, 2 * half, 2 * half), shapes, np.concatenate(recs), 1, dt=1 / 240, steps=480, iterations=20)
+
+
+def resting_stacks(rows=10, cols=10, height=3, spacing=3.0, gap=0.01, seed=None):
+    """Separated stacks of boxes on a ground box: each stack is `height` boxes with vertical axes,
+    each turned about the vertical by a random angle and placed `gap` m above the one below, so
+    the boxes drop flat and come to rest. The stacks are far apart (no pair between stacks), and
+    nothing tips over, so the trajectory is not chaotic: a perturbation stays of its own size."""
+    rng = rng_for(11, seed)
+    shapes = [("box", 0.6 * spacing * max(rows, cols), 0.5, 0.6 * spacing * max(rows, cols))]
+    recs = [_static(0, (0.0, -0.5, 0.0))]
+    n = rows * cols * height
+    r = _records(n)
+    k = 0
+    for i in range(rows):
+        for j in range(cols):
+            x, z = (i - (rows - 1) / 2) * spacing, (j - (cols - 1) / 2) * spacing
+            y = 0.0
+            for lvl in range(height):
+                hx, hz = (0.5 - 0.08 * lvl) * rng.uniform(0.8, 1.0, 2)
+                hy = rng.uniform(0.15, 0.3)
+                shapes.append(("box", float(hx), float(hy), float(hz)))
+                m, I = box_mass(hx, hy, hz)
+                ang = rng.uniform(-0.3, 0.3)
+                r[k]["shape"] = len(shapes) - 1
+                r[k]["mass"] = m
+                r[k]["inertia"] = np.diag(I).reshape(-1)
+                r[k]["pos"] = (x, y + gap + hy, z)
+                r[k]["quat"] = (math.cos(ang / 2), 0.0, math.sin(ang / 2), 0.0)
+                y += gap + 2 * hy
+                k += 1
+    r["restitution"] = 0.0
+    r["friction"] = 0.5
+    recs.append(r)
+    return Scene("resting stacks: %dx%d stacks of %d boxes on a ground box, dt=1/120" % (rows, cols, height),
+                 shapes, np.concatenate(recs), 1, dt=1 / 120, steps=240, iterations=10)
 
 
 def small_pile(n=60, seed=7, extent=3.0, kinds=(1,), ground=True, restitution=0.0):
@@ -320,7 +362,8 @@ def load(world, scene: Scene, shape_offset_map=None):
     return world.create_rigids(rec)
 
 
-def make_world(scene: Scene, precision="f64", pair_factor=8, iterations=None, max_bodies_per_world=0):
+def make_world(scene: Scene, precision="f64", pair_factor=8, iterations=None, max_bodies_per_world=0,
+               contact_factor=0):
     from .world import World, world_desc
 
     nb = len(scene.bodies)
@@ -331,7 +374,8 @@ def make_world(scene: Scene, precision="f64", pair_factor=8, iterations=None, ma
          .with_precision(precision)
          .with_capacity(max_bodies=nb, max_pairs=max(pair_factor * nb, 1024), max_worlds=scene.nworlds,
                         max_bodies_per_world=per_world, max_shape_vertices=scene.vertex_count() + 16,
-                        max_shapes=len(scene.shapes) + 4))
+                        max_shapes=len(scene.shapes) + 4,
+                        max_contact_pairs=int(contact_factor * nb) if contact_factor else 0))
     w = World(d)
     handles = load(w, scene)
     return w, handles

@@ -30,14 +30,15 @@ PK_ERR_DEVICE_STATUS = -5
 PK_ERR_NO_DEVICE = -6
 PRECISION = {"f64": 0, "f32": 1}
 
-STATUS_BITS = {1: "pair_overflow", 2: "epa_cap", 4: "colour_cap", 8: "traversal_stack", 16: "nan"}
+STATUS_BITS = {1: "pair_overflow", 2: "epa_cap", 4: "colour_cap", 8: "traversal_stack", 16: "nan",
+               32: "contact_overflow"}
 
 
 class WorldDescC(C.Structure):
     _fields_ = [("gravity", C.c_double * 3), ("solver_iterations", C.c_int32), ("precision", C.c_int32),
                 ("max_bodies", C.c_int32), ("max_pairs", C.c_int32), ("max_worlds", C.c_int32),
                 ("max_bodies_per_world", C.c_int32), ("max_shape_vertices", C.c_int32),
-                ("max_shapes", C.c_int32)]
+                ("max_shapes", C.c_int32), ("max_contact_pairs", C.c_int32)]
 
 
 BODY_DTYPE = np.dtype([("type", np.int32), ("shape", np.int32), ("world", np.int32), ("reserved", np.int32),
@@ -170,6 +171,8 @@ def _check(rc, what):
         raise RuntimeError(f"{what}: no CUDA device (physkit_gb300 has no CPU fallback)")
     if rc == PK_ERR_CUDA:
         raise RuntimeError(f"{what}: CUDA error {lib().pk_last_cuda_error()}")
+    if rc == PK_ERR_DEVICE_STATUS:
+        raise RuntimeError(f"{what}: a device status bit was raised (a capacity of the device path was hit)")
     raise RuntimeError(f"{what}: error {rc}")
 
 
@@ -186,6 +189,7 @@ class world_desc:
         self.max_bodies_per_world = 0
         self.max_shape_vertices = 0
         self.max_shapes = 0
+        self.max_contact_pairs = 0
 
     @staticmethod
     def make():
@@ -206,10 +210,11 @@ class world_desc:
         return self
 
     def with_capacity(self, max_bodies, max_pairs=0, max_worlds=1, max_bodies_per_world=0,
-                      max_shape_vertices=0, max_shapes=0):
+                      max_shape_vertices=0, max_shapes=0, max_contact_pairs=0):
         self.max_bodies, self.max_pairs, self.max_worlds = int(max_bodies), int(max_pairs), int(max_worlds)
         self.max_bodies_per_world = int(max_bodies_per_world)
         self.max_shape_vertices, self.max_shapes = int(max_shape_vertices), int(max_shapes)
+        self.max_contact_pairs = int(max_contact_pairs)
         return self
 
     def to_c(self):
@@ -225,6 +230,7 @@ class world_desc:
         d.max_bodies_per_world = self.max_bodies_per_world
         d.max_shape_vertices = self.max_shape_vertices
         d.max_shapes = self.max_shapes
+        d.max_contact_pairs = self.max_contact_pairs
         return d
 
 

@@ -35,7 +35,7 @@ def test_descriptor_layouts_match_header():
     from physkit_gb300 import world
 
     assert world.BODY_DTYPE.itemsize == 216
-    assert C.sizeof(world.WorldDescC) == 56
+    assert C.sizeof(world.WorldDescC) == 64  # 3 doubles, 9 int32, padded to 8 bytes
     assert C.sizeof(world.CollideShapeC) == 88
     assert C.sizeof(world.RayC) == 64
 
@@ -70,3 +70,31 @@ def test_tune_result_layout():
     # tiny_world, tiny_threads (the doubles start at offset 16)
     assert C.sizeof(world.TuneResultC) == 48
     assert world.TuneResultC.step_ms_before.offset == 16
+
+
+def _function_body(src, signature_start):
+    i = src.index(signature_start)
+    j = src.index("{", i)
+    depth, k = 0, j
+    while True:
+        if src[k] == "{":
+            depth += 1
+        elif src[k] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[j:k + 1]
+        k += 1
+
+
+def test_noalloc_path_names_no_allocation():
+    # pk_collide_noalloc and everything it calls on the device path: no device or host allocation
+    csrc = os.path.join(ROOT, "physkit_gb300", "csrc")
+    capi = open(os.path.join(csrc, "pk_capi.cu")).read()
+    host = open(os.path.join(csrc, "pk_engine_host.cuh")).read()
+    bodies = [_function_body(capi, "int pk_collide_noalloc("),
+              _function_body(capi, "int scratch_for_world_device("),
+              _function_body(host, "int collide_device(")]
+    banned = re.compile(r"cudaMalloc|cudaFree|cuMem|malloc\(|\bnew\b|std::vector|torch")
+    for b in bodies:
+        assert not banned.search(b), banned.search(b).group(0)
+    assert "cudaGetSymbolAddress" in bodies[1]

@@ -75,3 +75,28 @@ def test_noalloc_rejects_oversized_batch():
     with pytest.raises(MemoryError):
         w.collide([shape] * 4097, [shape] * 4097, noalloc=True)
     w.close()
+
+
+def test_noalloc_leaves_free_device_memory_unchanged():
+    # The property the entry point exists for, seen from outside: free device memory is the same
+    # before and after a few hundred calls (a leaked allocation on this path would show up here;
+    # test_noalloc_path_names_no_allocation in test_capi_cpu.py reads the code path itself).
+    import torch
+
+    from physkit_gb300 import World, world_desc
+
+    w = World(world_desc.make().with_capacity(64))
+    cache = {}
+    pairs = _pairs()
+    A = [_shape(w, a, cache) for a, _ in pairs]
+    B = [_shape(w, b, cache) for _, b in pairs]
+    w.collide(A, B)  # uploads the shapes
+    w.collide(A, B, noalloc=True)  # first call on the device: looks up the array's address
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(300):
+        w.collide(A, B, noalloc=True)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+    w.close()
