@@ -187,6 +187,9 @@ int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n
  * pk_world_read_bodies copies straight into it; unregister before freeing it. */
 int pk_host_register(void *ptr, size_t bytes);
 int pk_host_unregister(void *ptr);
+/* PK_OK while the handle names a live body, PK_ERR_STALE_HANDLE after its removal: the arena's
+ * generation check of get_rigid (arena.h:234-253), without touching the device. */
+int pk_body_alive(pk_world *w, uint64_t handle);
 /* Overwrite pos/quat/vel/ang_vel of one body and refresh its cached world inertia. */
 int pk_world_write_body(pk_world *w, uint64_t handle, const double *state13);
 /* Sorted broadphase pairs of the last step. keys use the reference layout

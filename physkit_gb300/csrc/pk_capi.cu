@@ -1083,6 +1083,13 @@ int pk_host_unregister(void *ptr)
     return PK_OK;
 }
 
+int pk_body_alive(pk_world *w, uint64_t handle)
+{
+    if (!w) return PK_ERR_INVALID;
+    int slot;
+    return resolve(w, handle, &slot) ? PK_OK : PK_ERR_STALE_HANDLE;
+}
+
 int pk_world_write_body(pk_world *w, uint64_t handle, const double *s)
 {
     if (!w || !s) return PK_ERR_INVALID;

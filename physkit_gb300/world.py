@@ -127,6 +127,7 @@ def lib():
             "pk_host_register": (C.c_int, [vp, C.c_size_t]),
             "pk_host_unregister": (C.c_int, [vp]),
             "pk_world_write_body": (C.c_int, [vp, C.c_uint64, dp]),
+            "pk_body_alive": (C.c_int, [vp, C.c_uint64]),
             "pk_world_read_pairs": (C.c_int, [vp, u64p, i32p, C.c_int32, i32p]),
             "pk_world_read_manifolds": (C.c_int, [vp, u64p, i32p, i32p, dp, C.c_int32, i32p]),
             "pk_world_read_events": (C.c_int, [vp, u64p, i32p, i32p, C.c_int32, i32p]),
