@@ -1566,9 +1566,84 @@ std::optional<ContactRows> build_contact(Body &a, Body &b, V3 la, V3 lb, V3 wn, 
 // Deterministic colouring of the step's active manifolds (in key order), as the device solver
 // colours them. A world of at most 4,096 arena slots is coloured first-fit: each manifold takes
 // the lowest colour that no earlier manifold on one of its dynamic bodies has, unless that needs a
-// colour above 127. Other worlds are coloured by min-index claiming rounds: in each round every uncoloured manifold claims its
-// dynamic bodies with the minimum manifold index, and the manifolds that won all their dynamic
-// bodies take the round number as colour.
+// colour above 127. Other worlds are coloured by rounds of parallel first fit: in each round every
+// uncoloured manifold picks the lowest colour (below 128) taken on neither of its dynamic bodies,
+// and claims both bodies with the key (colour, scramble of the pair's arena indices, index in key
+// order) (ff_key); the manifolds that hold the lowest key on all their dynamic bodies keep their
+// colour. Where a body would need a colour above 127 there too, the world is coloured by min-index
+// claiming rounds: in each round every uncoloured manifold claims its dynamic bodies with its
+// index, and the manifolds that won all their dynamic bodies take the round number as colour.
+static uint64_t ff_key(int colour, uint32_t la, uint32_t lb, uint32_t pos)
+{
+    const uint32_t lo = std::min(la, lb), hi = std::max(la, lb);
+    uint64_t x = (uint64_t(lo) << 32) | hi;
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return (uint64_t(uint32_t(colour)) << 56) | ((x >> 40) << 32) | pos;
+}
+
+static bool colour_first_fit_rounds(const std::vector<std::pair<uint32_t, uint32_t>> &bodies,
+                                    const std::vector<std::pair<bool, bool>> &stat, size_t nslots,
+                                    std::vector<int> &col, int *ncolours)
+{
+    const size_t m = bodies.size();
+    std::vector<std::array<uint64_t, 2>> used(nslots, {0ull, 0ull});
+    std::vector<uint64_t> owner(nslots, ~0ull);
+    std::vector<int> tcol(m, 0);
+    std::fill(col.begin(), col.end(), -1);
+    size_t left = m;
+    int top = 0;
+    for (int round = 0; left > 0; ++round)
+    {
+        if (round >= 512) return false;
+        for (size_t i = 0; i < m; ++i)
+        {
+            if (col[i] >= 0) continue;
+            uint64_t u0 = 0ull, u1 = 0ull;
+            for (auto [b, st] : {std::pair<uint32_t, bool>{bodies[i].first, stat[i].first},
+                                 std::pair<uint32_t, bool>{bodies[i].second, stat[i].second}})
+            {
+                if (st) continue;
+                u0 |= used[b][0];
+                u1 |= used[b][1];
+                owner[b] = ~0ull;
+            }
+            int c = -1;
+            for (int k = 0; k < 128 && c < 0; ++k)
+                if (!((((k < 64) ? u0 : u1) >> (k & 63)) & 1ull)) c = k;
+            if (c < 0) return false; // a body with all 128 colours taken
+            tcol[i] = c;
+        }
+        for (size_t i = 0; i < m; ++i)
+        {
+            if (col[i] >= 0) continue;
+            const uint64_t key = ff_key(tcol[i], bodies[i].first, bodies[i].second, uint32_t(i));
+            if (!stat[i].first) owner[bodies[i].first] = std::min(owner[bodies[i].first], key);
+            if (!stat[i].second) owner[bodies[i].second] = std::min(owner[bodies[i].second], key);
+        }
+        for (size_t i = 0; i < m; ++i)
+        {
+            if (col[i] >= 0) continue;
+            const uint64_t key = ff_key(tcol[i], bodies[i].first, bodies[i].second, uint32_t(i));
+            if ((stat[i].first || owner[bodies[i].first] == key) && (stat[i].second || owner[bodies[i].second] == key))
+            {
+                const int c = tcol[i];
+                col[i] = c;
+                for (auto [b, st] : {std::pair<uint32_t, bool>{bodies[i].first, stat[i].first},
+                                     std::pair<uint32_t, bool>{bodies[i].second, stat[i].second}})
+                    if (!st) used[b][size_t(c >> 6)] |= 1ull << (c & 63);
+                top = std::max(top, c + 1);
+                --left;
+            }
+        }
+    }
+    *ncolours = top;
+    return true;
+}
+
 std::vector<int> colour_manifolds(const std::vector<std::pair<uint32_t, uint32_t>> &bodies,
                                   const std::vector<std::pair<bool, bool>> &stat, size_t nslots,
                                   int *ncolours)
@@ -1602,6 +1677,8 @@ std::vector<int> colour_manifolds(const std::vector<std::pair<uint32_t, uint32_t
         }
         std::fill(col.begin(), col.end(), -1);
     }
+    if (colour_first_fit_rounds(bodies, stat, nslots, col, ncolours)) return col;
+    std::fill(col.begin(), col.end(), -1);
     std::vector<uint32_t> owner(nslots, 0xFFFFFFFFu);
     size_t left = m;
     int round = 0;

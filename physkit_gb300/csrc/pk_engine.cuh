@@ -256,7 +256,8 @@ template <class T> struct Dev
     int *colour;      // solver scratch: compacted active manifolds of each world
     int *colour_tmp;  // solver scratch: colour of each compacted manifold
     int *pair_colour; // colour of each pair of the last step (-2: no contact rows)
-    uint32_t *owner;
+    uint64_t *owner;       // colouring rounds: the lowest key on each body
+    ulonglong2 *used;      // parallel first fit: colours (0..127) taken on each body
     uint32_t *order;
     int *ncolours;
     const int *world_order; // solver CTA -> world, largest worlds first
@@ -314,6 +315,24 @@ __device__ __forceinline__ int warp_push(int *counter)
     if (lane == leader) base = atomicAdd(counter, __popc(m));
     base = __shfl_sync(m, base, leader);
     return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// Key of a manifold in a round of parallel first fit (colour_rounds_pick / _claim / _commit): its
+// tentative colour on top, then a scramble of its pair's world-local indices (MurmurHash3's 64-bit
+// finaliser), then its position in the world's key order. Of the uncoloured manifolds on one body,
+// the lowest key keeps its colour in a round; the scramble keeps neighbouring manifolds from
+// forming long chains of falling priority in a dense pile. Local indices and key order do not
+// depend on the batch, so a world gets the same colours alone and in any mix.
+__host__ __device__ __forceinline__ uint64_t ff_key(int colour, uint32_t la, uint32_t lb, uint32_t pos)
+{
+    const uint32_t lo = la < lb ? la : lb, hi = la < lb ? lb : la;
+    uint64_t x = (uint64_t(lo) << 32) | hi;
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return (uint64_t(uint32_t(colour)) << 56) | ((x >> 40) << 32) | pos;
 }
 
 #define PK_GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += blockDim.x * gridDim.x)
@@ -2160,6 +2179,53 @@ template <class T> __device__ __forceinline__ void solve_manifold_rec(const Dev<
     store_rec_body(d, rec.z, lb, cache, B);
 }
 
+// One round of parallel first fit, in three phases separated by block- or grid-wide barriers.
+// pick: the lowest colour taken on neither dynamic body (and both bodies' keys reset); all 128
+// taken sets *over. claim: the lowest key wins each body. commit: a manifold that won both bodies
+// takes its colour, marked on its bodies for the next rounds.
+template <class T> __device__ __forceinline__ int colour_rounds_pick(const Dev<T> &d, uint4 r, int *over)
+{
+    unsigned long long u0 = 0ull, u1 = 0ull;
+    if (!(r.y >> 31))
+    {
+        const ulonglong2 u = __ldcg(d.used + r.y);
+        u0 |= u.x;
+        u1 |= u.y;
+        d.owner[r.y] = ~0ull;
+    }
+    if (!(r.z >> 31))
+    {
+        const ulonglong2 u = __ldcg(d.used + (r.z & 0x7FFFFFFFu));
+        u0 |= u.x;
+        u1 |= u.y;
+        d.owner[r.z & 0x7FFFFFFFu] = ~0ull;
+    }
+    if (~u0) return __ffsll(~u0) - 1;
+    if (~u1) return 64 + __ffsll(~u1) - 1;
+    *over = 1;
+    return 0;
+}
+template <class T> __device__ __forceinline__ void colour_rounds_claim(const Dev<T> &d, uint4 r, uint64_t key)
+{
+    if (!(r.y >> 31)) atomicMin(reinterpret_cast<unsigned long long *>(d.owner + r.y), (unsigned long long)key);
+    if (!(r.z >> 31)) atomicMin(reinterpret_cast<unsigned long long *>(d.owner + (r.z & 0x7FFFFFFFu)), (unsigned long long)key);
+}
+template <class T> __device__ __forceinline__ bool colour_rounds_commit(const Dev<T> &d, uint4 r, uint64_t key, int c)
+{
+    const bool da = !(r.y >> 31), db = !(r.z >> 31);
+    const int sa = int(r.y & 0x7FFFFFFFu), sb = int(r.z & 0x7FFFFFFFu);
+    const bool won = (!da || __ldcg(reinterpret_cast<const unsigned long long *>(d.owner + sa)) == key) &&
+                     (!db || __ldcg(reinterpret_cast<const unsigned long long *>(d.owner + sb)) == key);
+    if (!won) return false;
+    unsigned long long *ua = reinterpret_cast<unsigned long long *>(d.used + sa);
+    unsigned long long *ub = reinterpret_cast<unsigned long long *>(d.used + sb);
+    const int w = c >> 6;
+    const unsigned long long bit = 1ull << (c & 63);
+    if (da) atomicOr(ua + w, bit);
+    if (db) atomicOr(ub + w, bit);
+    return true;
+}
+
 // MAXT: the largest CTA the instance is compiled for (256, or 512 for the FP32 form's large worlds;
 // the 512 instance gives up registers for threads).
 template <class T, int MAXT, bool JOINTS>
@@ -2187,7 +2253,7 @@ __global__ void __launch_bounds__(MAXT)
     }
     const bool fits = d.world_nlocal[w] <= cache_bodies;
     Vel<T> *cache = fits ? reinterpret_cast<Vel<T> *>(solve_smem) : nullptr;
-    uint32_t *sowner = fits ? reinterpret_cast<uint32_t *>(solve_smem) : nullptr; // during colouring only
+    uint64_t *sowner = fits ? reinterpret_cast<uint64_t *>(solve_smem) : nullptr; // during colouring only
     uint4 *rec = d.crec + ms; // solve records of the active manifolds, ascending pair index
 
     // 1. compact the manifolds that have contact rows (stable: ascending pair index). Each thread
@@ -2236,9 +2302,10 @@ __global__ void __launch_bounds__(MAXT)
     // 2. colouring. Worlds up to kFirstFitMax local indices: first fit in pair order, each manifold
     //    taking the lowest colour that none of the earlier manifolds on its dynamic bodies has
     //    (one thread; a 128-bit used-colour mask per body). Larger worlds, and worlds where a body
-    //    would need a first-fit colour above 127: each uncoloured manifold claims its dynamic bodies
-    //    with its index; the winners of all their bodies take the round number. Bodies are keyed by
-    //    world-local index when the table fits in shared memory, else by slot.
+    //    would need a first-fit colour above 127: rounds of parallel first fit (ff_key); where a
+    //    body would need a colour above 127 there too: each uncoloured manifold claims its dynamic
+    //    bodies with its index; the winners of all their bodies take the round number. Bodies are
+    //    keyed by world-local index when the table fits in shared memory, else by slot.
     __shared__ int ff_ncol;
     int round = 0;
     bool coloured = false;
@@ -2315,6 +2382,67 @@ __global__ void __launch_bounds__(MAXT)
             __syncthreads();
         }
     }
+    if (!coloured)
+    {
+        // rounds of parallel first fit, global tables by slot (16 B of taken colours, 8 B of key)
+        __shared__ int rb_left, rb_over, rb_top;
+        int *tcol = reinterpret_cast<int *>(d.order) + ms; // free until the grid solver's ordering
+        for (int k = tid; k < na; k += nt)
+        {
+            colour[k] = -1;
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) d.used[r.y] = make_ulonglong2(0ull, 0ull);
+            if (!(r.z >> 31)) d.used[r.z & 0x7FFFFFFFu] = make_ulonglong2(0ull, 0ull);
+        }
+        if (tid == 0)
+        {
+            rb_left = 0;
+            rb_over = 0;
+            rb_top = 0;
+        }
+        __syncthreads();
+        for (int rr = 0;; ++rr)
+        {
+            for (int k = tid; k < na; k += nt)
+                if (colour[k] < 0) tcol[k] = colour_rounds_pick(d, rec[k], &rb_over);
+            __syncthreads();
+            if (rb_over) break; // a body would need a colour above 127
+            for (int k = tid; k < na; k += nt)
+                if (colour[k] < 0) colour_rounds_claim(d, rec[k], ff_key(tcol[k], rec[k].w & 0xFFFFu, rec[k].w >> 16, uint32_t(k)));
+            __syncthreads();
+            int left = 0;
+            for (int k = tid; k < na; k += nt)
+            {
+                if (colour[k] >= 0) continue;
+                const int c = tcol[k];
+                if (colour_rounds_commit(d, rec[k], ff_key(c, rec[k].w & 0xFFFFu, rec[k].w >> 16, uint32_t(k)), c))
+                {
+                    colour[k] = c;
+                    atomicMax(&rb_top, c + 1);
+                }
+                else
+                    ++left;
+            }
+            if (left) atomicAdd(&rb_left, left);
+            __syncthreads();
+            const int lft = rb_left;
+            __syncthreads(); // every thread has read rb_left before it is reset
+            if (lft == 0)
+            {
+                coloured = true;
+                round = rb_top;
+                break;
+            }
+            if (rr + 1 >= kMaxColours) break;
+            if (tid == 0) rb_left = 0;
+        }
+        __syncthreads();
+        if (!coloured)
+        {
+            for (int k = tid; k < na; k += nt) colour[k] = -1; // claiming rounds from scratch
+            __syncthreads();
+        }
+    }
     while (!coloured && remaining > 0)
     {
         __syncthreads();
@@ -2322,8 +2450,8 @@ __global__ void __launch_bounds__(MAXT)
         {
             if (colour[k] != -1) continue;
             const uint4 r = rec[k];
-            if (!(r.y >> 31)) { if (sowner) sowner[r.w & 0xFFFFu] = 0xFFFFFFFFu; else d.owner[r.y] = 0xFFFFFFFFu; }
-            if (!(r.z >> 31)) { if (sowner) sowner[r.w >> 16] = 0xFFFFFFFFu; else d.owner[r.z] = 0xFFFFFFFFu; }
+            if (!(r.y >> 31)) { if (sowner) sowner[r.w & 0xFFFFu] = ~0ull; else d.owner[r.y & 0x7FFFFFFFu] = ~0ull; }
+            if (!(r.z >> 31)) { if (sowner) sowner[r.w >> 16] = ~0ull; else d.owner[r.z & 0x7FFFFFFFu] = ~0ull; }
         }
         if (tid == 0) remaining = 0;
         __syncthreads();
@@ -2331,8 +2459,9 @@ __global__ void __launch_bounds__(MAXT)
         {
             if (colour[k] != -1) continue;
             const uint4 r = rec[k];
-            if (!(r.y >> 31)) { if (sowner) atomicMin(sowner + (r.w & 0xFFFFu), uint32_t(k)); else atomicMin(d.owner + r.y, uint32_t(k)); }
-            if (!(r.z >> 31)) { if (sowner) atomicMin(sowner + (r.w >> 16), uint32_t(k)); else atomicMin(d.owner + r.z, uint32_t(k)); }
+            const unsigned long long key = uint32_t(k);
+            if (!(r.y >> 31)) { if (sowner) atomicMin(reinterpret_cast<unsigned long long *>(sowner + (r.w & 0xFFFFu)), key); else atomicMin(reinterpret_cast<unsigned long long *>(d.owner + (r.y & 0x7FFFFFFFu)), key); }
+            if (!(r.z >> 31)) { if (sowner) atomicMin(reinterpret_cast<unsigned long long *>(sowner + (r.w >> 16)), key); else atomicMin(reinterpret_cast<unsigned long long *>(d.owner + (r.z & 0x7FFFFFFFu)), key); }
         }
         __syncthreads();
         int left = 0;
@@ -2340,8 +2469,9 @@ __global__ void __launch_bounds__(MAXT)
         {
             if (colour[k] != -1) continue;
             const uint4 r = rec[k];
-            bool oka = (r.y >> 31) || (sowner ? sowner[r.w & 0xFFFFu] : d.owner[r.y]) == uint32_t(k);
-            bool okb = (r.z >> 31) || (sowner ? sowner[r.w >> 16] : d.owner[r.z]) == uint32_t(k);
+            const uint64_t key = uint32_t(k);
+            bool oka = (r.y >> 31) || (sowner ? sowner[r.w & 0xFFFFu] : d.owner[r.y & 0x7FFFFFFFu]) == key;
+            bool okb = (r.z >> 31) || (sowner ? sowner[r.w >> 16] : d.owner[r.z & 0x7FFFFFFFu]) == key;
             if (oka && okb)
                 colour[k] = round;
             else
@@ -2451,9 +2581,10 @@ __global__ void __launch_bounds__(MAXT)
 }
 
 // The same colouring and colour-ordered sweeps for one world too large for a CTA: every block of a
-// cooperative launch takes part, and grid-wide barriers separate the phases. Claim priority is
-// the pair index itself (monotone in the compacted index the CTA solver uses), so the colours are
-// the same as the CTA solver's and the oracle's.
+// cooperative launch takes part, and grid-wide barriers separate the phases. The keys of the
+// parallel first fit and the claim priority of the fallback use the pair index (monotone in the
+// compacted index the CTA solver uses), so the colours are the same as the CTA solver's and the
+// oracle's.
 struct GridScratch
 {
     int ccount[kMaxColours];
@@ -2461,6 +2592,7 @@ struct GridScratch
     int cursor[kMaxColours];
     int left[2];
     int ncol;
+    int ff_left, ff_over, ff_top; // rounds of parallel first fit
 };
 
 template <class T>
@@ -2488,6 +2620,81 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
     grid.sync();
     int round = 0;
     int active_left = 1;
+    // rounds of parallel first fit (as the CTA solver for worlds above kFirstFitMax local indices),
+    // keyed by the bodies' full local indices; claiming rounds if a body would need a colour above 127
+    {
+        int *tcol = reinterpret_cast<int *>(d.order); // free until the colour-ordered list is built
+        auto rec_of = [&](int p) {
+            const uint64_t v = sval[p];
+            const uint32_t a = uint32_t(v >> 32), b = uint32_t(v & 0xFFFFFFFFu);
+            return make_uint4(uint32_t(p), a | ((d.meta[a].flags & BODY_STATIC) ? 0x80000000u : 0u),
+                              b | ((d.meta[b].flags & BODY_STATIC) ? 0x80000000u : 0u), 0u);
+        };
+        auto key_of = [&](int p, int c) {
+            const uint64_t v = sval[p];
+            return ff_key(c, d.meta[uint32_t(v >> 32)].local, d.meta[uint32_t(v & 0xFFFFFFFFu)].local, uint32_t(p));
+        };
+        for (int p = ms + gtid; p < me; p += gn)
+        {
+            if (colour[p] != -1) continue;
+            const uint4 r = rec_of(p);
+            if (!(r.y >> 31)) d.used[r.y] = make_ulonglong2(0ull, 0ull);
+            if (!(r.z >> 31)) d.used[r.z & 0x7FFFFFFFu] = make_ulonglong2(0ull, 0ull);
+        }
+        if (gtid == 0)
+        {
+            g->ff_left = 0;
+            g->ff_over = 0;
+            g->ff_top = 0;
+        }
+        grid.sync();
+        bool coloured = false;
+        for (int rr = 0;; ++rr)
+        {
+            for (int p = ms + gtid; p < me; p += gn)
+                if (colour[p] == -1) tcol[p] = colour_rounds_pick(d, rec_of(p), &g->ff_over);
+            grid.sync();
+            if (*((volatile int *)&g->ff_over)) break;
+            for (int p = ms + gtid; p < me; p += gn)
+                if (colour[p] == -1) colour_rounds_claim(d, rec_of(p), key_of(p, tcol[p]));
+            grid.sync();
+            int left = 0;
+            for (int p = ms + gtid; p < me; p += gn)
+            {
+                if (colour[p] != -1) continue;
+                const int c = tcol[p];
+                if (colour_rounds_commit(d, rec_of(p), key_of(p, c), c))
+                {
+                    colour[p] = c;
+                    atomicMax(&g->ff_top, c + 1);
+                }
+                else
+                    ++left;
+            }
+            if (left) atomicAdd(&g->ff_left, left);
+            grid.sync();
+            const int lft = *((volatile int *)&g->ff_left);
+            grid.sync(); // every thread has read ff_left before it is reset
+            if (lft == 0)
+            {
+                coloured = true;
+                break;
+            }
+            if (rr + 1 >= kMaxColours) break;
+            if (gtid == 0) g->ff_left = 0;
+        }
+        if (coloured)
+        {
+            round = *((volatile int *)&g->ff_top);
+            active_left = 0; // the claiming rounds below do not run
+        }
+        else
+        {
+            for (int p = ms + gtid; p < me; p += gn)
+                if (colour[p] >= 0) colour[p] = -1; // claiming rounds from scratch
+            grid.sync();
+        }
+    }
     while (active_left > 0)
     {
         int *cnt = &g->left[round & 1];
@@ -2496,8 +2703,8 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
             if (colour[p] != -1) continue;
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            if (!(d.meta[a].flags & BODY_STATIC)) d.owner[a] = 0xFFFFFFFFu;
-            if (!(d.meta[b].flags & BODY_STATIC)) d.owner[b] = 0xFFFFFFFFu;
+            if (!(d.meta[a].flags & BODY_STATIC)) d.owner[a] = ~0ull;
+            if (!(d.meta[b].flags & BODY_STATIC)) d.owner[b] = ~0ull;
         }
         if (gtid == 0) *cnt = 0;
         grid.sync();
@@ -2506,8 +2713,8 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
             if (colour[p] != -1) continue;
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            if (!(d.meta[a].flags & BODY_STATIC)) atomicMin(d.owner + a, uint32_t(p));
-            if (!(d.meta[b].flags & BODY_STATIC)) atomicMin(d.owner + b, uint32_t(p));
+            if (!(d.meta[a].flags & BODY_STATIC)) atomicMin(reinterpret_cast<unsigned long long *>(d.owner + a), (unsigned long long)uint32_t(p));
+            if (!(d.meta[b].flags & BODY_STATIC)) atomicMin(reinterpret_cast<unsigned long long *>(d.owner + b), (unsigned long long)uint32_t(p));
         }
         grid.sync();
         int left = 0;
@@ -2516,8 +2723,8 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
             if (colour[p] != -1) continue;
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
-            bool oka = (d.meta[a].flags & BODY_STATIC) || __ldcg(d.owner + a) == uint32_t(p);
-            bool okb = (d.meta[b].flags & BODY_STATIC) || __ldcg(d.owner + b) == uint32_t(p);
+            bool oka = (d.meta[a].flags & BODY_STATIC) || __ldcg(reinterpret_cast<const unsigned long long *>(d.owner + a)) == uint64_t(uint32_t(p));
+            bool okb = (d.meta[b].flags & BODY_STATIC) || __ldcg(reinterpret_cast<const unsigned long long *>(d.owner + b)) == uint64_t(uint32_t(p));
             if (oka && okb)
                 colour[p] = round;
             else

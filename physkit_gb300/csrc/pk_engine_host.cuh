@@ -241,6 +241,7 @@ public:
         PK_CUDA(alloc(&d.srec, P));
         PK_CUDA(alloc(&d.crec, P));
         PK_CUDA(alloc(&d.owner, N));
+        PK_CUDA(alloc(&d.used, N));
         int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
         PK_CUDA(alloc(&hist_, size_t(kSortRadix) * (hb + 1))); // digit table + one row of digit totals
         PK_CUDA(alloc(&d.verts, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
@@ -969,7 +970,7 @@ private:
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
                       d_.epa_list, d_.epa_simplex, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
-                      d_.order, d_.srec, d_.crec, d_.owner, const_cast<int *>(d_.world_order),
+                      d_.order, d_.srec, d_.crec, d_.owner, d_.used, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
