@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-raycast", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip configs 2 and 5")
+    ap.add_argument("--config5-bodies", type=int, default=1_000_000)
     ap.add_argument("--no-stages", action="store_true")
     ap.add_argument("--served-rates", default="1000,2000,5000,10000,20000,50000",
                     help="Poisson request rates (req/s) for the served form; empty to skip")
@@ -247,11 +249,11 @@ def run_reference(a, rank, world_size):
     print(json.dumps(line), flush=True)
 
 
-def _make(scene, precision, tuned):
+def _make(scene, precision, tuned, pair_factor=12, contact_factor=0):
     from physkit_gb300 import scenes
 
     # pair capacity 12 per body: settled piles keep ~6 fat-box pairs per body
-    world, _ = scenes.make_world(scene, precision=precision, pair_factor=12)
+    world, _ = scenes.make_world(scene, precision=precision, pair_factor=pair_factor, contact_factor=contact_factor)
     if tuned:
         world.set_tuning(tuned)
     return world
@@ -410,6 +412,10 @@ def run_ours(a, rank, world_size, local_rank):
                                  f"ratio_to_{a.precision}": v2 / value, "autotune": t2,
                                  "accuracy": "per-quantity error against the FP64 form: precision_f32_vs_f64"}
 
+    if rank == 0 and not a.no_configs:
+        out["config2"] = config2_report(a)
+        out["config5"] = config5_report(a)
+        out["config5_replica_f32_vs_f64"] = config5_replica_report()
     if rank == 0 and not a.no_raycast:
         out["raycast"] = raycast_bench(scene, a, rank)
     if rank == 0 and not a.no_plain:
@@ -435,6 +441,130 @@ def run_ours(a, rank, world_size, local_rank):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def _stage_split(world, dt, steps):
+    world.set_timing(True)
+    world.stage_times()  # clear
+    for _ in range(steps):
+        world.step_async(dt)
+    world.synchronize()
+    st = world.stage_times()
+    world.set_timing(False)
+    return {k: round(v[0] / max(v[1], 1), 4) for k, v in st.items()}
+
+
+def _roofline(stages, units):
+    dom = max(stages, key=stages.get)
+    unit, bpu = BYTES[dom]
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = json.load(open(peaks_path))["hbm_gbs"] if os.path.exists(peaks_path) else 6800.0
+    achieved = bpu * units[unit] / (stages[dom] / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "model": f"{bpu:g} B per {unit} x {units[unit]} {unit}s per launch"}
+
+
+def config2_report(a):
+    """Config 2: one world of 100,000 mixed convex bodies (1/3 UV spheres of 482 vertices, 1/3
+    boxes, 1/3 hulls of 16 points) in a 200 m cube with v ~ N(0, 1 m/s): the LBVH broadphase, the
+    grid-wide solver and GJK/EPA on large meshes in a single world; FP64 and FP32 forms."""
+    from physkit_gb300 import scenes
+
+    sc = scenes.config2()
+    w_, k_ = a.warmup, a.steps
+    out = {"workload": "config2: 100,000 mixed convex bodies in a 200 m cube, one world, dt=1/120, 10 iterations",
+           "window": f"steps {w_ + 1}-{w_ + k_} after {w_} warm-up steps", "dynamic_bodies": sc.n_dynamic}
+    for prec in ("f64", "f32"):
+        world = _make(sc, prec, None, pair_factor=4)
+        ms, info, _ = _device_window(world, sc.dt, w_, k_, None, 0)
+        keys, counts, _ = world.manifolds()
+        stages = _stage_split(world, sc.dt, 5)
+        world.close()
+        units = {"body": sc.n_dynamic, "pair": len(keys), "contact": int(counts.sum()),
+                 "contact_iter": int(counts.sum()) * (sc.iterations + 1)}
+        out[prec] = {"value": sc.n_dynamic * k_ / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / k_,
+                     "pairs": len(keys), "contacts": int(counts.sum()), "status": info["flags"],
+                     "stage_ms_per_step": stages, "roofline": _roofline(stages, units),
+                     "stage_window": f"steps {w_ + k_ + 1}-{w_ + k_ + 5}"}
+    return out
+
+
+def config5_report(a):
+    """Config 5: dense-contact stress, N spheres (r ~ lognormal(ln 0.05, 0.3)) poured into a
+    20 x 20 m box, 20 iterations, dt = 1/240, FP32 form (FP64 is compared on the 10k replica)."""
+    from physkit_gb300 import scenes
+
+    n = a.config5_bodies
+    sc = scenes.config5(n=n)
+    w_, k_ = min(a.warmup, 3), max(1, min(a.steps, 5))
+    world = _make(sc, "f32", None, pair_factor=128, contact_factor=8)
+    ms, info, clk = _device_window(world, sc.dt, w_, k_, None, 0, clocks=True)
+    keys, counts, _ = world.manifolds()
+    stages = _stage_split(world, sc.dt, 2)
+    world.close()
+    units = {"body": sc.n_dynamic, "pair": len(keys), "contact": int(counts.sum()),
+             "contact_iter": int(counts.sum()) * (sc.iterations + 1)}
+    return {"workload": f"config5: {n:,} spheres poured into a 20 x 20 m box (jittered lattice, falls into a dense "
+                        f"pile), FP32 form, dt=1/240, 20 iterations",
+            "window": f"steps {w_ + 1}-{w_ + k_} after {w_} warm-up steps (the pour's first steps: every sphere "
+                      f"falls onto the ones below)",
+            "dynamic_bodies": sc.n_dynamic, "value": sc.n_dynamic * k_ / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": ms / k_, "pairs": len(keys), "pairs_per_body": len(keys) / sc.n_dynamic,
+            "contacts": int(counts.sum()), "contacts_per_body": int(counts.sum()) / sc.n_dynamic,
+            "status": info["flags"], "clocks": clk, "stage_ms_per_step": stages,
+            "roofline": _roofline(stages, units), "stage_window": f"steps {w_ + k_ + 1}-{w_ + k_ + 2}"}
+
+
+def pile_stats(world, scene):
+    """Kinetic and potential energy, penetration depth percentiles over the contacts with positive
+    depth, pairs and contacts of a world after its last step."""
+    import numpy as np
+
+    b = world.bodies()
+    dyn = scene.bodies["type"] == 0
+    m, I = scene.bodies["mass"][dyn], scene.bodies["inertia"][dyn]
+    v, w = b[dyn, 7:10], b[dyn, 10:13]
+    ke = 0.5 * (m * (v * v).sum(1)).sum() + 0.5 * (I[:, 0] * w[:, 0] ** 2 + I[:, 4] * w[:, 1] ** 2
+                                                  + I[:, 8] * w[:, 2] ** 2).sum()
+    pe = float((m * 9.81 * b[dyn, 1]).sum())
+    k, c, ct = world.manifolds()
+    depth = np.concatenate([ct[i, :c[i], 9] for i in np.nonzero(c)[0]]) if c.sum() else np.zeros(0)
+    pos = depth[depth > 0]
+    q = (lambda p: float(np.percentile(pos, p)) if len(pos) else 0.0)
+    return {"ke_j": float(ke), "pe_j": pe, "depth_mean_m": float(pos.mean()) if len(pos) else 0.0,
+            "depth_p50_m": q(50), "depth_p99_m": q(99), "depth_max_m": float(pos.max()) if len(pos) else 0.0,
+            "pairs": int(len(k)), "contacts": int(c.sum())}
+
+
+def config5_replica_report(steps=(20, 60, 120, 240, 480)):
+    """Config 5's 10,000-sphere sub-region replica (same lattice, radii and depth on a 2 x 2 m
+    footprint), 480 steps: FP32 form against the FP64 form (bit-identical to the FP64 oracle) for
+    kinetic energy and penetration depth; control: the FP64 form from the float32-rounded start,
+    which bounds what rounding alone does to this chaotic pile."""
+    from physkit_gb300 import scenes
+
+    sc = scenes.config5(n=10_000, half=1.0)
+    ws = {"f32": _make(sc, "f32", None, 128, 8), "f64": _make(sc, "f64", None, 128, 8),
+          "control": _make(_rounded_to_f32(sc), "f64", None, 128, 8)}
+    rows, flags = [], set()
+    for s in range(1, max(steps) + 1):
+        for name, w in ws.items():
+            if w.step(sc.dt, check=False):
+                flags.add(f"{name}: device status raised")
+        if s in steps:
+            r = {"step": s}
+            for name, w in ws.items():
+                r[name] = pile_stats(w, sc)
+            ref = r["f64"]
+            for name in ("f32", "control"):
+                r[name]["ke_rel_err"] = abs(r[name]["ke_j"] - ref["ke_j"]) / max(ref["ke_j"], 1e-12)
+                r[name]["pe_rel_err"] = abs(r[name]["pe_j"] - ref["pe_j"]) / max(abs(ref["pe_j"]), 1e-12)
+                r[name]["depth_p99_abs_err_m"] = abs(r[name]["depth_p99_m"] - ref["depth_p99_m"])
+            rows.append(r)
+    for w in ws.values():
+        w.close()
+    return {"workload": "config5 replica: 10,000 spheres on a 2 x 2 m footprint, dt=1/240, 20 iterations", "rows": rows,
+            "status": sorted(flags)}
 
 
 def raycast_bench(scene, a, rank):
