@@ -312,6 +312,71 @@ int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b
 int pk_collide_noalloc(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b, int32_t n, double *out,
                        int32_t *hit);
 
+/* Serving: continuous batching of step requests over one device-resident pool of worlds.
+ * The reference steps one world per call (world_base::step, world.h:234-242); a server holding
+ * many such worlds calls this instead. Worlds are admitted into slots of the pool (their state
+ * stays on the device), each request asks for one step of one world, and pk_batch_step_async
+ * enqueues one batched step of every world with a request not yet in flight, behind the steps
+ * already enqueued (up to pipeline_depth), without waiting for the GPU. Admission, request and
+ * retirement never wait for the GPU either: uploads are staged through pinned memory and ordered
+ * behind the steps in flight. pk_batch_poll returns the requests whose steps have completed (and
+ * the worlds retired) in completion order. A world sits out every batched step that does not
+ * serve one of its requests, unchanged (pk_world_set_active), so its trajectory is the same alone
+ * and in any mix. Admission is by device memory: with max_bodies 0 the pool takes
+ * memory_fraction of the HBM free at creation, and a world that does not fit in what is left gets
+ * PK_ERR_CAPACITY until a retirement frees room. One pk_batch is single-threaded. */
+typedef struct pk_batch pk_batch;
+typedef struct pk_batch_desc
+{
+    double gravity[3];
+    double dt;                    /* the step every request asks for */
+    int32_t solver_iterations;
+    int32_t precision;            /* PK_PRECISION_* (default F32) */
+    int32_t max_worlds;           /* world slots (default 1024) */
+    int32_t max_bodies_per_world; /* default 4101 */
+    int64_t max_bodies;           /* body pool; 0: from free device memory (memory_fraction) */
+    double memory_fraction;       /* default 0.5 */
+    int32_t pair_factor;          /* broadphase pairs per body of the pool (default 6) */
+    int32_t contact_factor;       /* pairs with contact rows per body (default 2) */
+    int32_t max_shapes, max_shape_vertices;
+    int32_t pipeline_depth;       /* batched steps enqueued ahead of completion (default 1) */
+    int32_t reserved;
+} pk_batch_desc;
+enum
+{
+    PK_BATCH_STEPPED = 1, /* the request `tag` of `world` got its step */
+    PK_BATCH_RETIRED = 2  /* `world` was retired; its slot and bodies are free */
+};
+typedef struct pk_batch_event
+{
+    int64_t tag;
+    int32_t world;
+    int32_t kind;
+} pk_batch_event;
+typedef struct pk_batch_info
+{
+    int64_t pool_bodies, bodies_in_use, steps, pending_requests;
+    int32_t worlds_live, worlds_free, steps_in_flight, reserved;
+} pk_batch_info;
+void pk_batch_desc_init(pk_batch_desc *desc);
+int pk_batch_create(const pk_batch_desc *desc, pk_batch **out);
+void pk_batch_destroy(pk_batch *b);
+/* The pool's world object: shapes (pk_shape_*) are made on it before admissions, and tuning
+ * (pk_world_set_tuning) and read-backs go through it. */
+pk_world *pk_batch_world(pk_batch *b);
+/* Open a world of n bodies (their `world` field is ignored); returns its slot. */
+int pk_batch_admit(pk_batch *b, const pk_body_desc *bodies, int32_t n, uint64_t *out_handles, int32_t *out_world);
+int pk_batch_request(pk_batch *b, int32_t world, int64_t tag);
+/* Retire a world once its pending requests are served (reported as PK_BATCH_RETIRED). */
+int pk_batch_retire(pk_batch *b, int32_t world);
+int pk_batch_step_async(pk_batch *b, int32_t *nworlds);
+/* Completed requests and retirements, up to cap; wait = 1 first waits for the oldest step in flight. */
+int pk_batch_poll(pk_batch *b, pk_batch_event *out, int32_t cap, int32_t *n, int32_t wait);
+int pk_batch_stats(pk_batch *b, pk_batch_info *st);
+/* State rows (14 doubles, as pk_world_read_bodies) of one world's live bodies in creation order;
+ * waits for the steps in flight. */
+int pk_batch_read_world(pk_batch *b, int32_t world, double *out14, int32_t cap, int32_t *n);
+
 int pk_last_cuda_error(void);
 const char *pk_version(void);
 

@@ -12,6 +12,7 @@
 #include "pk_math.cuh"
 
 #include <algorithm>
+#include <deque>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -403,7 +404,7 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out, in
 }
 
 // Solver CTAs take worlds largest first so the longest solves start earliest.
-static int flush_order(pk_world *w)
+static int flush_order(pk_world *w, bool async = false)
 {
     if (!w->order_dirty) return PK_OK;
     int nw = w->cfg.max_worlds;
@@ -422,7 +423,8 @@ static int flush_order(pk_world *w)
         if (nlocal[size_t(a)] != nlocal[size_t(b)]) return nlocal[size_t(a)] > nlocal[size_t(b)];
         return cnt[size_t(a)] > cnt[size_t(b)];
     });
-    if (w->eng->set_world_order(order.data(), nlocal.data(), nw))
+    if (async ? w->eng->set_world_order_async(order.data(), nlocal.data(), nw)
+              : w->eng->set_world_order(order.data(), nlocal.data(), nw))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
@@ -549,7 +551,12 @@ int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)
     return add_shape(w, v, out);
 }
 
+static int add_bodies(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out, bool async);
+
 int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out)
+{ return add_bodies(w, descs, n, out, false); }
+
+static int add_bodies(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out, bool async)
 {
     if (!w || (n > 0 && !descs)) return PK_ERR_INVALID;
     int nshapes = int(w->ranges.size() / 8);
@@ -643,7 +650,8 @@ int pk_body_add(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out
         hb.push_back(h);
         if (out) out[i] = uint64_t(uint32_t(slot)) | (uint64_t(si.gen) << 32);
     }
-    if (w->eng->upload_bodies(slots.data(), hb.data(), n, w->nslots))
+    if (async ? w->eng->upload_bodies_async(slots.data(), hb.data(), n, w->nslots)
+              : w->eng->upload_bodies(slots.data(), hb.data(), n, w->nslots))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
@@ -691,7 +699,11 @@ int pk_body_remove(pk_world *w, uint64_t handle)
     return kill_slot(w, slot);
 }
 
-int pk_world_clear(pk_world *w, int32_t world)
+static int clear_world(pk_world *w, int32_t world, bool async);
+
+int pk_world_clear(pk_world *w, int32_t world) { return clear_world(w, world, false); }
+
+static int clear_world(pk_world *w, int32_t world, bool async)
 {
     if (!w || world < 0 || world >= w->cfg.max_worlds) return PK_ERR_INVALID;
     SubWorld &sw = w->worlds[size_t(world)];
@@ -717,7 +729,8 @@ int pk_world_clear(pk_world *w, int32_t world)
         sw.jfree[t].clear();
     }
     // one kernel kills the bodies, one empties every cached manifold of the world
-    if (w->eng->kill_world(dead.data(), int(dead.size()), world))
+    if (async ? w->eng->kill_world_async(dead.data(), int(dead.size()), world)
+              : w->eng->kill_world(dead.data(), int(dead.size()), world))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
@@ -763,11 +776,11 @@ int pk_world_set_gravity(pk_world *w, int32_t world, const double g[3])
     return PK_OK;
 }
 
-int pk_world_step_async(pk_world *w, double dt)
+static int step_async(pk_world *w, double dt, bool async_order)
 {
     if (!w || !(dt > 0.0)) return PK_ERR_INVALID;
     if (int frc = flush_shapes(w)) return frc;
-    if (int orc = flush_order(w)) return orc;
+    if (int orc = flush_order(w, async_order)) return orc;
     if (int jrc = flush_joints(w)) return jrc;
     int rc = w->eng->step(dt);
     if (rc)
@@ -778,6 +791,8 @@ int pk_world_step_async(pk_world *w, double dt)
     w->steps++;
     return PK_OK;
 }
+
+int pk_world_step_async(pk_world *w, double dt) { return step_async(w, dt, false); }
 
 int pk_world_synchronize(pk_world *w, pk_step_info *info)
 {
@@ -1461,6 +1476,326 @@ int pk_collide(pk_world *w, const pk_collide_shape *a, const pk_collide_shape *b
     }
     for (int i = 0; i < n; ++i)
         if (status[size_t(i)]) return PK_ERR_DEVICE_STATUS; // results written; a pair hit a capacity cap
+    return PK_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Serving: continuous batching of step requests over one device-resident pool of worlds
+// ------------------------------------------------------------------------------------------------
+} // extern "C"
+
+struct pk_batch
+{
+    pk_world *w = nullptr;
+    pk_batch_desc desc{};
+    int64_t pool_bodies = 0, bodies_in_use = 0;
+    struct Slot
+    {
+        bool live = false, retiring = false;
+        int32_t nbodies = 0;
+        int in_flight = 0;           // pending requests already in enqueued steps
+        std::deque<int64_t> pending; // request tags, oldest first
+    };
+    std::vector<Slot> slots;
+    std::deque<int32_t> free_ids;
+    struct Flight
+    {
+        cudaEvent_t ev;
+        std::vector<std::pair<int32_t, int64_t>> served;
+    };
+    std::deque<Flight> flight;
+    std::vector<cudaEvent_t> spare;
+    std::vector<uint8_t> mask;
+    std::deque<pk_batch_event> ready; // completions not yet returned by pk_batch_poll
+    int64_t steps = 0;
+};
+
+namespace
+{
+int batch_retire_now(pk_batch *b, int32_t wid)
+{
+    pk_batch::Slot &s = b->slots[size_t(wid)];
+    if (int rc = clear_world(b->w, wid, true)) return rc;
+    b->bodies_in_use -= s.nbodies;
+    s = pk_batch::Slot{};
+    b->free_ids.push_back(wid);
+    pk_batch_event e{};
+    e.tag = -1;
+    e.world = wid;
+    e.kind = PK_BATCH_RETIRED;
+    b->ready.push_back(e);
+    return PK_OK;
+}
+} // namespace
+
+extern "C" {
+
+void pk_batch_desc_init(pk_batch_desc *d)
+{
+    std::memset(d, 0, sizeof(*d));
+    d->gravity[1] = -9.81;
+    d->dt = 1.0 / 120.0;
+    d->solver_iterations = 10;
+    d->precision = PK_PRECISION_F32;
+    d->max_worlds = 1024;
+    d->max_bodies_per_world = 4096 + 5;
+    d->max_bodies = 0;
+    d->memory_fraction = 0.5;
+    d->pair_factor = 6;
+    d->contact_factor = 2;
+    d->max_shapes = 1024;
+    d->max_shape_vertices = 65536;
+    d->pipeline_depth = 1;
+}
+
+int pk_batch_create(const pk_batch_desc *desc, pk_batch **out)
+{
+    if (!desc || !out) return PK_ERR_INVALID;
+    *out = nullptr;
+    if (desc->max_worlds <= 0 || desc->max_bodies < 0 || !(desc->dt > 0.0) || desc->pair_factor <= 0 ||
+        desc->contact_factor < 0 || desc->pipeline_depth < 0 || desc->pipeline_depth > 8 ||
+        !(desc->memory_fraction >= 0.0 && desc->memory_fraction <= 0.9))
+        return PK_ERR_INVALID;
+    int64_t pool = desc->max_bodies;
+    if (pool == 0)
+    {
+        // admission is by device memory: the pool takes a share of the HBM free now, at the
+        // engine's cost per body slot (body state and its share of the pair and contact capacity)
+        size_t free_b = 0, total_b = 0;
+        cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+        if (e != cudaSuccess)
+        {
+            g_last_cuda = int(e);
+            return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? PK_ERR_NO_DEVICE : PK_ERR_CUDA;
+        }
+        const double scale = desc->precision == PK_PRECISION_F64 ? 1.5 : 1.0;
+        const double per_body = scale * (600.0 + 720.0 * desc->pair_factor + 1250.0 * desc->contact_factor);
+        const double frac = desc->memory_fraction > 0.0 ? desc->memory_fraction : 0.5;
+        pool = int64_t(double(free_b) * frac / per_body);
+        const int64_t lim = (int64_t(1) << 30) / std::max(1, desc->pair_factor);
+        if (pool > lim) pool = lim;
+    }
+    if (pool <= 0 || pool > INT32_MAX / 16) return PK_ERR_CAPACITY;
+    pk_world_desc wd;
+    pk_world_desc_init(&wd);
+    for (int k = 0; k < 3; ++k) wd.gravity[k] = desc->gravity[k];
+    wd.solver_iterations = desc->solver_iterations;
+    wd.precision = desc->precision;
+    wd.max_bodies = int32_t(pool);
+    wd.max_pairs = int32_t(std::min<int64_t>(int64_t(desc->pair_factor) * pool, INT32_MAX));
+    wd.max_contact_pairs =
+        desc->contact_factor > 0 ? int32_t(std::min<int64_t>(int64_t(desc->contact_factor) * pool, INT32_MAX)) : 0;
+    wd.max_worlds = desc->max_worlds;
+    wd.max_bodies_per_world = desc->max_bodies_per_world;
+    wd.max_shapes = desc->max_shapes;
+    wd.max_shape_vertices = desc->max_shape_vertices;
+    pk_world *w = nullptr;
+    if (int rc = pk_world_create(&wd, &w)) return rc;
+    auto *b = new (std::nothrow) pk_batch;
+    if (!b)
+    {
+        pk_world_destroy(w);
+        return PK_ERR_CAPACITY;
+    }
+    b->w = w;
+    b->desc = *desc;
+    if (b->desc.pipeline_depth == 0) b->desc.pipeline_depth = 1;
+    b->pool_bodies = pool;
+    b->slots.resize(size_t(desc->max_worlds));
+    for (int32_t i = 0; i < desc->max_worlds; ++i) b->free_ids.push_back(i);
+    b->mask.assign(size_t(desc->max_worlds), 0);
+    // every world sits out until a request names it
+    if (w->eng->set_active_mask_async(b->mask.data(), desc->max_worlds))
+    {
+        g_last_cuda = w->eng->last_error();
+        pk_world_destroy(w);
+        delete b;
+        return PK_ERR_CUDA;
+    }
+    for (int32_t i = 0; i < desc->max_worlds; ++i) w->worlds[size_t(i)].active = 0;
+    *out = b;
+    return PK_OK;
+}
+
+void pk_batch_destroy(pk_batch *b)
+{
+    if (!b) return;
+    cudaStreamSynchronize(static_cast<cudaStream_t>(b->w->eng->stream()));
+    for (auto &f : b->flight) cudaEventDestroy(f.ev);
+    for (cudaEvent_t e : b->spare) cudaEventDestroy(e);
+    pk_world_destroy(b->w);
+    delete b;
+}
+
+pk_world *pk_batch_world(pk_batch *b) { return b ? b->w : nullptr; }
+
+int pk_batch_admit(pk_batch *b, const pk_body_desc *bodies, int32_t n, uint64_t *out_handles, int32_t *out_world)
+{
+    if (!b || n <= 0 || !bodies || !out_world) return PK_ERR_INVALID;
+    if (n > b->desc.max_bodies_per_world) return PK_ERR_INVALID;
+    if (b->free_ids.empty() || b->bodies_in_use + n > b->pool_bodies) return PK_ERR_CAPACITY; // wait for a retirement
+    const int32_t wid = b->free_ids.front();
+    std::vector<pk_body_desc> d(bodies, bodies + n);
+    for (pk_body_desc &x : d) x.world = wid;
+    std::vector<uint64_t> h(static_cast<size_t>(n));
+    if (int rc = add_bodies(b->w, d.data(), n, out_handles ? out_handles : h.data(), true)) return rc;
+    b->free_ids.pop_front();
+    pk_batch::Slot &s = b->slots[size_t(wid)];
+    s.live = true;
+    s.retiring = false;
+    s.nbodies = n;
+    s.in_flight = 0;
+    s.pending.clear();
+    b->bodies_in_use += n;
+    *out_world = wid;
+    return PK_OK;
+}
+
+int pk_batch_request(pk_batch *b, int32_t world, int64_t tag)
+{
+    if (!b || world < 0 || world >= b->desc.max_worlds) return PK_ERR_INVALID;
+    pk_batch::Slot &s = b->slots[size_t(world)];
+    if (!s.live || s.retiring) return PK_ERR_STALE_HANDLE;
+    s.pending.push_back(tag);
+    return PK_OK;
+}
+
+int pk_batch_retire(pk_batch *b, int32_t world)
+{
+    if (!b || world < 0 || world >= b->desc.max_worlds) return PK_ERR_INVALID;
+    pk_batch::Slot &s = b->slots[size_t(world)];
+    if (!s.live || s.retiring) return PK_ERR_STALE_HANDLE;
+    s.retiring = true;
+    if (s.pending.empty() && s.in_flight == 0) return batch_retire_now(b, world);
+    return PK_OK; // after its pending steps (pk_batch_poll reports PK_BATCH_RETIRED)
+}
+
+int pk_batch_step_async(pk_batch *b, int32_t *nworlds)
+{
+    if (!b) return PK_ERR_INVALID;
+    if (nworlds) *nworlds = 0;
+    if (int(b->flight.size()) >= b->desc.pipeline_depth) return PK_OK;
+    pk_batch::Flight f;
+    int32_t cnt = 0;
+    for (size_t i = 0; i < b->slots.size(); ++i)
+    {
+        pk_batch::Slot &s = b->slots[i];
+        const bool go = s.live && int(s.pending.size()) > s.in_flight;
+        b->mask[i] = go ? 1 : 0;
+        if (!go) continue;
+        f.served.push_back({int32_t(i), s.pending[size_t(s.in_flight)]});
+        s.in_flight++;
+        ++cnt;
+    }
+    if (cnt == 0) return PK_OK;
+    pk_world *w = b->w;
+    for (size_t i = 0; i < b->slots.size(); ++i) w->worlds[i].active = b->mask[i];
+    if (w->eng->set_active_mask_async(b->mask.data(), b->desc.max_worlds))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    if (int rc = step_async(w, b->desc.dt, true)) return rc;
+    if (!b->spare.empty())
+    {
+        f.ev = b->spare.back();
+        b->spare.pop_back();
+    }
+    else if (cudaError_t e = cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming); e != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    if (cudaError_t e = cudaEventRecord(f.ev, static_cast<cudaStream_t>(w->eng->stream())); e != cudaSuccess)
+    {
+        g_last_cuda = int(e);
+        return PK_ERR_CUDA;
+    }
+    b->flight.push_back(std::move(f));
+    b->steps++;
+    if (nworlds) *nworlds = cnt;
+    return PK_OK;
+}
+
+int pk_batch_poll(pk_batch *b, pk_batch_event *out, int32_t cap, int32_t *n, int32_t wait)
+{
+    if (!b || !n || cap < 0 || (cap > 0 && !out)) return PK_ERR_INVALID;
+    bool first = true;
+    while (!b->flight.empty())
+    {
+        pk_batch::Flight &f = b->flight.front();
+        cudaError_t e = (wait && first) ? cudaEventSynchronize(f.ev) : cudaEventQuery(f.ev);
+        if (e == cudaErrorNotReady) break;
+        if (e != cudaSuccess)
+        {
+            g_last_cuda = int(e);
+            return PK_ERR_CUDA;
+        }
+        first = false;
+        for (auto &[wid, tag] : f.served)
+        {
+            pk_batch::Slot &s = b->slots[size_t(wid)];
+            s.pending.pop_front();
+            s.in_flight--;
+            pk_batch_event ev{};
+            ev.tag = tag;
+            ev.world = wid;
+            ev.kind = PK_BATCH_STEPPED;
+            b->ready.push_back(ev);
+            if (s.retiring && s.pending.empty() && s.in_flight == 0)
+                if (int rc = batch_retire_now(b, wid)) return rc;
+        }
+        b->spare.push_back(f.ev);
+        b->flight.pop_front();
+    }
+    int32_t k = 0;
+    while (k < cap && !b->ready.empty())
+    {
+        out[k++] = b->ready.front();
+        b->ready.pop_front();
+    }
+    *n = k;
+    return PK_OK;
+}
+
+int pk_batch_stats(pk_batch *b, pk_batch_info *st)
+{
+    if (!b || !st) return PK_ERR_INVALID;
+    std::memset(st, 0, sizeof(*st));
+    st->pool_bodies = b->pool_bodies;
+    st->bodies_in_use = b->bodies_in_use;
+    st->worlds_free = int32_t(b->free_ids.size());
+    st->worlds_live = b->desc.max_worlds - st->worlds_free;
+    st->steps_in_flight = int32_t(b->flight.size());
+    st->steps = b->steps;
+    int64_t pend = 0;
+    for (const auto &s : b->slots) pend += int64_t(s.pending.size());
+    st->pending_requests = pend;
+    return PK_OK;
+}
+
+int pk_batch_read_world(pk_batch *b, int32_t world, double *out14, int32_t cap, int32_t *n)
+{
+    if (!b || !n || world < 0 || world >= b->desc.max_worlds) return PK_ERR_INVALID;
+    pk_world *w = b->w;
+    const pk_batch::Slot &s = b->slots[size_t(world)];
+    if (!s.live) return PK_ERR_STALE_HANDLE;
+    const SubWorld &sw = w->worlds[size_t(world)];
+    std::vector<double> rows(size_t(w->nslots) * 14);
+    if (w->eng->read_bodies(rows.data(), w->nslots) < 0)
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    int32_t k = 0;
+    for (size_t l = 0; l < sw.local_slot.size(); ++l)
+    {
+        if (!sw.local_alive[l]) continue;
+        if (k < cap && out14)
+            std::memcpy(out14 + size_t(k) * 14, rows.data() + size_t(sw.local_slot[l]) * 14, 14 * sizeof(double));
+        ++k;
+    }
+    *n = k;
     return PK_OK;
 }
 

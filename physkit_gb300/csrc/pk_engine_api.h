@@ -77,6 +77,12 @@ public:
     virtual int set_active_mask(const uint8_t *mask, int n) = 0;    // stream-ordered, no sync
     // solver schedule (largest worlds first) and local indices in use per world
     virtual int set_world_order(const int *order, const int *nlocal, int n) = 0;
+    // The same four updates without waiting for the GPU (pinned staging, stream-ordered behind the
+    // work already enqueued): the serving loop changes worlds while earlier steps run.
+    virtual int upload_bodies_async(const int *slots, const HostBody *b, int n, int nslots) = 0;
+    virtual int kill_world_async(const int *slots, int n, int world) = 0;
+    virtual int set_active_mask_async(const uint8_t *mask, int n) = 0;
+    virtual int set_world_order_async(const int *order, const int *nlocal, int n) = 0;
     virtual int step(double dt) = 0;                 // enqueue only
     virtual int synchronize(StepCounters *c) = 0;   // wait + read counters, clears status
     virtual int read_bodies(double *out14, int nslots) = 0;

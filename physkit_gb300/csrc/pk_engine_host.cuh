@@ -9,9 +9,109 @@
 
 #include <cstring>
 #include <cuda_runtime.h>
+#include <deque>
 
 namespace pk
 {
+
+// Page-locked host staging mirrored by device memory, for uploads that must not wait for the GPU
+// (the serving loop admits and retires worlds while earlier steps run). Regions are handed out in
+// ring order; a region is reused only after the event recorded behind its last use has completed.
+class StagingRing
+{
+public:
+    cudaError_t init(size_t bytes)
+    {
+        cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(&host_), bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) return e;
+        e = cudaMalloc(reinterpret_cast<void **>(&dev_), bytes);
+        if (e != cudaSuccess) return e;
+        cap_ = bytes;
+        return cudaSuccess;
+    }
+    void release()
+    {
+        for (Region &r : busy_) cudaEventDestroy(r.ev);
+        for (cudaEvent_t e : spare_) cudaEventDestroy(e);
+        busy_.clear();
+        spare_.clear();
+        if (host_) cudaFreeHost(host_);
+        if (dev_) cudaFree(dev_);
+        host_ = dev_ = nullptr;
+        cap_ = head_ = 0;
+    }
+    bool ready() const { return cap_ > 0; }
+    // n bytes at a 256-byte aligned offset; waits only for earlier users of the same bytes
+    cudaError_t reserve(size_t n, size_t *off)
+    {
+        n = (n + 255) & ~size_t(255);
+        if (n > cap_) return cudaErrorMemoryAllocation;
+        size_t s = head_;
+        if (s + n > cap_) s = 0;
+        for (auto it = busy_.begin(); it != busy_.end();)
+        {
+            const bool overlap = it->lo < s + n && s < it->hi;
+            if (overlap || cudaEventQuery(it->ev) == cudaSuccess)
+            {
+                cudaError_t e = cudaEventSynchronize(it->ev);
+                if (e != cudaSuccess) return e;
+                spare_.push_back(it->ev);
+                it = busy_.erase(it);
+            }
+            else
+                ++it;
+        }
+        *off = s;
+        head_ = s + n;
+        pending_lo_ = s;
+        pending_hi_ = s + n;
+        return cudaSuccess;
+    }
+    // the last reserved region is in use by the work enqueued on `st` up to now
+    cudaError_t commit(cudaStream_t st)
+    {
+        cudaEvent_t ev;
+        if (!spare_.empty())
+        {
+            ev = spare_.back();
+            spare_.pop_back();
+        }
+        else
+        {
+            cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
+        cudaError_t e = cudaEventRecord(ev, st);
+        if (e != cudaSuccess) return e;
+        busy_.push_back(Region{pending_lo_, pending_hi_, ev});
+        return cudaSuccess;
+    }
+    unsigned char *host(size_t off) const { return host_ + off; }
+    unsigned char *dev(size_t off) const { return dev_ + off; }
+
+private:
+    struct Region
+    {
+        size_t lo, hi;
+        cudaEvent_t ev;
+    };
+    unsigned char *host_ = nullptr, *dev_ = nullptr;
+    size_t cap_ = 0, head_ = 0, pending_lo_ = 0, pending_hi_ = 0;
+    std::deque<Region> busy_;
+    std::vector<cudaEvent_t> spare_;
+};
+
+// Sub-array offsets inside one staging region (each 256-byte aligned).
+struct StageLayout
+{
+    size_t total = 0;
+    size_t add(size_t bytes)
+    {
+        size_t o = total;
+        total += (bytes + 255) & ~size_t(255);
+        return o;
+    }
+};
 
 #define PK_CUDA(x)                                                                                     \
     do                                                                                                 \
@@ -303,6 +403,64 @@ public:
         return 0;
     }
 
+    // The same upload without waiting for the GPU: staged through pinned memory and enqueued on
+    // the world's stream behind the steps already in flight.
+    int upload_bodies_async(const int *slots, const HostBody *b, int n, int nslots) override
+    {
+        PK_CUDA(ensure_staging());
+        StageLayout L;
+        const size_t o_sl = L.add(sizeof(int) * size_t(n)), o_pose = L.add(sizeof(Pose<T>) * size_t(n)),
+                     o_vel = L.add(sizeof(Vel<T>) * size_t(n)), o_prm = L.add(sizeof(Params<T>) * size_t(n)),
+                     o_meta = L.add(sizeof(Meta) * size_t(n)), o_ns = L.add(sizeof(int));
+        size_t base = 0;
+        PK_CUDA(stage_.reserve(L.total, &base));
+        unsigned char *h = stage_.host(base), *dv = stage_.dev(base);
+        int *sl = reinterpret_cast<int *>(h + o_sl);
+        Pose<T> *pose = reinterpret_cast<Pose<T> *>(h + o_pose);
+        Vel<T> *vel = reinterpret_cast<Vel<T> *>(h + o_vel);
+        Params<T> *prm = reinterpret_cast<Params<T> *>(h + o_prm);
+        Meta *meta = reinterpret_cast<Meta *>(h + o_meta);
+        for (int i = 0; i < n; ++i)
+        {
+            sl[i] = slots[i];
+            convert_body(b[i], pose[i], vel[i], prm[i], meta[i]);
+        }
+        *reinterpret_cast<int *>(h + o_ns) = nslots;
+        PK_CUDA(cudaMemcpyAsync(dv, h, L.total, cudaMemcpyHostToDevice, st_));
+        if (n > 0)
+            k_install_bodies<T><<<grid(n), 256, 0, st_>>>(d_, reinterpret_cast<const int *>(dv + o_sl),
+                                                          reinterpret_cast<const Pose<T> *>(dv + o_pose),
+                                                          reinterpret_cast<const Vel<T> *>(dv + o_vel),
+                                                          reinterpret_cast<const Params<T> *>(dv + o_prm),
+                                                          reinterpret_cast<const Meta *>(dv + o_meta), n);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.nslots), dv + o_ns, sizeof(int), cudaMemcpyDeviceToDevice, st_));
+        PK_CUDA(stage_.commit(st_));
+        nslots_ = nslots;
+        return 0;
+    }
+
+    static void convert_body(const HostBody &h, Pose<T> &pose, Vel<T> &vel, Params<T> &prm, Meta &meta)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            pose.p[k] = T(h.pos[k]);
+            vel.v[k] = T(h.vel[k]);
+            vel.w[k] = T(h.ang_vel[k]);
+        }
+        for (int k = 0; k < 4; ++k) pose.q[k] = T(h.quat[k]);
+        prm.mass = T(h.mass);
+        prm.inv_mass = T(h.inv_mass);
+        prm.restitution = T(h.restitution);
+        prm.friction = T(h.friction);
+        for (int k = 0; k < 9; ++k)
+        {
+            prm.il[k] = T(h.il[k]);
+            prm.il_inv[k] = T(h.il_inv[k]);
+        }
+        meta = Meta{uint32_t(h.world), uint32_t(h.local), uint32_t(h.shape), uint32_t(h.flags), h.created, -1};
+    }
+
     int upload_bodies(const int *slots, const HostBody *b, int n, int nslots) override
     {
         if (n > 0)
@@ -312,27 +470,7 @@ public:
             std::vector<Vel<T>> vel(n);
             std::vector<Params<T>> prm(n);
             std::vector<Meta> meta(n);
-            for (int i = 0; i < n; ++i)
-            {
-                const HostBody &h = b[i];
-                for (int k = 0; k < 3; ++k)
-                {
-                    pose[i].p[k] = T(h.pos[k]);
-                    vel[i].v[k] = T(h.vel[k]);
-                    vel[i].w[k] = T(h.ang_vel[k]);
-                }
-                for (int k = 0; k < 4; ++k) pose[i].q[k] = T(h.quat[k]);
-                prm[i].mass = T(h.mass);
-                prm[i].inv_mass = T(h.inv_mass);
-                prm[i].restitution = T(h.restitution);
-                prm[i].friction = T(h.friction);
-                for (int k = 0; k < 9; ++k)
-                {
-                    prm[i].il[k] = T(h.il[k]);
-                    prm[i].il_inv[k] = T(h.il_inv[k]);
-                }
-                meta[i] = Meta{uint32_t(h.world), uint32_t(h.local), uint32_t(h.shape), uint32_t(h.flags), h.created, -1};
-            }
+            for (int i = 0; i < n; ++i) convert_body(b[i], pose[i], vel[i], prm[i], meta[i]);
             int *dsl;
             Pose<T> *dpose;
             Vel<T> *dvel;
@@ -359,6 +497,28 @@ public:
         nslots_ = nslots;
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.nslots), &nslots_, sizeof(int), cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int set_world_order_async(const int *order, const int *nlocal, int n) override
+    {
+        if (n != cfg_.max_worlds) return -3;
+        PK_CUDA(ensure_staging());
+        size_t base = 0;
+        const size_t bytes = sizeof(int) * size_t(n);
+        StageLayout L;
+        const size_t o_ord = L.add(bytes), o_nl = L.add(bytes);
+        PK_CUDA(stage_.reserve(L.total, &base));
+        std::memcpy(stage_.host(base + o_ord), order, bytes);
+        std::memcpy(stage_.host(base + o_nl), nlocal, bytes);
+        PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_order), stage_.host(base + o_ord), bytes,
+                                cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_nlocal), stage_.host(base + o_nl), bytes,
+                                cudaMemcpyHostToDevice, st_));
+        PK_CUDA(stage_.commit(st_));
+        order_.assign(order, order + n);
+        nlocal_.assign(nlocal, nlocal + n);
+        split_worlds();
         return 0;
     }
 
@@ -411,6 +571,40 @@ public:
         return 0;
     }
     Tunables tunables() const override { return tune_; }
+
+    int kill_world_async(const int *slots, int n, int world) override
+    {
+        Dev<T> d = d_;
+        d.man_old = man_[parity_];
+        if (n > 0)
+        {
+            PK_CUDA(ensure_staging());
+            size_t base = 0;
+            PK_CUDA(stage_.reserve(sizeof(int) * size_t(n), &base));
+            std::memcpy(stage_.host(base), slots, sizeof(int) * size_t(n));
+            PK_CUDA(cudaMemcpyAsync(stage_.dev(base), stage_.host(base), sizeof(int) * size_t(n),
+                                    cudaMemcpyHostToDevice, st_));
+            k_kill_bodies<T><<<grid(n), 256, 0, st_>>>(d, reinterpret_cast<const int *>(stage_.dev(base)), n);
+            PK_CUDA(stage_.commit(st_));
+        }
+        k_purge_world<T><<<grid(cfg_.pair_cap), 256, 0, st_>>>(d, uint32_t(world));
+        PK_CUDA(cudaGetLastError());
+        return 0;
+    }
+
+    int set_active_mask_async(const uint8_t *mask, int n) override
+    {
+        if (n != cfg_.max_worlds) return -3;
+        PK_CUDA(ensure_staging());
+        size_t base = 0;
+        PK_CUDA(stage_.reserve(size_t(n), &base));
+        std::memcpy(stage_.host(base), mask, size_t(n));
+        PK_CUDA(cudaMemcpyAsync(stage_.dev(base), stage_.host(base), size_t(n), cudaMemcpyHostToDevice, st_));
+        k_set_active<T><<<grid(n), 256, 0, st_>>>(d_, stage_.dev(base), n);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(stage_.commit(st_));
+        return 0;
+    }
 
     int kill_world(const int *slots, int n, int world) override
     {
@@ -892,6 +1086,8 @@ private:
     bool timing_ = false;
     bool capturing_ = false;
     uint8_t *mask_dev_ = nullptr;
+    StagingRing stage_; // pinned staging of the asynchronous uploads (allocated on first use)
+    cudaError_t ensure_staging() { return stage_.ready() ? cudaSuccess : stage_.init(size_t(64) << 20); }
     int launches_ = 0;
     std::vector<cudaEvent_t> events_; // kStages + 1 per timed step
     int timed_steps_ = 0;
@@ -978,6 +1174,7 @@ private:
         if (pack_) cudaFree(pack_);
         pack_ = nullptr;
         pack_cap_ = 0;
+        stage_.release();
         for (cudaEvent_t e : events_) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         st_ = nullptr;

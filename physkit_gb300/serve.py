@@ -1,24 +1,23 @@
-"""Serving form: continuous batching of world-step requests on one device-resident pool.
+"""Serving form: continuous batching of world-step requests over the C ABI server (pk_batch_*).
 
-A pool is one device world object with `max_worlds` world slots and a fixed body capacity that
-was reserved in device memory at creation (admission is by that memory: a world is admitted when a
-world slot and room for its bodies are free). Requests are either "open a world of n bodies that
-lives for L steps" or "advance world w by one step". Each iteration of the loop
+The server (include/physkit_gb300.h, pk_batch_*) keeps a device-resident pool of world slots whose
+size is set by device memory at creation, and its loop runs in C++: admission into a free slot
+(refused while the pool is full), one request per step of one world, batched steps enqueued behind
+the ones in flight without waiting for the GPU, and completions polled from CUDA events. This
+module adds the request bookkeeping of a caller (arrival times, world lifetimes) and a Poisson
+load driver. Requests are either "open a world of n bodies that lives for L steps" or "advance
+world w by one step"; a request that arrives while steps are on the device joins the next batched
+step that is enqueued.
 
-  1. admits waiting opens while a slot and body capacity are free (FIFO),
-  2. marks every world with at least one pending step request active, the rest inactive,
-  3. runs one batched step on the device for all active worlds at once,
-  4. completes the oldest pending request of each stepped world, and retires worlds whose
-     lifetime is used up (their slot and bodies become free for the next admission).
-
-Requests that arrive while a step is on the device join the next iteration. A world's results do
-not depend on the mix: inactive worlds keep their pairs and manifolds untouched, pair keys and the
-per-world solver use world-local indices only, so a world stepped k times in any mix ends in the
-same state as the same world stepped k times alone.
+A world's results do not depend on the mix: a world sits out every batched step that serves none
+of its requests, with its pairs and manifolds untouched, and pair keys and the per-world solver use
+world-local indices only, so a world stepped k times in any mix ends in the same state as the same
+world stepped k times alone.
 """
 from __future__ import annotations
 
 import collections
+import ctypes as C
 import dataclasses
 import math
 import time
@@ -26,7 +25,8 @@ import time
 import numpy as np
 
 from . import scenes
-from .world import BODY_DTYPE, World, world_desc
+from .world import (BATCH_STEPPED, BODY_DTYPE, PK_ERR_CAPACITY, PRECISION, BatchDescC, BatchEventC, BatchInfoC,
+                    World, _check, _ptr, lib)
 
 
 @dataclasses.dataclass
@@ -86,29 +86,53 @@ class BoxPileTemplates:
 
 
 class StepServer:
+    """A caller of the C ABI server: request tags index the arrival times kept here."""
+
     def __init__(self, max_worlds=1024, max_bodies=2_000_000, max_bodies_per_world=4101, precision="f32",
-                 pair_factor=6, iterations=10, dt=1.0 / 120.0, seed=4):
-        d = (world_desc.make().with_precision(precision).with_solver_iterations(iterations)
-             .with_capacity(max_bodies=max_bodies, max_pairs=pair_factor * max_bodies, max_worlds=max_worlds,
-                            max_bodies_per_world=max_bodies_per_world, max_shape_vertices=4096, max_shapes=256))
-        self.world = World(d)
+                 pair_factor=6, contact_factor=2, iterations=10, dt=1.0 / 120.0, seed=4, pipeline_depth=1,
+                 memory_fraction=0.5, tuning=None):
+        self.L = lib()
+        d = BatchDescC()
+        self.L.pk_batch_desc_init(C.byref(d))
+        d.dt = dt
+        d.solver_iterations = iterations
+        d.precision = PRECISION[precision]
+        d.max_worlds = max_worlds
+        d.max_bodies_per_world = max_bodies_per_world
+        d.max_bodies = max_bodies  # 0: sized from free device memory (memory_fraction)
+        d.memory_fraction = memory_fraction
+        d.pair_factor = pair_factor
+        d.contact_factor = contact_factor
+        d.max_shapes = 256
+        d.max_shape_vertices = 4096
+        d.pipeline_depth = pipeline_depth
+        h = C.c_void_p()
+        _check(self.L.pk_batch_create(C.byref(d), C.byref(h)), "pk_batch_create")
+        self.b = h
+        self.world = World(_borrow=self.L.pk_batch_world(self.b))
         # latency first: the largest worlds set a step's length, so they get the widest solver CTA
-        self.world.set_tuning({"solve_threads": 128, "small_world": 1024, "narrow_grid": 2, "traverse_threads": 128,
-                               "big_threads": 512})
+        self.world.set_tuning(tuning or {"solve_threads": 128, "small_world": 1024, "narrow_grid": 2,
+                                         "traverse_threads": 128, "big_threads": 512})
         self.dt = dt
         self.templates = BoxPileTemplates(self.world, seed)
         self.rng = np.random.Generator(np.random.PCG64(seed))
-        self.max_worlds, self.max_bodies = max_worlds, max_bodies
-        self.free_ids = collections.deque(range(max_worlds))
-        self.bodies_in_use = 0
         self.live: dict[int, LiveWorld] = {}
         self.waiting = collections.deque()      # (req_id, nbodies, lifetime, t_arrival, records or None)
-        self.mask = np.zeros(max_worlds, dtype=np.uint8)
+        self.arrival = []                       # request tag -> arrival time
         self.latency = []                       # seconds, completed step requests
         self.body_steps = 0
-        self.steps = 0
         self.admit_wait = []
-        self.world.set_active_mask(self.mask)
+        self.events = (BatchEventC * 4096)()
+        self.max_worlds = max_worlds
+
+    def stats(self):
+        st = BatchInfoC()
+        _check(self.L.pk_batch_stats(self.b, C.byref(st)), "pk_batch_stats")
+        return {f: getattr(st, f) for f, _ in BatchInfoC._fields_}
+
+    @property
+    def steps(self):
+        return self.stats()["steps"]
 
     # requests -----------------------------------------------------------------------------------
     def open(self, req_id, nbodies, lifetime, t_arrival, records=None):
@@ -116,67 +140,87 @@ class StepServer:
 
     def advance(self, wid, t_arrival):
         lw = self.live.get(wid)
-        if lw is None:
+        if lw is None or lw.steps_left <= len(lw.pending):
             return False
-        lw.pending.append(t_arrival)
+        tag = len(self.arrival)
+        self.arrival.append(t_arrival)
+        _check(self.L.pk_batch_request(self.b, int(wid), tag), "pk_batch_request")
+        lw.pending.append(tag)
         return True
 
     # loop ---------------------------------------------------------------------------------------
     def admit(self, now):
         admitted = []
-        while self.waiting and self.free_ids:
+        wid = C.c_int32()
+        while self.waiting:
             req_id, n, life, t_arr, rec = self.waiting[0]
-            if self.bodies_in_use + n + 5 > self.max_bodies:
-                break  # device memory reserved for bodies is full: wait for a retirement
+            if rec is None:  # drawn once: a request that waits for room keeps its bodies
+                rec = self.templates.records(self.rng, n, 0)
+                self.waiting[0] = (req_id, n, life, t_arr, rec)
+            rec = np.ascontiguousarray(rec, dtype=BODY_DTYPE)
+            hs = np.zeros(len(rec), dtype=np.uint64)
+            rc = self.L.pk_batch_admit(self.b, rec.ctypes.data, len(rec), _ptr(hs, C.c_uint64), C.byref(wid))
+            if rc == PK_ERR_CAPACITY:
+                break  # no free slot or no room in the pool: wait for a retirement
+            _check(rc, "pk_batch_admit")
             self.waiting.popleft()
-            wid = self.free_ids.popleft()
-            if rec is None:
-                rec = self.templates.records(self.rng, n, wid)
-            else:
-                rec = rec.copy()
-                rec["world"] = wid
-            handles = self.world.create_rigids(rec)
-            self.bodies_in_use += len(rec)
-            self.live[wid] = LiveWorld(wid, n, life, collections.deque(), (handles & 0xFFFFFFFF).astype(np.int64))
+            self.live[wid.value] = LiveWorld(wid.value, n, life, collections.deque(), (hs & 0xFFFFFFFF).astype(np.int64))
             self.admit_wait.append(now - t_arr)
-            admitted.append((req_id, wid))
+            admitted.append((req_id, wid.value))
         return admitted
 
-    def step_once(self):
-        """One batched device step over every world with a pending step request."""
-        batch = [lw for lw in self.live.values() if lw.pending]
-        if not batch:
-            return 0
-        self.mask[:] = 0
-        for lw in batch:
-            self.mask[lw.wid] = 1
-        self.world.set_active_mask(self.mask)
-        self.world.step_async(self.dt)
-        self.world.synchronize()
-        t_done = time.perf_counter()
-        for lw in batch:
-            t_arr = lw.pending.popleft()
-            self.latency.append(t_done - t_arr)
-            lw.steps_left -= 1
-            lw.steps_done += 1
-            self.body_steps += lw.nbodies
-            if lw.steps_left <= 0:
-                self.retire(lw.wid)
-        self.steps += 1
-        return len(batch)
+    def launch(self):
+        """Enqueue one batched step of every world with a request not yet in flight."""
+        n = C.c_int32()
+        _check(self.L.pk_batch_step_async(self.b, C.byref(n)), "pk_batch_step_async")
+        return n.value
 
-    def retire(self, wid):
-        lw = self.live.pop(wid)
-        self.world.clear_world(wid)
-        self.bodies_in_use -= lw.nbodies + 5
-        self.free_ids.append(wid)
+    def poll(self, wait=False):
+        """Account the completed requests; returns how many completed."""
+        done = 0
+        while True:
+            n = C.c_int32()
+            _check(self.L.pk_batch_poll(self.b, self.events, len(self.events), C.byref(n), int(wait)), "pk_batch_poll")
+            wait = False
+            t_done = time.perf_counter()
+            for i in range(n.value):
+                e = self.events[i]
+                if e.kind != BATCH_STEPPED:
+                    continue
+                self.latency.append(t_done - self.arrival[e.tag])
+                lw = self.live[e.world]
+                lw.pending.popleft()
+                lw.steps_left -= 1
+                lw.steps_done += 1
+                self.body_steps += lw.nbodies
+                done += 1
+                if lw.steps_left <= 0:
+                    self.live.pop(e.world)
+                    _check(self.L.pk_batch_retire(self.b, e.world), "pk_batch_retire")
+            if n.value < len(self.events):
+                return done
+
+    def step_once(self):
+        """One batched step over every world with a pending request, waited for."""
+        served = self.launch()
+        if served:
+            self.poll(wait=True)
+        return served
 
     def world_state(self, wid):
         """Body states (14 doubles each) of a live world in creation order."""
-        return self.world.bodies()[self.live[wid].slots]
+        n = C.c_int32()
+        cap = self.live[wid].slots.size
+        out = np.zeros((max(cap, 1), 14))
+        _check(self.L.pk_batch_read_world(self.b, int(wid), _ptr(out, C.c_double), cap, C.byref(n)),
+               "pk_batch_read_world")
+        return out[: n.value]
 
     def close(self):
-        self.world.close()
+        if self.b:
+            self.world.close()
+            self.L.pk_batch_destroy(self.b)
+            self.b = None
 
 
 def poisson_load(rate, duration, target_live=256, nmin=16, nmax=4096, life=(60, 600), seed=5):
@@ -196,15 +240,19 @@ def poisson_load(rate, duration, target_live=256, nmin=16, nmax=4096, life=(60, 
 
 
 def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=1024, max_bodies=1_500_000,
-               nmax=4096, seed=5):
-    """Drive a StepServer with a Poisson request stream in real time; returns the latency report."""
-    srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision)
+               nmax=4096, seed=5, pipeline_depth=1):
+    """Drive a StepServer with a Poisson request stream in real time; returns the latency report.
+    The host loop takes arrivals, admits opens, enqueues a batched step whenever the pipeline has
+    room and polls completions; it blocks on the GPU only when it has nothing else to do."""
+    srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision,
+                     pipeline_depth=pipeline_depth)
     rng = np.random.Generator(np.random.PCG64(seed + 1))
     # start from a populated pool so the measured window is in steady state
     for i in range(warm_live):
         n = int(round(math.exp(rng.uniform(math.log(16), math.log(nmax)))))
         srv.open(-1 - i, n, int(rng.integers(60, 601)), time.perf_counter())
     srv.admit(time.perf_counter())
+    srv.poll()
     t, kind, sizes, lifes, pick, _ = poisson_load(rate, duration, nmax=nmax, seed=seed)
     t0 = time.perf_counter()
     i, nreq = 0, len(t)
@@ -222,19 +270,27 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
                     dropped += 1
             i += 1
         srv.admit(time.perf_counter())
-        served = srv.step_once()
-        if i >= nreq and not any(lw.pending for lw in srv.live.values()):
+        srv.launch()
+        srv.poll()
+        st = srv.stats()
+        if i >= nreq and st["pending_requests"] == 0 and st["steps_in_flight"] == 0:
             break
-        if served == 0 and i < nreq:
+        if st["steps_in_flight"] > 0 and (st["steps_in_flight"] >= pipeline_depth or i >= nreq):
+            srv.poll(wait=True)
+        elif st["steps_in_flight"] == 0 and i < nreq:
             time.sleep(max(0.0, min(1e-4, t[i] - (time.perf_counter() - t0))))
     wall = time.perf_counter() - t0
     lat = np.array(srv.latency) * 1e3
+    st = srv.stats()
     rep = {"rate_req_s": rate, "duration_s": duration, "requests": int(nreq), "completed_steps": int(len(lat)),
-           "dropped": dropped, "batched_steps": srv.steps,
+           "dropped": dropped, "batched_steps": st["steps"],
            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
            "p999_ms": float(np.percentile(lat, 99.9)) if len(lat) else None,
            "body_steps_per_s": srv.body_steps / wall, "live_worlds_end": len(srv.live),
-           "admission_wait_p99_ms": float(np.percentile(np.array(srv.admit_wait) * 1e3, 99)) if srv.admit_wait else None}
+           "admission_wait_p99_ms": float(np.percentile(np.array(srv.admit_wait) * 1e3, 99)) if srv.admit_wait else None,
+           "pool_bodies": st["pool_bodies"], "pipeline_depth": pipeline_depth,
+           "loop": "C ABI server (pk_batch_*): admission, batching and completion in C++; Poisson arrivals and "
+                   "latency accounting in Python"}
     srv.close()
     return rep

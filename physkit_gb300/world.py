@@ -85,6 +85,27 @@ HANDLE_ANY = 0xFFFFFFFFFFFFFFFF
 WAIT_COLLISION, WAIT_SEPARATION, WAIT_DESTROYED = 1, 2, 3
 
 
+class BatchDescC(C.Structure):
+    _fields_ = [("gravity", C.c_double * 3), ("dt", C.c_double), ("solver_iterations", C.c_int32),
+                ("precision", C.c_int32), ("max_worlds", C.c_int32), ("max_bodies_per_world", C.c_int32),
+                ("max_bodies", C.c_int64), ("memory_fraction", C.c_double), ("pair_factor", C.c_int32),
+                ("contact_factor", C.c_int32), ("max_shapes", C.c_int32), ("max_shape_vertices", C.c_int32),
+                ("pipeline_depth", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchEventC(C.Structure):
+    _fields_ = [("tag", C.c_int64), ("world", C.c_int32), ("kind", C.c_int32)]
+
+
+class BatchInfoC(C.Structure):
+    _fields_ = [("pool_bodies", C.c_int64), ("bodies_in_use", C.c_int64), ("steps", C.c_int64),
+                ("pending_requests", C.c_int64), ("worlds_live", C.c_int32), ("worlds_free", C.c_int32),
+                ("steps_in_flight", C.c_int32), ("reserved", C.c_int32)]
+
+
+BATCH_STEPPED, BATCH_RETIRED = 1, 2
+
+
 class CollideShapeC(C.Structure):
     _fields_ = [("kind", C.c_int32), ("shape", C.c_int32), ("p", C.c_double * 10)]
 
@@ -146,6 +167,17 @@ def lib():
             "pk_world_set_tuning": (C.c_int, [vp, P(TuneResultC)]),
             "pk_world_read_stage_times": (C.c_int, [vp, dp, i32p, C.c_int32, i32p]),
             "pk_stage_name": (C.c_char_p, [C.c_int32]),
+            "pk_batch_desc_init": (None, [P(BatchDescC)]),
+            "pk_batch_create": (C.c_int, [P(BatchDescC), P(C.c_void_p)]),
+            "pk_batch_destroy": (None, [vp]),
+            "pk_batch_world": (C.c_void_p, [vp]),
+            "pk_batch_admit": (C.c_int, [vp, C.c_void_p, C.c_int32, u64p, i32p]),
+            "pk_batch_request": (C.c_int, [vp, C.c_int32, C.c_int64]),
+            "pk_batch_retire": (C.c_int, [vp, C.c_int32]),
+            "pk_batch_step_async": (C.c_int, [vp, i32p]),
+            "pk_batch_poll": (C.c_int, [vp, P(BatchEventC), C.c_int32, i32p, C.c_int32]),
+            "pk_batch_stats": (C.c_int, [vp, P(BatchInfoC)]),
+            "pk_batch_read_world": (C.c_int, [vp, C.c_int32, dp, C.c_int32, i32p]),
             "pk_last_cuda_error": (C.c_int, []),
             "pk_version": (C.c_char_p, []),
         }
@@ -321,17 +353,23 @@ class object_desc:
 class World:
     """A device-resident world (or batch of independent worlds) behind the C ABI."""
 
-    def __init__(self, desc: world_desc | None = None):
-        self.desc = desc or world_desc()
+    def __init__(self, desc: world_desc | None = None, _borrow=None):
         self.L = lib()
+        self.last_info = None
+        self.owned = _borrow is None
+        if _borrow is not None:  # the world object of a pk_batch (the batch owns it)
+            self.desc = None
+            self.h = C.c_void_p(_borrow)
+            return
+        self.desc = desc or world_desc()
         h = C.c_void_p()
         _check(self.L.pk_world_create(C.byref(self.desc.to_c()), C.byref(h)), "pk_world_create")
         self.h = h
-        self.last_info = None
 
     def close(self):
         if getattr(self, "h", None):
-            self.L.pk_world_destroy(self.h)
+            if self.owned:
+                self.L.pk_world_destroy(self.h)
             self.h = None
 
     def __del__(self):
