@@ -2593,6 +2593,7 @@ struct GridScratch
     int left[2];
     int ncol;
     int ff_left, ff_over, ff_top; // rounds of parallel first fit
+    int nact;                     // the world's pairs with contact rows
 };
 
 template <class T>
@@ -2609,15 +2610,28 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         if (gtid == 0) d.ncolours[w] = 0;
         return;
     }
+    // the world's pairs with contact rows, compacted once (in any order: colours depend on the
+    // keys only, and manifolds of one colour are solved in any order); the colouring rounds and
+    // the orderings below run over this list instead of all of the world's pairs
     int *colour = d.colour_tmp;
-    for (int p = ms + gtid; p < me; p += gn) colour[p] = d.rowmask[p] ? -1 : -2;
+    int *alist = d.colour + ms;
     for (int c = gtid; c < kMaxColours; c += gn) g->ccount[c] = g->cursor[c] = 0;
     if (gtid == 0)
     {
         g->left[0] = 1; // any value > 0: first round runs
         g->left[1] = 0;
+        g->nact = 0;
     }
     grid.sync();
+    for (int p = ms + gtid; p < me; p += gn)
+    {
+        const bool act = d.rowmask[p] != 0;
+        colour[p] = act ? -1 : -2;
+        d.pair_colour[p] = -2;
+        if (act) alist[warp_push(&g->nact)] = p;
+    }
+    grid.sync();
+    const int na = *((volatile int *)&g->nact);
     int round = 0;
     int active_left = 1;
     // rounds of parallel first fit (as the CTA solver for worlds above kFirstFitMax local indices),
@@ -2634,10 +2648,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
             const uint64_t v = sval[p];
             return ff_key(c, d.meta[uint32_t(v >> 32)].local, d.meta[uint32_t(v & 0xFFFFFFFFu)].local, uint32_t(p));
         };
-        for (int p = ms + gtid; p < me; p += gn)
+        for (int k = gtid; k < na; k += gn)
         {
-            if (colour[p] != -1) continue;
-            const uint4 r = rec_of(p);
+            const uint4 r = rec_of(alist[k]);
             if (!(r.y >> 31)) d.used[r.y] = make_ulonglong2(0ull, 0ull);
             if (!(r.z >> 31)) d.used[r.z & 0x7FFFFFFFu] = make_ulonglong2(0ull, 0ull);
         }
@@ -2651,16 +2664,23 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         bool coloured = false;
         for (int rr = 0;; ++rr)
         {
-            for (int p = ms + gtid; p < me; p += gn)
+            for (int k = gtid; k < na; k += gn)
+            {
+                const int p = alist[k];
                 if (colour[p] == -1) tcol[p] = colour_rounds_pick(d, rec_of(p), &g->ff_over);
+            }
             grid.sync();
             if (*((volatile int *)&g->ff_over)) break;
-            for (int p = ms + gtid; p < me; p += gn)
+            for (int k = gtid; k < na; k += gn)
+            {
+                const int p = alist[k];
                 if (colour[p] == -1) colour_rounds_claim(d, rec_of(p), key_of(p, tcol[p]));
+            }
             grid.sync();
             int left = 0;
-            for (int p = ms + gtid; p < me; p += gn)
+            for (int k = gtid; k < na; k += gn)
             {
+                const int p = alist[k];
                 if (colour[p] != -1) continue;
                 const int c = tcol[p];
                 if (colour_rounds_commit(d, rec_of(p), key_of(p, c), c))
@@ -2690,16 +2710,16 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         }
         else
         {
-            for (int p = ms + gtid; p < me; p += gn)
-                if (colour[p] >= 0) colour[p] = -1; // claiming rounds from scratch
+            for (int k = gtid; k < na; k += gn) colour[alist[k]] = -1; // claiming rounds from scratch
             grid.sync();
         }
     }
     while (active_left > 0)
     {
         int *cnt = &g->left[round & 1];
-        for (int p = ms + gtid; p < me; p += gn)
+        for (int k = gtid; k < na; k += gn)
         {
+            const int p = alist[k];
             if (colour[p] != -1) continue;
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
@@ -2708,8 +2728,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         }
         if (gtid == 0) *cnt = 0;
         grid.sync();
-        for (int p = ms + gtid; p < me; p += gn)
+        for (int k = gtid; k < na; k += gn)
         {
+            const int p = alist[k];
             if (colour[p] != -1) continue;
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
@@ -2718,8 +2739,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         }
         grid.sync();
         int left = 0;
-        for (int p = ms + gtid; p < me; p += gn)
+        for (int k = gtid; k < na; k += gn)
         {
+            const int p = alist[k];
             if (colour[p] != -1) continue;
             uint64_t v = sval[p];
             int a = int(v >> 32), b = int(v & 0xFFFFFFFFu);
@@ -2741,9 +2763,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
         }
     }
     const int ncol_guess = round;
-    for (int p = ms + gtid; p < me; p += gn)
+    for (int k = gtid; k < na; k += gn)
     {
-        int c = colour[p];
+        int c = colour[alist[k]];
         if (c >= 0 && c < kMaxColours) atomicAdd(&g->ccount[c], 1);
     }
     grid.sync();
@@ -2761,8 +2783,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
     }
     grid.sync();
     const int ncol = *((volatile int *)&g->ncol);
-    for (int p = ms + gtid; p < me; p += gn)
+    for (int k = gtid; k < na; k += gn)
     {
+        const int p = alist[k];
         int c = colour[p];
         if (c >= 0 && c < kMaxColours) d.order[ms + __ldcg(&g->cstart[c]) + atomicAdd(&g->cursor[c], 1)] = uint32_t(p);
         d.pair_colour[p] = c >= 0 ? c : -2;
@@ -2786,8 +2809,9 @@ __global__ void __launch_bounds__(256) k_solve_grid(Dev<T> d, const uint64_t *__
             grid.sync();
         }
     }
-    for (int p = ms + gtid; p < me; p += gn)
+    for (int k = gtid; k < na; k += gn)
     {
+        const int p = alist[k];
         uint8_t mask = d.rowmask[p];
         for (int q = 0; q < 4; ++q)
         {
