@@ -180,6 +180,7 @@ template <class T> struct Dev
     const int *nslots;
     // shapes
     const T *verts;
+    const float *verts32;    // FP64 form: the vertices rounded to FP32 (exact support filter); else null
     const ShapeRange *shape_range;
     const Aabb<T> *shape_box;
     const T *clusters;       // 4 per cluster: centre xyz, radius
@@ -1054,6 +1055,7 @@ template <class T> __device__ __forceinline__ ShapeRef<T> body_shape(const Dev<T
     s.rmax = d.shape_rmax[m.shape];
     s.uv_stacks = r.uv_stacks;
     s.uv_sectors = r.uv_sectors;
+    s.v32 = d.verts32 ? d.verts32 + 3 * r.vstart : nullptr;
     const Pose<T> &p = d.pose[slot];
     s.pos = ld3(p.p);
     s.q = ldq(p.q);
@@ -1231,6 +1233,28 @@ __device__ __forceinline__ bool obb_separated(const Aabb<T> &la, Qt<T> qa, V3<T>
     return false;
 }
 
+// The pre-pass tests of the FP64 form run first in FP32. They only decide that a pair is certainly
+// apart (GJK would then return no collision, collision.cpp:181-182), so they need no FP64 result:
+// the margin, 1024 FP32 epsilons of the pair's scale plus the FP64 test's own terms, covers the
+// rounding of FP32 poses, boxes and products many times over, and every pair it cannot settle
+// takes the FP64 tests as before. GB300 issues FP64 at a small fraction of the FP32 rate.
+__device__ __forceinline__ bool apart_f32(const Aabb<double> &la, const Pose<double> &pa, double rma,
+                                          const Aabb<double> &lb, const Pose<double> &pb, double rmb)
+{
+    const V3<float> xa{float(pa.p[0]), float(pa.p[1]), float(pa.p[2])};
+    const V3<float> xb{float(pb.p[0]), float(pb.p[1]), float(pb.p[2])};
+    const float rs = float(rma) + float(rmb);
+    const float margin = (rs + norm(xa) + norm(xb)) * (1024.0f * EpsOf<float>::v) + 1e-6f + 1e-5f * rs;
+    const float cull = rs + margin;
+    const V3<float> dc = xb - xa;
+    if (sqnorm(dc) > cull * cull) return true;
+    const Qt<float> qa{float(pa.q[0]), float(pa.q[1]), float(pa.q[2]), float(pa.q[3])};
+    const Qt<float> qb{float(pb.q[0]), float(pb.q[1]), float(pb.q[2]), float(pb.q[3])};
+    const Aabb<float> ba{{float(la.mn.x), float(la.mn.y), float(la.mn.z)}, {float(la.mx.x), float(la.mx.y), float(la.mx.z)}};
+    const Aabb<float> bb{{float(lb.mn.x), float(lb.mn.y), float(lb.mn.z)}, {float(lb.mx.x), float(lb.mx.y), float(lb.mx.z)}};
+    return obb_separated(ba, qa, xa, bb, qb, xb, margin);
+}
+
 // Last step's manifold of each pair of an active world. Last step's pairs of a world are the
 // segment [mstart_old, mend_old) of last step's sorted keys, and this step's pairs are sorted the
 // same way, so each thread takes a run of consecutive pairs: one binary search for the first,
@@ -1304,13 +1328,21 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
         }
         const int old_idx = d.old_idx[p]; // k_old_index
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
-        V3<T> dc = B.pos - A.pos;
-        T rs = A.rmax + B.rmax;
-        T cull = rs + (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
-        const T margin = (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
-        if (sqnorm(dc) > cull * cull ||
-            obb_separated(d.shape_box[d.meta[sa].shape], A.q, A.pos, d.shape_box[d.meta[sb].shape], B.q, B.pos,
-                          margin + T(1e-5) * rs))
+        bool apart = false;
+        if constexpr (sizeof(T) == 8)
+            apart = apart_f32(d.shape_box[d.meta[sa].shape], d.pose[sa], A.rmax, d.shape_box[d.meta[sb].shape],
+                              d.pose[sb], B.rmax);
+        if (!apart)
+        {
+            V3<T> dc = B.pos - A.pos;
+            T rs = A.rmax + B.rmax;
+            T cull = rs + (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
+            const T margin = (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
+            apart = sqnorm(dc) > cull * cull ||
+                    obb_separated(d.shape_box[d.meta[sa].shape], A.q, A.pos, d.shape_box[d.meta[sb].shape], B.q,
+                                  B.pos, margin + T(1e-5) * rs);
+        }
+        if (apart)
         {
             Collision<T> none;
             manifold_update(d, p, old_idx, A, B, false, none);

@@ -75,6 +75,7 @@ template <class T> struct ShapeRef
     T rmax;
     int uv_stacks;  // > 0: the vertex list is a UV sphere of this layout (pk_shape_sphere)
     int uv_sectors;
+    const float *v32 = nullptr; // FP64 form: the same vertices rounded to FP32 (support filter)
 
     // First strictly maximal vertex of v.ld over the vertex list, in index order.
     PK_HD int argmax_linear(V3<T> ld, int lo, int hi, int best, T &bd) const
@@ -162,32 +163,39 @@ template <class T> struct ShapeRef
     // are compared by value, then by lower index, so ties resolve as in the linear scan.
     PK_HD int argmax_uv(V3<T> ld) const
     {
-        const int S = uv_stacks, K = uv_sectors, last = nverts - 1;
         int best = -1;
         T bd = T(0);
-        auto take = [&](int i) {
+        T dn = norm(ld);
+        if (!(dn > T(0))) return 0; // every value is zero: the first vertex
+        uv_window(ld, dn, [&](int i) {
             T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
             if (best < 0 || v > bd || (v == bd && i < best))
             {
                 bd = v;
                 best = i;
             }
-        };
-        T dn = norm(ld);
-        if (!(dn > T(0))) return 0; // every value is zero: the first vertex
-        T cy = ld.y / dn;
-        cy = cy > T(1) ? T(1) : (cy < T(-1) ? T(-1) : cy);
-        const T pi = T(3.14159265358979323846);
-        T f = pk_acos(cy) * T(S) / pi; // fractional ring index, 0 at the north pole
+        });
+        return best;
+    }
+
+    // The UV-sphere vertices argmax_uv compares (see there), visited in the window's order; U is
+    // the precision of the angle arithmetic (dn = |ld| > 0).
+    template <class U, class F> PK_HD void uv_window(V3<U> ld, U dn, F take) const
+    {
+        const int S = uv_stacks, K = uv_sectors, last = nverts - 1;
+        U cy = ld.y / dn;
+        cy = cy > U(1) ? U(1) : (cy < U(-1) ? U(-1) : cy);
+        const U pi = U(3.14159265358979323846);
+        U f = pk_acos(cy) * U(S) / pi; // fractional ring index, 0 at the north pole
         int i0 = int(f);
         i0 = i0 < 0 ? 0 : (i0 > S ? S : i0);
         int ilo = i0 - 1, ihi = i0 + 2;
-        T sphi2 = T(1) - cy * cy;
+        U sphi2 = U(1) - cy * cy;
         // sin(phi) below which the sector gap could fall under 1e-4: 1e-4 / (sin(pi/S) *
         // (cos(pi/K) - cos(4 pi/K))), with x - x^3/6 <= sin x making it an over-estimate
-        const T dp = pi / T(S), a1 = T(2.5) * pi / T(K), a2 = T(1.5) * pi / T(K);
-        const T lb = (dp - dp * dp * dp / T(6)) * T(2) * (a1 - a1 * a1 * a1 / T(6)) * (a2 - a2 * a2 * a2 / T(6));
-        const T thr = T(1e-4) / lb;
+        const U dp = pi / U(S), a1 = U(2.5) * pi / U(K), a2 = U(1.5) * pi / U(K);
+        const U lb = (dp - dp * dp * dp / U(6)) * U(2) * (a1 - a1 * a1 * a1 / U(6)) * (a2 - a2 * a2 * a2 / U(6));
+        const U thr = U(1e-4) / lb;
         if (sphi2 < thr * thr)
         {
             // within asin(0.2) of a pole: the pole and whole rings
@@ -196,11 +204,11 @@ template <class T> struct ShapeRef
             int a = ilo < 1 ? 1 : ilo, b = ihi > S - 1 ? S - 1 : ihi;
             for (int i = a; i <= b; ++i)
                 for (int j = 0; j < K; ++j) take(1 + (i - 1) * K + j);
-            return best;
+            return;
         }
-        T th = pk_atan2(ld.z, ld.x);
-        if (th < T(0)) th = th + T(2) * pi;
-        int j0 = int(th * T(K) / (T(2) * pi));
+        U th = pk_atan2(ld.z, ld.x);
+        if (th < U(0)) th = th + U(2) * pi;
+        int j0 = int(th * U(K) / (U(2) * pi));
         j0 = j0 > K - 1 ? K - 1 : j0;
         for (int i = ilo; i <= ihi; ++i)
         {
@@ -220,6 +228,59 @@ template <class T> struct ShapeRef
                 take(1 + (i - 1) * K + j);
             }
         }
+    }
+
+    // FP64 form: the same vertex as the FP64 search (first strictly maximal value, in index
+    // order), found with FP32 arithmetic wherever it decides. ld and every vertex value are
+    // evaluated in FP32 from the FP32 copies of q, d and the vertices; each differs from its FP64
+    // value by at most 16 FP32 ulps of rmax |d| (rotation 12, dot product 3, vertex rounding 1),
+    // so a vertex whose FP32 value lies more than tol = 128 ulps below the FP32 maximum cannot
+    // reach the FP64 maximum or tie with it. When one vertex is within tol of the maximum it is the
+    // answer; otherwise only those within tol are evaluated in FP64, in index order, from the
+    // FP64 direction. The UV window is the one argmax_uv uses (angles in FP32: near a ring or
+    // sector boundary the window can shift by one, and it still holds the maximum and every vertex
+    // within rounding of it, the others trailing by at least 1e-4 relative).
+    PK_HD int argmax_filtered(V3<T> d) const
+    {
+        const V3<float> df{float(d.x), float(d.y), float(d.z)};
+        const Qt<float> qf{float(q.w), float(q.x), float(q.y), float(q.z)};
+        const V3<float> l = rotate(conj(qf), df);
+        const float dn = norm(df);
+        const float tol = 128.0f * EpsOf<float>::v * float(rmax) * dn;
+        float mx = -3.0e38f;
+        int arg = 0, cnt = 0;
+        auto value = [&](int i) { return v32[3 * i] * l.x + v32[3 * i + 1] * l.y + v32[3 * i + 2] * l.z; };
+        auto scan = [&](auto &&visit) {
+            if (uv_stacks > 0 && dn > 0.0f)
+                uv_window(l, norm(l), visit);
+            else
+                for (int i = 0; i < nverts; ++i) visit(i);
+        };
+        scan([&](int i) {
+            const float v = value(i);
+            if (v > mx) mx = v;
+        });
+        scan([&](int i) {
+            if (value(i) >= mx - tol)
+            {
+                ++cnt;
+                arg = i;
+            }
+        });
+        if (cnt == 1) return arg;
+        // near-ties: the FP64 values of the candidates decide, as in the FP64 scan
+        const V3<T> ld = rotate(conj(q), d);
+        int best = -1;
+        T bd = T(0);
+        scan([&](int i) {
+            if (value(i) < mx - tol) return;
+            const T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
+            if (best < 0 || v > bd || (v == bd && i < best))
+            {
+                bd = v;
+                best = i;
+            }
+        });
         return best;
     }
 
@@ -239,6 +300,15 @@ template <class T> struct ShapeRef
         }
         // mesh::instance::support -> mesh::support: first strictly maximal vertex
         // (mesh.cpp:341-358, 442-448)
+        if constexpr (sizeof(T) == 8)
+        {
+            if (v32 && ncl == 0)
+            {
+                const int best = argmax_filtered(d);
+                V3<T> lv{verts[3 * best], verts[3 * best + 1], verts[3 * best + 2]};
+                return rotate(q, lv) + pos;
+            }
+        }
         V3<T> ld = rotate(conj(q), d);
         int best;
         if (uv_stacks > 0)
