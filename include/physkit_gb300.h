@@ -357,6 +357,8 @@ typedef struct pk_batch_info
 {
     int64_t pool_bodies, bodies_in_use, steps, pending_requests;
     int32_t worlds_live, worlds_free, steps_in_flight, reserved;
+    int64_t graph_captures; /* the batched step is replayed from a CUDA graph, captured again after
+                               admissions or retirements change the solver schedule */
 } pk_batch_info;
 void pk_batch_desc_init(pk_batch_desc *desc);
 int pk_batch_create(const pk_batch_desc *desc, pk_batch **out);

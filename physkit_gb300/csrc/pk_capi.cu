@@ -100,6 +100,7 @@ struct pk_world
     size_t wake_head = 0;
     int dispatched_step = 0;     // host step whose events were last offered to the waiters
     int device = 0;              // CUDA device current at pk_world_create: its stream and buffers live there
+    int launch_version = 0;      // bumped when launch shapes change (a captured step graph is stale)
 };
 
 // Allocation-free narrowphase (pk_collide_noalloc). Its device staging lives in this file-scope
@@ -1061,6 +1062,7 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
     tu.tiny_world = t->tiny_world;
     tu.tiny_threads = t->tiny_threads > 0 ? t->tiny_threads : 32;
     w->eng->set_tunables(tu);
+    w->launch_version++;
     return PK_OK;
 }
 
@@ -1508,6 +1510,8 @@ struct pk_batch
     std::vector<uint8_t> mask;
     std::deque<pk_batch_event> ready; // completions not yet returned by pk_batch_poll
     int64_t steps = 0;
+    int graph_version = -1; // launch_version of the world when the step graph was captured
+    int64_t captures = 0;
 };
 
 namespace
@@ -1695,7 +1699,22 @@ int pk_batch_step_async(pk_batch *b, int32_t *nworlds)
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
     }
-    if (int rc = step_async(w, b->desc.dt, true)) return rc;
+    // The step is replayed from a CUDA graph: one launch instead of ~60. Its launch shapes depend
+    // on the solver schedule (which changes with admissions and retirements) and the tuning, so it
+    // is captured again after either changed; the active mask lives in device memory.
+    if (w->order_dirty || b->graph_version != w->launch_version)
+    {
+        if (int rc = flush_shapes(w)) return rc;
+        if (int rc = flush_order(w, true)) return rc;
+        if (w->eng->capture_graph(b->desc.dt))
+        {
+            g_last_cuda = w->eng->last_error();
+            return PK_ERR_CUDA;
+        }
+        b->graph_version = w->launch_version;
+        b->captures++;
+    }
+    if (int rc = pk_world_step_graph(w)) return rc;
     if (!b->spare.empty())
     {
         f.ev = b->spare.back();
@@ -1768,6 +1787,7 @@ int pk_batch_stats(pk_batch *b, pk_batch_info *st)
     st->worlds_live = b->desc.max_worlds - st->worlds_free;
     st->steps_in_flight = int32_t(b->flight.size());
     st->steps = b->steps;
+    st->graph_captures = b->captures;
     int64_t pend = 0;
     for (const auto &s : b->slots) pend += int64_t(s.pending.size());
     st->pending_requests = pend;

@@ -2268,6 +2268,9 @@ __global__ void __launch_bounds__(MAXT)
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
+    // per colour, manifolds of each class (one body static or not, x 1..4 contacts): each colour
+    // is laid out class by class, so the lanes of a warp run the same contact loop
+    __shared__ int sub[8][kMaxColours];
     __shared__ int wsum[MAXT / 32];
     __shared__ int remaining;
     __shared__ int nactive;
@@ -2327,6 +2330,7 @@ __global__ void __launch_bounds__(MAXT)
     {
         ccount[c] = 0;
         cursor[c] = 0;
+        for (int q = 0; q < 8; ++q) sub[q][c] = 0;
     }
     if (tid == 0) remaining = na;
     __syncthreads();
@@ -2519,10 +2523,18 @@ __global__ void __launch_bounds__(MAXT)
         }
     }
     const int ncol = round;
+    // a manifold's class: with a static body or not, and its number of contact rows
+    auto mclass = [&](const uint4 &r) {
+        return (((r.y | r.z) >> 31) ? 4 : 0) + (__popc(unsigned(d.rowmask[r.x])) - 1);
+    };
     for (int k = tid; k < na; k += nt)
     {
         int c = colour[k];
-        if (c >= 0 && c < kMaxColours) atomicAdd(&ccount[c], 1);
+        if (c >= 0 && c < kMaxColours)
+        {
+            atomicAdd(&ccount[c], 1);
+            atomicAdd(&sub[mclass(rec[k])][c], 1);
+        }
     }
     __syncthreads();
     if (tid == 0)
@@ -2531,16 +2543,22 @@ __global__ void __launch_bounds__(MAXT)
         for (int c = 0; c < ncol; ++c)
         {
             cstart[c] = s;
-            s += ccount[c];
+            for (int q = 0; q < 8; ++q)
+            {
+                const int t = sub[q][c];
+                sub[q][c] = s; // the class's first position, then its cursor
+                s += t;
+            }
         }
         d.ncolours[w] = ncol;
     }
     __syncthreads();
+    // within a colour no two manifolds share a dynamic body, so their order does not change results
     for (int k = tid; k < na; k += nt)
     {
         int c = colour[k];
         const uint4 r = rec[k];
-        if (c >= 0 && c < kMaxColours) d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = r;
+        if (c >= 0 && c < kMaxColours) d.srec[ms + atomicAdd(&sub[mclass(r)][c], 1)] = r;
         d.pair_colour[r.x] = c; // per-pair colour for read-back (-2: no contact rows)
     }
     __syncthreads();

@@ -100,7 +100,7 @@ class BatchEventC(C.Structure):
 class BatchInfoC(C.Structure):
     _fields_ = [("pool_bodies", C.c_int64), ("bodies_in_use", C.c_int64), ("steps", C.c_int64),
                 ("pending_requests", C.c_int64), ("worlds_live", C.c_int32), ("worlds_free", C.c_int32),
-                ("steps_in_flight", C.c_int32), ("reserved", C.c_int32)]
+                ("steps_in_flight", C.c_int32), ("reserved", C.c_int32), ("graph_captures", C.c_int64)]
 
 
 BATCH_STEPPED, BATCH_RETIRED = 1, 2
