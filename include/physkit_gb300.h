@@ -218,6 +218,35 @@ typedef struct pk_ray
 } pk_ray;
 int pk_world_raycast(pk_world *w, const pk_ray *rays, int32_t n, int32_t cap, uint64_t *handles, double *distances,
                      int32_t *counts);
+/* Ray against one mesh instance: mesh::instance::ray_intersect (mesh.cpp:400-415) over
+ * mesh::ray_intersect (mesh.cpp:169-197) and ray::intersect (bvh.h:97-135, Moeller-Trumbore,
+ * |a| < 1e-12 parallel). The ray goes into the body frame (its direction normalised, bvh.h:47-50),
+ * the nearest triangle hit within max_distance is kept, and its point and normal come back in world
+ * space. `body` names a live body (its shape and its pose after the last step); with
+ * body = PK_HANDLE_ANY, `shape` and the pose given here are used (identity pose: the mesh's own
+ * frame, mesh::ray_intersect). Triangles hit at exactly the same distance resolve to the later
+ * triangle index; the reference takes the later one in its static BVH's visiting order. */
+typedef struct pk_mesh_ray
+{
+    uint64_t body;
+    int32_t shape;
+    int32_t reserved;
+    double pos[3];
+    double quat[4]; /* w, x, y, z */
+    double origin[3];
+    double direction[3];
+    double max_distance;
+} pk_mesh_ray;
+typedef struct pk_mesh_hit
+{
+    double pos[3];
+    double normal[3];
+    double distance;
+    int32_t hit;      /* 1 on a hit */
+    int32_t triangle; /* index of the triangle in the shape's triangle list */
+} pk_mesh_hit;
+int pk_mesh_raycast(pk_world *w, const pk_mesh_ray *rays, int32_t n, pk_mesh_hit *hits);
+
 /* Joints, replacing constraint_solver::add_constraint / remove_constraint (constraint.h:1036-1049)
  * and the joint types of constraint.h:139-865, added through the world's command queue
  * (world.h:155-175). type: 0 distance (local_a, local_b, distance), 1 ball_socket (anchor, world

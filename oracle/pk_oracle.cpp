@@ -419,6 +419,65 @@ std::shared_ptr<Mesh> mesh_pyramid(double b, double h)
     return make_mesh(std::move(v), std::move(t));
 }
 
+// ray::intersect, Moeller-Trumbore (bvh.h:97-135): the hit of one triangle within max_d.
+struct TriHit
+{
+    V3 pos, normal;
+    double t;
+};
+inline bool ray_triangle(const V3 &o, const V3 &d, const V3 &v0, const V3 &v1, const V3 &v2, double max_d, TriHit &out)
+{
+    const double eps = 1e-12;
+    V3 e1 = v1 - v0, e2 = v2 - v0;
+    V3 h = cross(d, e2);
+    double a = dot(e1, h);
+    if (a > -eps && a < eps) return false;
+    double f = 1.0 / a;
+    V3 sv = o - v0;
+    double u = f * dot(sv, h);
+    if (u < 0.0 || u > 1.0) return false;
+    V3 q = cross(sv, e1);
+    double v = f * dot(d, q);
+    if (v < 0.0 || u + v > 1.0) return false;
+    double t = f * dot(e2, q);
+    if (t < 0.0 || t > max_d) return false;
+    out = {o + d * t, normalized(cross(e1, e2)), t};
+    return true;
+}
+
+// mesh::instance::ray_intersect (mesh.cpp:400-415) over mesh::ray_intersect (mesh.cpp:169-197):
+// the ray goes into the body frame (and its direction is normalised again by the ray
+// constructor), every triangle is tested with the running best distance as the limit, so a later
+// triangle at the same distance replaces an earlier one, and the hit comes back to world space.
+// Triangles are visited in index order: the reference visits them in its static BVH's order, which
+// can only differ where two triangles are hit at exactly the same distance.
+inline bool mesh_ray_intersect(const Mesh &m, V3 pos, Qt q, V3 origin, V3 dir, double max_d, TriHit &out, int &tri)
+{
+    Ray world(origin, dir);
+    Qt inv = conj(q);
+    Ray local(rotate(inv, world.o - pos), rotate(inv, world.d));
+    double best_t = max_d;
+    bool found = false;
+    for (size_t i = 0; i < m.tris.size(); ++i)
+    {
+        TriHit h;
+        const auto &t = m.tris[i];
+        if (ray_triangle(local.o, local.d, m.verts[t[0]], m.verts[t[1]], m.verts[t[2]], best_t, h))
+        {
+            best_t = h.t;
+            out = h;
+            tri = int(i);
+            found = true;
+        }
+    }
+    if (found)
+    {
+        out.pos = rotate(q, out.pos) + pos;
+        out.normal = rotate(q, out.normal);
+    }
+    return found;
+}
+
 struct MeshInst
 {
     const Mesh *mesh;
@@ -2279,6 +2338,13 @@ int pko_shape_mesh(pko_world *w, const double *v, int nv, const int *t, int nt)
     return add_shape(w, make_mesh(std::move(vv), std::move(tt)));
 }
 int pko_shape_vertex_count(pko_world *w, int s) { return static_cast<int>(w->w.shapes[s]->verts.size()); }
+int pko_shape_triangles(pko_world *w, int s, int *out, int cap)
+{
+    const auto &t = w->w.shapes[size_t(s)]->tris;
+    for (size_t i = 0; i < t.size() && int(i) < cap; ++i)
+        for (int k = 0; k < 3; ++k) out[3 * i + size_t(k)] = int(t[i][size_t(k)]);
+    return int(t.size());
+}
 int pko_shape_vertices(pko_world *w, int s, double *out, int cap)
 {
     auto &v = w->w.shapes[s]->verts;
@@ -2421,6 +2487,21 @@ int pko_gjk_epa(pko_world *w, int ka, const double *pa, int sa, int kb, const do
     double v[10] = {r->normal.x, r->normal.y, r->normal.z, r->world_a.x, r->world_a.y,
                     r->world_a.z, r->world_b.x, r->world_b.y, r->world_b.z, r->depth};
     std::copy(v, v + 10, out);
+    return 1;
+}
+
+int pko_mesh_raycast(pko_world *w, int shape, const double *pose7, const double *origin, const double *dir,
+                     double max_dist, double *out7, int *tri)
+{
+    TriHit h;
+    int t = -1;
+    bool hit = mesh_ray_intersect(*w->w.shapes[size_t(shape)], {pose7[0], pose7[1], pose7[2]},
+                                  {pose7[3], pose7[4], pose7[5], pose7[6]}, {origin[0], origin[1], origin[2]},
+                                  {dir[0], dir[1], dir[2]}, max_dist, h, t);
+    if (!hit) return 0;
+    const double v[7] = {h.pos.x, h.pos.y, h.pos.z, h.normal.x, h.normal.y, h.normal.z, h.t};
+    std::copy(v, v + 7, out7);
+    *tri = t;
     return 1;
 }
 

@@ -38,6 +38,7 @@ int pko_shape_sphere(pko_world *w, double radius, int stacks, int sectors);
 int pko_shape_pyramid(pko_world *w, double base_half, double height);
 int pko_shape_mesh(pko_world *w, const double *verts, int nverts, const int *tris, int ntris);
 int pko_shape_vertex_count(pko_world *w, int shape);
+int pko_shape_triangles(pko_world *w, int shape, int *out, int cap); /* 3 vertex indices each; returns the count */
 int pko_shape_vertices(pko_world *w, int shape, double *out, int cap);
 double pko_shape_volume(pko_world *w, int shape);
 
@@ -72,6 +73,10 @@ uint64_t pko_joint_add(pko_world *w, int type, uint64_t a, uint64_t b, const dou
 int pko_joint_remove(pko_world *w, uint64_t handle);
 int pko_joint_impulses(pko_world *w, uint64_t handle, double *out6);
 /* world_base::raycast (world.h:260-319): hits in the reference's order; returns the hit count */
+/* mesh::instance::ray_intersect (mesh.cpp:400-415) of shape at pose7 (pos3, quat wxyz): 1 with
+ * out7 = hit pos3, normal3, distance and the triangle index; 0 on a miss. */
+int pko_mesh_raycast(pko_world *w, int shape, const double *pose7, const double *origin, const double *dir,
+                     double max_dist, double *out7, int *tri);
 int pko_world_raycast(pko_world *w, const double *origin, const double *dir, double max_dist, uint64_t *handles,
                       double *dist, int cap);
 /* Colour of each active manifold of the last step (key order) and the colour count. */

@@ -35,6 +35,7 @@ def lib():
             "pko_shape_pyramid": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
             "pko_shape_mesh": (C.c_int, [C.c_void_p, dp, C.c_int, ip, C.c_int]),
             "pko_shape_vertex_count": (C.c_int, [C.c_void_p, C.c_int]),
+            "pko_shape_triangles": (C.c_int, [C.c_void_p, C.c_int, ip, C.c_int]),
             "pko_shape_vertices": (C.c_int, [C.c_void_p, C.c_int, dp, C.c_int]),
             "pko_shape_volume": (C.c_double, [C.c_void_p, C.c_int]),
             "pko_body_add": (C.c_uint64, [C.c_void_p, C.c_int, dp, dp, dp, dp, C.c_double, dp,
@@ -48,6 +49,7 @@ def lib():
             "pko_read_manifolds": (C.c_int, [C.c_void_p, up, ip, dp, C.c_int]),
             "pko_read_events": (C.c_int, [C.c_void_p, up, ip, C.c_int]),
             "pko_world_raycast": (C.c_int, [C.c_void_p, dp, dp, C.c_double, up, dp, C.c_int]),
+            "pko_mesh_raycast": (C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, C.c_double, dp, ip]),
             "pko_joint_add": (C.c_uint64, [C.c_void_p, C.c_int, C.c_uint64, C.c_uint64, dp]),
             "pko_joint_remove": (C.c_int, [C.c_void_p, C.c_uint64]),
             "pko_joint_impulses": (C.c_int, [C.c_void_p, C.c_uint64, dp]),
@@ -125,6 +127,12 @@ class OracleWorld:
         out = np.zeros(3 * n)
         self.L.pko_shape_vertices(self.h, shape, out.ctypes.data_as(P(C.c_double)), n)
         return out.reshape(n, 3)
+
+    def triangles(self, shape):
+        n = self.L.pko_shape_triangles(self.h, shape, None, 0)
+        out = np.zeros(3 * max(n, 1), dtype=np.int32)
+        self.L.pko_shape_triangles(self.h, shape, out.ctypes.data_as(P(C.c_int)), n)
+        return out[: 3 * n].reshape(n, 3)
 
     def volume(self, shape):
         return self.L.pko_shape_volume(self.h, shape)
@@ -210,6 +218,19 @@ class OracleWorld:
         out, op = _dp(np.zeros(6))
         n = self.L.pko_joint_impulses(self.h, int(handle), op)
         return out[:max(n, 0)]
+
+    def mesh_raycast(self, shape, pose7, origin, direction, max_dist):
+        """mesh::instance::ray_intersect of `shape` at pose7 (pos, quat wxyz): None or
+        (pos3, normal3, distance, triangle)."""
+        p, pp = _dp(pose7)
+        o, op = _dp(origin)
+        d, dp_ = _dp(direction)
+        out = np.zeros(7)
+        tri = C.c_int()
+        if not self.L.pko_mesh_raycast(self.h, int(shape), pp, op, dp_, float(max_dist),
+                                       out.ctypes.data_as(P(C.c_double)), C.byref(tri)):
+            return None
+        return out[0:3].copy(), out[3:6].copy(), float(out[6]), tri.value
 
     def raycast(self, origin, direction, max_dist):
         """world_base::raycast (world.h:260-319): [(handle, distance)] in the reference's order."""

@@ -85,6 +85,8 @@ struct pk_world
     std::vector<double> clusters; // (centre xyz, radius) per cluster of 8 consecutive vertices
     std::vector<double> rmax;     // bounding radius of each shape about its origin
     std::vector<double> boxes;   // local aabb per shape
+    std::vector<int> tris;       // triangles of all shapes (vertex indices within the shape)
+    std::vector<int> tri_range;  // per shape: first triangle, triangle count
     std::vector<SubWorld> worlds;
     std::vector<SlotInfo> slots;
     std::vector<int> free_slots;
@@ -324,7 +326,8 @@ void pk_world_destroy(pk_world *w)
 
 // uv_stacks/uv_sectors: the layout of a UV sphere from pk_shape_sphere (0: any other vertex list);
 // the device's support search then looks only near the query direction.
-static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out, int uv_stacks = 0, int uv_sectors = 0)
+static int add_shape(pk_world *w, const std::vector<double> &v, const std::vector<int> &tris, int32_t *out,
+                     int uv_stacks = 0, int uv_sectors = 0)
 {
     size_t nv = v.size() / 3;
     if (nv == 0) return PK_ERR_INVALID;
@@ -399,6 +402,9 @@ static int add_shape(pk_world *w, const std::vector<double> &v, int32_t *out, in
     w->verts.insert(w->verts.end(), v.begin(), v.end());
     for (int k = 0; k < 3; ++k) w->boxes.push_back(mn[k]);
     for (int k = 0; k < 3; ++k) w->boxes.push_back(mx[k]);
+    w->tri_range.push_back(int(w->tris.size() / 3));
+    w->tri_range.push_back(int(tris.size() / 3));
+    w->tris.insert(w->tris.end(), tris.begin(), tris.end());
     w->shapes_dirty = true; // uploaded in one copy before the next use (flush_shapes)
     if (out) *out = id;
     return PK_OK;
@@ -494,7 +500,8 @@ static void drop_joint(pk_world *w, int j)
 static int flush_shapes(pk_world *w)
 {
     if (!w->shapes_dirty) return PK_OK;
-    if (w->eng->set_shapes(w->verts, w->ranges, w->boxes, w->clusters, w->rmax))
+    if (w->eng->set_shapes(w->verts, w->ranges, w->boxes, w->clusters, w->rmax) ||
+        w->eng->set_triangles(w->tris, w->tri_range))
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
@@ -508,7 +515,8 @@ int pk_shape_mesh(pk_world *w, const double *verts, int32_t nverts, const int32_
     if (!w || !verts || nverts <= 0 || ntris <= 0 || !tris) return PK_ERR_INVALID;
     for (int i = 0; i < 3 * ntris; ++i)
         if (tris[i] < 0 || tris[i] >= nverts) return PK_ERR_INVALID;
-    return add_shape(w, std::vector<double>(verts, verts + 3 * size_t(nverts)), out);
+    return add_shape(w, std::vector<double>(verts, verts + 3 * size_t(nverts)),
+                     std::vector<int>(tris, tris + 3 * size_t(ntris)), out);
 }
 
 int pk_shape_box(pk_world *w, double hx, double hy, double hz, int32_t *out)
@@ -517,7 +525,10 @@ int pk_shape_box(pk_world *w, double hx, double hy, double hz, int32_t *out)
     // mesh::box vertex order (mesh.cpp:31-40)
     std::vector<double> v = {-hx, -hy, -hz, +hx, -hy, -hz, +hx, +hy, -hz, -hx, +hy, -hz,
                              -hx, -hy, +hz, +hx, -hy, +hz, +hx, +hy, +hz, -hx, +hy, +hz};
-    return add_shape(w, v, out);
+    // its 12 triangles, two per face (mesh.cpp:41-52)
+    std::vector<int> t = {4, 5, 6, 4, 6, 7, 0, 3, 2, 0, 2, 1, 1, 2, 6, 1, 6, 5,
+                          0, 4, 7, 0, 7, 3, 3, 7, 6, 3, 6, 2, 0, 1, 5, 0, 5, 4};
+    return add_shape(w, v, t, out);
 }
 
 int pk_shape_sphere(pk_world *w, double r, int32_t stacks, int32_t sectors, int32_t *out)
@@ -539,9 +550,22 @@ int pk_shape_sphere(pk_world *w, double r, int32_t stacks, int32_t sectors, int3
     v.push_back(0.0);
     v.push_back(-r);
     v.push_back(0.0);
+    // triangles: the north cap, two per quad of each band, the south cap (mesh.cpp:83-113)
+    std::vector<int> t;
+    const int S = stacks, K = sectors, south = 1 + (S - 1) * K;
+    for (int j = 0; j < K; ++j) t.insert(t.end(), {0, 1 + (j + 1) % K, 1 + j});
+    for (int i = 1; i + 1 < S; ++i)
+        for (int j = 0; j < K; ++j)
+        {
+            const int top = 1 + (i - 1) * K + j, top_next = 1 + (i - 1) * K + (j + 1) % K;
+            const int bot = 1 + i * K + j, bot_next = 1 + i * K + (j + 1) % K;
+            t.insert(t.end(), {top, top_next, bot_next, top, bot_next, bot});
+        }
+    const int last = 1 + (S - 2) * K;
+    for (int j = 0; j < K; ++j) t.insert(t.end(), {south, last + j, last + (j + 1) % K});
     // the neighbourhood search is proven for these layouts (pk_narrow.cuh, argmax_uv)
     const bool uv = pk::uv_layout_ok(stacks, sectors);
-    return add_shape(w, v, out, uv ? stacks : 0, uv ? sectors : 0);
+    return add_shape(w, v, t, out, uv ? stacks : 0, uv ? sectors : 0);
 }
 
 int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)
@@ -549,7 +573,8 @@ int pk_shape_pyramid(pk_world *w, double b, double h, int32_t *out)
     if (!w) return PK_ERR_INVALID;
     // mesh::pyramid (mesh.cpp:117-137)
     std::vector<double> v = {-b, 0.0, -b, +b, 0.0, -b, +b, 0.0, +b, -b, 0.0, +b, 0.0, h, 0.0};
-    return add_shape(w, v, out);
+    std::vector<int> t = {0, 1, 2, 0, 2, 3, 1, 0, 4, 2, 1, 4, 3, 2, 4, 0, 3, 4};
+    return add_shape(w, v, t, out);
 }
 
 static int add_bodies(pk_world *w, const pk_body_desc *descs, int32_t n, uint64_t *out, bool async);
@@ -1452,6 +1477,46 @@ int pk_world_raycast(pk_world *w, const pk_ray *rays, int32_t n, int32_t cap, ui
             handles[size_t(i) * size_t(cap) + size_t(j)] = hit[size_t(j)].second;
             distances[size_t(i) * size_t(cap) + size_t(j)] = hit[size_t(j)].first;
         }
+    }
+    return PK_OK;
+}
+
+int pk_mesh_raycast(pk_world *w, const pk_mesh_ray *rays, int32_t n, pk_mesh_hit *hits)
+{
+    if (!w || n < 0 || (n > 0 && (!rays || !hits))) return PK_ERR_INVALID;
+    const int nshapes = int(w->ranges.size() / 8);
+    std::vector<pk::MeshRayIn> in(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i)
+    {
+        const pk_mesh_ray &r = rays[i];
+        pk::MeshRayIn &q = in[size_t(i)];
+        q.slot = -1;
+        q.shape = r.shape;
+        if (r.body != PK_HANDLE_ANY)
+        {
+            int slot;
+            if (!resolve(w, r.body, &slot)) return PK_ERR_STALE_HANDLE;
+            q.slot = slot;
+        }
+        else if (r.shape < 0 || r.shape >= nshapes)
+            return PK_ERR_INVALID;
+        if (!(r.max_distance >= 0.0)) return PK_ERR_INVALID;
+        for (int k = 0; k < 3; ++k)
+        {
+            q.pos[k] = r.pos[k];
+            q.o[k] = r.origin[k];
+            q.d[k] = r.direction[k];
+        }
+        for (int k = 0; k < 4; ++k) q.q[k] = r.quat[k];
+        q.maxd = r.max_distance;
+    }
+    if (int rc = flush_shapes(w)) return rc;
+    if (n == 0) return PK_OK;
+    static_assert(sizeof(pk_mesh_hit) == sizeof(pk::MeshHitOut), "layout shared with the device result");
+    if (w->eng->mesh_raycast(in.data(), n, reinterpret_cast<pk::MeshHitOut *>(hits)))
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
     }
     return PK_OK;
 }

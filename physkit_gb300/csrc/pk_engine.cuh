@@ -21,6 +21,7 @@
 // reinserted in the tree at or after the step in which the younger of the two was created.
 #pragma once
 
+#include "pk_engine_api.h"
 #include "pk_math.cuh"
 #include "pk_narrow.cuh"
 #include "pk_sort.cuh"
@@ -3105,6 +3106,79 @@ template <class T> __global__ void k_purge_pairs(Dev<T> d, uint32_t world, uint3
         uint32_t w = uint32_t(k >> (2 * d.lbits));
         uint32_t lo = uint32_t((k >> d.lbits) & mask), hi = uint32_t(k & mask);
         if (w == world && (lo == local || hi == local)) d.man_old[p].n = 0;
+    }
+}
+
+// Rays against mesh instances (mesh::instance::ray_intersect, mesh.cpp:400-415): one thread per
+// ray. The ray is moved into the body frame and its direction normalised again (the ray
+// constructor, bvh.h:47-50); every triangle is tested in index order by Moeller-Trumbore
+// (ray::intersect, bvh.h:97-135) with the running best distance as its limit, so a later triangle
+// at the same distance replaces an earlier one; the hit goes back to world space.
+template <class T>
+__global__ void k_mesh_raycast(Dev<T> d, const int *__restrict__ tris, const int2 *__restrict__ trange,
+                               const MeshRayIn *__restrict__ rays, int n, MeshHitOut *__restrict__ out)
+{
+    PK_GRID_STRIDE(i, n)
+    {
+        const MeshRayIn r = rays[i];
+        int shape = r.shape;
+        V3<T> P{T(r.pos[0]), T(r.pos[1]), T(r.pos[2])};
+        Qt<T> q{T(r.q[0]), T(r.q[1]), T(r.q[2]), T(r.q[3])};
+        if (r.slot >= 0)
+        {
+            shape = int(d.meta[r.slot].shape);
+            P = ld3(d.pose[r.slot].p);
+            q = ldq(d.pose[r.slot].q);
+        }
+        const V3<T> dw = normalized(V3<T>{T(r.d[0]), T(r.d[1]), T(r.d[2])});
+        const V3<T> ow{T(r.o[0]), T(r.o[1]), T(r.o[2])};
+        const Qt<T> iq = conj(q);
+        const V3<T> o = rotate(iq, ow - P);
+        const V3<T> dl = normalized(rotate(iq, dw));
+        const T *vb = d.verts + 3 * d.shape_range[shape].vstart;
+        const int2 tr = trange[shape];
+        T best = T(r.maxd);
+        int best_tri = -1;
+        V3<T> e1b{}, e2b{};
+        for (int k = 0; k < tr.y; ++k)
+        {
+            const int *t = tris + 3 * (tr.x + k);
+            const V3<T> v0 = ld3(vb + 3 * t[0]), v1 = ld3(vb + 3 * t[1]), v2 = ld3(vb + 3 * t[2]);
+            const V3<T> e1 = v1 - v0, e2 = v2 - v0;
+            const V3<T> h = cross(dl, e2);
+            const T a = dot(e1, h);
+            if (a > T(-1e-12) && a < T(1e-12)) continue;
+            const T f = T(1) / a;
+            const V3<T> sv = o - v0;
+            const T u = f * dot(sv, h);
+            if (u < T(0) || u > T(1)) continue;
+            const V3<T> qv = cross(sv, e1);
+            const T v = f * dot(dl, qv);
+            if (v < T(0) || u + v > T(1)) continue;
+            const T tt = f * dot(e2, qv);
+            if (tt < T(0) || tt > best) continue;
+            best = tt;
+            best_tri = k;
+            e1b = e1;
+            e2b = e2;
+        }
+        MeshHitOut h{};
+        h.hit = best_tri >= 0;
+        h.triangle = best_tri;
+        if (best_tri >= 0)
+        {
+            const V3<T> pl = o + dl * best;
+            const V3<T> pw = rotate(q, pl) + P;
+            const V3<T> nw = rotate(q, normalized(cross(e1b, e2b)));
+            h.pos[0] = double(pw.x);
+            h.pos[1] = double(pw.y);
+            h.pos[2] = double(pw.z);
+            h.normal[0] = double(nw.x);
+            h.normal[1] = double(nw.y);
+            h.normal[2] = double(nw.z);
+            h.distance = double(best);
+        }
+        out[i] = h;
     }
 }
 

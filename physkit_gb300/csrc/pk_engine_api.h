@@ -55,6 +55,19 @@ struct StepCounters
     long long gjk_iters = 0, epa_iters = 0, epa_iters_heavy = 0;
 };
 
+// A ray against one mesh instance (pk_mesh_raycast): the body's slot (its shape and current pose
+// on the device), or slot -1 with the shape and pose given here.
+struct MeshRayIn
+{
+    int slot, shape;
+    double pos[3], q[4], o[3], d[3], maxd;
+};
+struct MeshHitOut
+{
+    double pos[3], normal[3], distance;
+    int32_t hit, triangle;
+};
+
 constexpr int kStages = 9;
 extern const char *const kStageNames[kStages];
 
@@ -99,6 +112,9 @@ public:
     // rays: 8 doubles each (origin, direction, distance limit, world); per ray up to `cap` nearest
     // hits (device slot, distance) ordered by (distance, slot), and the total hit count
     virtual int raycast(const double *rays, int n, int cap, int *counts, int *slots, double *dists) = 0;
+    // triangles of every shape (3 vertex indices within the shape each) and each shape's range
+    virtual int set_triangles(const std::vector<int> &tris, const std::vector<int> &range) = 0;
+    virtual int mesh_raycast(const MeshRayIn *rays, int n, MeshHitOut *out) = 0;
     // The narrowphase launch of collide on device buffers the caller provides; allocates nothing.
     // status_any_dev (may be null): OR of every pair's status bits
     virtual int collide_device(const void *specs_a_dev, const void *specs_b_dev, int n, double *out_dev,

@@ -959,6 +959,46 @@ public:
         return 0;
     }
 
+    int set_triangles(const std::vector<int> &tris, const std::vector<int> &range) override
+    {
+        const size_t nt = tris.size(), ns = range.size() / 2;
+        if (nt > tri_cap_)
+        {
+            if (tris_) cudaFree(tris_);
+            tris_ = nullptr;
+            tri_cap_ = nt + nt / 2 + 64;
+            PK_CUDA(cudaMalloc(&tris_, sizeof(int) * tri_cap_));
+        }
+        if (ns > trange_cap_)
+        {
+            if (trange_) cudaFree(trange_);
+            trange_ = nullptr;
+            trange_cap_ = ns + ns / 2 + 16;
+            PK_CUDA(cudaMalloc(&trange_, sizeof(int2) * trange_cap_));
+        }
+        if (nt) PK_CUDA(cudaMemcpyAsync(tris_, tris.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st_));
+        if (ns) PK_CUDA(cudaMemcpyAsync(trange_, range.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int mesh_raycast(const MeshRayIn *rays, int n, MeshHitOut *out) override
+    {
+        if (n <= 0) return 0;
+        MeshRayIn *dr = nullptr;
+        MeshHitOut *dh = nullptr;
+        PK_CUDA(cudaMalloc(&dr, sizeof(MeshRayIn) * size_t(n)));
+        PK_CUDA(cudaMalloc(&dh, sizeof(MeshHitOut) * size_t(n)));
+        PK_CUDA(cudaMemcpyAsync(dr, rays, sizeof(MeshRayIn) * size_t(n), cudaMemcpyHostToDevice, st_));
+        k_mesh_raycast<T><<<(n + 127) / 128, 128, 0, st_>>>(d_, tris_, trange_, dr, n, dh);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaMemcpyAsync(out, dh, sizeof(MeshHitOut) * size_t(n), cudaMemcpyDeviceToHost, st_));
+        PK_CUDA(cudaStreamSynchronize(st_));
+        cudaFree(dr);
+        cudaFree(dh);
+        return 0;
+    }
+
     // Joints, ordered by (world, type, arena slot): 5 ints (type, slot a, slot b, local a, local b)
     // and 25 doubles (la3 lb3 axa3 axb3 va3 wa3 qrel4 distance stiffness damping) each, their
     // accumulated impulses (6 each) and every world's range. Growing the buffers drops a captured
@@ -1094,6 +1134,9 @@ private:
     bool timing_ = false;
     bool capturing_ = false;
     uint8_t *mask_dev_ = nullptr;
+    int *tris_ = nullptr;   // triangles of every shape (mesh ray queries)
+    int2 *trange_ = nullptr;
+    size_t tri_cap_ = 0, trange_cap_ = 0;
     StagingRing stage_; // pinned staging of the asynchronous uploads (allocated on first use)
     cudaError_t ensure_staging() { return stage_.ready() ? cudaSuccess : stage_.init(size_t(64) << 20); }
     int launches_ = 0;
@@ -1183,6 +1226,10 @@ private:
         pack_ = nullptr;
         pack_cap_ = 0;
         stage_.release();
+        if (tris_) cudaFree(tris_);
+        if (trange_) cudaFree(trange_);
+        tris_ = nullptr;
+        trange_ = nullptr;
         for (cudaEvent_t e : events_) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         st_ = nullptr;

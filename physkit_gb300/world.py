@@ -106,6 +106,17 @@ class BatchInfoC(C.Structure):
 BATCH_STEPPED, BATCH_RETIRED = 1, 2
 
 
+class MeshRayC(C.Structure):
+    _fields_ = [("body", C.c_uint64), ("shape", C.c_int32), ("reserved", C.c_int32), ("pos", C.c_double * 3),
+                ("quat", C.c_double * 4), ("origin", C.c_double * 3), ("direction", C.c_double * 3),
+                ("max_distance", C.c_double)]
+
+
+class MeshHitC(C.Structure):
+    _fields_ = [("pos", C.c_double * 3), ("normal", C.c_double * 3), ("distance", C.c_double), ("hit", C.c_int32),
+                ("triangle", C.c_int32)]
+
+
 class CollideShapeC(C.Structure):
     _fields_ = [("kind", C.c_int32), ("shape", C.c_int32), ("p", C.c_double * 10)]
 
@@ -178,6 +189,7 @@ def lib():
             "pk_batch_poll": (C.c_int, [vp, P(BatchEventC), C.c_int32, i32p, C.c_int32]),
             "pk_batch_stats": (C.c_int, [vp, P(BatchInfoC)]),
             "pk_batch_read_world": (C.c_int, [vp, C.c_int32, dp, C.c_int32, i32p]),
+            "pk_mesh_raycast": (C.c_int, [vp, P(MeshRayC), C.c_int32, P(MeshHitC)]),
             "pk_last_cuda_error": (C.c_int, []),
             "pk_version": (C.c_char_p, []),
         }
@@ -616,6 +628,28 @@ class World:
             k = min(int(cnt[i]), cap)
             out.append(list(zip(hs[i, :k].tolist(), ds[i, :k].tolist())))
         return out, cnt.copy()
+
+    def mesh_raycast(self, rays):
+        """Rays against mesh instances (mesh::instance::ray_intersect). rays: a list of dicts with
+        origin, direction, max_distance and either body (a handle) or shape + pos + quat (w,x,y,z).
+        Returns per ray None or (pos3, normal3, distance, triangle)."""
+        n = len(rays)
+        R = (MeshRayC * max(n, 1))()
+        for i, r in enumerate(rays):
+            R[i].body = int(r["body"]) if "body" in r else HANDLE_ANY
+            R[i].shape = int(r.get("shape", -1))
+            R[i].pos[:] = list(map(float, r.get("pos", (0, 0, 0))))
+            R[i].quat[:] = list(map(float, r.get("quat", (1, 0, 0, 0))))
+            R[i].origin[:] = list(map(float, r["origin"]))
+            R[i].direction[:] = list(map(float, r["direction"]))
+            R[i].max_distance = float(r.get("max_distance", 1e300))
+        H = (MeshHitC * max(n, 1))()
+        _check(self.L.pk_mesh_raycast(self.h, R, n, H), "pk_mesh_raycast")
+        out = []
+        for i in range(n):
+            h = H[i]
+            out.append((np.array(h.pos[:]), np.array(h.normal[:]), h.distance, h.triangle) if h.hit else None)
+        return out
 
     def pairs(self, with_worlds=False):
         n = C.c_int32()
