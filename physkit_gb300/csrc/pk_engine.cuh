@@ -1256,6 +1256,31 @@ __device__ __forceinline__ bool apart_f32(const Aabb<double> &la, const Pose<dou
     return obb_separated(ba, qa, xa, bb, qb, xb, margin);
 }
 
+// FP64 form: a body's shape in FP32 (pose rounded, the FP32 copies of its vertices) for tests that
+// only decide that two shapes are certainly apart. Shapes with clustered vertex blocks (large
+// non-UV meshes) have no FP32 form here: ok is false.
+__device__ __forceinline__ ShapeRef<float> body_shape32(const Dev<double> &d, int slot, bool &ok)
+{
+    ShapeRef<float> s;
+    const Meta m = d.meta[slot];
+    const ShapeRange r = d.shape_range[m.shape];
+    ok = r.ncl == 0 && d.verts32 != nullptr;
+    s.kind = SHAPE_MESH;
+    s.nverts = r.nverts;
+    s.verts = ok ? d.verts32 + 3 * r.vstart : nullptr;
+    s.ncl = 0;
+    s.cl = nullptr;
+    s.ngr = 0;
+    s.gr = nullptr;
+    s.rmax = float(d.shape_rmax[m.shape]);
+    s.uv_stacks = r.uv_stacks;
+    s.uv_sectors = r.uv_sectors;
+    const Pose<double> &p = d.pose[slot];
+    s.pos = V3<float>{float(p.p[0]), float(p.p[1]), float(p.p[2])};
+    s.q = Qt<float>{float(p.q[0]), float(p.q[1]), float(p.q[2]), float(p.q[3])};
+    return s;
+}
+
 // Last step's manifold of each pair of an active world. Last step's pairs of a world are the
 // segment [mstart_old, mend_old) of last step's sorted keys, and this step's pairs are sorted the
 // same way, so each thread takes a run of consecutive pairs: one binary search for the first,
@@ -1390,10 +1415,31 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
                 const uint64_t val = sval[p];
                 const int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
                 const ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+                if constexpr (sizeof(T) == 8)
+                {
+                    // FP32 first: support values within a few FP32 ulps of the pair's scale, far
+                    // inside a margin of 1024 FP32 epsilons of it
+                    bool oka, okb;
+                    const ShapeRef<float> A32 = body_shape32(d, sa, oka), B32 = body_shape32(d, sb, okb);
+                    if (oka && okb)
+                    {
+                        const float rs = A32.rmax + B32.rmax;
+                        const float m32 = (rs + norm(A32.pos) + norm(B32.pos)) * (1024.0f * EpsOf<float>::v) + 1e-6f +
+                                          1e-5f * rs;
+                        const V3<float> ax32{float(ax.x), float(ax.y), float(ax.z)};
+                        const SupPt<float> sp = minkowski(A32, B32, ax32);
+                        if (dot(sp.p, ax32) < -m32)
+                        {
+                            Collision<T> none;
+                            manifold_update(d, p, oi, A, B, false, none, ax);
+                            settled = true;
+                        }
+                    }
+                }
                 const T rs = A.rmax + B.rmax;
                 const T margin = (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6) + T(1e-5) * rs;
-                const SupPt<T> sp = minkowski(A, B, ax);
-                if (dot(sp.p, ax) < -margin)
+                const SupPt<T> sp = settled ? SupPt<T>{} : minkowski(A, B, ax);
+                if (!settled && dot(sp.p, ax) < -margin)
                 {
                     Collision<T> none;
                     manifold_update(d, p, oi, A, B, false, none, ax);

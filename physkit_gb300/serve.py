@@ -239,13 +239,80 @@ def poisson_load(rate, duration, target_live=256, nmin=16, nmax=4096, life=(60, 
     return t, kind, sizes, lifes, pick, target_live
 
 
+class LaneServer:
+    """Worlds split by size over independent servers (lanes), each with its own pool, stream and
+    step cadence: a request for a small world then waits only for the small worlds' steps, which
+    the GPU runs beside the large ones. World ids are (lane << 20) | slot."""
+
+    def __init__(self, lanes, precision="f32", pipeline_depth=1, **kw):
+        # lanes: (largest world in bodies, world slots, body pool) per lane, ascending
+        self.bounds = [b for b, _, _ in lanes]
+        self.lanes = [StepServer(max_worlds=mw, max_bodies=mb, max_bodies_per_world=b + 5, precision=precision,
+                                 pipeline_depth=pipeline_depth, **kw) for b, mw, mb in lanes]
+
+    def lane_of(self, n):
+        for k, b in enumerate(self.bounds):
+            if n <= b:
+                return k
+        return len(self.bounds) - 1
+
+    @property
+    def live(self):
+        return {(k << 20) | w: lw for k, srv in enumerate(self.lanes) for w, lw in srv.live.items()}
+
+    @property
+    def latency(self):
+        return [x for srv in self.lanes for x in srv.latency]
+
+    @property
+    def admit_wait(self):
+        return [x for srv in self.lanes for x in srv.admit_wait]
+
+    @property
+    def body_steps(self):
+        return sum(srv.body_steps for srv in self.lanes)
+
+    def open(self, req_id, nbodies, lifetime, t_arrival, records=None):
+        self.lanes[self.lane_of(nbodies)].open(req_id, nbodies, lifetime, t_arrival, records)
+
+    def advance(self, gid, t_arrival):
+        return self.lanes[gid >> 20].advance(gid & 0xFFFFF, t_arrival)
+
+    def admit(self, now):
+        return [(r, (k << 20) | w) for k, srv in enumerate(self.lanes) for r, w in srv.admit(now)]
+
+    def launch(self):
+        return sum(srv.launch() for srv in self.lanes)
+
+    def poll(self, wait=False):
+        done = sum(srv.poll() for srv in self.lanes)
+        while wait and done == 0 and any(srv.stats()["steps_in_flight"] for srv in self.lanes):
+            done = sum(srv.poll() for srv in self.lanes)  # spin: each lane completes on its own
+        return done
+
+    def stats(self):
+        st = [srv.stats() for srv in self.lanes]
+        return {k: sum(x[k] for x in st) for k in st[0]}
+
+    def close(self):
+        for srv in self.lanes:
+            srv.close()
+
+
 def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=1024, max_bodies=1_500_000,
-               nmax=4096, seed=5, pipeline_depth=1):
-    """Drive a StepServer with a Poisson request stream in real time; returns the latency report.
-    The host loop takes arrivals, admits opens, enqueues a batched step whenever the pipeline has
-    room and polls completions; it blocks on the GPU only when it has nothing else to do."""
-    srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision,
-                     pipeline_depth=pipeline_depth)
+               nmax=4096, seed=5, pipeline_depth=1, lanes=2):
+    """Drive the server with a Poisson request stream in real time; returns the latency report.
+    The host loop takes arrivals, admits opens, enqueues a batched step whenever a lane's pipeline
+    has room and polls completions; it waits on the GPU only when it has nothing else to do. With
+    lanes = 2, worlds up to 1,024 bodies and larger ones are served by separate pools (a quarter
+    of the world slots and 30 % of the bodies for the large worlds, which hold most bodies)."""
+    if lanes == 2:
+        srv = LaneServer([(1024, max_worlds - max_worlds // 4, int(0.3 * max_bodies)),
+                          (nmax, max_worlds // 4, max_bodies - int(0.3 * max_bodies))],
+                         precision=precision, pipeline_depth=pipeline_depth)
+    else:
+        srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision,
+                         pipeline_depth=pipeline_depth)
     rng = np.random.Generator(np.random.PCG64(seed + 1))
     # start from a populated pool so the measured window is in steady state
     for i in range(warm_live):
@@ -275,22 +342,24 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
         st = srv.stats()
         if i >= nreq and st["pending_requests"] == 0 and st["steps_in_flight"] == 0:
             break
-        if st["steps_in_flight"] > 0 and (st["steps_in_flight"] >= pipeline_depth or i >= nreq):
+        if lanes != 2 and st["steps_in_flight"] > 0 and (st["steps_in_flight"] >= pipeline_depth or i >= nreq):
             srv.poll(wait=True)
         elif st["steps_in_flight"] == 0 and i < nreq:
             time.sleep(max(0.0, min(1e-4, t[i] - (time.perf_counter() - t0))))
     wall = time.perf_counter() - t0
     lat = np.array(srv.latency) * 1e3
     st = srv.stats()
+    aw = srv.admit_wait
     rep = {"rate_req_s": rate, "duration_s": duration, "requests": int(nreq), "completed_steps": int(len(lat)),
            "dropped": dropped, "batched_steps": st["steps"],
            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
            "p999_ms": float(np.percentile(lat, 99.9)) if len(lat) else None,
            "body_steps_per_s": srv.body_steps / wall, "live_worlds_end": len(srv.live),
-           "admission_wait_p99_ms": float(np.percentile(np.array(srv.admit_wait) * 1e3, 99)) if srv.admit_wait else None,
-           "pool_bodies": st["pool_bodies"], "pipeline_depth": pipeline_depth,
-           "loop": "C ABI server (pk_batch_*): admission, batching and completion in C++; Poisson arrivals and "
-                   "latency accounting in Python"}
+           "admission_wait_p99_ms": float(np.percentile(np.array(aw) * 1e3, 99)) if aw else None,
+           "pool_bodies": st["pool_bodies"], "pipeline_depth": pipeline_depth, "lanes": lanes,
+           "graph_captures": st["graph_captures"],
+           "loop": "C ABI server (pk_batch_*): admission, batching and completion in C++, one server per size "
+                   "lane; Poisson arrivals and latency accounting in Python"}
     srv.close()
     return rep

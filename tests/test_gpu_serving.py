@@ -55,6 +55,14 @@ def test_world_same_alone_and_in_the_mix(precision):
 def test_poisson_load_report_small():
     from physkit_gb300.serve import run_served
 
-    rep = run_served(rate=2000, duration=0.5, warm_live=16, max_worlds=64, max_bodies=200_000, nmax=512)
+    rep = run_served(rate=2000, duration=0.5, warm_live=16, max_worlds=64, max_bodies=200_000, nmax=512, lanes=1)
     assert rep["completed_steps"] > 0 and rep["p99_ms"] is not None
+    assert rep["p50_ms"] <= rep["p99_ms"] <= rep["p999_ms"]
+
+
+def test_poisson_load_report_two_lanes():
+    from physkit_gb300.serve import run_served
+
+    rep = run_served(rate=2000, duration=0.5, warm_live=16, max_worlds=64, max_bodies=300_000, nmax=2048, lanes=2)
+    assert rep["completed_steps"] > 0 and rep["p99_ms"] is not None and rep["lanes"] == 2
     assert rep["p50_ms"] <= rep["p99_ms"] <= rep["p999_ms"]
