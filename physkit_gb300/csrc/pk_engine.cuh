@@ -181,7 +181,7 @@ template <class T> struct Dev
     const int *nslots;
     // shapes
     const T *verts;
-    const float *verts32;    // FP64 form: the vertices rounded to FP32 (exact support filter); else null
+    const float *verts32;    // FP64 form: the vertices rounded to FP32 (separation screens); else null
     const ShapeRange *shape_range;
     const Aabb<T> *shape_box;
     const T *clusters;       // 4 per cluster: centre xyz, radius
@@ -752,8 +752,10 @@ constexpr int kBroadQueue = 10240; // queued pairs per world (two 12-bit sorted 
 static_assert(kBroadPow2 >= kBroadMax && kBroadPow2 <= 4096, "sort capacity");
 static_assert(kBroadQueue * 4 >= kBroadPow2 * 8, "the sort keys live in the queue's space");
 
+// Shared memory of a sweep-and-prune CTA: the queue, then per leaf its box in FP32 (rounded outward
+// in the FP64 form), its lower bound on the sweep axis and its leaf index.
 template <class T> constexpr size_t broad_smem_bytes()
-{ return size_t(kBroadQueue) * 4 + (6 * sizeof(T) + 4 + 2) * size_t(kBroadMax); }
+{ return size_t(kBroadQueue) * 4 + (6 * sizeof(float) + 4 + 2) * size_t(kBroadMax); }
 
 template <class T>
 __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *__restrict__ skey,
@@ -770,7 +772,7 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
     while (P < n) P <<= 1;
     uint32_t *queue = reinterpret_cast<uint32_t *>(broad_smem); // kBroadQueue entries
     uint64_t *srt = reinterpret_cast<uint64_t *>(broad_smem);   // sort keys, before the sweep
-    T *box = reinterpret_cast<T *>(queue + kBroadQueue);         // 6 per sorted position: mn, mx
+    float *box = reinterpret_cast<float *>(queue + kBroadQueue); // 6 per sorted position: mn, mx
     float *lowax = reinterpret_cast<float *>(box + 6 * n);       // lower bound on the sweep axis
     uint16_t *leaf = reinterpret_cast<uint16_t *>(lowax + n);     // leaf index | 0x8000 if static
     const int tid = threadIdx.x, bs = blockDim.x;
@@ -829,13 +831,15 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
         const uint64_t e = srt[r];
         const int j = int(uint32_t(e));
         const Aabb<T> b = d.tbox[int(sval[lo + j])];
-        T *o = box + 6 * r;
-        o[0] = b.mn.x;
-        o[1] = b.mn.y;
-        o[2] = b.mn.z;
-        o[3] = b.mx.x;
-        o[4] = b.mx.y;
-        o[5] = b.mx.z;
+        float *o = box + 6 * r;
+        // FP64 form: rounded outward, so the FP32 test below never misses an overlap; the pairs
+        // it finds are confirmed on the exact boxes
+        o[0] = down_f(b.mn.x);
+        o[1] = down_f(b.mn.y);
+        o[2] = down_f(b.mn.z);
+        o[3] = up_f(b.mx.x);
+        o[4] = up_f(b.mx.y);
+        o[5] = up_f(b.mx.z);
         lowax[r] = ord2f(uint32_t(e >> 32));
         leaf[r] = uint16_t(j | (j >= nd ? 0x8000 : 0));
     }
@@ -846,9 +850,9 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
         if (pass == 1 && fill <= kBroadQueue) break;
         for (int r = warp; r < n - 1; r += nw)
         {
-            const T *qa = box + 6 * r;
-            const T qnx = qa[0], qny = qa[1], qnz = qa[2], qxx = qa[3], qxy = qa[4], qxz = qa[5];
-            const float upa = up_f(ax == 0 ? qxx : (ax == 1 ? qxy : qxz));
+            const float *qa = box + 6 * r;
+            const float qnx = qa[0], qny = qa[1], qnz = qa[2], qxx = qa[3], qxy = qa[4], qxz = qa[5];
+            const float upa = ax == 0 ? qxx : (ax == 1 ? qxy : qxz);
             const bool a_static = (leaf[r] & 0x8000) != 0;
             for (int base = r + 1; base < n; base += 32)
             {
@@ -857,9 +861,19 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
                 if (sb < n)
                 {
                     past = lowax[sb] > upa;
-                    const T *qb = box + 6 * sb;
+                    const float *qb = box + 6 * sb;
                     hit = !past && !(a_static && (leaf[sb] & 0x8000)) && qb[0] <= qxx && qb[3] >= qnx &&
                           qb[1] <= qxy && qb[4] >= qny && qb[2] <= qxz && qb[5] >= qnz;
+                    if constexpr (sizeof(T) == 8)
+                    {
+                        if (hit) // the inclusive compares of the exact fat boxes decide
+                        {
+                            const Aabb<T> ba = d.tbox[int(sval[lo + (leaf[r] & 0xFFF)])];
+                            const Aabb<T> bb = d.tbox[int(sval[lo + (leaf[sb] & 0xFFF)])];
+                            hit = bb.mn.x <= ba.mx.x && bb.mx.x >= ba.mn.x && bb.mn.y <= ba.mx.y &&
+                                  bb.mx.y >= ba.mn.y && bb.mn.z <= ba.mx.z && bb.mx.z >= ba.mn.z;
+                        }
+                    }
                 }
                 const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);
                 if (hits)
@@ -1056,7 +1070,6 @@ template <class T> __device__ __forceinline__ ShapeRef<T> body_shape(const Dev<T
     s.rmax = d.shape_rmax[m.shape];
     s.uv_stacks = r.uv_stacks;
     s.uv_sectors = r.uv_sectors;
-    s.v32 = d.verts32 ? d.verts32 + 3 * r.vstart : nullptr;
     const Pose<T> &p = d.pose[slot];
     s.pos = ld3(p.p);
     s.q = ldq(p.q);
@@ -1234,28 +1247,6 @@ __device__ __forceinline__ bool obb_separated(const Aabb<T> &la, Qt<T> qa, V3<T>
     return false;
 }
 
-// The pre-pass tests of the FP64 form run first in FP32. They only decide that a pair is certainly
-// apart (GJK would then return no collision, collision.cpp:181-182), so they need no FP64 result:
-// the margin, 1024 FP32 epsilons of the pair's scale plus the FP64 test's own terms, covers the
-// rounding of FP32 poses, boxes and products many times over, and every pair it cannot settle
-// takes the FP64 tests as before. GB300 issues FP64 at a small fraction of the FP32 rate.
-__device__ __forceinline__ bool apart_f32(const Aabb<double> &la, const Pose<double> &pa, double rma,
-                                          const Aabb<double> &lb, const Pose<double> &pb, double rmb)
-{
-    const V3<float> xa{float(pa.p[0]), float(pa.p[1]), float(pa.p[2])};
-    const V3<float> xb{float(pb.p[0]), float(pb.p[1]), float(pb.p[2])};
-    const float rs = float(rma) + float(rmb);
-    const float margin = (rs + norm(xa) + norm(xb)) * (1024.0f * EpsOf<float>::v) + 1e-6f + 1e-5f * rs;
-    const float cull = rs + margin;
-    const V3<float> dc = xb - xa;
-    if (sqnorm(dc) > cull * cull) return true;
-    const Qt<float> qa{float(pa.q[0]), float(pa.q[1]), float(pa.q[2]), float(pa.q[3])};
-    const Qt<float> qb{float(pb.q[0]), float(pb.q[1]), float(pb.q[2]), float(pb.q[3])};
-    const Aabb<float> ba{{float(la.mn.x), float(la.mn.y), float(la.mn.z)}, {float(la.mx.x), float(la.mx.y), float(la.mx.z)}};
-    const Aabb<float> bb{{float(lb.mn.x), float(lb.mn.y), float(lb.mn.z)}, {float(lb.mx.x), float(lb.mx.y), float(lb.mx.z)}};
-    return obb_separated(ba, qa, xa, bb, qb, xb, margin);
-}
-
 // FP64 form: a body's shape in FP32 (pose rounded, the FP32 copies of its vertices) for tests that
 // only decide that two shapes are certainly apart. Shapes with clustered vertex blocks (large
 // non-UV meshes) have no FP32 form here: ok is false.
@@ -1355,10 +1346,6 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
         const int old_idx = d.old_idx[p]; // k_old_index
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         bool apart = false;
-        if constexpr (sizeof(T) == 8)
-            apart = apart_f32(d.shape_box[d.meta[sa].shape], d.pose[sa], A.rmax, d.shape_box[d.meta[sb].shape],
-                              d.pose[sb], B.rmax);
-        if (!apart)
         {
             V3<T> dc = B.pos - A.pos;
             T rs = A.rmax + B.rmax;
@@ -2315,9 +2302,6 @@ __global__ void __launch_bounds__(MAXT)
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
-    // per colour, manifolds of each class (one body static or not, x 1..4 contacts): each colour
-    // is laid out class by class, so the lanes of a warp run the same contact loop
-    __shared__ int sub[8][kMaxColours];
     __shared__ int wsum[MAXT / 32];
     __shared__ int remaining;
     __shared__ int nactive;
@@ -2377,7 +2361,6 @@ __global__ void __launch_bounds__(MAXT)
     {
         ccount[c] = 0;
         cursor[c] = 0;
-        for (int q = 0; q < 8; ++q) sub[q][c] = 0;
     }
     if (tid == 0) remaining = na;
     __syncthreads();
@@ -2570,18 +2553,10 @@ __global__ void __launch_bounds__(MAXT)
         }
     }
     const int ncol = round;
-    // a manifold's class: with a static body or not, and its number of contact rows
-    auto mclass = [&](const uint4 &r) {
-        return (((r.y | r.z) >> 31) ? 4 : 0) + (__popc(unsigned(d.rowmask[r.x])) - 1);
-    };
     for (int k = tid; k < na; k += nt)
     {
         int c = colour[k];
-        if (c >= 0 && c < kMaxColours)
-        {
-            atomicAdd(&ccount[c], 1);
-            atomicAdd(&sub[mclass(rec[k])][c], 1);
-        }
+        if (c >= 0 && c < kMaxColours) atomicAdd(&ccount[c], 1);
     }
     __syncthreads();
     if (tid == 0)
@@ -2590,22 +2565,16 @@ __global__ void __launch_bounds__(MAXT)
         for (int c = 0; c < ncol; ++c)
         {
             cstart[c] = s;
-            for (int q = 0; q < 8; ++q)
-            {
-                const int t = sub[q][c];
-                sub[q][c] = s; // the class's first position, then its cursor
-                s += t;
-            }
+            s += ccount[c];
         }
         d.ncolours[w] = ncol;
     }
     __syncthreads();
-    // within a colour no two manifolds share a dynamic body, so their order does not change results
     for (int k = tid; k < na; k += nt)
     {
         int c = colour[k];
         const uint4 r = rec[k];
-        if (c >= 0 && c < kMaxColours) d.srec[ms + atomicAdd(&sub[mclass(r)][c], 1)] = r;
+        if (c >= 0 && c < kMaxColours) d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = r;
         d.pair_colour[r.x] = c; // per-pair colour for read-back (-2: no contact rows)
     }
     __syncthreads();

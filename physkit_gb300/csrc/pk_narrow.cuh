@@ -75,7 +75,6 @@ template <class T> struct ShapeRef
     T rmax;
     int uv_stacks;  // > 0: the vertex list is a UV sphere of this layout (pk_shape_sphere)
     int uv_sectors;
-    const float *v32 = nullptr; // FP64 form: the same vertices rounded to FP32 (support filter)
 
     // First strictly maximal vertex of v.ld over the vertex list, in index order.
     PK_HD int argmax_linear(V3<T> ld, int lo, int hi, int best, T &bd) const
@@ -230,60 +229,6 @@ template <class T> struct ShapeRef
         }
     }
 
-    // FP64 form: the same vertex as the FP64 search (first strictly maximal value, in index
-    // order), found with FP32 arithmetic wherever it decides. ld and every vertex value are
-    // evaluated in FP32 from the FP32 copies of q, d and the vertices; each differs from its FP64
-    // value by at most 16 FP32 ulps of rmax |d| (rotation 12, dot product 3, vertex rounding 1),
-    // so a vertex whose FP32 value lies more than tol = 128 ulps below the FP32 maximum cannot
-    // reach the FP64 maximum or tie with it. When one vertex is within tol of the maximum it is the
-    // answer; otherwise only those within tol are evaluated in FP64, in index order, from the
-    // FP64 direction. The UV window is the one argmax_uv uses (angles in FP32: near a ring or
-    // sector boundary the window can shift by one, and it still holds the maximum and every vertex
-    // within rounding of it, the others trailing by at least 1e-4 relative).
-    PK_HD int argmax_filtered(V3<T> d) const
-    {
-        const V3<float> df{float(d.x), float(d.y), float(d.z)};
-        const Qt<float> qf{float(q.w), float(q.x), float(q.y), float(q.z)};
-        const V3<float> l = rotate(conj(qf), df);
-        const float dn = norm(df);
-        const float tol = 128.0f * EpsOf<float>::v * float(rmax) * dn;
-        float mx = -3.0e38f;
-        int arg = 0, cnt = 0;
-        auto value = [&](int i) { return v32[3 * i] * l.x + v32[3 * i + 1] * l.y + v32[3 * i + 2] * l.z; };
-        auto scan = [&](auto &&visit) {
-            if (uv_stacks > 0 && dn > 0.0f)
-                uv_window(l, norm(l), visit);
-            else
-                for (int i = 0; i < nverts; ++i) visit(i);
-        };
-        scan([&](int i) {
-            const float v = value(i);
-            if (v > mx) mx = v;
-        });
-        scan([&](int i) {
-            if (value(i) >= mx - tol)
-            {
-                ++cnt;
-                arg = i;
-            }
-        });
-        if (cnt == 1) return arg;
-        // near-ties: the FP64 values of the candidates decide, as in the FP64 scan
-        const V3<T> ld = rotate(conj(q), d);
-        int best = -1;
-        T bd = T(0);
-        scan([&](int i) {
-            if (value(i) < mx - tol) return;
-            const T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
-            if (best < 0 || v > bd || (v == bd && i < best))
-            {
-                bd = v;
-                best = i;
-            }
-        });
-        return best;
-    }
-
     PK_HD V3<T> support(V3<T> d) const
     {
         if (kind == SHAPE_AABB)
@@ -300,15 +245,6 @@ template <class T> struct ShapeRef
         }
         // mesh::instance::support -> mesh::support: first strictly maximal vertex
         // (mesh.cpp:341-358, 442-448)
-        if constexpr (sizeof(T) == 8)
-        {
-            if (v32 && ncl == 0)
-            {
-                const int best = argmax_filtered(d);
-                V3<T> lv{verts[3 * best], verts[3 * best + 1], verts[3 * best + 2]};
-                return rotate(q, lv) + pos;
-            }
-        }
         V3<T> ld = rotate(conj(q), d);
         int best;
         if (uv_stacks > 0)

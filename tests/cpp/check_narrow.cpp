@@ -4,10 +4,7 @@
 //  2. the clustered support search returns the same vertex as the linear first-strict-max scan
 //     (mesh.cpp:341-358) for UV spheres and random hulls, in FP64 and FP32;
 //  3. so does the UV-sphere neighbourhood search, for every layout it accepts (uv_layout_ok),
-//     including directions at and near the poles, on ring planes and between sectors;
-//  4. the FP64 form's FP32-filtered search (ShapeRef::argmax_filtered) returns the vertex of the
-//     FP64 scan of the direction rotated into the body frame, for boxes, hulls and UV spheres
-//     under random and axis-aligned poses, with exact ties.
+//     including directions at and near the poles, on ring planes and between sectors.
 #include "../../physkit_gb300/csrc/pk_narrow.cuh"
 
 #include <algorithm>
@@ -178,71 +175,6 @@ template <class T> static int check_uv(const std::vector<double> &vd, int stacks
     return bad;
 }
 
-// argmax_filtered(d) against the FP64 reference: ld = rotate(conj(q), d), first strict max.
-static int check_filtered(const std::vector<double> &v, int stacks, int sectors, std::mt19937_64 &rng, int ndirs,
-                          long long *fallbacks)
-{
-    std::vector<float> v32(v.begin(), v.end());
-    ShapeRef<double> s{};
-    s.kind = SHAPE_MESH;
-    s.nverts = int(v.size() / 3);
-    s.verts = v.data();
-    s.v32 = v32.data();
-    s.uv_stacks = stacks;
-    s.uv_sectors = sectors;
-    double rm = 0.0;
-    for (int i = 0; i < s.nverts; ++i)
-        rm = std::max(rm, std::sqrt(v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]));
-    s.rmax = rm;
-    std::normal_distribution<double> nd(0.0, 1.0);
-    std::uniform_real_distribution<double> ud(-1.0, 1.0);
-    const double h = std::sqrt(0.5);
-    const Qt<double> exact_q[6] = {{1, 0, 0, 0}, {h, h, 0, 0}, {h, 0, h, 0}, {h, 0, 0, h}, {0, 1, 0, 0}, {0.5, 0.5, 0.5, 0.5}};
-    int bad = 0;
-    for (int k = 0; k < ndirs; ++k)
-    {
-        Qt<double> q;
-        V3<double> d;
-        if (k % 3 == 0)
-        { // axis-aligned poses and directions: exact ties between vertices
-            q = exact_q[rng() % 6];
-            int a = int(rng() % 26);
-            int x = a % 3 - 1, y = (a / 3) % 3 - 1, z = a / 9 - 1;
-            if (x == 0 && y == 0 && z == 0) y = -1;
-            d = V3<double>{double(x), double(y), double(z)};
-        }
-        else
-        {
-            q = qnormalized(Qt<double>{nd(rng), nd(rng), nd(rng), nd(rng)});
-            d = V3<double>{nd(rng), nd(rng), nd(rng)};
-            if (k % 3 == 2)
-            { // a vertex direction in the world frame: near-ties between neighbours
-                int i = int(rng() % uint64_t(s.nverts));
-                d = rotate(q, V3<double>{v[3 * i], v[3 * i + 1], v[3 * i + 2]});
-            }
-        }
-        double sc = std::pow(10.0, 2.0 * ud(rng));
-        d = V3<double>{d.x * sc, d.y * sc, d.z * sc};
-        s.q = q;
-        V3<double> ld = rotate(conj(q), d);
-        double bd;
-        int want = s.argmax_linear(ld, 0, s.nverts, -1, bd);
-        int got = s.argmax_filtered(d);
-        if (want != got) ++bad;
-        // how often near-ties sent the search to FP64 (informational)
-        const V3<float> df{float(d.x), float(d.y), float(d.z)};
-        const Qt<float> qf{float(q.w), float(q.x), float(q.y), float(q.z)};
-        const V3<float> l = rotate(conj(qf), df);
-        float mx = -3e38f;
-        for (int i = 0; i < s.nverts; ++i) mx = std::max(mx, v32[3 * i] * l.x + v32[3 * i + 1] * l.y + v32[3 * i + 2] * l.z);
-        int c = 0;
-        for (int i = 0; i < s.nverts; ++i)
-            c += (v32[3 * i] * l.x + v32[3 * i + 1] * l.y + v32[3 * i + 2] * l.z) >= mx - 128.0f * EpsOf<float>::v * float(rm) * norm(df);
-        *fallbacks += c > 1;
-    }
-    return bad;
-}
-
 static std::vector<double> uv_sphere(double r, int stacks, int sectors)
 {
     std::vector<double> v = {0.0, r, 0.0};
@@ -296,34 +228,7 @@ int main()
                 baduv64 += check_uv<double>(v, S, K, rng, 3000);
                 baduv32 += check_uv<float>(v, S, K, rng, 3000);
             }
-    int badf = 0;
-    long long fb = 0, nf = 0;
-    const std::vector<double> box = {-0.3, -0.2, -0.4, 0.3, -0.2, -0.4, -0.3, 0.2, -0.4, 0.3, 0.2, -0.4,
-                                     -0.3, -0.2, 0.4,  0.3, -0.2, 0.4,  -0.3, 0.2, 0.4,  0.3, 0.2, 0.4};
-    badf += check_filtered(box, 0, 0, rng, 60000, &fb);
-    nf += 60000;
-    for (int hh = 0; hh < 40; ++hh)
-    {
-        std::vector<double> v;
-        for (int i = 0; i < 16; ++i)
-        {
-            double x = nd(rng), y = nd(rng), z = nd(rng), n = std::sqrt(x * x + y * y + z * z);
-            v.insert(v.end(), {x / n * 0.45, y / n * 0.45, z / n * 0.45});
-        }
-        badf += check_filtered(v, 0, 0, rng, 1500, &fb);
-        nf += 1500;
-    }
-    for (int S : {8, 16, 24, 32})
-        for (int K : {8, 16, 32, 64})
-            for (double r : {0.05, 1.0})
-            {
-                if (!uv_layout_ok(S, K)) continue;
-                auto v = uv_sphere(r, S, K);
-                badf += check_filtered(v, S, K, rng, 4000, &fb);
-                nf += 4000;
-            }
     std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d uv_mismatch_f64=%d uv_mismatch_f32=%d "
-                "filtered_mismatch=%d uv_layouts=%d filtered_fp64_fallbacks=%lld/%lld\n", bad_heap, bad64, bad32, baduv64,
-                baduv32, badf, layouts, fb, nf);
-    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || badf || !uv_layout_ok(16, 32) || layouts < 60) ? 1 : 0;
+                "uv_layouts=%d\n", bad_heap, bad64, bad32, baduv64, baduv32, layouts);
+    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || !uv_layout_ok(16, 32) || layouts < 60) ? 1 : 0;
 }
