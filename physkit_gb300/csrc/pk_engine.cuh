@@ -754,25 +754,34 @@ static_assert(kBroadQueue * 4 >= kBroadPow2 * 8, "the sort keys live in the queu
 
 // Shared memory of a sweep-and-prune CTA: the queue, then per leaf its box in FP32 (rounded outward
 // in the FP64 form), its lower bound on the sweep axis and its leaf index.
-template <class T> constexpr size_t broad_smem_bytes()
-{ return size_t(kBroadQueue) * 4 + (6 * sizeof(float) + 4 + 2) * size_t(kBroadMax); }
-
-template <class T>
-__global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *__restrict__ skey,
-                                                     const uint64_t *__restrict__ sval)
+// Worlds are swept by size class, each class with CTAs and shared memory for its largest world,
+// so the many small worlds of a batch do not each hold the shared memory of a 2,304-leaf world:
+// (MINN, MAXN] leaves, QCAP queued pairs (a fuller queue moves the world to the second sweep).
+template <int MAXN, int QCAP> constexpr size_t broad_smem_bytes()
+{ return size_t(QCAP) * 4 + (6 * sizeof(float) + 4 + 2) * size_t(MAXN); }
+struct BroadClass
 {
+    int minn, maxn, qcap, threads;
+};
+constexpr BroadClass kBroadClasses[3] = {{1, 256, 4096, 128}, {256, 1024, 8192, 256}, {1024, kBroadMax, kBroadQueue, 512}};
+
+template <class T, int MINN, int MAXN, int QCAP, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_t *__restrict__ skey,
+                                                         const uint64_t *__restrict__ sval)
+{
+    static_assert(QCAP * 4 >= 8 * MAXN * 2 && MAXN <= 4096, "the sort keys live in the queue's space");
     extern __shared__ __align__(16) unsigned char broad_smem[];
     __shared__ int ndyn, fill, cta_base;
     __shared__ int warp_count[16];
     const int w = blockIdx.x;
     const int lo = d.wleaf_lo[w];
     const int n = d.wleaf_hi[w] - lo;
-    if (n < 2 || n > kBroadMax) return;
+    if (n < 2 || n <= MINN || n > MAXN) return;
     int P = 2;
     while (P < n) P <<= 1;
-    uint32_t *queue = reinterpret_cast<uint32_t *>(broad_smem); // kBroadQueue entries
+    uint32_t *queue = reinterpret_cast<uint32_t *>(broad_smem); // QCAP entries
     uint64_t *srt = reinterpret_cast<uint64_t *>(broad_smem);   // sort keys, before the sweep
-    float *box = reinterpret_cast<float *>(queue + kBroadQueue); // 6 per sorted position: mn, mx
+    float *box = reinterpret_cast<float *>(queue + QCAP);        // 6 per sorted position: mn, mx
     float *lowax = reinterpret_cast<float *>(box + 6 * n);       // lower bound on the sweep axis
     uint16_t *leaf = reinterpret_cast<uint16_t *>(lowax + n);     // leaf index | 0x8000 if static
     const int tid = threadIdx.x, bs = blockDim.x;
@@ -847,7 +856,7 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
     for (int pass = 0; pass < 2; ++pass)
     {
         // pass 0 queues; pass 1 only runs after a queue overflow and emits straight to the list
-        if (pass == 1 && fill <= kBroadQueue) break;
+        if (pass == 1 && fill <= QCAP) break;
         for (int r = warp; r < n - 1; r += nw)
         {
             const float *qa = box + 6 * r;
@@ -883,7 +892,7 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
                         int q0 = 0;
                         if (lane == 0) q0 = atomicAdd(&fill, __popc(hits));
                         q0 = __shfl_sync(0xFFFFFFFFu, q0, 0) + __popc(hits & ((1u << lane) - 1u));
-                        if (hit && q0 < kBroadQueue) queue[q0] = uint32_t(r) | (uint32_t(sb) << 12);
+                        if (hit && q0 < QCAP) queue[q0] = uint32_t(r) | (uint32_t(sb) << 12);
                     }
                     else if (hit)
                         broad_emit(d, w, lo, sval, int(leaf[r] & 0xFFF), int(leaf[sb] & 0xFFF), -1);
@@ -894,7 +903,7 @@ __global__ void __launch_bounds__(512) k_broad_small(Dev<T> d, const uint64_t *_
         __syncthreads();
     }
     const int nq = fill;
-    if (nq > kBroadQueue) return; // emitted by the second sweep
+    if (nq > QCAP) return; // emitted by the second sweep
     // drop the pairs the reference does not pair yet, then one reservation for the rest
     int mine = 0;
     for (int q = tid; q < nq; q += bs)

@@ -291,8 +291,18 @@ public:
             d.world_nlocal = wn;
         }
         PK_CUDA(radix_sort_prepare<uint64_t>());
-        PK_CUDA(cudaFuncSetAttribute(k_broad_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(broad_smem_bytes<T>())));
+        PK_CUDA(cudaFuncSetAttribute(k_broad_small<T, kBroadClasses[0].minn, kBroadClasses[0].maxn,
+                                                   kBroadClasses[0].qcap, kBroadClasses[0].threads>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(broad_smem_bytes<kBroadClasses[0].maxn, kBroadClasses[0].qcap>())));
+        PK_CUDA(cudaFuncSetAttribute(k_broad_small<T, kBroadClasses[1].minn, kBroadClasses[1].maxn,
+                                                   kBroadClasses[1].qcap, kBroadClasses[1].threads>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(broad_smem_bytes<kBroadClasses[1].maxn, kBroadClasses[1].qcap>())));
+        PK_CUDA(cudaFuncSetAttribute(k_broad_small<T, kBroadClasses[2].minn, kBroadClasses[2].maxn,
+                                                   kBroadClasses[2].qcap, kBroadClasses[2].threads>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(broad_smem_bytes<kBroadClasses[2].maxn, kBroadClasses[2].qcap>())));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1185,6 +1195,12 @@ private:
         return cudaMalloc(const_cast<void **>(reinterpret_cast<const void **>(p)), sizeof(U) * n);
     }
     static int solve_threads(int t) { return t < solve_max_threads<T>() ? t : solve_max_threads<T>(); }
+    template <int C> void launch_broad(const Dev<T> &d, const uint64_t *skey, const uint64_t *sval)
+    {
+        constexpr BroadClass c = kBroadClasses[C];
+        k_broad_small<T, c.minn, c.maxn, c.qcap, c.threads>
+            <<<cfg_.max_worlds, c.threads, broad_smem_bytes<c.maxn, c.qcap>(), st_>>>(d, skey, sval);
+    }
     // The joint-free instances serve batches that never had joints (buffers unallocated).
     void launch_solve(int blocks, int threads, size_t smem, const Dev<T> &d, const uint64_t *pv, int first, int cache,
                       cudaStream_t st)
@@ -1253,7 +1269,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 22 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
+        launches_ = 24 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1271,7 +1287,9 @@ private:
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval, true);
         PK_CUDA(mark(3));
         k_traverse<T><<<(N + tune_.traverse_threads - 1) / tune_.traverse_threads, tune_.traverse_threads, 0, st_>>>(d, sval);
-        k_broad_small<T><<<cfg_.max_worlds, 512, broad_smem_bytes<T>(), st_>>>(d, skey, sval);
+        launch_broad<0>(d, skey, sval);
+        launch_broad<1>(d, skey, sval);
+        launch_broad<2>(d, skey, sval);
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
         k_kept_count<T><<<cfg_.max_worlds, 256, 0, st_>>>(d);
         PK_CUDA(mark(4));
