@@ -393,6 +393,7 @@ def run_ours(a, rank, world_size, local_rank):
            "config": config_dict(a, nb, world_size), "e2e": e2e,
            "gpu_launches": info["launches"] * a.steps, "clocks": clk, "roofline": roof,
            "stage_ms_per_step": {k: round(v, 4) for k, v in per_stage.items()},
+           "roofline_support": _support_roofline(info, per_stage.get("narrow"), a.precision),
            "autotune": tuned,
            "counts": {"pairs": P, "contacts": Cn, "gjk": info["gjk"], "epa": info["epa"],
                       "gjk_large_mesh": info["gjk_large_mesh"], "epa_large_mesh": info["epa_large_mesh"],
@@ -452,6 +453,28 @@ def _stage_split(world, dt, steps):
     st = world.stage_times()
     world.set_timing(False)
     return {k: round(v[0] / max(v[1], 1), 4) for k, v in st.items()}
+
+
+def _support_roofline(info, narrow_ms, precision):
+    """Secondary bound of the narrowphase: the FLOPs of the reference's support scans (5 per
+    vertex a linear first-strict-max scan visits, over the separating-axis, GJK and EPA supports of
+    the last step) over the narrow stage's time, against the CUDA-core peak of the form's
+    precision (nominal: 152 SMs x FMA lanes x 2 FLOP x the maximum SM clock; 128 FP32 lanes, 2
+    FP64 lanes per SM per clock). The device search visits vertex clusters and UV-sphere
+    neighbourhoods instead of every vertex, so the fraction can exceed 1."""
+    sv = info.get("support_vertices")
+    if not narrow_ms or not sv:
+        return None
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    mhz = json.load(open(peaks_path)).get("sm_max_mhz", 2070.0) if os.path.exists(peaks_path) else 2070.0
+    lanes = 128 if precision == "f32" else 2
+    peak = 152 * lanes * 2 * mhz * 1e6 / 1e12
+    flops = 5.0 * sv
+    achieved = flops / (narrow_ms / 1e3) / 1e12
+    return {"bound": "fma", "pipe": "fp32" if precision == "f32" else "fp64", "kernel": "narrow",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "nominal", "flops_per_step": flops,
+            "model": "5 FLOP x vertices of linear support scans per step / narrow stage time"}
 
 
 def _roofline(stages, units):

@@ -101,6 +101,10 @@ typedef struct pk_step_info
     int64_t gjk_iterations; /* GJK iterations summed over the last step's pairs */
     int64_t epa_iterations; /* EPA expansions summed over the last step's pairs */
     int64_t epa_iterations_large_mesh;
+    /* Vertices that linear support scans (mesh::support, mesh.cpp:341-358) visit for the last
+     * step's supports (separating-axis pass, GJK, EPA expansions): x5 gives the reference's
+     * support FLOPs. The device search visits fewer (vertex clusters, UV neighbourhoods). */
+    int64_t support_vertices;
 } pk_step_info;
 
 /* Primitive shape for pk_collide: kind 0 aabb (p = min3 max3), 1 obb (p = center3 quat4 half3),

@@ -842,6 +842,7 @@ int pk_world_synchronize(pk_world *w, pk_step_info *info)
         info->gjk_iterations = c.gjk_iters;
         info->epa_iterations = c.epa_iters;
         info->epa_iterations_large_mesh = c.epa_iters_heavy;
+        info->support_vertices = c.support_verts;
     }
     return c.status ? PK_ERR_DEVICE_STATUS : PK_OK;
 }

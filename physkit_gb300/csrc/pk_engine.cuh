@@ -236,7 +236,10 @@ template <class T> struct Dev
     int *epa_count;
     int *epa_count_heavy;
     int *epa_total;        // items admitted to the EPA list (at most contact_cap)
+    int *epa_redo;         // contact_cap entries: EPA list slots the compact pass gave up on
+    int *epa_redo_count;
     unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
+    unsigned long long *np_verts; // vertices a linear support scan visits, summed over the supports
     int *clist;            // pairs of active worlds whose new manifold holds contacts (any order)
     int *ccount;
     // Contact rows live at the pair's position in clist (rowidx), so they take memory only for the
@@ -319,6 +322,22 @@ __device__ __forceinline__ int warp_push(int *counter)
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// Adds every active lane's value to a 64-bit counter: one atomic per warp.
+__device__ __forceinline__ void warp_add(unsigned long long *counter, unsigned v)
+{
+    const unsigned m = __activemask();
+    const unsigned s = __reduce_add_sync(m, v);
+    if (int(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(counter, (unsigned long long)s);
+}
+
+// Vertices the reference's support (mesh::support, mesh.cpp:341-358, a linear first-strict-max
+// scan) visits for one Minkowski support of the pair; a support costs the reference 5 FLOP per
+// vertex (a 3-term dot product and a compare).
+template <class T> __device__ __forceinline__ unsigned scan_verts(const ShapeRef<T> &A, const ShapeRef<T> &B)
+{
+    return unsigned((A.kind == SHAPE_MESH ? A.nverts : 8) + (B.kind == SHAPE_MESH ? B.nverts : 8));
+}
+
 // Key of a manifold in a round of parallel first fit (colour_rounds_pick / _claim / _commit): its
 // tentative colour on top, then a scramble of its pair's world-local indices (MurmurHash3's 64-bit
 // finaliser), then its position in the world's key order. Of the uncoloured manifolds on one body,
@@ -369,8 +388,10 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.gjk2_count_heavy = 0;
         *d.ccount = 0;
         *d.epa_total = 0;
+        *d.epa_redo_count = 0;
         *d.all_small = 1;
         d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
+        *d.np_verts = 0ull;
         *d.epoch += 1;
     }
 }
@@ -1411,6 +1432,7 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
                 const uint64_t val = sval[p];
                 const int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
                 const ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+                warp_add(d.np_verts, scan_verts(A, B));
                 if constexpr (sizeof(T) == 8)
                 {
                     // FP32 first: support values within a few FP32 ulps of the pair's scale, far
@@ -1469,7 +1491,8 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
         Simplex<T> s;
         V3<T> sep{T(0), T(0), T(0)};
         bool enclosed = gjk(A, B, s, &sep);
-        atomicAdd(d.np_iters, (unsigned long long)s.iters);
+        warp_add(d.np_iters, unsigned(s.iters));
+        warp_add(d.np_verts, unsigned(s.iters + 1) * scan_verts(A, B));
         // admitted first against the list's capacity, so the two ends never meet
         const bool admit = enclosed && warp_push(d.epa_total) < d.contact_cap;
         if (enclosed && !admit)
@@ -1498,27 +1521,58 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
 }
 
 // Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, then the manifold update.
+// The first pass runs every pair with the compact polytope (kEpaFacesSmall faces); the pairs that
+// outgrow it are queued and run from their GJK simplex again by k_narrow_epa_full.
+template <class T, bool FULL>
+__device__ __forceinline__ void narrow_epa_item(Dev<T> &d, const uint64_t *__restrict__ sval, int j)
+{
+    int p = d.epa_list[j];
+    uint64_t val = sval[p];
+    int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+    ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+    Simplex<T> s = d.epa_simplex[j];
+    Collision<T> col;
+    bool hit;
+    int status, iters;
+    if constexpr (FULL)
+    {
+        EpaState<T> es;
+        hit = epa(A, B, s, es, col);
+        status = es.status;
+        iters = es.iters;
+    }
+    else
+    {
+        EpaState<T, kEpaFacesSmall, kEpaPolySmall> es;
+        hit = epa(A, B, s, es, col);
+        status = es.status;
+        iters = es.iters;
+        if (status & PK_NP_REDO)
+        {
+            d.epa_redo[warp_push(d.epa_redo_count)] = j;
+            return;
+        }
+    }
+    if (status) atomicOr(d.status, ST_EPA_CAP);
+    warp_add(d.np_iters + 1, unsigned(iters));
+    if (A.ncl > 0 || B.ncl > 0) warp_add(d.np_iters + 2, unsigned(iters));
+    warp_add(d.np_verts, unsigned(iters) * scan_verts(A, B));
+    manifold_update(d, p, d.old_idx[p], A, B, hit, col);
+}
+
 template <class T>
 __global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.epa_count_heavy;
     const int n = nh + *d.epa_count;
-    PK_GRID_STRIDE(i, n)
-    {
-        int j = list_slot(i, nh, d.contact_cap);
-        int p = d.epa_list[j];
-        uint64_t val = sval[p];
-        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
-        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
-        Simplex<T> s = d.epa_simplex[j];
-        EpaState<T> es;
-        Collision<T> col;
-        bool hit = epa(A, B, s, es, col);
-        if (es.status) atomicOr(d.status, ST_EPA_CAP);
-        atomicAdd(d.np_iters + 1, (unsigned long long)es.iters);
-        if (A.ncl > 0 || B.ncl > 0) atomicAdd(d.np_iters + 2, (unsigned long long)es.iters);
-        manifold_update(d, p, d.old_idx[p], A, B, hit, col);
-    }
+    PK_GRID_STRIDE(i, n) narrow_epa_item<T, false>(d, sval, list_slot(i, nh, d.contact_cap));
+}
+
+template <class T>
+__global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa_full(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int n = *d.epa_redo_count;
+    PK_GRID_STRIDE(i, n) narrow_epa_item<T, true>(d, sval, d.epa_redo[i]);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -53,6 +53,7 @@ struct StepCounters
     int launches = 0; // kernels one step launches
     int gjk = 0, gjk_heavy = 0, epa = 0, epa_heavy = 0; // narrowphase work items of the last step
     long long gjk_iters = 0, epa_iters = 0, epa_iters_heavy = 0;
+    long long support_verts = 0; // vertices linear support scans would visit (separating axis, GJK, EPA)
 };
 
 // A ray against one mesh instance (pk_mesh_raycast): the body's slot (its shape and current pose

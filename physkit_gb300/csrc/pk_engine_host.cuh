@@ -249,6 +249,7 @@ public:
         d.gjk_count_heavy = counters_ + 8;
         d.epa_count_heavy = counters_ + 9;
         d.np_iters = reinterpret_cast<unsigned long long *>(counters_ + 10); // counters 10..15
+        d.np_verts = reinterpret_cast<unsigned long long *>(counters_ + 24); // counters 24..25
         d.nnew = counters_ + 16;
         d.njoints = counters_ + 17; // zero until joints are set
         d.ccount = counters_ + 18;
@@ -256,6 +257,7 @@ public:
         d.gjk2_count_heavy = counters_ + 20;
         d.all_small = counters_ + 21;
         d.epa_total = counters_ + 22;
+        d.epa_redo_count = counters_ + 23;
         PK_CUDA(alloc(&d.jstart, W));
         PK_CUDA(alloc(&d.jend, W));
         PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
@@ -338,6 +340,7 @@ public:
         PK_CUDA(alloc(&d.gjk_list2, P));
         PK_CUDA(alloc(&d.epa_list, CC));
         PK_CUDA(alloc(&d.epa_simplex, CC));
+        PK_CUDA(alloc(&d.epa_redo, CC));
         PK_CUDA(alloc(&d.rowidx, P));
         PK_CUDA(alloc(&d.rows, 4 * CC));
         PK_CUDA(alloc(&d.racc, 12 * CC));
@@ -727,7 +730,7 @@ public:
         PK_CUDA(cudaStreamSynchronize(st_));
         PK_CUDA(cudaGetLastError());
         PK_CUDA(accumulate_stage_times());
-        int h[16];
+        int h[32];
         PK_CUDA(cudaMemcpy(h, counters_, sizeof(h), cudaMemcpyDeviceToHost));
         if (c)
         {
@@ -744,6 +747,9 @@ public:
             c->gjk_iters = (long long)it[0];
             c->epa_iters = (long long)it[1];
             c->epa_iters_heavy = (long long)it[2];
+            unsigned long long sv;
+            std::memcpy(&sv, h + 24, sizeof(sv));
+            c->support_verts = (long long)sv;
         }
         int zero = 0;
         PK_CUDA(cudaMemcpy(counters_ + 4, &zero, sizeof(int), cudaMemcpyHostToDevice));
@@ -1232,7 +1238,7 @@ private:
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
-                      d_.epa_list, d_.epa_simplex, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
+                      d_.epa_list, d_.epa_simplex, d_.epa_redo, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.srec, d_.crec, d_.owner, d_.used, const_cast<int *>(d_.world_order),
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), const_cast<float *>(d_.verts32), shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
@@ -1269,7 +1275,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 24 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
+        launches_ = 25 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1314,6 +1320,7 @@ private:
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
+        k_narrow_epa_full<T><<<sms_ * 4, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         if (joint_cap_ > 0) k_joint_setup<T><<<grid(joint_cap_), 128, 0, st_>>>(d, dt);

@@ -51,7 +51,8 @@ assert BODY_DTYPE.itemsize == 216
 class StepInfoC(C.Structure):
     _fields_ = [("pairs", C.c_int32), ("leaves", C.c_int32), ("status", C.c_int32), ("launches", C.c_int32),
                 ("gjk", C.c_int32), ("epa", C.c_int32), ("gjk_large_mesh", C.c_int32), ("epa_large_mesh", C.c_int32),
-                ("gjk_iterations", C.c_int64), ("epa_iterations", C.c_int64), ("epa_iterations_large_mesh", C.c_int64)]
+                ("gjk_iterations", C.c_int64), ("epa_iterations", C.c_int64), ("epa_iterations_large_mesh", C.c_int64),
+                ("support_vertices", C.c_int64)]
 
 
 class TuneResultC(C.Structure):
@@ -478,6 +479,7 @@ class World:
                           "gjk_large_mesh": info.gjk_large_mesh, "epa_large_mesh": info.epa_large_mesh,
                           "gjk_iterations": info.gjk_iterations, "epa_iterations": info.epa_iterations,
                           "epa_iterations_large_mesh": info.epa_iterations_large_mesh,
+                          "support_vertices": info.support_vertices,
                           "flags": [v for k, v in STATUS_BITS.items() if info.status & k]}
         return self.last_info
 
