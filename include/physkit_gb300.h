@@ -178,8 +178,9 @@ typedef struct pk_tune_result
     double step_ms_after;
     int32_t steps_used;
     int32_t big_threads; /* solver CTA size of the worlds above small_world (0: solve_threads) */
-    int32_t tiny_world;   /* worlds up to this many local indices get their own launch (0: none) */
-    int32_t tiny_threads; /* its CTA size (0: 32) */
+    int32_t group_bodies;  /* solve groups: worlds below small_world packed up to 8 per CTA while
+                              their local indices sum to at most this (0: one world per CTA) */
+    int32_t group_threads; /* CTA size of the solve groups (0: 128) */
 } pk_tune_result;
 int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tune_result *out);
 /* Apply launch shapes found by pk_world_autotune (e.g. on a scratch copy of the same scene). */

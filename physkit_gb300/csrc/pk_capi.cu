@@ -991,17 +991,16 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
         }
         best = bc;
     }
-    // a launch of its own for the smallest worlds: many one- or two-warp CTAs per SM
+    // solve groups: small worlds packed several per CTA, their colours swept together
     {
         double bt = 1e300;
         pk::Tunables bc = best;
-        const int tw[][2] = {{0, 32}, {128, 32}, {256, 32}, {256, 64}, {512, 64}};
+        const int tw[][2] = {{0, 128}, {256, 64}, {512, 128}, {1024, 128}, {1024, 256}, {2048, 256}};
         for (const auto &c : tw)
         {
-            if (c[0] >= best.small_world) continue;
             pk::Tunables t = best;
-            t.tiny_world = c[0];
-            t.tiny_threads = c[1];
+            t.group_bodies = c[0];
+            t.group_threads = c[1];
             w->eng->set_tunables(t);
             if ((rc = timed_steps(w, dt, k, st))) return rc;
             used += k;
@@ -1065,8 +1064,8 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
         out->step_ms_after = total(st);
         out->steps_used = used;
         out->big_threads = best.big_threads;
-        out->tiny_world = best.tiny_world;
-        out->tiny_threads = best.tiny_threads;
+        out->group_bodies = best.group_bodies;
+        out->group_threads = best.group_threads;
     }
     return PK_OK;
 }
@@ -1077,7 +1076,7 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
     if (t->solve_threads < 32 || t->solve_threads > 512 || (t->solve_threads & 31) || t->small_world < 1 ||
         t->narrow_grid < 1 || t->narrow_grid > 16 || t->traverse_threads < 32 || t->traverse_threads > 1024 ||
         (t->traverse_threads & 31) || t->big_threads < 0 || t->big_threads > 512 || (t->big_threads & 31) ||
-        t->tiny_world < 0 || t->tiny_threads < 0 || t->tiny_threads > 256 || (t->tiny_threads & 31))
+        t->group_bodies < 0 || t->group_threads < 0 || t->group_threads > 256 || (t->group_threads & 31))
         return PK_ERR_INVALID;
     pk::Tunables tu;
     tu.solve_threads = t->solve_threads;
@@ -1085,8 +1084,8 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
     tu.narrow_grid = t->narrow_grid;
     tu.traverse_threads = t->traverse_threads;
     tu.big_threads = t->big_threads > 0 ? t->big_threads : t->solve_threads;
-    tu.tiny_world = t->tiny_world;
-    tu.tiny_threads = t->tiny_threads > 0 ? t->tiny_threads : 32;
+    tu.group_bodies = t->group_bodies;
+    tu.group_threads = t->group_threads > 0 ? t->group_threads : 128;
     w->eng->set_tunables(tu);
     w->launch_version++;
     return PK_OK;

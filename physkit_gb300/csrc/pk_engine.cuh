@@ -236,8 +236,6 @@ template <class T> struct Dev
     int *epa_count;
     int *epa_count_heavy;
     int *epa_total;        // items admitted to the EPA list (at most contact_cap)
-    int *epa_redo;         // contact_cap entries: EPA list slots the compact pass gave up on
-    int *epa_redo_count;
     unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
     unsigned long long *np_verts; // vertices a linear support scan visits, summed over the supports
     int *clist;            // pairs of active worlds whose new manifold holds contacts (any order)
@@ -388,7 +386,6 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.gjk2_count_heavy = 0;
         *d.ccount = 0;
         *d.epa_total = 0;
-        *d.epa_redo_count = 0;
         *d.all_small = 1;
         d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
         *d.np_verts = 0ull;
@@ -1521,58 +1518,28 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
 }
 
 // Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, then the manifold update.
-// The first pass runs every pair with the compact polytope (kEpaFacesSmall faces); the pairs that
-// outgrow it are queued and run from their GJK simplex again by k_narrow_epa_full.
-template <class T, bool FULL>
-__device__ __forceinline__ void narrow_epa_item(Dev<T> &d, const uint64_t *__restrict__ sval, int j)
-{
-    int p = d.epa_list[j];
-    uint64_t val = sval[p];
-    int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
-    ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
-    Simplex<T> s = d.epa_simplex[j];
-    Collision<T> col;
-    bool hit;
-    int status, iters;
-    if constexpr (FULL)
-    {
-        EpaState<T> es;
-        hit = epa(A, B, s, es, col);
-        status = es.status;
-        iters = es.iters;
-    }
-    else
-    {
-        EpaState<T, kEpaFacesSmall, kEpaPolySmall> es;
-        hit = epa(A, B, s, es, col);
-        status = es.status;
-        iters = es.iters;
-        if (status & PK_NP_REDO)
-        {
-            d.epa_redo[warp_push(d.epa_redo_count)] = j;
-            return;
-        }
-    }
-    if (status) atomicOr(d.status, ST_EPA_CAP);
-    warp_add(d.np_iters + 1, unsigned(iters));
-    if (A.ncl > 0 || B.ncl > 0) warp_add(d.np_iters + 2, unsigned(iters));
-    warp_add(d.np_verts, unsigned(iters) * scan_verts(A, B));
-    manifold_update(d, p, d.old_idx[p], A, B, hit, col);
-}
-
 template <class T>
 __global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.epa_count_heavy;
     const int n = nh + *d.epa_count;
-    PK_GRID_STRIDE(i, n) narrow_epa_item<T, false>(d, sval, list_slot(i, nh, d.contact_cap));
-}
-
-template <class T>
-__global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa_full(Dev<T> d, const uint64_t *__restrict__ sval)
-{
-    const int n = *d.epa_redo_count;
-    PK_GRID_STRIDE(i, n) narrow_epa_item<T, true>(d, sval, d.epa_redo[i]);
+    PK_GRID_STRIDE(i, n)
+    {
+        int j = list_slot(i, nh, d.contact_cap);
+        int p = d.epa_list[j];
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+        Simplex<T> s = d.epa_simplex[j];
+        EpaState<T> es;
+        Collision<T> col;
+        bool hit = epa(A, B, s, es, col);
+        if (es.status) atomicOr(d.status, ST_EPA_CAP);
+        warp_add(d.np_iters + 1, unsigned(es.iters));
+        if (A.ncl > 0 || B.ncl > 0) warp_add(d.np_iters + 2, unsigned(es.iters));
+        warp_add(d.np_verts, unsigned(es.iters) * scan_verts(A, B));
+        manifold_update(d, p, d.old_idx[p], A, B, hit, col);
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -2357,21 +2324,78 @@ template <class T> __device__ __forceinline__ bool colour_rounds_commit(const De
 
 // MAXT: the largest CTA the instance is compiled for (256, or 512 for the FP32 form's large worlds;
 // the 512 instance gives up registers for threads).
-template <class T, int MAXT, bool JOINTS>
-__global__ void __launch_bounds__(MAXT)
-    k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies, int grid_world)
+#ifndef PK_SOLVE_MIN_BLOCKS
+#define PK_SOLVE_MIN_BLOCKS 2
+#endif
+// First fit in pair order for one world (one thread): each manifold takes the lowest colour that
+// none of the earlier manifolds on its dynamic bodies has, from a 128-bit used-colour mask per
+// local index (`used`, 2 words per local index, zeroed by the caller). Returns the number of
+// colours, or -1 when a body would need a colour above 127.
+__device__ __forceinline__ int first_fit_colours(const uint4 *__restrict__ rec, int na, uint64_t *used, int *colour)
 {
-    extern __shared__ __align__(16) unsigned char solve_smem[];
+    int top = 0;
+    constexpr int kAhead = 8; // records loaded ahead of the mask chain
+    for (int k0 = 0; k0 < na; k0 += kAhead)
+    {
+        uint4 rr[kAhead];
+#pragma unroll
+        for (int j = 0; j < kAhead; ++j) rr[j] = k0 + j < na ? rec[k0 + j] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+        for (int j = 0; j < kAhead; ++j)
+        {
+            if (k0 + j >= na) break;
+            const uint4 r = rr[j];
+            const bool da = !(r.y >> 31), db = !(r.z >> 31);
+            const int la = int(r.w & 0xFFFFu), lb = int(r.w >> 16);
+            uint64_t u0 = 0ull, u1 = 0ull;
+            if (da)
+            {
+                u0 |= used[2 * la];
+                u1 |= used[2 * la + 1];
+            }
+            if (db)
+            {
+                u0 |= used[2 * lb];
+                u1 |= used[2 * lb + 1];
+            }
+            int c;
+            if (~u0)
+                c = __ffsll(~u0) - 1;
+            else if (~u1)
+                c = 64 + __ffsll(~u1) - 1;
+            else
+                return -1; // a body with 128 manifolds in one step
+            colour[k0 + j] = c;
+            const uint64_t b0 = c < 64 ? (1ull << c) : 0ull, b1 = c < 64 ? 0ull : (1ull << (c - 64));
+            if (da)
+            {
+                used[2 * la] |= b0;
+                used[2 * la + 1] |= b1;
+            }
+            if (db)
+            {
+                used[2 * lb] |= b0;
+                used[2 * lb + 1] |= b1;
+            }
+            top = c + 1 > top ? c + 1 : top;
+        }
+    }
+    return top;
+}
+
+// One active world's compaction, colouring, sweeps and write-back on the whole CTA (every thread
+// calls it). solve_smem caches the world's body velocities when it has at most cache_bodies local
+// indices.
+template <class T, int MAXT, bool JOINTS>
+__device__ __forceinline__ void solve_world_cta(const Dev<T> &d, const uint64_t *__restrict__ sval, int w,
+                                                int cache_bodies, unsigned char *solve_smem)
+{
     __shared__ int ccount[kMaxColours];
     __shared__ int cstart[kMaxColours];
     __shared__ int cursor[kMaxColours];
     __shared__ int wsum[MAXT / 32];
     __shared__ int remaining;
     __shared__ int nactive;
-    const int blk = first_block + int(blockIdx.x);
-    if (blk >= d.max_worlds) return;
-    const int w = d.world_order[blk];
-    if (!d.wp[w].active || d.world_nlocal[w] > grid_world) return; // large worlds: k_solve_grid
     const int ms = d.mstart[w], me = d.mend[w];
     const int js = JOINTS ? d.jstart[w] : 0, je = JOINTS ? d.jend[w] : 0; // instance without joints
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -2443,62 +2467,7 @@ __global__ void __launch_bounds__(MAXT)
         uint64_t *used = reinterpret_cast<uint64_t *>(solve_smem); // 2 words per local index
         for (int l = tid; l < 2 * d.world_nlocal[w]; l += nt) used[l] = 0ull;
         __syncthreads();
-        if (tid == 0)
-        {
-            int top = 0;
-            bool capped = false;
-            constexpr int kAhead = 8; // records loaded ahead of the mask chain
-            for (int k0 = 0; k0 < na; k0 += kAhead)
-            {
-                uint4 rr[kAhead];
-#pragma unroll
-                for (int j = 0; j < kAhead; ++j) rr[j] = k0 + j < na ? rec[k0 + j] : make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-                for (int j = 0; j < kAhead; ++j)
-                {
-                    if (k0 + j >= na) break;
-                    const uint4 r = rr[j];
-                    const bool da = !(r.y >> 31), db = !(r.z >> 31);
-                    const int la = int(r.w & 0xFFFFu), lb = int(r.w >> 16);
-                    uint64_t u0 = 0ull, u1 = 0ull;
-                    if (da)
-                    {
-                        u0 |= used[2 * la];
-                        u1 |= used[2 * la + 1];
-                    }
-                    if (db)
-                    {
-                        u0 |= used[2 * lb];
-                        u1 |= used[2 * lb + 1];
-                    }
-                    int c;
-                    if (~u0)
-                        c = __ffsll(~u0) - 1;
-                    else if (~u1)
-                        c = 64 + __ffsll(~u1) - 1;
-                    else
-                    {
-                        capped = true; // a body with 128 manifolds in one step
-                        c = -1;
-                    }
-                    colour[k0 + j] = c;
-                    if (c < 0) continue;
-                    const uint64_t b0 = c < 64 ? (1ull << c) : 0ull, b1 = c < 64 ? 0ull : (1ull << (c - 64));
-                    if (da)
-                    {
-                        used[2 * la] |= b0;
-                        used[2 * la + 1] |= b1;
-                    }
-                    if (db)
-                    {
-                        used[2 * lb] |= b0;
-                        used[2 * lb + 1] |= b1;
-                    }
-                    top = c + 1 > top ? c + 1 : top;
-                }
-            }
-            ff_ncol = capped ? -1 : top;
-        }
+        if (tid == 0) ff_ncol = first_fit_colours(rec, na, used, colour);
         __syncthreads();
         if (ff_ncol >= 0)
         {
@@ -2705,6 +2674,207 @@ __global__ void __launch_bounds__(MAXT)
         {
             if (!(mask & (1u << q))) continue;
             store_impulses(d, p, q);
+        }
+    }
+}
+
+template <class T, int MAXT, bool JOINTS>
+__global__ void __launch_bounds__(MAXT, MAXT == 256 ? PK_SOLVE_MIN_BLOCKS : 1)
+    k_solve_world(Dev<T> d, const uint64_t *__restrict__ sval, int first_block, int cache_bodies, int grid_world)
+{
+    extern __shared__ __align__(16) unsigned char solve_smem[];
+    const int blk = first_block + int(blockIdx.x);
+    if (blk >= d.max_worlds) return;
+    const int w = d.world_order[blk];
+    if (!d.wp[w].active || d.world_nlocal[w] > grid_world) return; // large worlds: k_solve_grid
+    solve_world_cta<T, MAXT, JOINTS>(d, sval, w, cache_bodies, solve_smem);
+}
+
+// Solve groups: several small worlds per CTA (worlds world_order[goff[g]] .. [goff[g + 1] - 1] for
+// group g, at most kGroupMax, their local indices together at most cache_bodies). Each member is
+// compacted and coloured on its own, one warp per member, by the same first fit in pair order as a
+// world alone; the sweeps then run colour c of every member together. Members share no bodies, so
+// each world gets its colours, its sweep order per body and its results exactly as alone, while the
+// CTA's lanes hold the manifolds of several worlds. If a member needs more than 128 colours the
+// group is solved member by member on the one-world path.
+constexpr int kGroupMax = 8;
+constexpr int kGroupColours = 128; // first fit's colours
+
+#ifndef PK_GROUP_MIN_BLOCKS
+#define PK_GROUP_MIN_BLOCKS 2
+#endif
+template <class T>
+__global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
+    k_solve_group(Dev<T> d, const uint64_t *__restrict__ sval, const int *__restrict__ goff, int cache_bodies)
+{
+    extern __shared__ __align__(16) unsigned char solve_smem[];
+    __shared__ int gw[kGroupMax], gms[kGroupMax], gna[kGroupMax], gbase[kGroupMax], gncol[kGroupMax];
+    __shared__ int ccount[kGroupMax][kGroupColours];
+    __shared__ int cstart[kGroupMax][kGroupColours];
+    __shared__ int cursor[kGroupMax][kGroupColours];
+    __shared__ int cpre[kGroupColours][kGroupMax + 1];
+    __shared__ int ng, ntotal, ncol, capped;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    if (tid == 0)
+    {
+        int n = 0, base = 0;
+        for (int k = goff[blockIdx.x]; k < goff[blockIdx.x + 1] && n < kGroupMax; ++k)
+        {
+            const int w = d.world_order[k];
+            if (!d.wp[w].active) continue;
+            gw[n] = w;
+            gms[n] = d.mstart[w];
+            gbase[n] = base;
+            base += d.world_nlocal[w];
+            ++n;
+        }
+        ng = n;
+        ntotal = base;
+        capped = 0;
+    }
+    __syncthreads();
+    const int G = ng;
+    if (G == 0) return;
+    if (ntotal > cache_bodies)
+    {
+        // the host packs groups within cache_bodies from the same local-index counts; a group
+        // beyond it has no room for its colour masks and is flagged, not solved
+        if (tid == 0) atomicOr(d.status, ST_COLOUR_CAP);
+        return;
+    }
+
+    // 1. per member, one warp: the manifolds with contact rows, ascending pair index; then first fit
+    for (int g = warp; g < G; g += nw)
+    {
+        const int w = gw[g], ms = gms[g], me = d.mend[w];
+        uint4 *rec = d.crec + ms;
+        int off = 0;
+        for (int p0 = ms; p0 < me; p0 += 32)
+        {
+            const int p = p0 + lane;
+            const bool on = p < me && d.rowmask[p] != 0;
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, on);
+            if (on) rec[off + __popc(m & ((1u << lane) - 1u))] = make_solve_rec(d, p, sval[p]);
+            off += __popc(m);
+        }
+        uint64_t *used = reinterpret_cast<uint64_t *>(solve_smem) + 2 * gbase[g];
+        for (int l = lane; l < 2 * d.world_nlocal[w]; l += 32) used[l] = 0ull;
+        __syncwarp();
+        if (lane == 0)
+        {
+            gna[g] = off;
+            const int c = first_fit_colours(rec, off, used, d.colour_tmp + ms);
+            gncol[g] = c;
+            if (c < 0) capped = 1;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (capped)
+    {
+        for (int g = 0; g < G; ++g) solve_world_cta<T, 256, false>(d, sval, gw[g], cache_bodies, solve_smem);
+        return;
+    }
+
+    // 2. each member's colours laid out in order (srec), and per colour the members' prefix counts
+    for (int i = tid; i < kGroupMax * kGroupColours; i += nt)
+    {
+        (&ccount[0][0])[i] = 0;
+        (&cursor[0][0])[i] = 0;
+    }
+    __syncthreads();
+    for (int g = 0; g < G; ++g)
+    {
+        const int *colour = d.colour_tmp + gms[g];
+        for (int k = tid; k < gna[g]; k += nt) atomicAdd(&ccount[g][colour[k]], 1);
+    }
+    __syncthreads();
+    if (tid < G)
+    {
+        int s = 0;
+        for (int c = 0; c < gncol[tid]; ++c)
+        {
+            cstart[tid][c] = s;
+            s += ccount[tid][c];
+        }
+        d.ncolours[gw[tid]] = gncol[tid];
+    }
+    if (tid == 0)
+    {
+        int m = 0;
+        for (int g = 0; g < G; ++g) m = gncol[g] > m ? gncol[g] : m;
+        ncol = m;
+    }
+    __syncthreads();
+    const int nc = ncol;
+    for (int c = tid; c < nc; c += nt)
+    {
+        int s = 0;
+        for (int g = 0; g < G; ++g)
+        {
+            cpre[c][g] = s;
+            s += ccount[g][c];
+        }
+        cpre[c][G] = s;
+    }
+    for (int g = 0; g < G; ++g)
+    {
+        const int ms = gms[g];
+        const int *colour = d.colour_tmp + ms;
+        const uint4 *rec = d.crec + ms;
+        for (int k = tid; k < gna[g]; k += nt)
+        {
+            const int c = colour[k];
+            const uint4 r = rec[k];
+            d.srec[ms + cstart[g][c] + atomicAdd(&cursor[g][c], 1)] = r;
+            d.pair_colour[r.x] = c; // per-pair colour for read-back
+        }
+    }
+    // the colour masks are done; the shared memory now caches the members' body velocities
+    Vel<T> *cache = reinterpret_cast<Vel<T> *>(solve_smem);
+    __syncthreads();
+    for (int g = 0; g < G; ++g)
+    {
+        const uint4 *rec = d.crec + gms[g];
+        Vel<T> *cg = cache + gbase[g];
+        for (int k = tid; k < gna[g]; k += nt)
+        {
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) cg[r.w & 0xFFFFu] = d.vel[r.y];
+            if (!(r.z >> 31)) cg[r.w >> 16] = d.vel[r.z];
+        }
+    }
+    __syncthreads();
+
+    // 3. warm start, then the iterations: colour c of every member in one sweep
+    for (int it = -1; it < d.iterations; ++it)
+        for (int c = 0; c < nc; ++c)
+        {
+            const int n = cpre[c][G];
+            for (int i = tid; i < n; i += nt)
+            {
+                int g = 0;
+                while (g + 1 < G && i >= cpre[c][g + 1]) ++g;
+                const uint4 r = d.srec[gms[g] + cstart[g][c] + (i - cpre[c][g])];
+                solve_manifold_rec(d, r, cache + gbase[g], it < 0);
+            }
+            __syncthreads();
+        }
+
+    // 4. velocities back to the bodies, accumulated impulses back into the manifold cache
+    for (int g = 0; g < G; ++g)
+    {
+        const uint4 *rec = d.crec + gms[g];
+        const Vel<T> *cg = cache + gbase[g];
+        for (int k = tid; k < gna[g]; k += nt)
+        {
+            const uint4 r = rec[k];
+            if (!(r.y >> 31)) d.vel[r.y] = cg[r.w & 0xFFFFu];
+            if (!(r.z >> 31)) d.vel[r.z] = cg[r.w >> 16];
+            const int p = int(r.x);
+            const uint8_t mask = d.rowmask[p];
+            for (int q = 0; q < 4; ++q)
+                if (mask & (1u << q)) store_impulses(d, p, q);
         }
     }
 }

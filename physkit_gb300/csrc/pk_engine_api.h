@@ -41,8 +41,8 @@ struct Tunables
     int narrow_grid = 2;       // GJK/EPA grid = narrow_grid x the default grid
     int traverse_threads = 128;
     int big_threads = 256;     // threads per solver CTA of the worlds above small_world
-    int tiny_world = 0;        // worlds up to this many local indices get a launch of their own
-    int tiny_threads = 32;     // (many small CTAs resident per SM: one colour sweep per warp)
+    int group_bodies = 0;      // solve groups: worlds packed up to 8 per CTA while their local
+    int group_threads = 128;   // indices sum to at most group_bodies (0: one world per CTA)
 };
 
 struct StepCounters

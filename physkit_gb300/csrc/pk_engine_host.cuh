@@ -257,7 +257,6 @@ public:
         d.gjk2_count_heavy = counters_ + 20;
         d.all_small = counters_ + 21;
         d.epa_total = counters_ + 22;
-        d.epa_redo_count = counters_ + 23;
         PK_CUDA(alloc(&d.jstart, W));
         PK_CUDA(alloc(&d.jend, W));
         PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
@@ -291,6 +290,7 @@ public:
             PK_CUDA(cudaMemset(wn, 0x7F, sizeof(int) * W)); // "too large to cache" until set
             d.world_order = wo;
             d.world_nlocal = wn;
+            PK_CUDA(alloc(&goff_dev_, W + 1));
         }
         PK_CUDA(radix_sort_prepare<uint64_t>());
         PK_CUDA(cudaFuncSetAttribute(k_broad_small<T, kBroadClasses[0].minn, kBroadClasses[0].maxn,
@@ -307,6 +307,7 @@ public:
                                      int(broad_smem_bytes<kBroadClasses[2].maxn, kBroadClasses[2].qcap>())));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
+        PK_CUDA(cudaFuncSetAttribute(k_solve_group<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, solve_max_threads<T>(), false>,
@@ -340,7 +341,6 @@ public:
         PK_CUDA(alloc(&d.gjk_list2, P));
         PK_CUDA(alloc(&d.epa_list, CC));
         PK_CUDA(alloc(&d.epa_simplex, CC));
-        PK_CUDA(alloc(&d.epa_redo, CC));
         PK_CUDA(alloc(&d.rowidx, P));
         PK_CUDA(alloc(&d.rows, 4 * CC));
         PK_CUDA(alloc(&d.racc, 12 * CC));
@@ -527,19 +527,22 @@ public:
         PK_CUDA(ensure_staging());
         size_t base = 0;
         const size_t bytes = sizeof(int) * size_t(n);
+        order_.assign(order, order + n);
+        nlocal_.assign(nlocal, nlocal + n);
+        split_worlds();
+        const size_t gbytes = sizeof(int) * goff_.size();
         StageLayout L;
-        const size_t o_ord = L.add(bytes), o_nl = L.add(bytes);
+        const size_t o_ord = L.add(bytes), o_nl = L.add(bytes), o_g = L.add(gbytes);
         PK_CUDA(stage_.reserve(L.total, &base));
         std::memcpy(stage_.host(base + o_ord), order, bytes);
         std::memcpy(stage_.host(base + o_nl), nlocal, bytes);
+        if (gbytes) std::memcpy(stage_.host(base + o_g), goff_.data(), gbytes);
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_order), stage_.host(base + o_ord), bytes,
                                 cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_nlocal), stage_.host(base + o_nl), bytes,
                                 cudaMemcpyHostToDevice, st_));
+        if (gbytes) PK_CUDA(cudaMemcpyAsync(goff_dev_, stage_.host(base + o_g), gbytes, cudaMemcpyHostToDevice, st_));
         PK_CUDA(stage_.commit(st_));
-        order_.assign(order, order + n);
-        nlocal_.assign(nlocal, nlocal + n);
-        split_worlds();
         return 0;
     }
 
@@ -548,10 +551,10 @@ public:
         if (n != cfg_.max_worlds) return -3;
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_order), order, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaMemcpyAsync(const_cast<int *>(d_.world_nlocal), nlocal, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
-        PK_CUDA(cudaStreamSynchronize(st_));
         order_.assign(order, order + n);
         nlocal_.assign(nlocal, nlocal + n);
         split_worlds();
+        PK_CUDA(upload_groups());
         return 0;
     }
 
@@ -560,7 +563,6 @@ public:
     void split_worlds()
     {
         big_worlds_ = 0;
-        tiny_worlds_ = 0;
         int maxl = 0;
         grid_worlds_.clear();
         for (size_t i = 0; i < order_.size(); ++i)
@@ -572,7 +574,6 @@ public:
                 continue;
             }
             if (nl > tune_.small_world) ++big_worlds_;
-            else if (tune_.tiny_world > 0 && tune_.tiny_world < tune_.small_world && nl <= tune_.tiny_world) ++tiny_worlds_;
             maxl = nl > maxl ? nl : maxl;
         }
         // worlds handled by the grid solver sort first (largest first): skip them in the CTA launches
@@ -583,12 +584,50 @@ public:
         big_smem_ = sizeof(Vel<T>) * size_t(big_cache_);
         const size_t ff = 16 * size_t(maxl < kFirstFitMax ? maxl : kFirstFitMax);
         if (ff > big_smem_) big_smem_ = ff;
+        // solve groups over the worlds after the large ones (in solve order, so sizes fall): up to
+        // kGroupMax consecutive worlds while their local indices fit group_bodies; a larger world
+        // is a group of its own. The groups are not used while the engine holds joints.
+        goff_.clear();
+        group_cache_ = 0;
+        const int glimit = limit < tune_.group_bodies ? limit : tune_.group_bodies;
+        if (glimit > 0 && !order_.empty())
+        {
+            const int n = int(order_.size());
+            int i = big_worlds_;
+            while (i < n)
+            {
+                goff_.push_back(i);
+                int sum = 0, m = 0;
+                while (i < n && m < kGroupMax)
+                {
+                    const int nl = nlocal_[size_t(order_[size_t(i)])];
+                    if (m > 0 && sum + nl > glimit) break;
+                    sum += nl;
+                    ++m;
+                    ++i;
+                }
+                group_cache_ = sum > group_cache_ ? sum : group_cache_;
+            }
+            if (!goff_.empty()) goff_.push_back(n);
+            if (group_cache_ > limit) goff_.clear(); // a single world above the cache (small_world > limit)
+        }
+    }
+    int ngroups() const { return goff_.empty() ? 0 : int(goff_.size()) - 1; }
+    cudaError_t upload_groups()
+    {
+        if (!goff_.empty())
+        {
+            cudaError_t e = cudaMemcpyAsync(goff_dev_, goff_.data(), sizeof(int) * goff_.size(), cudaMemcpyHostToDevice, st_);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaStreamSynchronize(st_);
     }
 
     int set_tunables(const Tunables &t) override
     {
         tune_ = t;
         split_worlds();
+        PK_CUDA(upload_groups());
         return 0;
     }
     Tunables tunables() const override { return tune_; }
@@ -1137,7 +1176,9 @@ private:
     static constexpr size_t kMaxSolveSmem = 160 * 1024;
     Tunables tune_{};
     int big_worlds_ = 0;
-    int tiny_worlds_ = 0; // the last worlds of the order: their own launch
+    std::vector<int> goff_; // solve groups: first index in the world order of each group, then the end
+    int *goff_dev_ = nullptr;
+    int group_cache_ = 0; // the largest group's local indices (its velocity cache)
     int big_cache_ = 0;
     size_t big_smem_ = 0; // dynamic shared memory of the large-world launch
     double *pack_ = nullptr; // read-back staging: 14 doubles per slot
@@ -1238,8 +1279,8 @@ private:
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
-                      d_.epa_list, d_.epa_simplex, d_.epa_redo, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
-                      d_.order, d_.srec, d_.crec, d_.owner, d_.used, const_cast<int *>(d_.world_order),
+                      d_.epa_list, d_.epa_simplex, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
+                      d_.order, d_.srec, d_.crec, d_.owner, d_.used, const_cast<int *>(d_.world_order), goff_dev_,
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), const_cast<float *>(d_.verts32), shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
@@ -1275,7 +1316,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 25 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_ + tiny_worlds_) + (tiny_worlds_ > 0) + 3 * mpasses + 3 * ppasses;
+        launches_ = 24 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1320,7 +1361,6 @@ private:
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
-        k_narrow_epa_full<T><<<sms_ * 4, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         if (joint_cap_ > 0) k_joint_setup<T><<<grid(joint_cap_), 128, 0, st_>>>(d, dt);
@@ -1346,12 +1386,12 @@ private:
         if (big_worlds_ > 0)
             launch_solve(big_worlds_, tune_.big_threads > 0 ? tune_.big_threads : tune_.solve_threads, big_smem_, d, pv,
                          0, big_cache_, st_);
-        if (cfg_.max_worlds > big_worlds_ + tiny_worlds_)
-            launch_solve(cfg_.max_worlds - big_worlds_ - tiny_worlds_, tune_.solve_threads,
+        if (ngroups() > 0 && joint_cap_ == 0)
+            k_solve_group<T><<<ngroups(), tune_.group_threads, sizeof(Vel<T>) * size_t(group_cache_), sst>>>(
+                d, pv, goff_dev_, group_cache_);
+        else if (cfg_.max_worlds > big_worlds_)
+            launch_solve(cfg_.max_worlds - big_worlds_, tune_.solve_threads,
                          sizeof(Vel<T>) * size_t(tune_.small_world), d, pv, big_worlds_, tune_.small_world, sst);
-        if (tiny_worlds_ > 0)
-            launch_solve(tiny_worlds_, tune_.tiny_threads, sizeof(Vel<T>) * size_t(tune_.tiny_world), d, pv,
-                         cfg_.max_worlds - tiny_worlds_, tune_.tiny_world, sst);
         if (side)
         {
             PK_CUDA(cudaEventRecord(join_, st2_));

@@ -23,16 +23,11 @@ enum : int
     PK_NP_FACE_CAP = 1 << 0,
     PK_NP_HORIZON_CAP = 1 << 1,
     PK_NP_STACK_CAP = 1 << 2,
-    PK_NP_REDO = 1 << 3, // a compact EPA state ran out of room: the pair runs again with the full one
 };
 
 constexpr int kMaxPoly = 4 + 64;
 constexpr int kMaxFaces = 512;
 constexpr int kMaxHorizon = 96;
-// Compact EPA state: enough for the pairs that end within about a dozen expansions (a box pair
-// ends in 4-5 on average, a pair with a UV sphere in 9), a tenth of the full state's footprint.
-constexpr int kEpaFacesSmall = 64;
-constexpr int kEpaPolySmall = 4 + 16;
 constexpr uint16_t kNull16 = 0xFFFF;
 
 enum : int
@@ -467,21 +462,18 @@ template <class T> PK_HD bool pad_simplex(const ShapeRef<T> &A, const ShapeRef<T
 
 template <class T> struct EpaFace
 {
-    V3<T> n;
-    T d;
     uint16_t v[3];
     uint16_t adj[3];
+    V3<T> n;
+    T d;
     uint8_t obsolete;
 };
 
-// EPA polytope with room for NF faces and NP support points. The full capacities are the
-// implementation's caps (reported as PK_NP_*_CAP); a smaller state gives up with PK_NP_REDO.
-template <class T, int NF = kMaxFaces, int NP = kMaxPoly> struct EpaState
+template <class T> struct EpaState
 {
-    static_assert(NF <= kMaxFaces && NP <= kMaxPoly, "capacities above the caps");
-    SupPt<T> poly[NP];
-    EpaFace<T> faces[NF];
-    uint16_t heap[NF];
+    SupPt<T> poly[kMaxPoly];
+    EpaFace<T> faces[kMaxFaces];
+    uint16_t heap[kMaxFaces];
     int npoly, nfaces, nheap;
     int status;
     int iters; // EPA expansions used
@@ -676,15 +668,10 @@ struct HorizonEdge
     uint16_t start, end, adj;
 };
 
-// epa_solver::solve (collision.cpp:411-504). Returns true with a collision. A compact state
-// (fewer faces or support points than the caps) that would need more room, or a longer horizon
-// than it keeps, stops with PK_NP_REDO in e.status and its result is void: the same simplex run
-// with the full state gives the pair's result, so both give identical results where both finish.
-template <class T, int NF, int NP>
-PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T, NF, NP> &e, Collision<T> &out)
+// epa_solver::solve (collision.cpp:411-504). Returns true with a collision.
+template <class T>
+PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T> &e, Collision<T> &out)
 {
-    constexpr int HC = NF < kMaxHorizon ? NF : kMaxHorizon; // horizon edges kept
-
     e.status = 0;
     e.iters = 0;
     if (s.n < 4 && !pad_simplex(A, B, s)) return false;
@@ -715,9 +702,9 @@ PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaSta
                 }
             }
 
-    HorizonEdge horizon[HC];
-    uint16_t stack[NF]; // each face is pushed at most once
-    uint16_t nf[HC];
+    HorizonEdge horizon[kMaxHorizon];
+    uint16_t stack[kMaxFaces];
+    uint16_t nf[kMaxHorizon];
     const T tol = T(1e-6);
     for (int iter = 0; iter < 64; ++iter)
     {
@@ -758,33 +745,22 @@ PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaSta
                 if (dot(nb.n, p.p) > nb.d + tol)
                 {
                     nb.obsolete = 1;
-                    if (sp < NF)
+                    if (sp < kMaxFaces)
                         stack[sp++] = n;
                     else
                         e.status |= PK_NP_STACK_CAP;
                 }
-                else if (nh < HC)
+                else if (nh < kMaxHorizon)
                     horizon[nh++] = {e.faces[cur].v[i], e.faces[cur].v[(i + 1) % 3], n};
                 else
-                    e.status |= HC < kMaxHorizon ? PK_NP_REDO : PK_NP_HORIZON_CAP;
+                    e.status |= PK_NP_HORIZON_CAP;
             }
         }
-        if (e.status & PK_NP_REDO) return false;
         if (nh == 0) break;
-        if (e.nfaces + nh > NF)
+        if (e.nfaces + nh > kMaxFaces)
         {
-            if (NF < kMaxFaces)
-            {
-                e.status |= PK_NP_REDO;
-                return false;
-            }
             e.status |= PK_NP_FACE_CAP;
             break;
-        }
-        if (NP < kMaxPoly && e.npoly >= NP)
-        {
-            e.status |= PK_NP_REDO;
-            return false;
         }
         e.poly[e.npoly] = p;
         int pi = e.npoly++;
@@ -812,8 +788,8 @@ PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaSta
 }
 
 // gjk_epa (collision.cpp:512-518)
-template <class T, int NF, int NP>
-PK_HD bool gjk_epa(const ShapeRef<T> &A, const ShapeRef<T> &B, EpaState<T, NF, NP> &e, Collision<T> &out, int *status)
+template <class T>
+PK_HD bool gjk_epa(const ShapeRef<T> &A, const ShapeRef<T> &B, EpaState<T> &e, Collision<T> &out, int *status)
 {
     Simplex<T> s;
     *status = 0;

@@ -4,15 +4,12 @@
 //  2. the clustered support search returns the same vertex as the linear first-strict-max scan
 //     (mesh.cpp:341-358) for UV spheres and random hulls, in FP64 and FP32;
 //  3. so does the UV-sphere neighbourhood search, for every layout it accepts (uv_layout_ok),
-//     including directions at and near the poles, on ring planes and between sectors;
-//  4. EPA with the compact polytope gives bit-identical results to the full one on every pair it
-//     finishes, and gives up (PK_NP_REDO) on the rest, for posed box, hull and UV-sphere pairs.
+//     including directions at and near the poles, on ring planes and between sectors.
 #include "../../physkit_gb300/csrc/pk_narrow.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
-#include <cstring>
 #include <random>
 #include <vector>
 
@@ -196,103 +193,6 @@ static std::vector<double> uv_sphere(double r, int stacks, int sectors)
     return v;
 }
 
-static std::vector<double> box_verts(double hx, double hy, double hz)
-{
-    std::vector<double> v;
-    for (int i = 0; i < 8; ++i)
-        v.insert(v.end(), {(i & 4) ? hx : -hx, (i & 2) ? hy : -hy, (i & 1) ? hz : -hz});
-    return v;
-}
-
-template <class T> static bool same_bits(const T &a, const T &b) { return std::memcmp(&a, &b, sizeof(T)) == 0; }
-
-template <class T> static bool same_collision(const Collision<T> &a, const Collision<T> &b)
-{
-    const V3<T> *x[3] = {&a.normal, &a.world_a, &a.world_b}, *y[3] = {&b.normal, &b.world_a, &b.world_b};
-    for (int k = 0; k < 3; ++k)
-        if (!same_bits(x[k]->x, y[k]->x) || !same_bits(x[k]->y, y[k]->y) || !same_bits(x[k]->z, y[k]->z)) return false;
-    return same_bits(a.depth, b.depth);
-}
-
-// Posed pairs of boxes, 16-point hulls and 16x32 UV spheres, placed to overlap by a random
-// fraction; every pair GJK encloses is run through both EPA states.
-template <class T> static int check_epa_compact(std::mt19937_64 &rng, int &finished, int &redone, int &pairs)
-{
-    std::uniform_real_distribution<double> u(0.0, 1.0);
-    std::normal_distribution<double> nd(0.0, 1.0);
-    std::vector<std::vector<double>> meshes;
-    std::vector<int> stacks;
-    for (int k = 0; k < 6; ++k)
-    {
-        meshes.push_back(box_verts(0.1 + 0.5 * u(rng), 0.1 + 0.5 * u(rng), 0.1 + 0.5 * u(rng)));
-        stacks.push_back(0);
-        std::vector<double> h;
-        double r = 0.2 + 0.4 * u(rng);
-        for (int i = 0; i < 16; ++i)
-        {
-            double x = nd(rng), y = nd(rng), z = nd(rng), n = std::sqrt(x * x + y * y + z * z);
-            h.insert(h.end(), {x / n * r, y / n * r, z / n * r});
-        }
-        meshes.push_back(h);
-        stacks.push_back(0);
-        meshes.push_back(uv_sphere(0.2 + 0.4 * u(rng), 16, 32));
-        stacks.push_back(16);
-    }
-    std::vector<std::vector<T>> mt;
-    for (auto &m : meshes) mt.emplace_back(m.begin(), m.end());
-    auto shape = [&](int m, V3<T> pos, Qt<T> q) {
-        ShapeRef<T> s{};
-        s.kind = SHAPE_MESH;
-        s.nverts = int(mt[m].size() / 3);
-        s.verts = mt[m].data();
-        s.pos = pos;
-        s.q = q;
-        double rm = 0;
-        for (size_t i = 0; i < meshes[m].size(); i += 3)
-            rm = std::fmax(rm, std::sqrt(meshes[m][i] * meshes[m][i] + meshes[m][i + 1] * meshes[m][i + 1] +
-                                         meshes[m][i + 2] * meshes[m][i + 2]));
-        s.rmax = T(rm);
-        if (stacks[m] > 0)
-        {
-            s.uv_stacks = stacks[m];
-            s.uv_sectors = 32;
-        }
-        return s;
-    };
-    auto rq = [&]() {
-        double w = nd(rng), x = nd(rng), y = nd(rng), z = nd(rng), n = std::sqrt(w * w + x * x + y * y + z * z);
-        return Qt<T>{T(w / n), T(x / n), T(y / n), T(z / n)};
-    };
-    int bad = 0;
-    for (int t = 0; t < 4000; ++t)
-    {
-        int ma = int(rng() % meshes.size()), mb = int(rng() % meshes.size());
-        double dx = nd(rng), dy = nd(rng), dz = nd(rng), dn = std::sqrt(dx * dx + dy * dy + dz * dz);
-        double sep = (0.05 + 0.9 * u(rng)) * 0.8;
-        V3<T> pa{T(0), T(0), T(0)}, pb{T(dx / dn * sep), T(dy / dn * sep), T(dz / dn * sep)};
-        if (t % 5 == 0) pb = V3<T>{T(0), T(sep), T(0)}; // axis-aligned offsets: ties and degenerate faces
-        ShapeRef<T> A = shape(ma, pa, t % 7 == 0 ? Qt<T>{T(1), T(0), T(0), T(0)} : rq());
-        ShapeRef<T> B = shape(mb, pb, t % 7 == 0 ? Qt<T>{T(1), T(0), T(0), T(0)} : rq());
-        Simplex<T> s0;
-        if (!gjk(A, B, s0)) continue;
-        ++pairs;
-        static EpaState<T> full;
-        EpaState<T, kEpaFacesSmall, kEpaPolySmall> small;
-        Simplex<T> s1 = s0, s2 = s0;
-        Collision<T> c1{}, c2{};
-        bool h1 = epa(A, B, s1, full, c1);
-        bool h2 = epa(A, B, s2, small, c2);
-        if (small.status & PK_NP_REDO)
-        {
-            ++redone;
-            continue;
-        }
-        ++finished;
-        if (h1 != h2 || small.status != full.status || small.iters != full.iters || (h1 && !same_collision(c1, c2))) ++bad;
-    }
-    return bad;
-}
-
 int main()
 {
     std::mt19937_64 rng(12345);
@@ -328,16 +228,7 @@ int main()
                 baduv64 += check_uv<double>(v, S, K, rng, 3000);
                 baduv32 += check_uv<float>(v, S, K, rng, 3000);
             }
-    int fin64 = 0, redo64 = 0, pairs64 = 0, fin32 = 0, redo32 = 0, pairs32 = 0;
-    int badepa64 = check_epa_compact<double>(rng, fin64, redo64, pairs64);
-    int badepa32 = check_epa_compact<float>(rng, fin32, redo32, pairs32);
     std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d uv_mismatch_f64=%d uv_mismatch_f32=%d "
-                "uv_layouts=%d epa_compact_mismatch_f64=%d epa_compact_mismatch_f32=%d epa_pairs_f64=%d "
-                "epa_compact_finished_f64=%d epa_redo_f64=%d epa_pairs_f32=%d epa_compact_finished_f32=%d epa_redo_f32=%d\n",
-                bad_heap, bad64, bad32, baduv64, baduv32, layouts, badepa64, badepa32, pairs64, fin64, redo64, pairs32,
-                fin32, redo32);
-    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || !uv_layout_ok(16, 32) || layouts < 60 || badepa64 ||
-            badepa32 || fin64 < pairs64 / 2 || redo64 == 0 || pairs64 < 1000)
-               ? 1
-               : 0;
+                "uv_layouts=%d\n", bad_heap, bad64, bad32, baduv64, baduv32, layouts);
+    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || !uv_layout_ok(16, 32) || layouts < 60) ? 1 : 0;
 }

@@ -67,7 +67,7 @@ def test_tune_result_layout():
     from physkit_gb300 import world
 
     # solve_threads, small_world, narrow_grid, traverse_threads, 2 doubles, steps_used, big_threads,
-    # tiny_world, tiny_threads (the doubles start at offset 16)
+    # group_bodies, group_threads (the doubles start at offset 16)
     assert C.sizeof(world.TuneResultC) == 48
     assert world.TuneResultC.step_ms_before.offset == 16
 

@@ -98,11 +98,20 @@ def test_fp64_remove_and_add_bodies():
     world.close()
 
 
-def test_fp64_dense_cluster_queue_overflow_and_colour_fallback():
+# launch shapes of pk_world_set_tuning: the defaults, and solve groups (several small worlds per
+# solver CTA, their colours swept together) at two packings
+DEFAULT_TUNING = {"solve_threads": 256, "small_world": 512, "narrow_grid": 2, "traverse_threads": 128,
+                  "big_threads": 256, "group_bodies": 0, "group_threads": 128}
+GROUPS = [dict(DEFAULT_TUNING, group_bodies=512, group_threads=128),
+          dict(DEFAULT_TUNING, group_bodies=256, group_threads=64)]
+
+
+@pytest.mark.parametrize("tuning", [None, GROUPS[0]], ids=["one_world_per_cta", "solve_groups"])
+def test_fp64_dense_cluster_queue_overflow_and_colour_fallback(tuning):
     # 150 boxes crammed into 0.4 m: about 11,000 overlapping pairs, more than the sweep-and-prune
     # queue holds (10,240), so the world's pairs come from its second sweep; and bodies carry ~150
-    # manifolds, so first-fit colouring (128 colours at most) gives way to claiming rounds. Both
-    # paths must give the oracle's bits.
+    # manifolds, so first-fit colouring (128 colours at most) gives way to claiming rounds (in a
+    # solve group: the group falls back to one world at a time). All paths give the oracle's bits.
     scene = scenes.small_pile(n=150, seed=13, kinds=(1,))
     rng = np.random.default_rng(0)
     dyn = scene.bodies["type"] == 0
@@ -110,6 +119,8 @@ def test_fp64_dense_cluster_queue_overflow_and_colour_fallback():
     scene.bodies["pos"][dyn] = np.stack([rng.uniform(-0.2, 0.2, m), 1.5 + rng.uniform(-0.2, 0.2, m),
                                          rng.uniform(-0.2, 0.2, m)], 1)
     world, _ = scenes.make_world(scene, precision="f64", pair_factor=200)
+    if tuning:
+        world.set_tuning(tuning)
     ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
     pyoracle.load_scene(ow, scene)
     for step in range(4):
@@ -184,6 +195,45 @@ def test_batched_worlds_equal_alone_and_oracle():
         alone.close()
         ow.close()
     batch.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_solve_groups_same_bits_as_one_world_per_cta(precision):
+    # worlds of 8-300 bodies packed up to 8 per solver CTA: every body, pair and colour equals the
+    # one-world-per-CTA launch bit for bit (members share no bodies, and each keeps its own colours
+    # and per-body sweep order); in FP64 three of the worlds are also checked against the oracle
+    scene = scenes.config3(nworlds=40, nmin=8, nmax=300, seed=5)
+    steps = 60
+    ref, _ = scenes.make_world(scene, precision=precision)
+    runs = []
+    for t in GROUPS:
+        w, _ = scenes.make_world(scene, precision=precision)
+        w.set_tuning(t)
+        runs.append(w)
+    for step in range(steps):
+        ref.step(scene.dt)
+        for w in runs:
+            w.step(scene.dt)
+    rk, rc, rn = ref.colours()
+    assert rn > 1 and len(rk) > 100  # contacts were solved
+    for w in runs:
+        assert np.array_equal(w.bodies(), ref.bodies())
+        assert np.array_equal(w.pairs(), ref.pairs())
+        k, c, n = w.colours()
+        assert np.array_equal(k, rk) and np.array_equal(c, rc) and n == rn
+    if precision == "f64":
+        bb = runs[0].bodies()
+        for wi in (0, 17, 39):
+            sub = scenes.Scene("world %d" % wi, scene.shapes, scene.world_slice(wi).copy(), 1)
+            sub.bodies["world"] = 0
+            ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
+            pyoracle.load_scene(ow, sub)
+            for _ in range(steps):
+                ow.step(scene.dt)
+            assert np.array_equal(bb[scene.bodies["world"] == wi][:, :13], ow.bodies()[:, :13]), f"world {wi}"
+            ow.close()
+    for w in [ref] + runs:
+        w.close()
 
 
 def test_fp64_all_pairs_and_tree_worlds_in_one_batch():
