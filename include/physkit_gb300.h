@@ -172,7 +172,7 @@ typedef struct pk_tune_result
 {
     int32_t solve_threads;
     int32_t small_world;
-    int32_t narrow_grid;   /* CTAs per SM of the GJK and EPA passes (work queues, 128 threads) */
+    int32_t narrow_grid;
     int32_t traverse_threads;
     double step_ms_before; /* summed stage times per step before and after tuning */
     double step_ms_after;

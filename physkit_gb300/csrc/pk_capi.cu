@@ -1016,7 +1016,7 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
     {
         double bt = 1e300;
         pk::Tunables bc = best;
-        for (int g : {1, 2, 3, 4})
+        for (int g : {1, 2, 4})
         {
             pk::Tunables t = best;
             t.narrow_grid = g;

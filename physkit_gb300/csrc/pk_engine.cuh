@@ -236,7 +236,6 @@ template <class T> struct Dev
     int *epa_count;
     int *epa_count_heavy;
     int *epa_total;        // items admitted to the EPA list (at most contact_cap)
-    int *gjk_next, *epa_next; // work queues of the GJK and EPA passes (items taken so far)
     unsigned long long *np_iters; // [0] GJK iterations, [1] EPA expansions, [2] of which in heavy pairs
     unsigned long long *np_verts; // vertices a linear support scan visits, summed over the supports
     int *clist;            // pairs of active worlds whose new manifold holds contacts (any order)
@@ -387,8 +386,6 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.gjk2_count_heavy = 0;
         *d.ccount = 0;
         *d.epa_total = 0;
-        *d.gjk_next = 0;
-        *d.epa_next = 0;
         *d.all_small = 1;
         d.np_iters[0] = d.np_iters[1] = d.np_iters[2] = 0ull;
         *d.np_verts = 0ull;
@@ -1475,136 +1472,73 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
     }
 }
 
-// Narrowphase passes 2b and 3 run GJK and EPA as resumable runs, one iteration at a time: a lane
-// that finishes its pair takes the next one from the pass's queue (a counter shared by the grid),
-// so a warp's lanes stay busy until the queue is empty, although a pair's iteration count ranges
-// from 1 to 100 (GJK) or 64 (EPA). The grid is a few CTAs per SM. Each pair's arithmetic is the
-// same whichever lane runs it and in whatever order.
-
-// GJK's outcome for one pair (collision.cpp:165-189): an enclosing simplex is queued for EPA,
-// otherwise the pair is settled without a new contact and keeps GJK's separating direction.
-template <class T>
-__device__ __forceinline__ void gjk_settle(const Dev<T> &d, int p, const ShapeRef<T> &A, const ShapeRef<T> &B,
-                                           const GjkRun<T> &g, int r)
-{
-    warp_add(d.np_iters, unsigned(g.s.iters));
-    warp_add(d.np_verts, unsigned(g.s.iters + 1) * scan_verts(A, B));
-    const bool enclosed = r == GJK_ENCLOSED;
-    // admitted first against the list's capacity, so the two ends never meet
-    const bool admit = enclosed && warp_push(d.epa_total) < d.contact_cap;
-    if (enclosed && !admit)
-    {
-        // no room for this pair's EPA: flagged, and the pair keeps last step's contacts
-        atomicOr(d.status, ST_CONTACT_OVERFLOW);
-        Collision<T> none;
-        manifold_update(d, p, d.old_idx[p], A, B, false, none);
-    }
-    else if (admit)
-    {
-        int j;
-        if (A.ncl > 0 || B.ncl > 0)
-            j = d.contact_cap - 1 - warp_push(d.epa_count_heavy);
-        else
-            j = warp_push(d.epa_count);
-        d.epa_list[j] = p;
-        d.epa_simplex[j] = g.s;
-    }
-    else
-    {
-        Collision<T> none;
-        const V3<T> sep = r == GJK_SEPARATED ? g.dir : V3<T>{T(0), T(0), T(0)};
-        manifold_update(d, p, d.old_idx[p], A, B, false, none, sep);
-    }
-}
-
-// Narrowphase pass 2b: GJK over the pairs the separating-direction pass left.
+// Narrowphase pass 2b: GJK (collision.cpp:165-189) over the remaining pairs; enclosing simplices are
+// queued for EPA, the rest are settled without a new contact and keep GJK's separating direction.
 template <class T>
 __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.gjk2_count_heavy;
     const int n = nh + *d.gjk2_count;
-    int p = -1;
-    bool more = true; // the queue may still hold pairs for this lane
-    ShapeRef<T> A, B;
-    GjkRun<T> g;
-    while (true)
+    PK_GRID_STRIDE(i, n)
     {
-        int r = GJK_RUNNING;
-        if (p < 0 && more)
+        int p = d.gjk_list2[list_slot(i, nh, d.pair_cap)];
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+        Simplex<T> s;
+        V3<T> sep{T(0), T(0), T(0)};
+        bool enclosed = gjk(A, B, s, &sep);
+        warp_add(d.np_iters, unsigned(s.iters));
+        warp_add(d.np_verts, unsigned(s.iters + 1) * scan_verts(A, B));
+        // admitted first against the list's capacity, so the two ends never meet
+        const bool admit = enclosed && warp_push(d.epa_total) < d.contact_cap;
+        if (enclosed && !admit)
         {
-            const int i = warp_push(d.gjk_next);
-            if (i < n)
-            {
-                p = d.gjk_list2[list_slot(i, nh, d.pair_cap)];
-                const uint64_t val = sval[p];
-                A = body_shape(d, int(val >> 32));
-                B = body_shape(d, int(val & 0xFFFFFFFFu));
-                r = gjk_begin(A, B, g);
-            }
+            // no room for this pair's EPA: flagged, and the pair keeps last step's contacts
+            atomicOr(d.status, ST_CONTACT_OVERFLOW);
+            Collision<T> none;
+            manifold_update(d, p, d.old_idx[p], A, B, false, none);
+        }
+        else if (admit)
+        {
+            int j;
+            if (A.ncl > 0 || B.ncl > 0)
+                j = d.contact_cap - 1 - warp_push(d.epa_count_heavy);
             else
-                more = false;
+                j = warp_push(d.epa_count);
+            d.epa_list[j] = p;
+            d.epa_simplex[j] = s;
         }
-        else if (p >= 0)
-            r = gjk_step(A, B, g);
-        if (p >= 0 && r != GJK_RUNNING)
+        else
         {
-            gjk_settle(d, p, A, B, g, r);
-            p = -1;
+            Collision<T> none;
+            manifold_update(d, p, d.old_idx[p], A, B, false, none, sep);
         }
-        if (!__any_sync(0xFFFFFFFFu, p >= 0 || more)) break;
     }
 }
 
-// EPA's outcome for one pair, then the manifold update.
-template <class T>
-__device__ __forceinline__ void epa_settle(const Dev<T> &d, int p, const ShapeRef<T> &A, const ShapeRef<T> &B,
-                                           const EpaState<T> &es, bool hit, const Collision<T> &col)
-{
-    if (es.status) atomicOr(d.status, ST_EPA_CAP);
-    warp_add(d.np_iters + 1, unsigned(es.iters));
-    if (A.ncl > 0 || B.ncl > 0) warp_add(d.np_iters + 2, unsigned(es.iters));
-    warp_add(d.np_verts, unsigned(es.iters) * scan_verts(A, B));
-    manifold_update(d, p, d.old_idx[p], A, B, hit, col);
-}
-
-// Narrowphase pass 3: EPA (collision.cpp:411-504) over the intersecting pairs.
+// Narrowphase pass 3: EPA (collision.cpp:411-504) over intersecting pairs, then the manifold update.
 template <class T>
 __global__ void __launch_bounds__(128, PK_EPA_MIN_BLOCKS) k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
     const int nh = *d.epa_count_heavy;
     const int n = nh + *d.epa_count;
-    int p = -1;
-    bool more = true;
-    ShapeRef<T> A, B;
-    EpaState<T> es;
-    Collision<T> col;
-    while (true)
+    PK_GRID_STRIDE(i, n)
     {
-        int r = EPA_RUNNING;
-        if (p < 0 && more)
-        {
-            const int i = warp_push(d.epa_next);
-            if (i < n)
-            {
-                const int j = list_slot(i, nh, d.contact_cap);
-                p = d.epa_list[j];
-                const uint64_t val = sval[p];
-                A = body_shape(d, int(val >> 32));
-                B = body_shape(d, int(val & 0xFFFFFFFFu));
-                Simplex<T> s = d.epa_simplex[j];
-                r = epa_begin(A, B, s, es);
-            }
-            else
-                more = false;
-        }
-        else if (p >= 0)
-            r = epa_step(A, B, es, col);
-        if (p >= 0 && r != EPA_RUNNING)
-        {
-            epa_settle(d, p, A, B, es, r == EPA_HIT, col);
-            p = -1;
-        }
-        if (!__any_sync(0xFFFFFFFFu, p >= 0 || more)) break;
+        int j = list_slot(i, nh, d.contact_cap);
+        int p = d.epa_list[j];
+        uint64_t val = sval[p];
+        int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
+        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+        Simplex<T> s = d.epa_simplex[j];
+        EpaState<T> es;
+        Collision<T> col;
+        bool hit = epa(A, B, s, es, col);
+        if (es.status) atomicOr(d.status, ST_EPA_CAP);
+        warp_add(d.np_iters + 1, unsigned(es.iters));
+        if (A.ncl > 0 || B.ncl > 0) warp_add(d.np_iters + 2, unsigned(es.iters));
+        warp_add(d.np_verts, unsigned(es.iters) * scan_verts(A, B));
+        manifold_update(d, p, d.old_idx[p], A, B, hit, col);
     }
 }
 

@@ -38,7 +38,7 @@ struct Tunables
 {
     int solve_threads = 256;   // threads per solver CTA (one CTA per world)
     int small_world = 512;     // worlds up to this many local indices share the small solver launch
-    int narrow_grid = 2;       // CTAs per SM of the GJK and EPA passes (128 threads, work queues)
+    int narrow_grid = 2;       // GJK/EPA grid = narrow_grid x the default grid
     int traverse_threads = 128;
     int big_threads = 256;     // threads per solver CTA of the worlds above small_world
     int group_bodies = 0;      // solve groups: worlds packed up to 8 per CTA while their local

@@ -257,8 +257,6 @@ public:
         d.gjk2_count_heavy = counters_ + 20;
         d.all_small = counters_ + 21;
         d.epa_total = counters_ + 22;
-        d.gjk_next = counters_ + 23;
-        d.epa_next = counters_ + 26;
         PK_CUDA(alloc(&d.jstart, W));
         PK_CUDA(alloc(&d.jend, W));
         PK_CUDA(cudaMemset(d.jstart, 0, sizeof(int) * W));
@@ -1361,8 +1359,8 @@ private:
         k_old_index<T><<<gp, 256, 0, st_>>>(d, pk);
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
-        k_narrow_gjk<T><<<sms_ * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
-        k_narrow_epa<T><<<sms_ * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
+        k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
+        k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
         if (joint_cap_ > 0) k_joint_setup<T><<<grid(joint_cap_), 128, 0, st_>>>(d, dt);

@@ -401,56 +401,31 @@ template <class T> PK_HD bool gjk_simplex(Simplex<T> &s, V3<T> &dir)
     return false;
 }
 
-// gjk_collision (collision.cpp:165-189) as a resumable run: gjk_begin takes the first support,
-// each gjk_step one iteration (at most 100). A kernel can interleave the iterations of different
-// pairs on one lane; gjk() runs them back to back.
-enum : int
-{
-    GJK_RUNNING = 0,
-    GJK_ENCLOSED = 1,  // the simplex encloses the origin
-    GJK_SEPARATED = 2, // the support along dir does not pass the origin: dir separates the shapes
-    GJK_EXHAUSTED = 3, // 100 iterations without a decision: no collision, no separating direction
-};
-
-template <class T> struct GjkRun
-{
-    Simplex<T> s;
-    V3<T> dir;
-};
-
-template <class T> PK_HD int gjk_begin(const ShapeRef<T> &A, const ShapeRef<T> &B, GjkRun<T> &g)
-{
-    g.s.n = 0;
-    g.s.iters = 0;
-    g.dir = V3<T>{T(1), T(0), T(0)};
-    SupPt<T> pt = minkowski(A, B, g.dir);
-    g.s.push(pt);
-    if (sqnorm(pt.p) < T(1e-12)) return GJK_ENCLOSED;
-    g.dir = -normalized(pt.p);
-    return GJK_RUNNING;
-}
-
-template <class T> PK_HD int gjk_step(const ShapeRef<T> &A, const ShapeRef<T> &B, GjkRun<T> &g)
-{
-    if (g.s.iters >= 100) return GJK_EXHAUSTED;
-    g.s.iters += 1;
-    SupPt<T> np = minkowski(A, B, g.dir);
-    if (dot(np.p, g.dir) <= T(0)) return GJK_SEPARATED;
-    g.s.push(np);
-    return gjk_simplex(g.s, g.dir) ? GJK_ENCLOSED : GJK_RUNNING;
-}
-
-// Returns true with the enclosing simplex. On the exit where the support in the search direction
-// does not pass the origin, that direction (unit length) goes to *sep: no point of A - B lies
-// beyond the origin along it.
+// gjk_collision (collision.cpp:165-189). Returns true with the enclosing simplex. On the exit
+// where the support in the search direction does not pass the origin, that direction (unit
+// length) goes to *sep: no point of A - B lies beyond the origin along it.
 template <class T> PK_HD bool gjk(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, V3<T> *sep = nullptr)
 {
-    GjkRun<T> g;
-    int r = gjk_begin(A, B, g);
-    while (r == GJK_RUNNING) r = gjk_step(A, B, g);
-    s = g.s;
-    if (r == GJK_SEPARATED && sep) *sep = g.dir;
-    return r == GJK_ENCLOSED;
+    s.n = 0;
+    s.iters = 0;
+    V3<T> dir{T(1), T(0), T(0)};
+    SupPt<T> pt = minkowski(A, B, dir);
+    s.push(pt);
+    if (sqnorm(pt.p) < T(1e-12)) return true;
+    dir = -normalized(pt.p);
+    for (int iter = 0; iter < 100; ++iter)
+    {
+        s.iters = iter + 1;
+        SupPt<T> np = minkowski(A, B, dir);
+        if (dot(np.p, dir) <= T(0))
+        {
+            if (sep) *sep = dir;
+            return false;
+        }
+        s.push(np);
+        if (gjk_simplex(s, dir)) return true;
+    }
+    return false;
 }
 
 template <class T> PK_HD bool pad_simplex(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s)
@@ -693,22 +668,13 @@ struct HorizonEdge
     uint16_t start, end, adj;
 };
 
-// epa_solver::solve (collision.cpp:411-504) as a resumable run: epa_begin pads the simplex and
-// builds the first polytope, each epa_step one expansion (at most 64), then the closest face gives
-// the collision. epa() runs the steps back to back.
-enum : int
-{
-    EPA_RUNNING = 0,
-    EPA_HIT = 1,
-    EPA_MISS = 2,
-};
-
+// epa_solver::solve (collision.cpp:411-504). Returns true with a collision.
 template <class T>
-PK_HD int epa_begin(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T> &e)
+PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T> &e, Collision<T> &out)
 {
     e.status = 0;
     e.iters = 0;
-    if (s.n < 4 && !pad_simplex(A, B, s)) return EPA_MISS;
+    if (s.n < 4 && !pad_simplex(A, B, s)) return false;
     e.npoly = 4;
     for (int i = 0; i < 4; ++i) e.poly[i] = s.v[i];
     e.nfaces = 0;
@@ -735,29 +701,16 @@ PK_HD int epa_begin(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, E
                     }
                 }
             }
-    return EPA_RUNNING;
-}
 
-// The closest remaining face after the expansions stop (collision.cpp:500-504).
-template <class T> PK_HD int epa_finish(EpaState<T> &e, Collision<T> &out)
-{
-    int mf = e.pop_face();
-    if (mf < 0) return EPA_MISS;
-    out = e.barycentric(e.faces[mf]);
-    return EPA_HIT;
-}
-
-template <class T> PK_HD int epa_step(const ShapeRef<T> &A, const ShapeRef<T> &B, EpaState<T> &e, Collision<T> &out)
-{
-    if (e.iters >= 64) return epa_finish(e, out);
     HorizonEdge horizon[kMaxHorizon];
     uint16_t stack[kMaxFaces];
     uint16_t nf[kMaxHorizon];
     const T tol = T(1e-6);
+    for (int iter = 0; iter < 64; ++iter)
     {
-        e.iters += 1;
+        e.iters = iter + 1;
         int mf = e.pop_face();
-        if (mf < 0) return epa_finish(e, out);
+        if (mf < 0) break;
         const EpaFace<T> minf = e.faces[mf];
         SupPt<T> p = minkowski(A, B, minf.n);
         T pd = dot(minf.n, p.p);
@@ -774,7 +727,7 @@ template <class T> PK_HD int epa_step(const ShapeRef<T> &A, const ShapeRef<T> &B
         if (done)
         {
             out = e.barycentric(minf);
-            return EPA_HIT;
+            return true;
         }
         // find_silhouette (collision.cpp:315-353): depth-first flood over visible faces
         int nh = 0, sp = 0;
@@ -803,11 +756,11 @@ template <class T> PK_HD int epa_step(const ShapeRef<T> &A, const ShapeRef<T> &B
                     e.status |= PK_NP_HORIZON_CAP;
             }
         }
-        if (nh == 0) return epa_finish(e, out);
+        if (nh == 0) break;
         if (e.nfaces + nh > kMaxFaces)
         {
             e.status |= PK_NP_FACE_CAP;
-            return epa_finish(e, out);
+            break;
         }
         e.poly[e.npoly] = p;
         int pi = e.npoly++;
@@ -828,16 +781,10 @@ template <class T> PK_HD int epa_step(const ShapeRef<T> &A, const ShapeRef<T> &B
                     e.link(nf[j], nf[i], horizon[j].end, pi);
             }
     }
-    return EPA_RUNNING;
-}
-
-// Returns true with a collision.
-template <class T>
-PK_HD bool epa(const ShapeRef<T> &A, const ShapeRef<T> &B, Simplex<T> &s, EpaState<T> &e, Collision<T> &out)
-{
-    int r = epa_begin(A, B, s, e);
-    while (r == EPA_RUNNING) r = epa_step(A, B, e, out);
-    return r == EPA_HIT;
+    int mf = e.pop_face();
+    if (mf < 0) return false;
+    out = e.barycentric(e.faces[mf]);
+    return true;
 }
 
 // gjk_epa (collision.cpp:512-518)
