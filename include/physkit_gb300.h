@@ -158,7 +158,8 @@ void *pk_world_stream(pk_world *w);
 
 /* Stage timing: with timing on, plain (non-graph) steps record CUDA events around each stage;
  * pk_world_read_stage_times returns the summed milliseconds and step counts per stage since the
- * last read. The reference has no timers; this is the per-stage trace of the step. */
+ * last read. The reference has no timers; this is the per-stage trace of the step. The first 9
+ * rows are the step's stages in order; rows named "narrow:..." then split the narrowphase. */
 int pk_world_set_timing(pk_world *w, int32_t enable);
 int pk_world_read_stage_times(pk_world *w, double *total_ms, int32_t *counts, int32_t cap, int32_t *nstages);
 const char *pk_stage_name(int32_t stage);

@@ -26,9 +26,9 @@
 
 namespace pk
 {
-const char *const kStageNames[kStages] = {"integrate_vel", "morton_sort", "lbvh_build_refit", "traverse",
-                                          "pair_sort",     "narrow",      "contact_setup",    "solve",
-                                          "integrate_pos"};
+const char *const kStageNames[kStageRows] = {"integrate_vel", "morton_sort",   "lbvh_build_refit", "traverse",
+                                             "pair_sort",     "narrow",        "contact_setup",    "solve",
+                                             "integrate_pos", "narrow:pre",    "narrow:gjk",       "narrow:epa"};
 }
 
 namespace
@@ -894,15 +894,15 @@ int pk_world_set_timing(pk_world *w, int32_t enable)
 int pk_world_read_stage_times(pk_world *w, double *total_ms, int32_t *counts, int32_t cap, int32_t *nstages)
 {
     if (!w) return PK_ERR_INVALID;
-    double ms[pk::kStages];
-    int cnt[pk::kStages];
+    double ms[pk::kStageRows];
+    int cnt[pk::kStageRows];
     if (w->eng->read_stage_times(ms, cnt) < 0)
     {
         g_last_cuda = w->eng->last_error();
         return PK_ERR_CUDA;
     }
-    if (nstages) *nstages = pk::kStages;
-    for (int k = 0; k < pk::kStages && k < cap; ++k)
+    if (nstages) *nstages = pk::kStageRows;
+    for (int k = 0; k < pk::kStageRows && k < cap; ++k)
     {
         if (total_ms) total_ms[k] = ms[k];
         if (counts) counts[k] = cnt[k];
@@ -912,15 +912,15 @@ int pk_world_read_stage_times(pk_world *w, double *total_ms, int32_t *counts, in
 
 const char *pk_stage_name(int32_t stage)
 {
-    if (stage < 0 || stage >= pk::kStages) return nullptr;
+    if (stage < 0 || stage >= pk::kStageRows) return nullptr;
     return pk::kStageNames[stage];
 }
 
 // Time `k` plain steps with per-stage CUDA events; returns mean ms per step of every stage.
 static int timed_steps(pk_world *w, double dt, int k, double *stage_ms)
 {
-    double ms[pk::kStages];
-    int cnt[pk::kStages];
+    double ms[pk::kStageRows];
+    int cnt[pk::kStageRows];
     if (w->eng->read_stage_times(ms, cnt) < 0) return PK_ERR_CUDA; // clear
     for (int i = 0; i < k; ++i)
         if (int rc = pk_world_step_async(w, dt)) return rc;

@@ -69,8 +69,9 @@ struct MeshHitOut
     int32_t hit, triangle;
 };
 
-constexpr int kStages = 9;
-extern const char *const kStageNames[kStages];
+constexpr int kStages = 9;     // the step's stages, in order (they sum to the step)
+constexpr int kStageRows = 12; // then the narrowphase's parts: pre-pass, separating axis + GJK, EPA
+extern const char *const kStageNames[kStageRows];
 
 class EngineBase
 {

@@ -754,14 +754,14 @@ public:
     {
         PK_CUDA(cudaStreamSynchronize(st_));
         PK_CUDA(accumulate_stage_times());
-        for (int k = 0; k < kStages; ++k)
+        for (int k = 0; k < kStageRows; ++k)
         {
             ms[k] = stage_ms_[k];
             count[k] = stage_n_[k];
             stage_ms_[k] = 0.0;
             stage_n_[k] = 0;
         }
-        return kStages;
+        return kStageRows;
     }
 
     int synchronize(StepCounters *c) override
@@ -1197,15 +1197,17 @@ private:
     StagingRing stage_; // pinned staging of the asynchronous uploads (allocated on first use)
     cudaError_t ensure_staging() { return stage_.ready() ? cudaSuccess : stage_.init(size_t(64) << 20); }
     int launches_ = 0;
-    std::vector<cudaEvent_t> events_; // kStages + 1 per timed step
+    // per timed step: the kStages + 1 stage boundaries, then two marks inside the narrowphase
+    static constexpr int kMarks = kStages + 3;
+    std::vector<cudaEvent_t> events_;
     int timed_steps_ = 0;
-    double stage_ms_[kStages] = {};
-    int stage_n_[kStages] = {};
+    double stage_ms_[kStageRows] = {};
+    int stage_n_[kStageRows] = {};
 
     cudaError_t mark(int stage)
     {
         if (!timing_ || capturing_) return cudaSuccess;
-        size_t idx = size_t(timed_steps_) * (kStages + 1) + size_t(stage);
+        size_t idx = size_t(timed_steps_) * kMarks + size_t(stage);
         while (events_.size() <= idx)
         {
             cudaEvent_t e;
@@ -1217,12 +1219,15 @@ private:
     }
     cudaError_t accumulate_stage_times()
     {
+        // rows: stage k spans marks k..k+1; the narrowphase's parts span 5..10, 10..11, 11..6
+        const int from[kStageRows] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 5, kStages + 1, kStages + 2};
+        const int to[kStageRows] = {1, 2, 3, 4, 5, 6, 7, 8, 9, kStages + 1, kStages + 2, 6};
         for (int s = 0; s < timed_steps_; ++s)
-            for (int k = 0; k < kStages; ++k)
+            for (int k = 0; k < kStageRows; ++k)
             {
                 float ms = 0.f;
-                cudaError_t e = cudaEventElapsedTime(&ms, events_[size_t(s) * (kStages + 1) + k],
-                                                     events_[size_t(s) * (kStages + 1) + k + 1]);
+                cudaError_t e = cudaEventElapsedTime(&ms, events_[size_t(s) * kMarks + from[k]],
+                                                     events_[size_t(s) * kMarks + to[k]]);
                 if (e != cudaSuccess) return e;
                 stage_ms_[k] += ms;
                 stage_n_[k] += 1;
@@ -1358,8 +1363,10 @@ private:
         PK_CUDA(mark(5));
         k_old_index<T><<<gp, 256, 0, st_>>>(d, pk);
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
+        PK_CUDA(mark(kStages + 1));
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
+        PK_CUDA(mark(kStages + 2));
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
