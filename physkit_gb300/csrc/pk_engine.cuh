@@ -1299,6 +1299,30 @@ __device__ __forceinline__ ShapeRef<float> body_shape32(const Dev<double> &d, in
     return s;
 }
 
+// FP64 form: the pre-pass tests (bounding spheres, then the 15-axis test of the oriented local
+// boxes) in FP32. They only decide that a pair is certainly apart (GJK then returns no collision,
+// collision.cpp:181-182), so no FP64 result is needed: the margin, 1024 FP32 epsilons of the
+// pair's scale plus the FP64 test's own terms, covers the rounding of the FP32 poses, boxes and
+// products many times over. A pair it cannot settle goes on to the separating-axis pass and GJK.
+#ifndef PK_PRE_F32
+#define PK_PRE_F32 1
+#endif
+__device__ __forceinline__ bool apart_f32(const Aabb<double> &la, const ShapeRef<double> &A, const Aabb<double> &lb,
+                                          const ShapeRef<double> &B)
+{
+    const V3<float> xa{float(A.pos.x), float(A.pos.y), float(A.pos.z)};
+    const V3<float> xb{float(B.pos.x), float(B.pos.y), float(B.pos.z)};
+    const float rs = float(A.rmax) + float(B.rmax);
+    const float margin = (rs + norm(xa) + norm(xb)) * (1024.0f * EpsOf<float>::v) + 1e-6f + 1e-5f * rs;
+    const float cull = rs + margin;
+    if (sqnorm(xb - xa) > cull * cull) return true;
+    const Qt<float> qa{float(A.q.w), float(A.q.x), float(A.q.y), float(A.q.z)};
+    const Qt<float> qb{float(B.q.w), float(B.q.x), float(B.q.y), float(B.q.z)};
+    const Aabb<float> ba{{float(la.mn.x), float(la.mn.y), float(la.mn.z)}, {float(la.mx.x), float(la.mx.y), float(la.mx.z)}};
+    const Aabb<float> bb{{float(lb.mn.x), float(lb.mn.y), float(lb.mn.z)}, {float(lb.mx.x), float(lb.mx.y), float(lb.mx.z)}};
+    return obb_separated(ba, qa, xa, bb, qb, xb, margin);
+}
+
 // Last step's manifold of each pair of an active world. Last step's pairs of a world are the
 // segment [mstart_old, mend_old) of last step's sorted keys, and this step's pairs are sorted the
 // same way, so each thread takes a run of consecutive pairs: one binary search for the first,
@@ -1373,6 +1397,11 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
         const int old_idx = d.old_idx[p]; // k_old_index
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         bool apart = false;
+#if PK_PRE_F32
+        if constexpr (sizeof(T) == 8)
+            apart = apart_f32(d.shape_box[d.meta[sa].shape], A, d.shape_box[d.meta[sb].shape], B);
+        else
+#endif
         {
             V3<T> dc = B.pos - A.pos;
             T rs = A.rmax + B.rmax;
@@ -1472,6 +1501,9 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
     }
 }
 
+#ifndef PK_GJK_F32
+#define PK_GJK_F32 1
+#endif
 // Narrowphase pass 2b: GJK (collision.cpp:165-189) over the remaining pairs; enclosing simplices are
 // queued for EPA, the rest are settled without a new contact and keep GJK's separating direction.
 template <class T>
@@ -1485,6 +1517,34 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
+#if PK_GJK_F32
+        if constexpr (sizeof(T) == 8)
+        {
+            // FP64 form: GJK in FP32 first; a separating direction it finds, confirmed with the
+            // separating-axis pass's margin, settles the pair as apart (collision.cpp:181-182)
+            bool oka, okb;
+            const ShapeRef<float> A32 = body_shape32(d, sa, oka), B32 = body_shape32(d, sb, okb);
+            if (oka && okb)
+            {
+                Simplex<float> s32;
+                V3<float> sep32{0.f, 0.f, 0.f};
+                if (!gjk(A32, B32, s32, &sep32) && sqnorm(sep32) > 0.f)
+                {
+                    const float rs = A32.rmax + B32.rmax;
+                    const float m32 = (rs + norm(A32.pos) + norm(B32.pos)) * (1024.0f * EpsOf<float>::v) + 1e-6f +
+                                      1e-5f * rs;
+                    const SupPt<float> sp = minkowski(A32, B32, sep32);
+                    if (dot(sp.p, sep32) < -m32)
+                    {
+                        warp_add(d.np_verts, unsigned(s32.iters + 2) * scan_verts(A, B));
+                        Collision<T> none;
+                        manifold_update(d, p, d.old_idx[p], A, B, false, none, V3<T>{T(sep32.x), T(sep32.y), T(sep32.z)});
+                        continue;
+                    }
+                }
+            }
+        }
+#endif
         Simplex<T> s;
         V3<T> sep{T(0), T(0), T(0)};
         bool enclosed = gjk(A, B, s, &sep);
