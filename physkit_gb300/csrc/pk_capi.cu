@@ -28,7 +28,8 @@ namespace pk
 {
 const char *const kStageNames[kStageRows] = {"integrate_vel", "morton_sort",   "lbvh_build_refit", "traverse",
                                              "pair_sort",     "narrow",        "contact_setup",    "solve",
-                                             "integrate_pos", "narrow:pre",    "narrow:gjk",       "narrow:epa"};
+                                             "integrate_pos", "narrow:pre",    "narrow:axis",      "narrow:gjk",
+                                             "narrow:epa"};
 }
 
 namespace

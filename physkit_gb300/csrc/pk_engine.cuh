@@ -1304,9 +1304,6 @@ __device__ __forceinline__ ShapeRef<float> body_shape32(const Dev<double> &d, in
 // collision.cpp:181-182), so no FP64 result is needed: the margin, 1024 FP32 epsilons of the
 // pair's scale plus the FP64 test's own terms, covers the rounding of the FP32 poses, boxes and
 // products many times over. A pair it cannot settle goes on to the separating-axis pass and GJK.
-#ifndef PK_PRE_F32
-#define PK_PRE_F32 1
-#endif
 __device__ __forceinline__ bool apart_f32(const Aabb<double> &la, const ShapeRef<double> &A, const Aabb<double> &lb,
                                           const ShapeRef<double> &B)
 {
@@ -1397,11 +1394,9 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
         const int old_idx = d.old_idx[p]; // k_old_index
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         bool apart = false;
-#if PK_PRE_F32
         if constexpr (sizeof(T) == 8)
             apart = apart_f32(d.shape_box[d.meta[sa].shape], A, d.shape_box[d.meta[sb].shape], B);
         else
-#endif
         {
             V3<T> dc = B.pos - A.pos;
             T rs = A.rmax + B.rmax;
@@ -1501,9 +1496,6 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
     }
 }
 
-#ifndef PK_GJK_F32
-#define PK_GJK_F32 1
-#endif
 // Narrowphase pass 2b: GJK (collision.cpp:165-189) over the remaining pairs; enclosing simplices are
 // queued for EPA, the rest are settled without a new contact and keep GJK's separating direction.
 template <class T>
@@ -1517,34 +1509,6 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
-#if PK_GJK_F32
-        if constexpr (sizeof(T) == 8)
-        {
-            // FP64 form: GJK in FP32 first; a separating direction it finds, confirmed with the
-            // separating-axis pass's margin, settles the pair as apart (collision.cpp:181-182)
-            bool oka, okb;
-            const ShapeRef<float> A32 = body_shape32(d, sa, oka), B32 = body_shape32(d, sb, okb);
-            if (oka && okb)
-            {
-                Simplex<float> s32;
-                V3<float> sep32{0.f, 0.f, 0.f};
-                if (!gjk(A32, B32, s32, &sep32) && sqnorm(sep32) > 0.f)
-                {
-                    const float rs = A32.rmax + B32.rmax;
-                    const float m32 = (rs + norm(A32.pos) + norm(B32.pos)) * (1024.0f * EpsOf<float>::v) + 1e-6f +
-                                      1e-5f * rs;
-                    const SupPt<float> sp = minkowski(A32, B32, sep32);
-                    if (dot(sp.p, sep32) < -m32)
-                    {
-                        warp_add(d.np_verts, unsigned(s32.iters + 2) * scan_verts(A, B));
-                        Collision<T> none;
-                        manifold_update(d, p, d.old_idx[p], A, B, false, none, V3<T>{T(sep32.x), T(sep32.y), T(sep32.z)});
-                        continue;
-                    }
-                }
-            }
-        }
-#endif
         Simplex<T> s;
         V3<T> sep{T(0), T(0), T(0)};
         bool enclosed = gjk(A, B, s, &sep);

@@ -70,7 +70,7 @@ struct MeshHitOut
 };
 
 constexpr int kStages = 9;     // the step's stages, in order (they sum to the step)
-constexpr int kStageRows = 12; // then the narrowphase's parts: pre-pass, separating axis + GJK, EPA
+constexpr int kStageRows = 13; // then the narrowphase's parts: pre-pass, separating axis, GJK, EPA
 extern const char *const kStageNames[kStageRows];
 
 class EngineBase

@@ -1174,7 +1174,8 @@ private:
     cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
     int joint_cap_ = 0, njoints_ = 0;
     static constexpr size_t kMaxSolveSmem = 160 * 1024;
-    Tunables tune_{};
+    // the FP64 form's solver sweeps are long FP64 chains: small worlds share CTAs (solve groups)
+    Tunables tune_ = sizeof(T) == 8 ? Tunables{256, 512, 2, 128, 256, 1024, 128} : Tunables{};
     int big_worlds_ = 0;
     std::vector<int> goff_; // solve groups: first index in the world order of each group, then the end
     int *goff_dev_ = nullptr;
@@ -1197,8 +1198,8 @@ private:
     StagingRing stage_; // pinned staging of the asynchronous uploads (allocated on first use)
     cudaError_t ensure_staging() { return stage_.ready() ? cudaSuccess : stage_.init(size_t(64) << 20); }
     int launches_ = 0;
-    // per timed step: the kStages + 1 stage boundaries, then two marks inside the narrowphase
-    static constexpr int kMarks = kStages + 3;
+    // per timed step: the kStages + 1 stage boundaries, then three marks inside the narrowphase
+    static constexpr int kMarks = kStages + 4;
     std::vector<cudaEvent_t> events_;
     int timed_steps_ = 0;
     double stage_ms_[kStageRows] = {};
@@ -1219,9 +1220,9 @@ private:
     }
     cudaError_t accumulate_stage_times()
     {
-        // rows: stage k spans marks k..k+1; the narrowphase's parts span 5..10, 10..11, 11..6
-        const int from[kStageRows] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 5, kStages + 1, kStages + 2};
-        const int to[kStageRows] = {1, 2, 3, 4, 5, 6, 7, 8, 9, kStages + 1, kStages + 2, 6};
+        // rows: stage k spans marks k..k+1; the narrowphase's parts span 5..10, 10..11, 11..12, 12..6
+        const int from[kStageRows] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 5, kStages + 1, kStages + 2, kStages + 3};
+        const int to[kStageRows] = {1, 2, 3, 4, 5, 6, 7, 8, 9, kStages + 1, kStages + 2, kStages + 3, 6};
         for (int s = 0; s < timed_steps_; ++s)
             for (int k = 0; k < kStageRows; ++k)
             {
@@ -1365,8 +1366,9 @@ private:
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         PK_CUDA(mark(kStages + 1));
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
-        k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(kStages + 2));
+        k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
+        PK_CUDA(mark(kStages + 3));
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);

@@ -304,12 +304,20 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
     """Drive the server with a Poisson request stream in real time; returns the latency report.
     The host loop takes arrivals, admits opens, enqueues a batched step whenever a lane's pipeline
     has room and polls completions; it waits on the GPU only when it has nothing else to do. With
-    lanes = 2, worlds up to 1,024 bodies and larger ones are served by separate pools (a quarter
-    of the world slots and 30 % of the bodies for the large worlds, which hold most bodies)."""
-    if lanes == 2:
-        srv = LaneServer([(1024, max_worlds - max_worlds // 4, int(0.3 * max_bodies)),
-                          (nmax, max_worlds // 4, max_bodies - int(0.3 * max_bodies))],
-                         precision=precision, pipeline_depth=pipeline_depth)
+    lanes > 1, worlds are served by separate pools by size (2 lanes: up to 1,024 bodies and above;
+    3: 512 / 2,048 / 4,096; 4: 256 / 1,024 / 2,048 / 4,096), each with its own stream."""
+    if lanes > 1:
+        # lanes by world size, finer at the top (the largest worlds set a step's length); world
+        # slots follow each lane's share of worlds under the log-uniform size law, bodies its share
+        # of bodies
+        lo = 16
+        bounds = {2: [1024, nmax], 3: [512, 2048, nmax], 4: [256, 1024, 2048, nmax]}[lanes]
+        edges = [lo] + bounds
+        wshare = [math.log(edges[k + 1] / edges[k]) / math.log(nmax / lo) for k in range(lanes)]
+        bshare = [(edges[k + 1] - edges[k]) / (nmax - lo) for k in range(lanes)]
+        srv = LaneServer([(b, max(16, int(max_worlds * ws)), max(4 * b, int(max_bodies * bs)))
+                          for b, ws, bs in zip(bounds, wshare, bshare)], precision=precision,
+                         pipeline_depth=pipeline_depth)
     else:
         srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision,
                          pipeline_depth=pipeline_depth)

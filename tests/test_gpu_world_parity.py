@@ -98,15 +98,15 @@ def test_fp64_remove_and_add_bodies():
     world.close()
 
 
-# launch shapes of pk_world_set_tuning: the defaults, and solve groups (several small worlds per
-# solver CTA, their colours swept together) at two packings
-DEFAULT_TUNING = {"solve_threads": 256, "small_world": 512, "narrow_grid": 2, "traverse_threads": 128,
-                  "big_threads": 256, "group_bodies": 0, "group_threads": 128}
-GROUPS = [dict(DEFAULT_TUNING, group_bodies=512, group_threads=128),
-          dict(DEFAULT_TUNING, group_bodies=256, group_threads=64)]
+# launch shapes of pk_world_set_tuning: one world per solver CTA, and solve groups (several small
+# worlds per solver CTA, their colours swept together) at two packings
+PER_WORLD = {"solve_threads": 256, "small_world": 512, "narrow_grid": 2, "traverse_threads": 128,
+             "big_threads": 256, "group_bodies": 0, "group_threads": 128}
+GROUPS = [dict(PER_WORLD, group_bodies=512, group_threads=128),
+          dict(PER_WORLD, group_bodies=256, group_threads=64)]
 
 
-@pytest.mark.parametrize("tuning", [None, GROUPS[0]], ids=["one_world_per_cta", "solve_groups"])
+@pytest.mark.parametrize("tuning", [PER_WORLD, GROUPS[0]], ids=["one_world_per_cta", "solve_groups"])
 def test_fp64_dense_cluster_queue_overflow_and_colour_fallback(tuning):
     # 150 boxes crammed into 0.4 m: about 11,000 overlapping pairs, more than the sweep-and-prune
     # queue holds (10,240), so the world's pairs come from its second sweep; and bodies carry ~150
@@ -119,8 +119,7 @@ def test_fp64_dense_cluster_queue_overflow_and_colour_fallback(tuning):
     scene.bodies["pos"][dyn] = np.stack([rng.uniform(-0.2, 0.2, m), 1.5 + rng.uniform(-0.2, 0.2, m),
                                          rng.uniform(-0.2, 0.2, m)], 1)
     world, _ = scenes.make_world(scene, precision="f64", pair_factor=200)
-    if tuning:
-        world.set_tuning(tuning)
+    world.set_tuning(tuning)
     ow = pyoracle.OracleWorld(gravity=scene.gravity, iterations=scene.iterations, order="colour")
     pyoracle.load_scene(ow, scene)
     for step in range(4):
@@ -205,6 +204,7 @@ def test_solve_groups_same_bits_as_one_world_per_cta(precision):
     scene = scenes.config3(nworlds=40, nmin=8, nmax=300, seed=5)
     steps = 60
     ref, _ = scenes.make_world(scene, precision=precision)
+    ref.set_tuning(PER_WORLD)
     runs = []
     for t in GROUPS:
         w, _ = scenes.make_world(scene, precision=precision)
