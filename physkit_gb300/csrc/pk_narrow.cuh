@@ -164,8 +164,10 @@ template <class T> struct ShapeRef
     {
         int best = -1;
         T bd = T(0);
-        T dn = norm(ld);
-        if (!(dn > T(0))) return 0; // every value is zero: the first vertex
+        const T n2 = sqnorm(ld);
+        if (!(n2 > T(0))) return 0; // every value is zero: the first vertex
+        // |ld| only for the FP32 form's polar angle (the FP64 form takes the angles in FP32)
+        const T dn = sizeof(T) == 8 ? T(0) : pk_sqrt(n2);
         uv_window(ld, dn, [&](int i) {
             T v = verts[3 * i] * ld.x + verts[3 * i + 1] * ld.y + verts[3 * i + 2] * ld.z;
             if (best < 0 || v > bd || (v == bd && i < best))
@@ -178,24 +180,37 @@ template <class T> struct ShapeRef
     }
 
     // The UV-sphere vertices argmax_uv compares (see there), visited in the window's order; U is
-    // the precision of the angle arithmetic (dn = |ld| > 0).
+    // the precision of the vertex values (dn = |ld| > 0). The angles are found in FP32 in both
+    // forms. In the FP64 form the window is then widened by a ring (a sector) on the side of a
+    // boundary within 1/16 of the FP32 fractional index, and the pole band is entered 6 % early, so
+    // it holds every vertex of the window the angles in FP64 would give: the FP32 angle error is
+    // below 1e-2 ring or sector (1e-4 away from the poles). Extra candidates are compared exactly
+    // like the others, so the result is the same vertex. (Query directions are unit vectors, or
+    // zero, which argmax_uv settles first, so the FP32 copy neither underflows nor overflows.)
     template <class U, class F> PK_HD void uv_window(V3<U> ld, U dn, F take) const
     {
         const int S = uv_stacks, K = uv_sectors, last = nverts - 1;
-        U cy = ld.y / dn;
-        cy = cy > U(1) ? U(1) : (cy < U(-1) ? U(-1) : cy);
-        const U pi = U(3.14159265358979323846);
-        U f = pk_acos(cy) * U(S) / pi; // fractional ring index, 0 at the north pole
+        constexpr bool wide = sizeof(U) == 8;
+        const float lx = float(ld.x), ly = float(ld.y), lz = float(ld.z);
+        float cy = wide ? ly / pk_sqrt(lx * lx + ly * ly + lz * lz) : float(ld.y / dn);
+        cy = cy > 1.0f ? 1.0f : (cy < -1.0f ? -1.0f : cy);
+        const float pi = 3.14159265358979323846f;
+        const float f = pk_acos(cy) * float(S) / pi; // fractional ring index, 0 at the north pole
         int i0 = int(f);
         i0 = i0 < 0 ? 0 : (i0 > S ? S : i0);
         int ilo = i0 - 1, ihi = i0 + 2;
-        U sphi2 = U(1) - cy * cy;
+        if (wide)
+        {
+            ilo -= f - float(i0) < 0.0625f;
+            ihi += f - float(i0) > 0.9375f;
+        }
+        const float sphi2 = 1.0f - cy * cy;
         // sin(phi) below which the sector gap could fall under 1e-4: 1e-4 / (sin(pi/S) *
         // (cos(pi/K) - cos(4 pi/K))), with x - x^3/6 <= sin x making it an over-estimate
-        const U dp = pi / U(S), a1 = U(2.5) * pi / U(K), a2 = U(1.5) * pi / U(K);
-        const U lb = (dp - dp * dp * dp / U(6)) * U(2) * (a1 - a1 * a1 * a1 / U(6)) * (a2 - a2 * a2 * a2 / U(6));
-        const U thr = U(1e-4) / lb;
-        if (sphi2 < thr * thr)
+        const float dp = pi / float(S), a1 = 2.5f * pi / float(K), a2 = 1.5f * pi / float(K);
+        const float lb = (dp - dp * dp * dp / 6.0f) * 2.0f * (a1 - a1 * a1 * a1 / 6.0f) * (a2 - a2 * a2 * a2 / 6.0f);
+        const float thr = 1e-4f / lb;
+        if (sphi2 < thr * thr * (wide ? 1.0625f : 1.0f))
         {
             // within asin(0.2) of a pole: the pole and whole rings
             if (ilo <= 0) take(0);
@@ -205,10 +220,17 @@ template <class T> struct ShapeRef
                 for (int j = 0; j < K; ++j) take(1 + (i - 1) * K + j);
             return;
         }
-        U th = pk_atan2(ld.z, ld.x);
-        if (th < U(0)) th = th + U(2) * pi;
-        int j0 = int(th * U(K) / (U(2) * pi));
+        float th = wide ? pk_atan2(lz, lx) : float(pk_atan2(ld.z, ld.x));
+        if (th < 0.0f) th = th + 2.0f * pi;
+        const float g = th * float(K) / (2.0f * pi);
+        int j0 = int(g);
         j0 = j0 > K - 1 ? K - 1 : j0;
+        int jlo = j0 - 1, jhi = j0 + 2;
+        if (wide)
+        {
+            jlo -= g - float(j0) < 0.0625f;
+            jhi += g - float(j0) > 0.9375f;
+        }
         for (int i = ilo; i <= ihi; ++i)
         {
             if (i <= 0)
@@ -221,9 +243,9 @@ template <class T> struct ShapeRef
                 take(last);
                 continue;
             }
-            for (int jj = j0 - 1; jj <= j0 + 2; ++jj)
+            for (int jj = jlo; jj <= jhi; ++jj)
             {
-                int j = jj < 0 ? jj + K : (jj >= K ? jj - K : jj); // jj in [-1, K + 1]
+                int j = jj < 0 ? jj + K : (jj >= K ? jj - K : jj); // jj in [-2, K + 2]
                 take(1 + (i - 1) * K + j);
             }
         }
