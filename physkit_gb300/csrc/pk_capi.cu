@@ -325,13 +325,28 @@ void pk_world_destroy(pk_world *w)
     delete w;
 }
 
+// True for mesh::box's layout (mesh.cpp:31-40): 8 vertices (+-hx, +-hy, +-hz) with its sign pattern,
+// exactly (vertex 6 holds +h).
+static bool box_layout(const std::vector<double> &v)
+{
+    if (v.size() != 24) return false;
+    static const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                 {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    for (int i = 0; i < 8; ++i)
+        for (int k = 0; k < 3; ++k)
+            if (!(v[size_t(3 * i + k)] == double(sg[i][k]) * v[size_t(18 + k)])) return false;
+    return true;
+}
+
 // uv_stacks/uv_sectors: the layout of a UV sphere from pk_shape_sphere (0: any other vertex list);
-// the device's support search then looks only near the query direction.
+// the device's support search then looks only near the query direction. A vertex list in
+// mesh::box's layout is marked (kBoxLayout) for the box support search.
 static int add_shape(pk_world *w, const std::vector<double> &v, const std::vector<int> &tris, int32_t *out,
                      int uv_stacks = 0, int uv_sectors = 0)
 {
     size_t nv = v.size() / 3;
     if (nv == 0) return PK_ERR_INVALID;
+    if (uv_stacks == 0 && box_layout(v)) uv_stacks = pk::kBoxLayout;
     if (w->verts.size() / 3 + nv > size_t(w->cfg.vert_cap) || w->ranges.size() / 8 + 1 > size_t(w->cfg.shape_cap))
         return PK_ERR_CAPACITY;
     // aabb::from_points (bounds.h:33-49)
@@ -996,7 +1011,8 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
     {
         double bt = 1e300;
         pk::Tunables bc = best;
-        const int tw[][2] = {{0, 128}, {256, 64}, {512, 128}, {1024, 128}, {1024, 256}, {2048, 256}};
+        const int tw[][2] = {{0, 128},    {128, 32},   {256, 32},   {256, 64},
+                             {512, 128},  {1024, 128}, {1024, 256}, {2048, 256}};
         for (const auto &c : tw)
         {
             pk::Tunables t = best;

@@ -29,6 +29,7 @@ constexpr int kMaxPoly = 4 + 64;
 constexpr int kMaxFaces = 512;
 constexpr int kMaxHorizon = 96;
 constexpr uint16_t kNull16 = 0xFFFF;
+constexpr int kBoxLayout = -1; // ShapeRef::uv_stacks of a mesh in mesh::box's layout
 
 enum : int
 {
@@ -73,7 +74,8 @@ template <class T> struct ShapeRef
     int ngr;       // groups of kClusterSize consecutive clusters (64 vertices), same layout
     const T *gr;
     T rmax;
-    int uv_stacks;  // > 0: the vertex list is a UV sphere of this layout (pk_shape_sphere)
+    int uv_stacks;  // > 0: the vertex list is a UV sphere of this layout (pk_shape_sphere);
+                    // kBoxLayout: mesh::box's 8 vertices (+-hx, +-hy, +-hz) in its order
     int uv_sectors;
 
     // First strictly maximal vertex of v.ld over the vertex list, in index order.
@@ -160,6 +162,28 @@ template <class T> struct ShapeRef
     //    whole.
     // Rounding of any vertex value is below 1e-6 |ld| r in FP32 (below 1e-15 in FP64). Candidates
     // are compared by value, then by lower index, so ties resolve as in the linear scan.
+    // mesh::box (mesh.cpp:31-40): with px = hx lx, py = hy ly, pz = hz lz, vertex i's value
+    // (x lx + y ly) + z lz is +-((px +- py) +- pz), since rounding to nearest commutes with
+    // negation; 3 products and 6 sums give the linear scan's 8 values bit for bit (an exact zero may
+    // differ in sign, which compares equal), and the same first strict maximum.
+    PK_HD int argmax_box(V3<T> ld) const
+    {
+        const T px = verts[18] * ld.x, py = verts[19] * ld.y, pz = verts[20] * ld.z; // vertex 6: +h
+        const T sa = px + py, sd = px - py;
+        const T a = sa + pz, b = sa - pz, c = sd + pz, e = sd - pz;
+        const T val[8] = {-a, e, b, -c, -b, c, a, -e};
+        int best = 0;
+        T bd = val[0];
+#pragma unroll
+        for (int i = 1; i < 8; ++i)
+            if (val[i] > bd)
+            {
+                bd = val[i];
+                best = i;
+            }
+        return best;
+    }
+
     PK_HD int argmax_uv(V3<T> ld) const
     {
         int best = -1;
@@ -269,7 +293,9 @@ template <class T> struct ShapeRef
         // (mesh.cpp:341-358, 442-448)
         V3<T> ld = rotate(conj(q), d);
         int best;
-        if (uv_stacks > 0)
+        if (sizeof(T) == 8 && uv_stacks == kBoxLayout)
+            best = argmax_box(ld); // FP64 form (the FP32 form's scan may contract products into FMAs)
+        else if (uv_stacks > 0)
             best = argmax_uv(ld);
         else if (ncl > 0)
             best = argmax_clustered(ld);

@@ -4,7 +4,9 @@
 //  2. the clustered support search returns the same vertex as the linear first-strict-max scan
 //     (mesh.cpp:341-358) for UV spheres and random hulls, in FP64 and FP32;
 //  3. so does the UV-sphere neighbourhood search, for every layout it accepts (uv_layout_ok),
-//     including directions at and near the poles, on ring planes and between sectors.
+//     including directions at and near the poles, on ring planes and between sectors;
+//  4. so does the box search of the FP64 form (mesh::box layout), including axis directions,
+//     exact ties, zero and negative-zero components.
 #include "../../physkit_gb300/csrc/pk_narrow.cuh"
 
 #include <algorithm>
@@ -193,6 +195,46 @@ static std::vector<double> uv_sphere(double r, int stacks, int sectors)
     return v;
 }
 
+static int check_box(std::mt19937_64 &rng)
+{
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    int bad = 0;
+    for (int b = 0; b < 300; ++b)
+    {
+        const double sc = std::pow(10.0, 4.0 * u(rng) - 2.0);
+        double h[3] = {sc * (0.1 + u(rng)), sc * (0.1 + u(rng)), sc * (0.1 + u(rng))};
+        if (b % 10 == 0) h[1] = h[0];            // square faces: exact ties
+        if (b % 25 == 0) h[2] = 0.0;             // a flat box
+        std::vector<double> v;
+        const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1}};
+        for (int i = 0; i < 8; ++i)
+            for (int k = 0; k < 3; ++k) v.push_back(double(sg[i][k]) * h[k]);
+        ShapeRef<double> s{};
+        s.kind = SHAPE_MESH;
+        s.nverts = 8;
+        s.verts = v.data();
+        s.uv_stacks = kBoxLayout;
+        for (int k = 0; k < 2000; ++k)
+        {
+            V3<double> d{nd(rng), nd(rng), nd(rng)};
+            const int mode = k % 5;
+            if (mode == 1)
+            { // axis and diagonal directions, some components exactly zero or negative zero
+                const double c[5] = {0.0, -0.0, 1.0, -1.0, 0.5};
+                d = V3<double>{c[rng() % 5], c[rng() % 5], c[rng() % 5]};
+            }
+            else if (mode == 2)
+                d.x = 0.0;
+            else if (mode == 3)
+                d = V3<double>{d.x * 1e-300, d.y, -0.0};
+            double bd;
+            if (s.argmax_linear(d, 0, 8, -1, bd) != s.argmax_box(d)) ++bad;
+        }
+    }
+    return bad;
+}
+
 int main()
 {
     std::mt19937_64 rng(12345);
@@ -228,7 +270,8 @@ int main()
                 baduv64 += check_uv<double>(v, S, K, rng, 3000);
                 baduv32 += check_uv<float>(v, S, K, rng, 3000);
             }
+    const int badbox = check_box(rng);
     std::printf("heap_mismatch=%d support_mismatch_f64=%d support_mismatch_f32=%d uv_mismatch_f64=%d uv_mismatch_f32=%d "
-                "uv_layouts=%d\n", bad_heap, bad64, bad32, baduv64, baduv32, layouts);
-    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || !uv_layout_ok(16, 32) || layouts < 60) ? 1 : 0;
+                "uv_layouts=%d box_mismatch=%d\n", bad_heap, bad64, bad32, baduv64, baduv32, layouts, badbox);
+    return (bad_heap || bad64 || bad32 || baduv64 || baduv32 || !uv_layout_ok(16, 32) || layouts < 60 || badbox) ? 1 : 0;
 }

@@ -13,6 +13,7 @@ def test_heap_order_and_clustered_support(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "heap_mismatch=0 support_mismatch_f64=0 support_mismatch_f32=0 uv_mismatch_f64=0 uv_mismatch_f32=0" in r.stdout
+    assert "box_mismatch=0" in r.stdout
 
 
 def test_event_dispatcher_rules(tmp_path):
