@@ -626,6 +626,9 @@ public:
     int set_tunables(const Tunables &t) override
     {
         tune_ = t;
+        // the small-world launch caches small_world bodies' velocities in shared memory
+        const int limit = int(kMaxSolveSmem / sizeof(Vel<T>));
+        if (tune_.small_world > limit) tune_.small_world = limit;
         split_worlds();
         PK_CUDA(upload_groups());
         return 0;

@@ -350,7 +350,9 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
         st = srv.stats()
         if i >= nreq and st["pending_requests"] == 0 and st["steps_in_flight"] == 0:
             break
-        if lanes != 2 and st["steps_in_flight"] > 0 and (st["steps_in_flight"] >= pipeline_depth or i >= nreq):
+        # one server: with its pipeline full there is nothing to launch until a step ends, so wait
+        # for it; with several lanes the others may still launch, so keep polling
+        if lanes <= 1 and st["steps_in_flight"] > 0 and (st["steps_in_flight"] >= pipeline_depth or i >= nreq):
             srv.poll(wait=True)
         elif st["steps_in_flight"] == 0 and i < nreq:
             time.sleep(max(0.0, min(1e-4, t[i] - (time.perf_counter() - t0))))
@@ -367,6 +369,9 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
            "admission_wait_p99_ms": float(np.percentile(np.array(aw) * 1e3, 99)) if aw else None,
            "pool_bodies": st["pool_bodies"], "pipeline_depth": pipeline_depth, "lanes": lanes,
            "graph_captures": st["graph_captures"],
+           "lane_p99_ms": ([float(np.percentile(np.array(x.latency) * 1e3, 99)) if x.latency else None
+                            for x in srv.lanes] if lanes > 1 else None),
+           "lane_bounds": srv.bounds if lanes > 1 else None,
            "loop": "C ABI server (pk_batch_*): admission, batching and completion in C++, one server per size "
                    "lane; Poisson arrivals and latency accounting in Python"}
     srv.close()
