@@ -242,19 +242,31 @@ def poisson_load(rate, duration, target_live=256, nmin=16, nmax=4096, life=(60, 
 class LaneServer:
     """Worlds split by size over independent servers (lanes), each with its own pool, stream and
     step cadence: a request for a small world then waits only for the small worlds' steps, which
-    the GPU runs beside the large ones. World ids are (lane << 20) | slot."""
+    the GPU runs beside the large ones. A lane may have several servers (replicas), its worlds
+    dealt to them in turn, so that a request for one large world does not wait for the step of
+    another. World ids are (server << 20) | slot."""
 
     def __init__(self, lanes, precision="f32", pipeline_depth=1, **kw):
-        # lanes: (largest world in bodies, world slots, body pool) per lane, ascending
-        self.bounds = [b for b, _, _ in lanes]
-        self.lanes = [StepServer(max_worlds=mw, max_bodies=mb, max_bodies_per_world=b + 5, precision=precision,
-                                 pipeline_depth=pipeline_depth, **kw) for b, mw, mb in lanes]
+        # lanes: (largest world in bodies, world slots, body pool[, servers]) per lane, ascending
+        self.bounds = [ln[0] for ln in lanes]
+        self.lanes, self.servers_of = [], []
+        for ln in lanes:
+            b, mw, mb = ln[:3]
+            reps = ln[3] if len(ln) > 3 else 1
+            self.servers_of.append(list(range(len(self.lanes), len(self.lanes) + reps)))
+            self.lanes += [StepServer(max_worlds=max(8, mw // reps), max_bodies=max(2 * b, mb // reps),
+                                      max_bodies_per_world=b + 5, precision=precision,
+                                      pipeline_depth=pipeline_depth, **kw) for _ in range(reps)]
+        self.next = [0] * len(lanes)
 
     def lane_of(self, n):
         for k, b in enumerate(self.bounds):
             if n <= b:
                 return k
         return len(self.bounds) - 1
+
+    def lane_latency(self, k):
+        return [x for s in self.servers_of[k] for x in self.lanes[s].latency]
 
     @property
     def live(self):
@@ -273,7 +285,10 @@ class LaneServer:
         return sum(srv.body_steps for srv in self.lanes)
 
     def open(self, req_id, nbodies, lifetime, t_arrival, records=None):
-        self.lanes[self.lane_of(nbodies)].open(req_id, nbodies, lifetime, t_arrival, records)
+        k = self.lane_of(nbodies)
+        srv = self.servers_of[k][self.next[k] % len(self.servers_of[k])]
+        self.next[k] += 1
+        self.lanes[srv].open(req_id, nbodies, lifetime, t_arrival, records)
 
     def advance(self, gid, t_arrival):
         return self.lanes[gid >> 20].advance(gid & 0xFFFFF, t_arrival)
@@ -300,12 +315,13 @@ class LaneServer:
 
 
 def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=1024, max_bodies=1_500_000,
-               nmax=4096, seed=5, pipeline_depth=1, lanes=2):
+               nmax=4096, seed=5, pipeline_depth=1, lanes=2, lane_servers=1):
     """Drive the server with a Poisson request stream in real time; returns the latency report.
     The host loop takes arrivals, admits opens, enqueues a batched step whenever a lane's pipeline
     has room and polls completions; it waits on the GPU only when it has nothing else to do. With
     lanes > 1, worlds are served by separate pools by size (2 lanes: up to 1,024 bodies and above;
-    3: 512 / 2,048 / 4,096; 4: 256 / 1,024 / 2,048 / 4,096), each with its own stream."""
+    3: 512 / 2,048 / 4,096; 4: 256 / 1,024 / 2,048 / 4,096), each with its own stream, and the
+    lanes of worlds above 1,024 bodies by `lane_servers` servers each."""
     if lanes > 1:
         # lanes by world size, finer at the top (the largest worlds set a step's length); world
         # slots follow each lane's share of worlds under the log-uniform size law, bodies its share
@@ -315,8 +331,11 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
         edges = [lo] + bounds
         wshare = [math.log(edges[k + 1] / edges[k]) / math.log(nmax / lo) for k in range(lanes)]
         bshare = [(edges[k + 1] - edges[k]) / (nmax - lo) for k in range(lanes)]
-        srv = LaneServer([(b, max(16, int(max_worlds * ws)), max(4 * b, int(max_bodies * bs)))
-                          for b, ws, bs in zip(bounds, wshare, bshare)], precision=precision,
+        # worlds above 1,024 bodies take about a millisecond per step: their lanes get servers
+        # enough that a request rarely waits for another world's step
+        reps = [1 if b <= 1024 else lane_servers for b in bounds]
+        srv = LaneServer([(b, max(16, int(max_worlds * ws)), max(4 * b, int(max_bodies * bs)), r)
+                          for b, ws, bs, r in zip(bounds, wshare, bshare, reps)], precision=precision,
                          pipeline_depth=pipeline_depth)
     else:
         srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision,
@@ -369,8 +388,9 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
            "admission_wait_p99_ms": float(np.percentile(np.array(aw) * 1e3, 99)) if aw else None,
            "pool_bodies": st["pool_bodies"], "pipeline_depth": pipeline_depth, "lanes": lanes,
            "graph_captures": st["graph_captures"],
-           "lane_p99_ms": ([float(np.percentile(np.array(x.latency) * 1e3, 99)) if x.latency else None
-                            for x in srv.lanes] if lanes > 1 else None),
+           "lane_p99_ms": ([float(np.percentile(np.array(srv.lane_latency(k)) * 1e3, 99))
+                            if srv.lane_latency(k) else None for k in range(lanes)] if lanes > 1 else None),
+           "lane_servers": lane_servers,
            "lane_bounds": srv.bounds if lanes > 1 else None,
            "loop": "C ABI server (pk_batch_*): admission, batching and completion in C++, one server per size "
                    "lane; Poisson arrivals and latency accounting in Python"}
