@@ -716,13 +716,11 @@ public:
         return 0;
     }
 
+    // Captures the step of each parity. A graph of the same shape as the one instantiated (the
+    // usual case when worlds are admitted or retired: the same launches with other grid sizes or
+    // arguments) updates the executable graph in place, which costs a fraction of instantiating.
     int capture_graph(double dt) override
     {
-        for (int k = 0; k < 2; ++k)
-        {
-            if (graph_exec_[k]) cudaGraphExecDestroy(graph_exec_[k]);
-            graph_exec_[k] = nullptr;
-        }
         for (int k = 0; k < 2; ++k)
         {
             cudaGraph_t g;
@@ -731,9 +729,32 @@ public:
             int rc = enqueue_step(T(dt), k);
             capturing_ = false;
             cudaError_t e = cudaStreamEndCapture(st_, &g);
-            if (rc) return rc;
+            if (rc)
+            {
+                if (e == cudaSuccess) cudaGraphDestroy(g);
+                return rc;
+            }
             PK_CUDA(e);
-            PK_CUDA(cudaGraphInstantiate(&graph_exec_[k], g, 0));
+            if (graph_exec_[k])
+            {
+                cudaGraphExecUpdateResultInfo info;
+                if (cudaGraphExecUpdate(graph_exec_[k], g, &info) != cudaSuccess)
+                {
+                    (void)cudaGetLastError(); // not updatable (another shape): instantiate anew
+                    cudaGraphExecDestroy(graph_exec_[k]);
+                    graph_exec_[k] = nullptr;
+                }
+            }
+            if (!graph_exec_[k])
+            {
+                cudaError_t ie = cudaGraphInstantiate(&graph_exec_[k], g, 0);
+                if (ie != cudaSuccess)
+                {
+                    cudaGraphDestroy(g);
+                    graph_exec_[k] = nullptr;
+                    PK_CUDA(ie);
+                }
+            }
             cudaGraphDestroy(g);
         }
         return 0;
