@@ -182,6 +182,8 @@ template <class T> struct Dev
     // shapes
     const T *verts;
     const float *verts32;    // FP64 form: the vertices rounded to FP32 (separation screens); else null
+    const float *shape32;    // FP64 form: per shape its local box and bounding radius in FP32 (8 floats)
+    float4 *pose32;          // FP64 form: per body its position and orientation (w, x, y, z) in FP32
     const ShapeRange *shape_range;
     const Aabb<T> *shape_box;
     const T *clusters;       // 4 per cluster: centre xyz, radius
@@ -426,6 +428,13 @@ template <class T> __global__ void k_integrate_vel(Dev<T> d, T dt)
         const bool live = (m.flags & BODY_ALIVE) && d.wp[m.world].active;
         Aabb<T> tb{};
         if (live) tb = d.tbox[i];
+        if (live && d.pose32)
+        {
+            // the FP32 copy the narrowphase's separation screens read this step
+            const Pose<T> &ps = d.pose[i];
+            d.pose32[2 * i] = make_float4(float(ps.p[0]), float(ps.p[1]), float(ps.p[2]), 0.0f);
+            d.pose32[2 * i + 1] = make_float4(float(ps.q[0]), float(ps.q[1]), float(ps.q[2]), float(ps.q[3]));
+        }
         if (live && !(m.flags & BODY_STATIC))
         {
             const Params<T> &pr = d.prm[i];
@@ -1290,12 +1299,12 @@ __device__ __forceinline__ ShapeRef<float> body_shape32(const Dev<double> &d, in
     s.cl = nullptr;
     s.ngr = 0;
     s.gr = nullptr;
-    s.rmax = float(d.shape_rmax[m.shape]);
+    s.rmax = d.shape32[8 * m.shape + 6];
     s.uv_stacks = r.uv_stacks;
     s.uv_sectors = r.uv_sectors;
-    const Pose<double> &p = d.pose[slot];
-    s.pos = V3<float>{float(p.p[0]), float(p.p[1]), float(p.p[2])};
-    s.q = Qt<float>{float(p.q[0]), float(p.q[1]), float(p.q[2]), float(p.q[3])};
+    const float4 p = d.pose32[2 * slot], q = d.pose32[2 * slot + 1];
+    s.pos = V3<float>{p.x, p.y, p.z};
+    s.q = Qt<float>{q.x, q.y, q.z, q.w};
     return s;
 }
 
@@ -1304,19 +1313,21 @@ __device__ __forceinline__ ShapeRef<float> body_shape32(const Dev<double> &d, in
 // collision.cpp:181-182), so no FP64 result is needed: the margin, 1024 FP32 epsilons of the
 // pair's scale plus the FP64 test's own terms, covers the rounding of the FP32 poses, boxes and
 // products many times over. A pair it cannot settle goes on to the separating-axis pass and GJK.
-__device__ __forceinline__ bool apart_f32(const Aabb<double> &la, const ShapeRef<double> &A, const Aabb<double> &lb,
-                                          const ShapeRef<double> &B)
+// The FP32 copies of poses (written each step by k_integrate_vel) and of shape boxes and radii
+// (written with the shapes) spare the per-pair conversions, which GB300 issues on the FP64 pipe.
+__device__ __forceinline__ bool apart_f32(const Dev<double> &d, int sa, int sb)
 {
-    const V3<float> xa{float(A.pos.x), float(A.pos.y), float(A.pos.z)};
-    const V3<float> xb{float(B.pos.x), float(B.pos.y), float(B.pos.z)};
-    const float rs = float(A.rmax) + float(B.rmax);
+    const float *fa = d.shape32 + 8 * d.meta[sa].shape, *fb = d.shape32 + 8 * d.meta[sb].shape;
+    const float4 pa = d.pose32[2 * sa], pb = d.pose32[2 * sb];
+    const V3<float> xa{pa.x, pa.y, pa.z}, xb{pb.x, pb.y, pb.z};
+    const float rs = fa[6] + fb[6];
     const float margin = (rs + norm(xa) + norm(xb)) * (1024.0f * EpsOf<float>::v) + 1e-6f + 1e-5f * rs;
     const float cull = rs + margin;
     if (sqnorm(xb - xa) > cull * cull) return true;
-    const Qt<float> qa{float(A.q.w), float(A.q.x), float(A.q.y), float(A.q.z)};
-    const Qt<float> qb{float(B.q.w), float(B.q.x), float(B.q.y), float(B.q.z)};
-    const Aabb<float> ba{{float(la.mn.x), float(la.mn.y), float(la.mn.z)}, {float(la.mx.x), float(la.mx.y), float(la.mx.z)}};
-    const Aabb<float> bb{{float(lb.mn.x), float(lb.mn.y), float(lb.mn.z)}, {float(lb.mx.x), float(lb.mx.y), float(lb.mx.z)}};
+    const float4 ra = d.pose32[2 * sa + 1], rb = d.pose32[2 * sb + 1];
+    const Qt<float> qa{ra.x, ra.y, ra.z, ra.w}, qb{rb.x, rb.y, rb.z, rb.w};
+    const Aabb<float> ba{{fa[0], fa[1], fa[2]}, {fa[3], fa[4], fa[5]}};
+    const Aabb<float> bb{{fb[0], fb[1], fb[2]}, {fb[3], fb[4], fb[5]}};
     return obb_separated(ba, qa, xa, bb, qb, xb, margin);
 }
 
@@ -1395,7 +1406,7 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         bool apart = false;
         if constexpr (sizeof(T) == 8)
-            apart = apart_f32(d.shape_box[d.meta[sa].shape], A, d.shape_box[d.meta[sb].shape], B);
+            apart = apart_f32(d, sa, sb);
         else
         {
             V3<T> dc = B.pos - A.pos;

@@ -358,7 +358,12 @@ public:
         int hb = cfg.sort_blocks_bodies > cfg.sort_blocks_pairs ? cfg.sort_blocks_bodies : cfg.sort_blocks_pairs;
         PK_CUDA(alloc(&hist_, size_t(kSortRadix) * (hb + 1))); // digit table + one row of digit totals
         PK_CUDA(alloc(&d.verts, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
-        if (sizeof(T) == 8) PK_CUDA(alloc(&d.verts32, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
+        if (sizeof(T) == 8)
+        {
+            PK_CUDA(alloc(&d.verts32, 3 * size_t(cfg.vert_cap > 0 ? cfg.vert_cap : 1)));
+            PK_CUDA(alloc(&d.shape32, 8 * size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
+            PK_CUDA(alloc(&d.pose32, 2 * size_t(N)));
+        }
         PK_CUDA(alloc(&shape_range_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
         PK_CUDA(alloc(&shape_box_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
         PK_CUDA(alloc(&shape_rmax_, size_t(cfg.shape_cap > 0 ? cfg.shape_cap : 1)));
@@ -396,11 +401,20 @@ public:
         d_.clusters = clusters_;
         PK_CUDA(cudaMemcpyAsync(const_cast<T *>(d_.verts), v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st_));
         std::vector<float> v32(verts.size());
+        std::vector<float> s32(8 * ns);
         if (d_.verts32)
         {
             for (size_t i = 0; i < verts.size(); ++i) v32[i] = float(verts[i]);
             PK_CUDA(cudaMemcpyAsync(const_cast<float *>(d_.verts32), v32.data(), sizeof(float) * v32.size(),
                                     cudaMemcpyHostToDevice, st_));
+            for (size_t i = 0; i < ns; ++i)
+            {
+                for (int k = 0; k < 6; ++k) s32[8 * i + k] = float(boxes[6 * i + k]);
+                s32[8 * i + 6] = float(T(rmax[i]));
+                s32[8 * i + 7] = 0.0f;
+            }
+            if (ns) PK_CUDA(cudaMemcpyAsync(const_cast<float *>(d_.shape32), s32.data(), sizeof(float) * s32.size(),
+                                            cudaMemcpyHostToDevice, st_));
         }
         PK_CUDA(cudaMemcpyAsync(shape_range_, ranges.data(), sizeof(int) * ranges.size(), cudaMemcpyHostToDevice, st_));
         PK_CUDA(cudaMemcpyAsync(shape_box_, b.data(), sizeof(Aabb<T>) * ns, cudaMemcpyHostToDevice, st_));
@@ -1311,7 +1325,8 @@ private:
                       d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
                       d_.epa_list, d_.epa_simplex, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.srec, d_.crec, d_.owner, d_.used, const_cast<int *>(d_.world_order), goff_dev_,
-                      const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), const_cast<float *>(d_.verts32), shape_range_, shape_box_,
+                      const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), const_cast<float *>(d_.verts32),
+                      const_cast<float *>(d_.shape32), d_.pose32, shape_range_, shape_box_,
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
             if (p) cudaFree(p);
