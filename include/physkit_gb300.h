@@ -182,6 +182,7 @@ typedef struct pk_tune_result
     int32_t group_bodies;  /* solve groups: worlds below small_world packed up to 8 per CTA while
                               their local indices sum to at most this (0: one world per CTA) */
     int32_t group_threads; /* CTA size of the solve groups (0: 128) */
+    int32_t group_warp;    /* 1: at most one world per warp of a group, each swept by its warp */
 } pk_tune_result;
 int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tune_result *out);
 /* Apply launch shapes found by pk_world_autotune (e.g. on a scratch copy of the same scene). */

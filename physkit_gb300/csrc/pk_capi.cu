@@ -1011,13 +1011,16 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
     {
         double bt = 1e300;
         pk::Tunables bc = best;
-        const int tw[][2] = {{0, 128},    {128, 32},   {256, 32},   {256, 64},
-                             {512, 128},  {1024, 128}, {1024, 256}, {2048, 256}};
+        // (local indices per group, CTA size, one member per warp)
+        const int tw[][3] = {{0, 128, 0},    {128, 32, 0},    {256, 64, 0},    {512, 128, 0},
+                             {1024, 128, 0}, {1024, 256, 0},  {2048, 256, 0},  {512, 128, 1},
+                             {1024, 256, 1}, {2048, 256, 1}};
         for (const auto &c : tw)
         {
             pk::Tunables t = best;
             t.group_bodies = c[0];
             t.group_threads = c[1];
+            t.group_warp = c[2];
             w->eng->set_tunables(t);
             if ((rc = timed_steps(w, dt, k, st))) return rc;
             used += k;
@@ -1083,6 +1086,7 @@ int pk_world_autotune(pk_world *w, double dt, int32_t steps_per_candidate, pk_tu
         out->big_threads = best.big_threads;
         out->group_bodies = best.group_bodies;
         out->group_threads = best.group_threads;
+        out->group_warp = best.group_warp;
     }
     return PK_OK;
 }
@@ -1093,7 +1097,8 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
     if (t->solve_threads < 32 || t->solve_threads > 512 || (t->solve_threads & 31) || t->small_world < 1 ||
         t->narrow_grid < 1 || t->narrow_grid > 16 || t->traverse_threads < 32 || t->traverse_threads > 1024 ||
         (t->traverse_threads & 31) || t->big_threads < 0 || t->big_threads > 512 || (t->big_threads & 31) ||
-        t->group_bodies < 0 || t->group_threads < 0 || t->group_threads > 256 || (t->group_threads & 31))
+        t->group_bodies < 0 || t->group_threads < 0 || t->group_threads > 256 || (t->group_threads & 31) ||
+        t->group_warp < 0 || t->group_warp > 1)
         return PK_ERR_INVALID;
     pk::Tunables tu;
     tu.solve_threads = t->solve_threads;
@@ -1103,6 +1108,7 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t)
     tu.big_threads = t->big_threads > 0 ? t->big_threads : t->solve_threads;
     tu.group_bodies = t->group_bodies;
     tu.group_threads = t->group_threads > 0 ? t->group_threads : 128;
+    tu.group_warp = t->group_warp;
     w->eng->set_tunables(tu);
     w->launch_version++;
     return PK_OK;

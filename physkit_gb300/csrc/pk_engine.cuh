@@ -2728,7 +2728,8 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? PK_SOLVE_MIN_BLOCKS : 1)
 // Solve groups: several small worlds per CTA (worlds world_order[goff[g]] .. [goff[g + 1] - 1] for
 // group g, at most kGroupMax, their local indices together at most cache_bodies). Each member is
 // compacted and coloured on its own, one warp per member, by the same first fit in pair order as a
-// world alone; the sweeps then run colour c of every member together. Members share no bodies, so
+// world alone; the sweeps then run colour c of every member together, or, in warp mode (at most
+// one member per warp), each member's sweeps run on its own warp with warp barriers only. Members share no bodies, so
 // each world gets its colours, its sweep order per body and its results exactly as alone, while the
 // CTA's lanes hold the manifolds of several worlds. If a member needs more than 128 colours the
 // group is solved member by member on the one-world path.
@@ -2740,7 +2741,8 @@ constexpr int kGroupColours = 128; // first fit's colours
 #endif
 template <class T>
 __global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
-    k_solve_group(Dev<T> d, const uint64_t *__restrict__ sval, const int *__restrict__ goff, int cache_bodies)
+    k_solve_group(Dev<T> d, const uint64_t *__restrict__ sval, const int *__restrict__ goff, int cache_bodies,
+                  int warp_mode)
 {
     extern __shared__ __align__(16) unsigned char solve_smem[];
     __shared__ int gw[kGroupMax], gms[kGroupMax], gna[kGroupMax], gbase[kGroupMax], gncol[kGroupMax];
@@ -2808,6 +2810,67 @@ __global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
     if (capped)
     {
         for (int g = 0; g < G; ++g) solve_world_cta<T, 256, false>(d, sval, gw[g], cache_bodies, solve_smem);
+        return;
+    }
+
+    if (warp_mode)
+    {
+        // warp mode (the host packs at most one member per warp): from here on each member is
+        // solved by its own warp, with __syncwarp between its colours and no CTA-wide barrier
+        Vel<T> *cache = reinterpret_cast<Vel<T> *>(solve_smem);
+        for (int g = warp; g < G; g += nw)
+        {
+            const int ms = gms[g], na = gna[g], ncg = gncol[g];
+            const int *colour = d.colour_tmp + ms;
+            const uint4 *rec = d.crec + ms;
+            for (int c = lane; c < ncg; c += 32)
+            {
+                ccount[g][c] = 0;
+                cursor[g][c] = 0;
+            }
+            __syncwarp();
+            for (int k = lane; k < na; k += 32) atomicAdd(&ccount[g][colour[k]], 1);
+            __syncwarp();
+            if (lane == 0)
+            {
+                int s = 0;
+                for (int c = 0; c < ncg; ++c)
+                {
+                    cstart[g][c] = s;
+                    s += ccount[g][c];
+                }
+                d.ncolours[gw[g]] = ncg;
+            }
+            __syncwarp();
+            Vel<T> *cg = cache + gbase[g];
+            for (int k = lane; k < na; k += 32)
+            {
+                const int c = colour[k];
+                const uint4 r = rec[k];
+                d.srec[ms + cstart[g][c] + atomicAdd(&cursor[g][c], 1)] = r;
+                d.pair_colour[r.x] = c; // per-pair colour for read-back
+                if (!(r.y >> 31)) cg[r.w & 0xFFFFu] = d.vel[r.y];
+                if (!(r.z >> 31)) cg[r.w >> 16] = d.vel[r.z];
+            }
+            __syncwarp();
+            for (int it = -1; it < d.iterations; ++it)
+                for (int c = 0; c < ncg; ++c)
+                {
+                    const int cs = ms + cstart[g][c], cn = ccount[g][c];
+                    for (int i = lane; i < cn; i += 32) solve_manifold_rec(d, d.srec[cs + i], cg, it < 0);
+                    __syncwarp();
+                }
+            for (int k = lane; k < na; k += 32)
+            {
+                const uint4 r = rec[k];
+                if (!(r.y >> 31)) d.vel[r.y] = cg[r.w & 0xFFFFu];
+                if (!(r.z >> 31)) d.vel[r.z] = cg[r.w >> 16];
+                const int p = int(r.x);
+                const uint8_t mask = d.rowmask[p];
+                for (int q = 0; q < 4; ++q)
+                    if (mask & (1u << q)) store_impulses(d, p, q);
+            }
+        }
         return;
     }
 

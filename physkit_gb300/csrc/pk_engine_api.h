@@ -43,6 +43,7 @@ struct Tunables
     int big_threads = 256;     // threads per solver CTA of the worlds above small_world
     int group_bodies = 0;      // solve groups: worlds packed up to 8 per CTA while their local
     int group_threads = 128;   // indices sum to at most group_bodies (0: one world per CTA)
+    int group_warp = 0;        // 1: one member per warp, each swept by its own warp
 };
 
 struct StepCounters

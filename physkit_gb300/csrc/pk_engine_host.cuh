@@ -612,7 +612,9 @@ public:
             {
                 goff_.push_back(i);
                 int sum = 0, m = 0;
-                while (i < n && m < kGroupMax)
+                const int mmax = tune_.group_warp ? (tune_.group_threads / 32 < kGroupMax ? tune_.group_threads / 32 : kGroupMax)
+                                                  : kGroupMax;
+                while (i < n && m < (mmax > 0 ? mmax : 1))
                 {
                     const int nl = nlocal_[size_t(order_[size_t(i)])];
                     if (m > 0 && sum + nl > glimit) break;
@@ -1213,7 +1215,7 @@ private:
     int joint_cap_ = 0, njoints_ = 0;
     static constexpr size_t kMaxSolveSmem = 160 * 1024;
     // the FP64 form's solver sweeps are long FP64 chains: small worlds share CTAs (solve groups)
-    Tunables tune_ = sizeof(T) == 8 ? Tunables{256, 512, 2, 128, 256, 1024, 128} : Tunables{};
+    Tunables tune_ = sizeof(T) == 8 ? Tunables{256, 512, 2, 128, 256, 1024, 128, 0} : Tunables{};
     int big_worlds_ = 0;
     std::vector<int> goff_; // solve groups: first index in the world order of each group, then the end
     int *goff_dev_ = nullptr;
@@ -1436,7 +1438,7 @@ private:
                          0, big_cache_, st_);
         if (ngroups() > 0 && joint_cap_ == 0)
             k_solve_group<T><<<ngroups(), tune_.group_threads, sizeof(Vel<T>) * size_t(group_cache_), sst>>>(
-                d, pv, goff_dev_, group_cache_);
+                d, pv, goff_dev_, group_cache_, tune_.group_warp);
         else if (cfg_.max_worlds > big_worlds_)
             launch_solve(cfg_.max_worlds - big_worlds_, tune_.solve_threads,
                          sizeof(Vel<T>) * size_t(tune_.small_world), d, pv, big_worlds_, tune_.small_world, sst);

@@ -59,7 +59,7 @@ class TuneResultC(C.Structure):
     _fields_ = [("solve_threads", C.c_int32), ("small_world", C.c_int32), ("narrow_grid", C.c_int32),
                 ("traverse_threads", C.c_int32), ("step_ms_before", C.c_double), ("step_ms_after", C.c_double),
                 ("steps_used", C.c_int32), ("big_threads", C.c_int32), ("group_bodies", C.c_int32),
-                ("group_threads", C.c_int32)]
+                ("group_threads", C.c_int32), ("group_warp", C.c_int32)]
 
 
 class RayC(C.Structure):

@@ -67,8 +67,8 @@ def test_tune_result_layout():
     from physkit_gb300 import world
 
     # solve_threads, small_world, narrow_grid, traverse_threads, 2 doubles, steps_used, big_threads,
-    # group_bodies, group_threads (the doubles start at offset 16)
-    assert C.sizeof(world.TuneResultC) == 48
+    # group_bodies, group_threads, group_warp (the doubles start at offset 16)
+    assert C.sizeof(world.TuneResultC) == 56
     assert world.TuneResultC.step_ms_before.offset == 16
 
 

@@ -101,12 +101,14 @@ def test_fp64_remove_and_add_bodies():
 # launch shapes of pk_world_set_tuning: one world per solver CTA, and solve groups (several small
 # worlds per solver CTA, their colours swept together) at two packings
 PER_WORLD = {"solve_threads": 256, "small_world": 512, "narrow_grid": 2, "traverse_threads": 128,
-             "big_threads": 256, "group_bodies": 0, "group_threads": 128}
+             "big_threads": 256, "group_bodies": 0, "group_threads": 128, "group_warp": 0}
 GROUPS = [dict(PER_WORLD, group_bodies=512, group_threads=128),
-          dict(PER_WORLD, group_bodies=256, group_threads=64)]
+          dict(PER_WORLD, group_bodies=256, group_threads=64),
+          dict(PER_WORLD, group_bodies=1024, group_threads=256, group_warp=1)]  # a warp per member
 
 
-@pytest.mark.parametrize("tuning", [PER_WORLD, GROUPS[0]], ids=["one_world_per_cta", "solve_groups"])
+@pytest.mark.parametrize("tuning", [PER_WORLD, GROUPS[0], GROUPS[2]],
+                         ids=["one_world_per_cta", "solve_groups", "solve_groups_warp"])
 def test_fp64_dense_cluster_queue_overflow_and_colour_fallback(tuning):
     # 150 boxes crammed into 0.4 m: about 11,000 overlapping pairs, more than the sweep-and-prune
     # queue holds (10,240), so the world's pairs come from its second sweep; and bodies carry ~150
@@ -198,8 +200,8 @@ def test_batched_worlds_equal_alone_and_oracle():
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_solve_groups_same_bits_as_one_world_per_cta(precision):
-    # worlds of 8-300 bodies packed up to 8 per solver CTA: every body, pair and colour equals the
-    # one-world-per-CTA launch bit for bit (members share no bodies, and each keeps its own colours
+    # worlds of 8-300 bodies packed up to 8 per solver CTA (colours swept together, or one member
+    # per warp): every body, pair and colour equals the one-world-per-CTA launch bit for bit (members share no bodies, and each keeps its own colours
     # and per-body sweep order); in FP64 three of the worlds are also checked against the oracle
     scene = scenes.config3(nworlds=40, nmin=8, nmax=300, seed=5)
     steps = 60
