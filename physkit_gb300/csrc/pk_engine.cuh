@@ -2739,10 +2739,9 @@ constexpr int kGroupColours = 128; // first fit's colours
 #ifndef PK_GROUP_MIN_BLOCKS
 #define PK_GROUP_MIN_BLOCKS 2
 #endif
-template <class T>
+template <class T, bool WARP>
 __global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
-    k_solve_group(Dev<T> d, const uint64_t *__restrict__ sval, const int *__restrict__ goff, int cache_bodies,
-                  int warp_mode)
+    k_solve_group(Dev<T> d, const uint64_t *__restrict__ sval, const int *__restrict__ goff, int cache_bodies)
 {
     extern __shared__ __align__(16) unsigned char solve_smem[];
     __shared__ int gw[kGroupMax], gms[kGroupMax], gna[kGroupMax], gbase[kGroupMax], gncol[kGroupMax];
@@ -2813,7 +2812,7 @@ __global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
         return;
     }
 
-    if (warp_mode)
+    if constexpr (WARP)
     {
         // warp mode (the host packs at most one member per warp): from here on each member is
         // solved by its own warp, with __syncwarp between its colours and no CTA-wide barrier

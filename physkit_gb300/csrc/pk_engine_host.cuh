@@ -307,7 +307,8 @@ public:
                                      int(broad_smem_bytes<kBroadClasses[2].maxn, kBroadClasses[2].qcap>())));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
-        PK_CUDA(cudaFuncSetAttribute(k_solve_group<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
+        PK_CUDA(cudaFuncSetAttribute(k_solve_group<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
+        PK_CUDA(cudaFuncSetAttribute(k_solve_group<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, 256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(kMaxSolveSmem)));
         PK_CUDA(cudaFuncSetAttribute(k_solve_world<T, solve_max_threads<T>(), false>,
@@ -1436,9 +1437,12 @@ private:
         if (big_worlds_ > 0)
             launch_solve(big_worlds_, tune_.big_threads > 0 ? tune_.big_threads : tune_.solve_threads, big_smem_, d, pv,
                          0, big_cache_, st_);
-        if (ngroups() > 0 && joint_cap_ == 0)
-            k_solve_group<T><<<ngroups(), tune_.group_threads, sizeof(Vel<T>) * size_t(group_cache_), sst>>>(
-                d, pv, goff_dev_, group_cache_, tune_.group_warp);
+        if (ngroups() > 0 && joint_cap_ == 0 && tune_.group_warp)
+            k_solve_group<T, true><<<ngroups(), tune_.group_threads, sizeof(Vel<T>) * size_t(group_cache_), sst>>>(
+                d, pv, goff_dev_, group_cache_);
+        else if (ngroups() > 0 && joint_cap_ == 0)
+            k_solve_group<T, false><<<ngroups(), tune_.group_threads, sizeof(Vel<T>) * size_t(group_cache_), sst>>>(
+                d, pv, goff_dev_, group_cache_);
         else if (cfg_.max_worlds > big_worlds_)
             launch_solve(cfg_.max_worlds - big_worlds_, tune_.solve_threads,
                          sizeof(Vel<T>) * size_t(tune_.small_world), d, pv, big_worlds_, tune_.small_world, sst);
