@@ -42,7 +42,7 @@ def _oracle_rounded_each_step(scene, steps):
 
 
 def test_fp32_resting_boxes_240_steps_within_1e4_relative_and_same_pairs():
-    # single boxes dropped flat onto the ground: the benchmark spec's bound holds outright
+    # single boxes dropped flat onto the ground: the 1e-4 bound after 240 steps holds outright
     scene = scenes.resting_stacks(height=1)
     world, _ = scenes.make_world(scene, precision="f32")
     ow = _oracle(scene)
