@@ -190,6 +190,11 @@ int pk_world_set_tuning(pk_world *w, const pk_tune_result *t);
 
 /* Per slot: pos3 quat4 vel3 ang_vel3 alive = 14 doubles (particle.h:135-149). */
 int pk_world_read_bodies(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);
+/* The same rows as of the steps enqueued so far, without waiting: they are packed on the world's
+ * stream and copied out on a copy stream while later steps run, and land in `out` by the next
+ * pk_world_synchronize (or pk_world_step). `out` must stay valid until then, and should be pinned
+ * (pk_host_register) for the copy to overlap; two calls in flight use two staging buffers in turn. */
+int pk_world_read_bodies_async(pk_world *w, double *out, int32_t cap_slots, int32_t *n_slots);
 /* Page-lock (pin) a host buffer the caller reads into or writes from every step, so that
  * pk_world_read_bodies copies straight into it; unregister before freeing it. */
 int pk_host_register(void *ptr, size_t bytes);

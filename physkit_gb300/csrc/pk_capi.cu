@@ -1124,6 +1124,20 @@ int pk_world_read_bodies(pk_world *w, double *out, int32_t cap, int32_t *n)
     return PK_OK;
 }
 
+int pk_world_read_bodies_async(pk_world *w, double *out, int32_t cap, int32_t *n)
+{
+    if (!w) return PK_ERR_INVALID;
+    if (n) *n = w->nslots;
+    if (!out || cap <= 0) return PK_OK;
+    int m = cap < w->nslots ? cap : w->nslots;
+    if (w->eng->read_bodies_async(out, m) < 0)
+    {
+        g_last_cuda = w->eng->last_error();
+        return PK_ERR_CUDA;
+    }
+    return PK_OK;
+}
+
 int pk_host_register(void *ptr, size_t bytes)
 {
     if (!ptr || bytes == 0) return PK_ERR_INVALID;

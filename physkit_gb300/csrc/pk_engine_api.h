@@ -102,6 +102,9 @@ public:
     virtual int step(double dt) = 0;                 // enqueue only
     virtual int synchronize(StepCounters *c) = 0;   // wait + read counters, clears status
     virtual int read_bodies(double *out14, int nslots) = 0;
+    // the same rows packed after the work enqueued so far and copied on a copy stream: the call
+    // returns at once and the rows land by the next synchronize (out stays valid until then)
+    virtual int read_bodies_async(double *out14, int nslots) = 0;
     virtual int write_state(int slot, const double *state13) = 0;
     virtual int read_pairs(uint64_t *keys, uint64_t *slots, int cap) = 0;
     virtual int read_manifolds(uint64_t *keys, int *counts, double *contacts13, int cap) = 0;

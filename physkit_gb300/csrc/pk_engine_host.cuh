@@ -218,6 +218,12 @@ public:
         PK_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         PK_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
         PK_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
+        PK_CUDA(cudaStreamCreateWithFlags(&cs_, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k)
+        {
+            PK_CUDA(cudaEventCreateWithFlags(&packed_[k], cudaEventDisableTiming));
+            PK_CUDA(cudaEventCreateWithFlags(&copied_[k], cudaEventDisableTiming));
+        }
         const size_t N = size_t(cfg.body_cap), P = size_t(cfg.pair_cap), W = size_t(cfg.max_worlds);
         const size_t CC = size_t(cfg.contact_cap > 0 && cfg.contact_cap < cfg.pair_cap ? cfg.contact_cap : cfg.pair_cap);
         Dev<T> &d = d_;
@@ -808,6 +814,7 @@ public:
     int synchronize(StepCounters *c) override
     {
         PK_CUDA(cudaStreamSynchronize(st_));
+        PK_CUDA(cudaStreamSynchronize(cs_)); // read-backs in flight
         PK_CUDA(cudaGetLastError());
         PK_CUDA(accumulate_stage_times());
         int h[32];
@@ -838,22 +845,54 @@ public:
 
     // The state rows are packed on the device (k_pack_bodies) and copied to the caller's buffer in
     // one transfer; a buffer pinned with pk_host_register takes the direct path.
+    cudaError_t ensure_pack(int n)
+    {
+        if (size_t(n) <= pack_cap_) return cudaSuccess;
+        // the copies in flight read the old buffers
+        cudaError_t e = cudaStreamSynchronize(cs_);
+        if (e != cudaSuccess) return e;
+        for (int k = 0; k < 2; ++k)
+        {
+            if (pack_[k]) cudaFree(pack_[k]);
+            pack_[k] = nullptr;
+        }
+        pack_cap_ = 0;
+        for (int k = 0; k < 2; ++k)
+            if ((e = cudaMalloc(&pack_[k], sizeof(double) * 14 * size_t(n))) != cudaSuccess) return e;
+        pack_cap_ = size_t(n);
+        return cudaSuccess;
+    }
+
     int read_bodies(double *out, int n) override
     {
         if (n > nslots_) n = nslots_;
         if (n <= 0) return 0;
-        if (size_t(n) > pack_cap_)
-        {
-            if (pack_) cudaFree(pack_);
-            pack_ = nullptr;
-            pack_cap_ = 0;
-            PK_CUDA(cudaMalloc(&pack_, sizeof(double) * 14 * size_t(n)));
-            pack_cap_ = size_t(n);
-        }
-        k_pack_bodies<T><<<grid(n), 256, 0, st_>>>(d_, pack_, n);
+        PK_CUDA(ensure_pack(n));
+        PK_CUDA(cudaStreamSynchronize(cs_)); // buffer 0 may still be in a read-back's copy
+        k_pack_bodies<T><<<grid(n), 256, 0, st_>>>(d_, pack_[0], n);
         PK_CUDA(cudaGetLastError());
-        PK_CUDA(cudaMemcpyAsync(out, pack_, sizeof(double) * 14 * size_t(n), cudaMemcpyDeviceToHost, st_));
+        PK_CUDA(cudaMemcpyAsync(out, pack_[0], sizeof(double) * 14 * size_t(n), cudaMemcpyDeviceToHost, st_));
         PK_CUDA(cudaStreamSynchronize(st_));
+        return n;
+    }
+
+    // Double-buffered: the rows of this call are packed into one buffer on the world's stream
+    // (after the steps enqueued so far, before the next ones) and copied out on the copy stream,
+    // while the next step runs; a buffer is packed again only after its previous copy has ended.
+    int read_bodies_async(double *out, int n) override
+    {
+        if (n > nslots_) n = nslots_;
+        if (n <= 0) return 0;
+        PK_CUDA(ensure_pack(n));
+        const int b = pack_next_;
+        pack_next_ ^= 1;
+        PK_CUDA(cudaStreamWaitEvent(st_, copied_[b], 0));
+        k_pack_bodies<T><<<grid(n), 256, 0, st_>>>(d_, pack_[b], n);
+        PK_CUDA(cudaGetLastError());
+        PK_CUDA(cudaEventRecord(packed_[b], st_));
+        PK_CUDA(cudaStreamWaitEvent(cs_, packed_[b], 0));
+        PK_CUDA(cudaMemcpyAsync(out, pack_[b], sizeof(double) * 14 * size_t(n), cudaMemcpyDeviceToHost, cs_));
+        PK_CUDA(cudaEventRecord(copied_[b], cs_));
         return n;
     }
 
@@ -1223,8 +1262,11 @@ private:
     int group_cache_ = 0; // the largest group's local indices (its velocity cache)
     int big_cache_ = 0;
     size_t big_smem_ = 0; // dynamic shared memory of the large-world launch
-    double *pack_ = nullptr; // read-back staging: 14 doubles per slot
+    double *pack_[2] = {nullptr, nullptr}; // read-back staging: 14 doubles per slot, double-buffered
     size_t pack_cap_ = 0;
+    int pack_next_ = 0;
+    cudaStream_t cs_ = nullptr; // read-back copies
+    cudaEvent_t packed_[2] = {nullptr, nullptr}, copied_[2] = {nullptr, nullptr};
     std::vector<int> order_, nlocal_;
     std::vector<int> grid_worlds_;             // worlds solved by the cooperative grid solver
     static constexpr int kGridWorld = 16384;   // local indices above which a world leaves the CTA solver
@@ -1333,9 +1375,18 @@ private:
                       shape_rmax_, clusters_, mask_dev_, grid_scratch_};
         for (void *p : ps)
             if (p) cudaFree(p);
-        if (pack_) cudaFree(pack_);
-        pack_ = nullptr;
+        if (cs_) cudaStreamSynchronize(cs_);
+        for (int k = 0; k < 2; ++k)
+        {
+            if (pack_[k]) cudaFree(pack_[k]);
+            pack_[k] = nullptr;
+            if (packed_[k]) cudaEventDestroy(packed_[k]);
+            if (copied_[k]) cudaEventDestroy(copied_[k]);
+            packed_[k] = copied_[k] = nullptr;
+        }
         pack_cap_ = 0;
+        if (cs_) cudaStreamDestroy(cs_);
+        cs_ = nullptr;
         stage_.release();
         if (tris_) cudaFree(tris_);
         if (trange_) cudaFree(trange_);

@@ -157,6 +157,7 @@ def lib():
             "pk_world_step_graph": (C.c_int, [vp]),
             "pk_world_stream": (C.c_void_p, [vp]),
             "pk_world_read_bodies": (C.c_int, [vp, dp, C.c_int32, i32p]),
+            "pk_world_read_bodies_async": (C.c_int, [vp, dp, C.c_int32, i32p]),
             "pk_host_register": (C.c_int, [vp, C.c_size_t]),
             "pk_host_unregister": (C.c_int, [vp]),
             "pk_world_write_body": (C.c_int, [vp, C.c_uint64, dp]),
@@ -526,6 +527,19 @@ class World:
         _check(self.L.pk_world_read_bodies(self.h, _ptr(out, C.c_double), n.value, C.byref(n)),
                "pk_world_read_bodies")
         return out[: n.value]
+
+    def bodies_async(self, out):
+        """Enqueue a read of the state rows into `out` (C-contiguous float64, shape (>= slots, 14),
+        pinned with pin() for the copy to overlap later steps); the rows land by the next
+        synchronize() or step(). Returns the number of rows."""
+        n = C.c_int32()
+        self.L.pk_world_read_bodies(self.h, None, 0, C.byref(n))
+        if out.dtype != np.float64 or out.ndim != 2 or out.shape[1] != 14 or not out.flags.c_contiguous \
+                or out.shape[0] < n.value:
+            raise ValueError("out must be a C-contiguous float64 array of shape (>= %d, 14)" % n.value)
+        _check(self.L.pk_world_read_bodies_async(self.h, _ptr(out, C.c_double), n.value, C.byref(n)),
+               "pk_world_read_bodies_async")
+        return n.value
 
     def pin(self, arr):
         """Page-lock a host array that is read into (or written from) every step."""

@@ -134,6 +134,31 @@ def test_fp64_dense_cluster_queue_overflow_and_colour_fallback(tuning):
     ow.close()
 
 
+def test_async_read_back_per_step_equals_synchronous_reads():
+    # pk_world_read_bodies_async after each enqueued step (two staging buffers in turn, copies on
+    # their own stream) delivers every step's rows, equal to a synchronous read after that step
+    scene = scenes.small_pile(n=60, seed=8)
+    a, _ = scenes.make_world(scene, precision="f64")
+    b, _ = scenes.make_world(scene, precision="f64")
+    want = []
+    for _ in range(6):
+        a.step(scene.dt)
+        want.append(a.bodies().copy())
+    outs = [np.full((len(scene.bodies), 14), -1.0) for _ in range(6)]
+    for o in outs:
+        b.pin(o)
+    for o in outs:
+        b.step_async(scene.dt)
+        b.bodies_async(o)
+    b.synchronize()
+    for k, (w, o) in enumerate(zip(want, outs)):
+        assert np.array_equal(w, o), f"step {k + 1}"
+    for o in outs:
+        b.unpin(o)
+    a.close()
+    b.close()
+
+
 def test_read_back_into_pinned_array_equals_fresh_read():
     # pk_world_read_bodies into a caller's page-locked buffer gives the same rows as a fresh read,
     # FP32 and FP64, with an empty slot reading as zeros
