@@ -431,7 +431,7 @@ def run_ours(a, rank, world_size, local_rank):
         from physkit_gb300.serve import run_served
 
         out["served"] = [run_served(rate=float(r), duration=a.served_seconds, warm_live=256, max_worlds=1024,
-                                    max_bodies=1_500_000, lanes=4, lane_servers=3)
+                                    max_bodies=1_500_000, lanes=4, lane_servers=6)
                          for r in a.served_rates.split(",")]
     if rank == 0 and not a.no_cpu_baseline:
         kw = {"nworlds": a.worlds, "nmin": a.nmin, "nmax": a.nmax}
