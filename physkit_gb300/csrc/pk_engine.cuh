@@ -1465,31 +1465,36 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
                 const int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
                 const ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
                 warp_add(d.np_verts, scan_verts(A, B));
+                bool overlaps = false; // A - B certainly reaches past the origin along ax
                 if constexpr (sizeof(T) == 8)
                 {
-                    // FP32 first: support values within a few FP32 ulps of the pair's scale, far
-                    // inside a margin of 1024 FP32 epsilons of it
+                    // FP32 first: support values within a few tens of FP32 ulps of the pair's
+                    // scale, far inside a margin of 1024 FP32 epsilons of it. Above +256 ulps the
+                    // FP64 value is positive too, so the FP64 test below cannot settle the pair.
                     bool oka, okb;
                     const ShapeRef<float> A32 = body_shape32(d, sa, oka), B32 = body_shape32(d, sb, okb);
                     if (oka && okb)
                     {
                         const float rs = A32.rmax + B32.rmax;
-                        const float m32 = (rs + norm(A32.pos) + norm(B32.pos)) * (1024.0f * EpsOf<float>::v) + 1e-6f +
-                                          1e-5f * rs;
+                        const float scale = rs + norm(A32.pos) + norm(B32.pos);
+                        const float m32 = scale * (1024.0f * EpsOf<float>::v) + 1e-6f + 1e-5f * rs;
                         const V3<float> ax32{float(ax.x), float(ax.y), float(ax.z)};
                         const SupPt<float> sp = minkowski(A32, B32, ax32);
-                        if (dot(sp.p, ax32) < -m32)
+                        const float v32 = dot(sp.p, ax32);
+                        if (v32 < -m32)
                         {
                             Collision<T> none;
                             manifold_update(d, p, oi, A, B, false, none, ax);
                             settled = true;
                         }
+                        else
+                            overlaps = v32 > scale * (256.0f * EpsOf<float>::v);
                     }
                 }
                 const T rs = A.rmax + B.rmax;
                 const T margin = (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6) + T(1e-5) * rs;
-                const SupPt<T> sp = settled ? SupPt<T>{} : minkowski(A, B, ax);
-                if (!settled && dot(sp.p, ax) < -margin)
+                const SupPt<T> sp = (settled || overlaps) ? SupPt<T>{} : minkowski(A, B, ax);
+                if (!settled && !overlaps && dot(sp.p, ax) < -margin)
                 {
                     Collision<T> none;
                     manifold_update(d, p, oi, A, B, false, none, ax);
