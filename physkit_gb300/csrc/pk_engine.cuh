@@ -902,7 +902,15 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
                           qb[1] <= qxy && qb[4] >= qny && qb[2] <= qxz && qb[5] >= qnz;
                     if constexpr (sizeof(T) == 8)
                     {
-                        if (hit) // the inclusive compares of the exact fat boxes decide
+                        // The FP32 boxes are rounded outward, so where every FP32 overlap exceeds
+                        // 4 FP32 ulps of its coordinates the exact boxes overlap as well; only the
+                        // near-touching hits are confirmed by the inclusive compares of the exact
+                        // fat boxes.
+                        auto clear = [](float hi, float lo) {
+                            return hi - lo > 4.0f * EpsOf<float>::v * fmaxf(fabsf(hi), fabsf(lo)) + 1e-30f;
+                        };
+                        if (hit && !(clear(qxx, qb[0]) && clear(qb[3], qnx) && clear(qxy, qb[1]) && clear(qb[4], qny) &&
+                                     clear(qxz, qb[2]) && clear(qb[5], qnz)))
                         {
                             const Aabb<T> ba = d.tbox[int(sval[lo + (leaf[r] & 0xFFF)])];
                             const Aabb<T> bb = d.tbox[int(sval[lo + (leaf[sb] & 0xFFF)])];
