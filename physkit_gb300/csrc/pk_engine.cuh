@@ -1411,12 +1411,23 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
             continue;
         }
         const int old_idx = d.old_idx[p]; // k_old_index
-        ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
         bool apart = false;
         if constexpr (sizeof(T) == 8)
+        {
             apart = apart_f32(d, sa, sb);
+            if (apart)
+            {
+                // the FP64 shapes are needed only to carry last step's contacts forward
+                const bool had = old_idx >= 0 && d.man_old[old_idx].n > 0;
+                const ShapeRef<T> A = had ? body_shape(d, sa) : ShapeRef<T>{};
+                const ShapeRef<T> B = had ? body_shape(d, sb) : ShapeRef<T>{};
+                Collision<T> none;
+                manifold_update(d, p, old_idx, A, B, false, none);
+            }
+        }
         else
         {
+            ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);
             V3<T> dc = B.pos - A.pos;
             T rs = A.rmax + B.rmax;
             T cull = rs + (rs + norm(A.pos) + norm(B.pos)) * T(1024) * EpsOf<T>::v + T(1e-6);
@@ -1424,16 +1435,20 @@ __global__ void __launch_bounds__(256, 3) k_narrow_pre(Dev<T> d, const uint64_t 
             apart = sqnorm(dc) > cull * cull ||
                     obb_separated(d.shape_box[d.meta[sa].shape], A.q, A.pos, d.shape_box[d.meta[sb].shape], B.q,
                                   B.pos, margin + T(1e-5) * rs);
+            if (apart)
+            {
+                Collision<T> none;
+                manifold_update(d, p, old_idx, A, B, false, none);
+            }
         }
-        if (apart)
+        if (!apart)
         {
-            Collision<T> none;
-            manifold_update(d, p, old_idx, A, B, false, none);
+            // pairs with a large mesh (vertex clusters) fill the list from its far end
+            if (d.shape_range[d.meta[sa].shape].ncl > 0 || d.shape_range[d.meta[sb].shape].ncl > 0)
+                d.gjk_list[d.pair_cap - 1 - warp_push(d.gjk_count_heavy)] = p;
+            else
+                d.gjk_list[warp_push(d.gjk_count)] = p;
         }
-        else if (A.ncl > 0 || B.ncl > 0)
-            d.gjk_list[d.pair_cap - 1 - warp_push(d.gjk_count_heavy)] = p;
-        else
-            d.gjk_list[warp_push(d.gjk_count)] = p;
     }
 }
 
