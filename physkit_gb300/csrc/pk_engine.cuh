@@ -56,6 +56,7 @@ enum : int
 };
 
 constexpr int kMaxColours = 512;
+constexpr int kPairClasses = 16; // GJK work classes: the support kinds of a pair's two shapes (4 x 4)
 // Worlds with at most this many local indices are coloured first-fit in pair order (one thread,
 // a 128-bit mask of used colours per body in shared memory); larger worlds by claiming rounds.
 constexpr int kFirstFitMax = 4096;
@@ -231,6 +232,7 @@ template <class T> struct Dev
     int *gjk_count;        // light items
     int *gjk_count_heavy;
     int *gjk_list2;        // the items the separating-direction check left for GJK, same two classes
+    int *gcls;             // per shape-kind class of those items: count[16], start[16], cursor[16]
     int *gjk2_count;
     int *gjk2_count_heavy;
     int *epa_list;         // contact_cap entries: light items from the start, heavy ones from the end
@@ -330,6 +332,17 @@ __device__ __forceinline__ void warp_add(unsigned long long *counter, unsigned v
     if (int(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(counter, (unsigned long long)s);
 }
 
+// Slot in a per-key list for every active lane: one atomic per key present in the warp.
+__device__ __forceinline__ int warp_push_key(int *counters, int key)
+{
+    const unsigned m = __match_any_sync(__activemask(), key);
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counters + key, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
 // Vertices the reference's support (mesh::support, mesh.cpp:341-358, a linear first-strict-max
 // scan) visits for one Minkowski support of the pair; a support costs the reference 5 FLOP per
 // vertex (a 3-term dot product and a compare).
@@ -386,6 +399,7 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.epa_count_heavy = 0;
         *d.gjk2_count = 0;
         *d.gjk2_count_heavy = 0;
+        for (int c = 0; c < kPairClasses; ++c) d.gcls[c] = 0;
         *d.ccount = 0;
         *d.epa_total = 0;
         *d.all_small = 1;
@@ -1321,6 +1335,21 @@ __device__ __forceinline__ ShapeRef<float> body_shape32(const Dev<double> &d, in
 // collision.cpp:181-182), so no FP64 result is needed: the margin, 1024 FP32 epsilons of the
 // pair's scale plus the FP64 test's own terms, covers the rounding of the FP32 poses, boxes and
 // products many times over. A pair it cannot settle goes on to the separating-axis pass and GJK.
+// Support kind of a shape, as ShapeRef::support dispatches: 0 the box search (FP64 form), 1 a
+// linear scan, 2 the UV-sphere neighbourhood, 3 vertex clusters.
+template <class T> __device__ __forceinline__ int support_kind(const Dev<T> &d, int slot)
+{
+    const ShapeRange r = d.shape_range[d.meta[slot].shape];
+    if (sizeof(T) == 8 && r.uv_stacks == kBoxLayout) return 0;
+    if (r.uv_stacks > 0) return 2;
+    return r.ncl > 0 ? 3 : 1;
+}
+// A pair's GJK work class: warps given one class run one support path per shape. Classes with a
+// UV sphere or a clustered mesh (the costly supports) come first in the class order.
+template <class T> __device__ __forceinline__ int pair_class(const Dev<T> &d, int sa, int sb)
+{ return 4 * support_kind(d, sa) + support_kind(d, sb); }
+__device__ __forceinline__ int class_rank(int c) { return ((c >> 2) >= 2 || (c & 3) >= 2) ? c : kPairClasses + c; }
+
 // The FP32 copies of poses (written each step by k_integrate_vel) and of shape boxes and radii
 // (written with the shapes) spare the per-pair conversions, which GB300 issues on the FP64 pipe.
 __device__ __forceinline__ bool apart_f32(const Dev<double> &d, int sa, int sb)
@@ -1536,7 +1565,48 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
                 d.gjk_list2[d.pair_cap - 1 - warp_push(d.gjk2_count_heavy)] = p;
             else
                 d.gjk_list2[warp_push(d.gjk2_count)] = p;
+            const uint64_t val = sval[p];
+            warp_push_key(d.gcls, pair_class(d, int(val >> 32), int(val & 0xFFFFFFFFu)));
         }
+    }
+}
+
+// GJK's list laid out by work class: class starts (one warp), then every item moved to its class's
+// range of the separating-direction pass's first list (free by then). Order within a class does
+// not matter: each pair's GJK is computed on its own.
+template <class T> __global__ void k_gjk_class_start(Dev<T> d)
+{
+    if (threadIdx.x != 0) return;
+    int *gcls = d.gcls;
+    int order[kPairClasses];
+    for (int c = 0; c < kPairClasses; ++c) order[c] = c;
+    for (int a = 1; a < kPairClasses; ++a) // by rank: the few classes, an insertion sort
+        for (int b = a; b > 0 && class_rank(order[b]) < class_rank(order[b - 1]); --b)
+        {
+            const int t = order[b];
+            order[b] = order[b - 1];
+            order[b - 1] = t;
+        }
+    int run = 0;
+    for (int k = 0; k < kPairClasses; ++k)
+    {
+        const int c = order[k];
+        gcls[kPairClasses + c] = run;
+        gcls[2 * kPairClasses + c] = 0;
+        run += gcls[c];
+    }
+}
+
+template <class T> __global__ void k_gjk_class_scatter(Dev<T> d, const uint64_t *__restrict__ sval)
+{
+    const int nh = *d.gjk2_count_heavy;
+    const int n = nh + *d.gjk2_count;
+    PK_GRID_STRIDE(i, n)
+    {
+        const int p = d.gjk_list2[list_slot(i, nh, d.pair_cap)];
+        const uint64_t val = sval[p];
+        const int c = pair_class(d, int(val >> 32), int(val & 0xFFFFFFFFu));
+        d.gjk_list[d.gcls[kPairClasses + c] + warp_push_key(d.gcls + 2 * kPairClasses, c)] = p;
     }
 }
 
@@ -1545,11 +1615,10 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
 template <class T>
 __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    const int nh = *d.gjk2_count_heavy;
-    const int n = nh + *d.gjk2_count;
+    const int n = *d.gjk2_count_heavy + *d.gjk2_count;
     PK_GRID_STRIDE(i, n)
     {
-        int p = d.gjk_list2[list_slot(i, nh, d.pair_cap)];
+        int p = d.gjk_list[i]; // in class order (k_gjk_class_scatter)
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);
         ShapeRef<T> A = body_shape(d, sa), B = body_shape(d, sb);

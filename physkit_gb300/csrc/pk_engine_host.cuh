@@ -346,6 +346,8 @@ public:
         PK_CUDA(alloc(&d.gjk_list, P));
         PK_CUDA(alloc(&d.clist, P));
         PK_CUDA(alloc(&d.gjk_list2, P));
+        PK_CUDA(alloc(&d.gcls, 3 * kPairClasses));
+        PK_CUDA(cudaMemset(d.gcls, 0, sizeof(int) * 3 * kPairClasses));
         PK_CUDA(alloc(&d.epa_list, CC));
         PK_CUDA(alloc(&d.epa_simplex, CC));
         PK_CUDA(alloc(&d.rowidx, P));
@@ -1367,7 +1369,7 @@ private:
                       d_.wroot, d_.wleaf_lo, d_.wleaf_hi, d_.wlive, d_.mstart, d_.mend, d_.mstart_old, d_.mend_old, d_.nstart, d_.nend, d_.jstart, d_.jend,
                       const_cast<JointDev<T> *>(d_.joints), d_.jrows, d_.jnrows, d_.jacc, d_.ncolours, mkey_[0], mkey_[1], mval_[0], mval_[1],
                       pkey_[0], pkey_[1], pval_[0], pval_[1], man_[0], man_[1], d_.nodes, d_.parent,
-                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2,
+                      d_.leaf_parent, d_.refit_flag, d_.key_old, d_.val_old, d_.event, d_.old_idx, d_.gjk_list, d_.clist, d_.gjk_list2, d_.gcls,
                       d_.epa_list, d_.epa_simplex, d_.rowidx, d_.rows, d_.racc, d_.raccf, d_.rdel, d_.rowmask, d_.colour, d_.colour_tmp, d_.pair_colour,
                       d_.order, d_.srec, d_.crec, d_.owner, d_.used, const_cast<int *>(d_.world_order), goff_dev_,
                       const_cast<int *>(d_.world_nlocal), hist_, const_cast<T *>(d_.verts), const_cast<float *>(d_.verts32),
@@ -1415,7 +1417,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 24 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 26 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1459,6 +1461,8 @@ private:
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         PK_CUDA(mark(kStages + 1));
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
+        k_gjk_class_start<T><<<1, 32, 0, st_>>>(d);
+        k_gjk_class_scatter<T><<<gp, 256, 0, st_>>>(d, pv);
         PK_CUDA(mark(kStages + 2));
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(kStages + 3));
