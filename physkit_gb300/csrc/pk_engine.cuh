@@ -232,7 +232,7 @@ template <class T> struct Dev
     int *gjk_count;        // light items
     int *gjk_count_heavy;
     int *gjk_list2;        // the items the separating-direction check left for GJK, same two classes
-    int *gcls;             // per pair class: GJK count[16], start[16], cursor[16], then the same for EPA
+    int *gcls;             // per shape-kind class of those items: count[16], start[16], cursor[16]
     int *gjk2_count;
     int *gjk2_count_heavy;
     int *epa_list;         // contact_cap entries: light items from the start, heavy ones from the end
@@ -399,7 +399,7 @@ template <class T> __global__ void k_begin_step(Dev<T> d)
         *d.epa_count_heavy = 0;
         *d.gjk2_count = 0;
         *d.gjk2_count_heavy = 0;
-        for (int c = 0; c < kPairClasses; ++c) d.gcls[c] = d.gcls[3 * kPairClasses + c] = 0;
+        for (int c = 0; c < kPairClasses; ++c) d.gcls[c] = 0;
         *d.ccount = 0;
         *d.epa_total = 0;
         *d.all_small = 1;
@@ -1571,14 +1571,13 @@ __global__ void __launch_bounds__(128) k_narrow_axis(Dev<T> d, const uint64_t *_
     }
 }
 
-// GJK's and EPA's lists laid out by work class: class starts (one thread; block 0 GJK, 1 EPA),
-// then every item moved to its class's range of a free list (the separating-direction pass's first
-// list for GJK, GJK's list for EPA). Order within a class does not matter: each pair's GJK or EPA
-// is computed on its own.
-template <class T> __global__ void k_class_start(Dev<T> d, int block)
+// GJK's list laid out by work class: class starts (one warp), then every item moved to its class's
+// range of the separating-direction pass's first list (free by then). Order within a class does
+// not matter: each pair's GJK is computed on its own.
+template <class T> __global__ void k_gjk_class_start(Dev<T> d)
 {
     if (threadIdx.x != 0) return;
-    int *gcls = d.gcls + 3 * kPairClasses * block;
+    int *gcls = d.gcls;
     int order[kPairClasses];
     for (int c = 0; c < kPairClasses; ++c) order[c] = c;
     for (int a = 1; a < kPairClasses; ++a) // by rank: the few classes, an insertion sort
@@ -1608,20 +1607,6 @@ template <class T> __global__ void k_gjk_class_scatter(Dev<T> d, const uint64_t 
         const uint64_t val = sval[p];
         const int c = pair_class(d, int(val >> 32), int(val & 0xFFFFFFFFu));
         d.gjk_list[d.gcls[kPairClasses + c] + warp_push_key(d.gcls + 2 * kPairClasses, c)] = p;
-    }
-}
-
-template <class T> __global__ void k_epa_class_scatter(Dev<T> d, const uint64_t *__restrict__ sval)
-{
-    const int nh = *d.epa_count_heavy;
-    const int n = nh + *d.epa_count;
-    const int *cls = d.gcls + 3 * kPairClasses;
-    PK_GRID_STRIDE(i, n)
-    {
-        const int j = list_slot(i, nh, d.contact_cap);
-        const uint64_t val = sval[d.epa_list[j]];
-        const int c = pair_class(d, int(val >> 32), int(val & 0xFFFFFFFFu));
-        d.gjk_list2[cls[kPairClasses + c] + warp_push_key(d.gcls + 5 * kPairClasses, c)] = j;
     }
 }
 
@@ -1660,7 +1645,6 @@ __global__ void __launch_bounds__(128, PK_GJK_MIN_BLOCKS) k_narrow_gjk(Dev<T> d,
                 j = warp_push(d.epa_count);
             d.epa_list[j] = p;
             d.epa_simplex[j] = s;
-            warp_push_key(d.gcls + 3 * kPairClasses, pair_class(d, sa, sb));
         }
         else
         {
@@ -1675,10 +1659,11 @@ template <class T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? PK_EPA_MIN_BLOCKS_F32 : PK_EPA_MIN_BLOCKS)
     k_narrow_epa(Dev<T> d, const uint64_t *__restrict__ sval)
 {
-    const int n = *d.epa_count_heavy + *d.epa_count;
+    const int nh = *d.epa_count_heavy;
+    const int n = nh + *d.epa_count;
     PK_GRID_STRIDE(i, n)
     {
-        const int j = d.gjk_list2[i]; // EPA list slots in class order (k_epa_class_scatter)
+        int j = list_slot(i, nh, d.contact_cap);
         int p = d.epa_list[j];
         uint64_t val = sval[p];
         int sa = int(val >> 32), sb = int(val & 0xFFFFFFFFu);

@@ -346,8 +346,8 @@ public:
         PK_CUDA(alloc(&d.gjk_list, P));
         PK_CUDA(alloc(&d.clist, P));
         PK_CUDA(alloc(&d.gjk_list2, P));
-        PK_CUDA(alloc(&d.gcls, 6 * kPairClasses));
-        PK_CUDA(cudaMemset(d.gcls, 0, sizeof(int) * 6 * kPairClasses));
+        PK_CUDA(alloc(&d.gcls, 3 * kPairClasses));
+        PK_CUDA(cudaMemset(d.gcls, 0, sizeof(int) * 3 * kPairClasses));
         PK_CUDA(alloc(&d.epa_list, CC));
         PK_CUDA(alloc(&d.epa_simplex, CC));
         PK_CUDA(alloc(&d.rowidx, P));
@@ -1417,7 +1417,7 @@ private:
         const int gb = grid(N);
         const int gp = grid(cfg_.pair_cap);
         const int mpasses = (cfg_.wbits + 31 + 7) / 8, ppasses = (cfg_.wbits + 2 * cfg_.lbits + 7) / 8;
-        launches_ = 28 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
+        launches_ = 26 + int(grid_worlds_.size()) + (big_worlds_ > 0) + (cfg_.max_worlds > big_worlds_) + 3 * mpasses + 3 * ppasses;
         PK_CUDA(mark(0));
         k_begin_step<T><<<grid(cfg_.max_worlds), 256, 0, st_>>>(d);
         k_integrate_vel<T><<<gb, 256, 0, st_>>>(d, dt);
@@ -1461,13 +1461,11 @@ private:
         k_narrow_pre<T><<<gp, 256, 0, st_>>>(d, pk, pv);
         PK_CUDA(mark(kStages + 1));
         k_narrow_axis<T><<<grid(cfg_.pair_cap) * 2, 128, 0, st_>>>(d, pv);
-        k_class_start<T><<<1, 32, 0, st_>>>(d, 0);
+        k_gjk_class_start<T><<<1, 32, 0, st_>>>(d);
         k_gjk_class_scatter<T><<<gp, 256, 0, st_>>>(d, pv);
         PK_CUDA(mark(kStages + 2));
         k_narrow_gjk<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(kStages + 3));
-        k_class_start<T><<<1, 32, 0, st_>>>(d, 1);
-        k_epa_class_scatter<T><<<gp, 256, 0, st_>>>(d, pv);
         k_narrow_epa<T><<<grid(cfg_.pair_cap) * tune_.narrow_grid, 128, 0, st_>>>(d, pv);
         PK_CUDA(mark(6));
         k_contact_setup<T><<<gp, 256, 0, st_>>>(d, pk, pv, dt);
