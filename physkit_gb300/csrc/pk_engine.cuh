@@ -2465,6 +2465,12 @@ template <class T> __device__ __forceinline__ bool colour_rounds_commit(const De
 #ifndef PK_SOLVE_MIN_BLOCKS
 #define PK_SOLVE_MIN_BLOCKS 2
 #endif
+// Solve records are laid out in two passes within each colour: first the manifolds with rows in
+// contact slots 2-3, then the others, so that the lanes of a warp mostly run the same contact
+// slots. Order within a colour does not change results: its manifolds share no dynamic body.
+template <class T> __device__ __forceinline__ bool wide_manifold(const Dev<T> &d, const uint4 &r)
+{ return (d.rowmask[r.x] >> 2) != 0; }
+
 // First fit in pair order for one world (one thread): each manifold takes the lowest colour that
 // none of the earlier manifolds on its dynamic bodies has, from a 128-bit used-colour mask per
 // local index (`used`, 2 words per local index, zeroed by the caller). Returns the number of
@@ -2740,14 +2746,18 @@ __device__ __forceinline__ void solve_world_cta(const Dev<T> &d, const uint64_t 
         d.ncolours[w] = ncol;
     }
     __syncthreads();
-    for (int k = tid; k < na; k += nt)
+    for (int pass = 0; pass < 2; ++pass)
     {
-        int c = colour[k];
-        const uint4 r = rec[k];
-        if (c >= 0 && c < kMaxColours) d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = r;
-        d.pair_colour[r.x] = c; // per-pair colour for read-back (-2: no contact rows)
+        for (int k = tid; k < na; k += nt)
+        {
+            const uint4 r = rec[k];
+            if (wide_manifold(d, r) != (pass == 0)) continue;
+            int c = colour[k];
+            if (c >= 0 && c < kMaxColours) d.srec[ms + cstart[c] + atomicAdd(&cursor[c], 1)] = r;
+            d.pair_colour[r.x] = c; // per-pair colour for read-back (-2: no contact rows)
+        }
+        __syncthreads();
     }
-    __syncthreads();
     if (cache)
     {
         // the owner table is done; the shared memory now caches body velocities
@@ -2945,16 +2955,20 @@ __global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
             }
             __syncwarp();
             Vel<T> *cg = cache + gbase[g];
-            for (int k = lane; k < na; k += 32)
+            for (int pass = 0; pass < 2; ++pass)
             {
-                const int c = colour[k];
-                const uint4 r = rec[k];
-                d.srec[ms + cstart[g][c] + atomicAdd(&cursor[g][c], 1)] = r;
-                d.pair_colour[r.x] = c; // per-pair colour for read-back
-                if (!(r.y >> 31)) cg[r.w & 0xFFFFu] = d.vel[r.y];
-                if (!(r.z >> 31)) cg[r.w >> 16] = d.vel[r.z];
+                for (int k = lane; k < na; k += 32)
+                {
+                    const uint4 r = rec[k];
+                    if (wide_manifold(d, r) != (pass == 0)) continue;
+                    const int c = colour[k];
+                    d.srec[ms + cstart[g][c] + atomicAdd(&cursor[g][c], 1)] = r;
+                    d.pair_colour[r.x] = c; // per-pair colour for read-back
+                    if (!(r.y >> 31)) cg[r.w & 0xFFFFu] = d.vel[r.y];
+                    if (!(r.z >> 31)) cg[r.w >> 16] = d.vel[r.z];
+                }
+                __syncwarp();
             }
-            __syncwarp();
             for (int it = -1; it < d.iterations; ++it)
                 for (int c = 0; c < ncg; ++c)
                 {
@@ -3017,18 +3031,23 @@ __global__ void __launch_bounds__(256, PK_GROUP_MIN_BLOCKS)
         }
         cpre[c][G] = s;
     }
-    for (int g = 0; g < G; ++g)
+    for (int pass = 0; pass < 2; ++pass)
     {
-        const int ms = gms[g];
-        const int *colour = d.colour_tmp + ms;
-        const uint4 *rec = d.crec + ms;
-        for (int k = tid; k < gna[g]; k += nt)
+        for (int g = 0; g < G; ++g)
         {
-            const int c = colour[k];
-            const uint4 r = rec[k];
-            d.srec[ms + cstart[g][c] + atomicAdd(&cursor[g][c], 1)] = r;
-            d.pair_colour[r.x] = c; // per-pair colour for read-back
+            const int ms = gms[g];
+            const int *colour = d.colour_tmp + ms;
+            const uint4 *rec = d.crec + ms;
+            for (int k = tid; k < gna[g]; k += nt)
+            {
+                const uint4 r = rec[k];
+                if (wide_manifold(d, r) != (pass == 0)) continue;
+                const int c = colour[k];
+                d.srec[ms + cstart[g][c] + atomicAdd(&cursor[g][c], 1)] = r;
+                d.pair_colour[r.x] = c; // per-pair colour for read-back
+            }
         }
+        __syncthreads();
     }
     // the colour masks are done; the shared memory now caches the members' body velocities
     Vel<T> *cache = reinterpret_cast<Vel<T> *>(solve_smem);
