@@ -314,6 +314,21 @@ class LaneServer:
             srv.close()
 
 
+def lane_layout(lanes, max_worlds, max_bodies, nmax=4096, lane_servers=1, nmin=16):
+    """(largest world in bodies, world slots, body pool, servers) per size lane, ascending. Lanes
+    are finer at the top (the largest worlds set a step's length); world slots follow each lane's
+    share of worlds under the log-uniform size law, bodies its share of bodies; lanes of worlds
+    above 1,024 bodies, whose steps take about a millisecond, get `lane_servers` servers so that a
+    request rarely waits for another large world's step."""
+    bounds = {2: [1024, nmax], 3: [512, 2048, nmax], 4: [256, 1024, 2048, nmax]}[lanes]
+    edges = [nmin] + bounds
+    wshare = [math.log(edges[k + 1] / edges[k]) / math.log(nmax / nmin) for k in range(lanes)]
+    bshare = [(edges[k + 1] - edges[k]) / (nmax - nmin) for k in range(lanes)]
+    reps = [1 if b <= 1024 else lane_servers for b in bounds]
+    return [(b, max(16, int(max_worlds * ws)), max(4 * b, int(max_bodies * bs)), r)
+            for b, ws, bs, r in zip(bounds, wshare, bshare, reps)]
+
+
 def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=1024, max_bodies=1_500_000,
                nmax=4096, seed=5, pipeline_depth=1, lanes=2, lane_servers=1):
     """Drive the server with a Poisson request stream in real time; returns the latency report.
@@ -323,19 +338,7 @@ def run_served(rate, duration=4.0, warm_live=128, precision="f32", max_worlds=10
     3: 512 / 2,048 / 4,096; 4: 256 / 1,024 / 2,048 / 4,096), each with its own stream, and the
     lanes of worlds above 1,024 bodies by `lane_servers` servers each."""
     if lanes > 1:
-        # lanes by world size, finer at the top (the largest worlds set a step's length); world
-        # slots follow each lane's share of worlds under the log-uniform size law, bodies its share
-        # of bodies
-        lo = 16
-        bounds = {2: [1024, nmax], 3: [512, 2048, nmax], 4: [256, 1024, 2048, nmax]}[lanes]
-        edges = [lo] + bounds
-        wshare = [math.log(edges[k + 1] / edges[k]) / math.log(nmax / lo) for k in range(lanes)]
-        bshare = [(edges[k + 1] - edges[k]) / (nmax - lo) for k in range(lanes)]
-        # worlds above 1,024 bodies take about a millisecond per step: their lanes get servers
-        # enough that a request rarely waits for another world's step
-        reps = [1 if b <= 1024 else lane_servers for b in bounds]
-        srv = LaneServer([(b, max(16, int(max_worlds * ws)), max(4 * b, int(max_bodies * bs)), r)
-                          for b, ws, bs, r in zip(bounds, wshare, bshare, reps)], precision=precision,
+        srv = LaneServer(lane_layout(lanes, max_worlds, max_bodies, nmax, lane_servers), precision=precision,
                          pipeline_depth=pipeline_depth)
     else:
         srv = StepServer(max_worlds=max_worlds, max_bodies=max_bodies, precision=precision,
