@@ -26,6 +26,7 @@
 #include "pk_narrow.cuh"
 #include "pk_sort.cuh"
 
+#include <climits>
 #include <cooperative_groups.h>
 #include <cstdint>
 #include <cstring>
@@ -776,13 +777,16 @@ __device__ __forceinline__ void broad_emit(const Dev<T> &d, int w, int lo, const
 // Broadphase of a world with at most kBroadMax leaves, one CTA per world, by sweep and prune in
 // shared memory:
 //  1. sort the leaves by the lower bound of their box along the axis on which the world's box
-//     centres spread most (bitonic sort of (bound, leaf) keys);
+//     centres spread most (bitonic sort of (bound, leaf) keys, the stages of strides below a
+//     warp's chunk on registers);
 //  2. copy the leaves' boxes into shared memory in that order;
-//  3. one warp per sorted leaf a tests the leaves after it until their lower bound passes a's upper
-//     bound, so every pair overlapping on the axis is met once, from its earlier leaf, and queues
-//     the overlapping pairs in shared memory;
-//  4. the CTA drops queued pairs the reference does not pair yet (pair_allowed), reserves its range
-//     of the pair list with one atomic and writes the pairs there.
+//  3. each sorted leaf a tests the leaves after it up to the first whose lower bound passes a's
+//     upper bound (found by binary search), so every pair overlapping on the axis is met once,
+//     from its earlier leaf: a lane per leaf, four candidates a turn, and the whole warp for the
+//     rest of long windows; the overlapping pairs are queued in shared memory;
+//  4. the CTA drops queued pairs the reference does not pair yet (pair_allowed; only checked in a
+//     world where some dynamic body was not reinserted since the newest creation), reserves its
+//     range of the pair list with one atomic and writes the pairs there.
 // A world's static leaves sort after its dynamic ones in the leaf list, so "leaf >= first static"
 // marks them and static-static pairs are skipped. The pair test is the traversal's (closed
 // intervals on the exact fat boxes), so the pair set is the same; sweep bounds are rounded outward
@@ -791,6 +795,9 @@ __device__ __forceinline__ void broad_emit(const Dev<T> &d, int w, int lo, const
 constexpr int kBroadPow2 = 4096;  // sort capacity, a power of two >= kBroadMax, indices in 12 bits
 constexpr int kBroadQueue = 10240; // queued pairs per world (two 12-bit sorted positions each)
 static_assert(kBroadPow2 >= kBroadMax && kBroadPow2 <= 4096, "sort capacity");
+constexpr int kBroadChunk = 64;               // queue entries a warp reserves at a time
+constexpr int kBroadLaneSpan = 64;            // window positions a lane tests before its warp helps
+constexpr uint32_t kBroadHole = 0xFFFFFFFFu;  // an unused queue entry (bit 31: skipped)
 static_assert(kBroadQueue * 4 >= kBroadPow2 * 8, "the sort keys live in the queue's space");
 
 // Shared memory of a sweep-and-prune CTA: the queue, then per leaf its box in FP32 (rounded outward
@@ -800,6 +807,44 @@ static_assert(kBroadQueue * 4 >= kBroadPow2 * 8, "the sort keys live in the queu
 // (MINN, MAXN] leaves, QCAP queued pairs (a fuller queue moves the world to the second sweep).
 template <int MAXN, int QCAP> constexpr size_t broad_smem_bytes()
 { return size_t(QCAP) * 4 + (6 * sizeof(float) + 4 + 2) * size_t(MAXN); }
+// Bitonic stages of one sequence size on a warp's chunk of 32 * E keys held in registers (key
+// cb + 32 k + lane in v[k]): strides below 32 exchange through shuffles, larger ones swap within
+// the thread. Strides from min(size, 32 E) / 2 down to 1; the stride loop is unrolled, so every
+// register index is a constant.
+template <int E> __device__ __forceinline__ void bitonic_warp_stages(uint64_t (&v)[E], int cb, int lane, int size)
+{
+#pragma unroll
+    for (int s = 16 * E; s > 0; s >>= 1)
+    {
+        if (s >= size) continue;
+        if (s >= 32)
+        {
+            const int sk = s >> 5;
+#pragma unroll
+            for (int k = 0; k < E; ++k)
+            {
+                if (k & sk) continue;
+                const bool asc = ((cb + 32 * k + lane) & size) == 0;
+                const uint64_t a = v[k], b = v[k + sk];
+                const bool sw = (a > b) == asc;
+                v[k] = sw ? b : a;
+                v[k + sk] = sw ? a : b;
+            }
+        }
+        else
+        {
+            const bool lower = (lane & s) == 0;
+#pragma unroll
+            for (int k = 0; k < E; ++k)
+            {
+                const uint64_t o = __shfl_xor_sync(0xFFFFFFFFu, v[k], s);
+                const bool take_min = lower == (((cb + 32 * k + lane) & size) == 0);
+                v[k] = take_min ? (o < v[k] ? o : v[k]) : (o > v[k] ? o : v[k]);
+            }
+        }
+    }
+}
+
 struct BroadClass
 {
     int minn, maxn, qcap, threads;
@@ -811,14 +856,18 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
                                                          const uint64_t *__restrict__ sval)
 {
     static_assert(QCAP * 4 >= 8 * MAXN * 2 && MAXN <= 4096, "the sort keys live in the queue's space");
+    // sort: E keys per thread, so that the CTA's warps hold the largest sequence in registers
+    constexpr int MAXP = MAXN <= 256 ? 256 : (MAXN <= 512 ? 512 : (MAXN <= 1024 ? 1024 : (MAXN <= 2048 ? 2048 : 4096)));
+    constexpr int E = MAXP / THREADS, SE = 32 * E;
+    static_assert(E >= 1 && E * THREADS == MAXP && QCAP * 4 >= 8 * MAXP, "sort layout");
     extern __shared__ __align__(16) unsigned char broad_smem[];
-    __shared__ int ndyn, fill, cta_base;
+    __shared__ int ndyn, fill, cta_base, newest_created, oldest_reinserted;
     __shared__ int warp_count[16];
     const int w = blockIdx.x;
     const int lo = d.wleaf_lo[w];
     const int n = d.wleaf_hi[w] - lo;
     if (n < 2 || n <= MINN || n > MAXN) return;
-    int P = 2;
+    int P = SE; // sorted length: a power of two, at least one warp's chunk (keys past n are ~0)
     while (P < n) P <<= 1;
     uint32_t *queue = reinterpret_cast<uint32_t *>(broad_smem); // QCAP entries
     uint64_t *srt = reinterpret_cast<uint64_t *>(broad_smem);   // sort keys, before the sweep
@@ -844,8 +893,11 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
     {
         ndyn = n;
         fill = 0;
+        newest_created = INT_MIN;
+        oldest_reinserted = INT_MAX;
     }
     __syncthreads();
+    int my_created = INT_MIN, my_reinserted = INT_MAX;
     for (int j = tid; j < P; j += bs)
     {
         if (j >= n)
@@ -853,28 +905,67 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
             srt[j] = ~0ull;
             continue;
         }
-        const Aabb<T> b = d.tbox[int(sval[lo + j])];
+        const int i = int(sval[lo + j]);
+        const Aabb<T> b = d.tbox[i];
         const T lower = ax == 0 ? b.mn.x : (ax == 1 ? b.mn.y : b.mn.z);
         srt[j] = (uint64_t(f2ord(down_f(lower))) << 32) | uint32_t(j);
-        if ((skey[lo + j] >> 30) & 1u) atomicMin(&ndyn, j);
+        my_created = max(my_created, int(d.meta[i].created));
+        if ((skey[lo + j] >> 30) & 1u)
+            atomicMin(&ndyn, j);
+        else
+            my_reinserted = min(my_reinserted, int(d.meta[i].reinserted));
+    }
+    my_created = __reduce_max_sync(0xFFFFFFFFu, my_created);
+    my_reinserted = __reduce_min_sync(0xFFFFFFFFu, my_reinserted);
+    if (lane == 0)
+    {
+        atomicMax(&newest_created, my_created);
+        atomicMin(&oldest_reinserted, my_reinserted);
     }
     __syncthreads();
-    for (int size = 2; size <= P; size <<= 1)
-        for (int stride = size >> 1; stride > 0; stride >>= 1)
+    {
+        // bitonic sort: stages with strides below SE on the registers of the warp holding the
+        // chunk, larger strides through shared memory
+        const int cb = warp * SE;
+        const bool holds = cb < P;
+        uint64_t v[E];
+        if (holds)
         {
-            for (int t = tid; t < (P >> 1); t += bs)
+#pragma unroll
+            for (int k = 0; k < E; ++k) v[k] = srt[cb + 32 * k + lane];
+            for (int size = 2; size <= SE; size <<= 1) bitonic_warp_stages<E>(v, cb, lane, size);
+#pragma unroll
+            for (int k = 0; k < E; ++k) srt[cb + 32 * k + lane] = v[k];
+        }
+        __syncthreads();
+        for (int size = 2 * SE; size <= P; size <<= 1)
+        {
+            for (int stride = size >> 1; stride >= SE; stride >>= 1)
             {
-                const int i = 2 * t - (t & (stride - 1));
-                const int j = i + stride;
-                const uint64_t x = srt[i], y = srt[j];
-                if ((x > y) == ((i & size) == 0))
+                for (int t = tid; t < (P >> 1); t += bs)
                 {
-                    srt[i] = y;
-                    srt[j] = x;
+                    const int i = 2 * t - (t & (stride - 1));
+                    const int j = i + stride;
+                    const uint64_t x = srt[i], y = srt[j];
+                    if ((x > y) == ((i & size) == 0))
+                    {
+                        srt[i] = y;
+                        srt[j] = x;
+                    }
                 }
+                __syncthreads();
+            }
+            if (holds)
+            {
+#pragma unroll
+                for (int k = 0; k < E; ++k) v[k] = srt[cb + 32 * k + lane];
+                bitonic_warp_stages<E>(v, cb, lane, size);
+#pragma unroll
+                for (int k = 0; k < E; ++k) srt[cb + 32 * k + lane] = v[k];
             }
             __syncthreads();
         }
+    }
     const int nd = ndyn;
     for (int r = tid; r < n; r += bs)
     {
@@ -894,72 +985,153 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
         leaf[r] = uint16_t(j | (j >= nd ? 0x8000 : 0));
     }
     __syncthreads(); // the sort keys are dead from here on; their space holds the queue
+    // The box test of sorted positions a < b: closed intervals on the exact fat boxes, static-static
+    // pairs skipped. Written without short-circuits, so that the loads of a test issue together.
+    // The FP32 boxes are rounded outward in the FP64 form, so where every FP32 overlap exceeds 4
+    // FP32 ulps of its coordinates the exact boxes overlap as well; only the near-touching hits
+    // are confirmed by the inclusive compares of the exact fat boxes.
+    auto overlaps = [&](int ra, const float *qa, bool a_static, int rb) {
+        const float *qb = box + 6 * rb;
+        const float b0 = qb[0], b1 = qb[1], b2 = qb[2], b3 = qb[3], b4 = qb[4], b5 = qb[5];
+        bool hit = !(a_static & ((leaf[rb] & 0x8000) != 0)) & (b0 <= qa[3]) & (b3 >= qa[0]) & (b1 <= qa[4]) &
+                   (b4 >= qa[1]) & (b2 <= qa[5]) & (b5 >= qa[2]);
+        if constexpr (sizeof(T) == 8)
+        {
+            auto clear = [](float hi, float lo) {
+                return hi - lo > 4.0f * EpsOf<float>::v * fmaxf(fabsf(hi), fabsf(lo)) + 1e-30f;
+            };
+            if (hit && !(clear(qa[3], b0) & clear(b3, qa[0]) & clear(qa[4], b1) & clear(b4, qa[1]) &
+                         clear(qa[5], b2) & clear(b5, qa[2])))
+            {
+                const Aabb<T> ba = d.tbox[int(sval[lo + (leaf[ra] & 0xFFF)])];
+                const Aabb<T> bb = d.tbox[int(sval[lo + (leaf[rb] & 0xFFF)])];
+                hit = bb.mn.x <= ba.mx.x && bb.mx.x >= ba.mn.x && bb.mn.y <= ba.mx.y && bb.mx.y >= ba.mn.y &&
+                      bb.mn.z <= ba.mx.z && bb.mx.z >= ba.mn.z;
+            }
+        }
+        return hit;
+    };
+    // the end of a window: the first sorted position after ra whose lower bound passes upa
+    auto window_end = [&](int ra, float upa) {
+        int a = ra + 1, b = n;
+        while (a < b)
+        {
+            const int m = (a + b) >> 1;
+            if (lowax[m] > upa)
+                b = m;
+            else
+                a = m + 1;
+        }
+        return a;
+    };
     for (int pass = 0; pass < 2; ++pass)
     {
         // pass 0 queues; pass 1 only runs after a queue overflow and emits straight to the list
         if (pass == 1 && fill <= QCAP) break;
-        for (int r = warp; r < n - 1; r += nw)
-        {
-            const float *qa = box + 6 * r;
-            const float qnx = qa[0], qny = qa[1], qnz = qa[2], qxx = qa[3], qxy = qa[4], qxz = qa[5];
-            const float upa = ax == 0 ? qxx : (ax == 1 ? qxy : qxz);
-            const bool a_static = (leaf[r] & 0x8000) != 0;
-            for (int base = r + 1; base < n; base += 32)
+        // Queue appends: a warp reserves kBroadChunk entries at a time with one shared atomic and
+        // fills them in order; what a warp leaves of a chunk holds kBroadHole entries.
+        int cbase = 0, cleft = 0; // warp-uniform
+        auto hole = [&](int from, int count) {
+            for (int t = lane; t < count; t += 32)
+                if (from + t < QCAP) queue[from + t] = kBroadHole;
+        };
+        auto push = [&](bool hit, int ra, int rb) {
+            const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);
+            if (!hits) return;
+            if (pass == 1)
             {
-                const int sb = base + lane;
-                bool past = true, hit = false;
-                if (sb < n)
-                {
-                    past = lowax[sb] > upa;
-                    const float *qb = box + 6 * sb;
-                    hit = !past && !(a_static && (leaf[sb] & 0x8000)) && qb[0] <= qxx && qb[3] >= qnx &&
-                          qb[1] <= qxy && qb[4] >= qny && qb[2] <= qxz && qb[5] >= qnz;
-                    if constexpr (sizeof(T) == 8)
-                    {
-                        // The FP32 boxes are rounded outward, so where every FP32 overlap exceeds
-                        // 4 FP32 ulps of its coordinates the exact boxes overlap as well; only the
-                        // near-touching hits are confirmed by the inclusive compares of the exact
-                        // fat boxes.
-                        auto clear = [](float hi, float lo) {
-                            return hi - lo > 4.0f * EpsOf<float>::v * fmaxf(fabsf(hi), fabsf(lo)) + 1e-30f;
-                        };
-                        if (hit && !(clear(qxx, qb[0]) && clear(qb[3], qnx) && clear(qxy, qb[1]) && clear(qb[4], qny) &&
-                                     clear(qxz, qb[2]) && clear(qb[5], qnz)))
-                        {
-                            const Aabb<T> ba = d.tbox[int(sval[lo + (leaf[r] & 0xFFF)])];
-                            const Aabb<T> bb = d.tbox[int(sval[lo + (leaf[sb] & 0xFFF)])];
-                            hit = bb.mn.x <= ba.mx.x && bb.mx.x >= ba.mn.x && bb.mn.y <= ba.mx.y &&
-                                  bb.mx.y >= ba.mn.y && bb.mn.z <= ba.mx.z && bb.mx.z >= ba.mn.z;
-                        }
-                    }
-                }
-                const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);
-                if (hits)
-                {
-                    if (pass == 0)
-                    {
-                        int q0 = 0;
-                        if (lane == 0) q0 = atomicAdd(&fill, __popc(hits));
-                        q0 = __shfl_sync(0xFFFFFFFFu, q0, 0) + __popc(hits & ((1u << lane) - 1u));
-                        if (hit && q0 < QCAP) queue[q0] = uint32_t(r) | (uint32_t(sb) << 12);
-                    }
-                    else if (hit)
-                        broad_emit(d, w, lo, sval, int(leaf[r] & 0xFFF), int(leaf[sb] & 0xFFF), -1);
-                }
-                if (__any_sync(0xFFFFFFFFu, past)) break; // sorted: every later leaf is past too
+                if (hit) broad_emit(d, w, lo, sval, int(leaf[ra] & 0xFFF), int(leaf[rb] & 0xFFF), -1);
+                return;
+            }
+            const int c = __popc(hits);
+            if (c > cleft)
+            {
+                hole(cbase, cleft);
+                int b0 = 0;
+                if (lane == 0) b0 = atomicAdd(&fill, kBroadChunk);
+                cbase = __shfl_sync(0xFFFFFFFFu, b0, 0);
+                cleft = kBroadChunk;
+            }
+            const int q = cbase + __popc(hits & ((1u << lane) - 1u));
+            if (hit && q < QCAP) queue[q] = uint32_t(ra) | (uint32_t(rb) << 12);
+            cbase += c;
+            cleft -= c;
+        };
+        // a warp tests sorted position ra against positions [from, to), 64 a turn
+        auto sweep_warp = [&](int ra, int from, int to) {
+            float qa[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) qa[k] = box[6 * ra + k];
+            const bool a_static = (leaf[ra] & 0x8000) != 0;
+            for (int base = from; base < to; base += 64)
+            {
+                const int s0 = base + lane, s1 = base + 32 + lane;
+                const bool h0 = (s0 < to) & overlaps(ra, qa, a_static, min(s0, n - 1));
+                const bool h1 = (s1 < to) & overlaps(ra, qa, a_static, min(s1, n - 1));
+                push(h0, ra, s0);
+                push(h1, ra, s1);
+            }
+        };
+        // A warp takes 32 consecutive sorted positions, one per lane; each lane finds the end of
+        // its window and tests up to kBroadLaneSpan candidates of it, four a turn (neighbouring
+        // positions have windows of similar length). The rest of longer windows, such as those of
+        // static walls that span the world, is tested by the whole warp.
+        for (int g = warp * 32; g < n - 1; g += nw * 32)
+        {
+            const int r = g + lane;
+            const bool has = r < n - 1;
+            float qa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool a_static = false;
+            int end = r + 1;
+            if (has)
+            {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) qa[k] = box[6 * r + k];
+                a_static = (leaf[r] & 0x8000) != 0;
+                end = window_end(r, ax == 0 ? qa[3] : (ax == 1 ? qa[4] : qa[5]));
+            }
+            const int lane_end = min(end, r + 1 + kBroadLaneSpan);
+            for (int k = r + 1; __any_sync(0xFFFFFFFFu, k < lane_end); k += 4)
+            {
+                bool h[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) h[u] = (k + u < lane_end) & overlaps(r, qa, a_static, min(k + u, n - 1));
+#pragma unroll
+                for (int u = 0; u < 4; ++u) push(h[u], r, k + u);
+            }
+            unsigned rest = __ballot_sync(0xFFFFFFFFu, end > lane_end);
+            while (rest)
+            {
+                const int l = __ffs(rest) - 1;
+                rest &= rest - 1;
+                sweep_warp(g + l, __shfl_sync(0xFFFFFFFFu, lane_end, l), __shfl_sync(0xFFFFFFFFu, end, l));
             }
         }
+        if (pass == 0) hole(cbase, cleft);
         __syncthreads();
     }
     const int nq = fill;
     if (nq > QCAP) return; // emitted by the second sweep
-    // drop the pairs the reference does not pair yet, then one reservation for the rest
+    // Per sorted position its device slot and world-local index, in the space of the boxes (no
+    // longer read): the pair checks and writes below then read shared memory only.
+    uint32_t *pslot = reinterpret_cast<uint32_t *>(box), *ploc = pslot + n;
+    for (int r = tid; r < n; r += bs)
+    {
+        const int i = int(sval[lo + (leaf[r] & 0xFFF)]);
+        pslot[r] = uint32_t(i);
+        ploc[r] = d.meta[i].local;
+    }
+    __syncthreads();
+    // drop the pairs the reference does not pair yet, then one reservation for the rest. Every
+    // pair has a dynamic end, so where each dynamic body was reinserted at or after the newest
+    // creation in the world, every pair is allowed and the check is skipped.
+    const bool young = oldest_reinserted < newest_created;
     int mine = 0;
     for (int q = tid; q < nq; q += bs)
     {
         const uint32_t e = queue[q];
-        const int ja = leaf[e & 0xFFFu] & 0xFFF, jb = leaf[(e >> 12) & 0xFFFu] & 0xFFF;
-        if (pair_allowed<T>(d.meta[int(sval[lo + ja])], d.meta[int(sval[lo + jb])]))
+        if (e & 0x80000000u) continue; // a hole
+        if (!young || pair_allowed<T>(d.meta[pslot[e & 0xFFFu]], d.meta[pslot[(e >> 12) & 0xFFFu]]))
             ++mine;
         else
             queue[q] = e | 0x80000000u;
@@ -985,11 +1157,22 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
     }
     __syncthreads();
     int slot = cta_base + warp_count[warp] + before - mine;
+    const uint64_t wkey = uint64_t(w) << (2 * d.lbits);
     for (int q = tid; q < nq; q += bs)
     {
         const uint32_t e = queue[q];
         if (e & 0x80000000u) continue;
-        broad_emit(d, w, lo, sval, int(leaf[e & 0xFFFu] & 0xFFF), int(leaf[(e >> 12) & 0xFFFu] & 0xFFF), slot++);
+        const int ra = int(e & 0xFFFu), rb = int((e >> 12) & 0xFFFu);
+        const uint32_t la = ploc[ra], lb = ploc[rb];
+        const bool a_first = la < lb;
+        if (slot < d.pair_cap)
+        {
+            d.pkey[slot] = wkey | (uint64_t(a_first ? la : lb) << d.lbits) | uint64_t(a_first ? lb : la);
+            d.pval[slot] = (uint64_t(a_first ? pslot[ra] : pslot[rb]) << 32) | (a_first ? pslot[rb] : pslot[ra]);
+        }
+        else
+            atomicOr(d.status, ST_PAIR_OVERFLOW);
+        ++slot;
     }
 }
 
