@@ -795,9 +795,8 @@ __device__ __forceinline__ void broad_emit(const Dev<T> &d, int w, int lo, const
 constexpr int kBroadPow2 = 4096;  // sort capacity, a power of two >= kBroadMax, indices in 12 bits
 constexpr int kBroadQueue = 10240; // queued pairs per world (two 12-bit sorted positions each)
 static_assert(kBroadPow2 >= kBroadMax && kBroadPow2 <= 4096, "sort capacity");
-constexpr int kBroadChunk = 64;               // queue entries a warp reserves at a time
-constexpr int kBroadLaneSpan = 64;            // window positions a lane tests before its warp helps
-constexpr uint32_t kBroadHole = 0xFFFFFFFFu;  // an unused queue entry (bit 31: skipped)
+constexpr int kBroadLaneSpan = 64; // window positions a lane tests before its warp helps
+constexpr int kBroadLong = 32;     // long windows shared out to every warp of the CTA
 static_assert(kBroadQueue * 4 >= kBroadPow2 * 8, "the sort keys live in the queue's space");
 
 // Shared memory of a sweep-and-prune CTA: the queue, then per leaf its box in FP32 (rounded outward
@@ -860,8 +859,14 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
     constexpr int MAXP = MAXN <= 256 ? 256 : (MAXN <= 512 ? 512 : (MAXN <= 1024 ? 1024 : (MAXN <= 2048 ? 2048 : 4096)));
     constexpr int E = MAXP / THREADS, SE = 32 * E;
     static_assert(E >= 1 && E * THREADS == MAXP && QCAP * 4 >= 8 * MAXP, "sort layout");
+    // Queue: SLICE entries per thread (entry c of thread t at c * THREADS + t, so a warp's stores
+    // touch distinct banks), then OCAP entries that threads with full slices take by an atomic.
+    constexpr int SLICE = QCAP * 3 / 4 / THREADS, OCAP = QCAP - SLICE * THREADS;
+    static_assert(SLICE >= 8 && OCAP > 0, "queue layout");
     extern __shared__ __align__(16) unsigned char broad_smem[];
-    __shared__ int ndyn, fill, cta_base, newest_created, oldest_reinserted;
+    __shared__ int ndyn, ofill, cta_base, newest_created, oldest_reinserted, nlong;
+    __shared__ unsigned coord_max; // largest |coordinate| of the world's FP32 boxes (as bits)
+    __shared__ int long_at[kBroadLong], long_from[kBroadLong], long_to[kBroadLong];
     __shared__ int warp_count[16];
     const int w = blockIdx.x;
     const int lo = d.wleaf_lo[w];
@@ -892,7 +897,8 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
     if (tid == 0)
     {
         ndyn = n;
-        fill = 0;
+        ofill = 0;
+        coord_max = 0u;
         newest_created = INT_MIN;
         oldest_reinserted = INT_MAX;
     }
@@ -967,6 +973,7 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
         }
     }
     const int nd = ndyn;
+    float my_max = 0.f;
     for (int r = tid; r < n; r += bs)
     {
         const uint64_t e = srt[r];
@@ -983,25 +990,40 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
         o[5] = up_f(b.mx.z);
         lowax[r] = ord2f(uint32_t(e >> 32));
         leaf[r] = uint16_t(j | (j >= nd ? 0x8000 : 0));
+        if constexpr (sizeof(T) == 8)
+            my_max = fmaxf(my_max, fmaxf(fmaxf(fmaxf(fabsf(o[0]), fabsf(o[1])), fmaxf(fabsf(o[2]), fabsf(o[3]))),
+                                         fmaxf(fabsf(o[4]), fabsf(o[5]))));
+    }
+    if constexpr (sizeof(T) == 8)
+    {
+        const unsigned mb = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(my_max)); // >= 0: orders as bits
+        if (lane == 0) atomicMax(&coord_max, mb);
     }
     __syncthreads(); // the sort keys are dead from here on; their space holds the queue
     // The box test of sorted positions a < b: closed intervals on the exact fat boxes, static-static
     // pairs skipped. Written without short-circuits, so that the loads of a test issue together.
-    // The FP32 boxes are rounded outward in the FP64 form, so where every FP32 overlap exceeds 4
-    // FP32 ulps of its coordinates the exact boxes overlap as well; only the near-touching hits
-    // are confirmed by the inclusive compares of the exact fat boxes.
-    auto overlaps = [&](int ra, const float *qa, bool a_static, int rb) {
+    // The FP32 boxes are rounded outward in the FP64 form. Two FP32 roundings move an overlap by
+    // less than 2 eps M, M the largest coordinate magnitude of the world, so where the FP32 boxes
+    // overlap by more than slack = 4 eps M on every axis (tested on a's box shrunk by the slack,
+    // rounded inward: qs) the exact boxes overlap as well; only the other hits are confirmed by the
+    // inclusive compares of the exact fat boxes.
+    const float slack = 4.0f * EpsOf<float>::v * __uint_as_float(coord_max) + 1e-30f;
+    auto shrink = [&](const float *qa, float *qs) {
+        for (int k = 0; k < 3; ++k)
+        {
+            qs[k] = __fadd_ru(qa[k], slack);
+            qs[k + 3] = __fsub_rd(qa[k + 3], slack);
+        }
+    };
+    auto overlaps = [&](int ra, const float *qa, const float *qs, bool a_static, int rb) {
         const float *qb = box + 6 * rb;
         const float b0 = qb[0], b1 = qb[1], b2 = qb[2], b3 = qb[3], b4 = qb[4], b5 = qb[5];
         bool hit = !(a_static & ((leaf[rb] & 0x8000) != 0)) & (b0 <= qa[3]) & (b3 >= qa[0]) & (b1 <= qa[4]) &
                    (b4 >= qa[1]) & (b2 <= qa[5]) & (b5 >= qa[2]);
         if constexpr (sizeof(T) == 8)
         {
-            auto clear = [](float hi, float lo) {
-                return hi - lo > 4.0f * EpsOf<float>::v * fmaxf(fabsf(hi), fabsf(lo)) + 1e-30f;
-            };
-            if (hit && !(clear(qa[3], b0) & clear(b3, qa[0]) & clear(qa[4], b1) & clear(b4, qa[1]) &
-                         clear(qa[5], b2) & clear(b5, qa[2])))
+            const bool sure = (b0 < qs[3]) & (b3 > qs[0]) & (b1 < qs[4]) & (b4 > qs[1]) & (b2 < qs[5]) & (b5 > qs[2]);
+            if (hit & !sure)
             {
                 const Aabb<T> ba = d.tbox[int(sval[lo + (leaf[ra] & 0xFFF)])];
                 const Aabb<T> bb = d.tbox[int(sval[lo + (leaf[rb] & 0xFFF)])];
@@ -1024,50 +1046,43 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
         }
         return a;
     };
+    int own = 0; // pairs this thread queued (those past SLICE went to the overflow region)
     for (int pass = 0; pass < 2; ++pass)
     {
         // pass 0 queues; pass 1 only runs after a queue overflow and emits straight to the list
-        if (pass == 1 && fill <= QCAP) break;
-        // Queue appends: a warp reserves kBroadChunk entries at a time with one shared atomic and
-        // fills them in order; what a warp leaves of a chunk holds kBroadHole entries.
-        int cbase = 0, cleft = 0; // warp-uniform
-        auto hole = [&](int from, int count) {
-            for (int t = lane; t < count; t += 32)
-                if (from + t < QCAP) queue[from + t] = kBroadHole;
-        };
+        if (pass == 1 && ofill <= OCAP) break;
+        if (tid == 0) nlong = 0;
+        __syncthreads();
         auto push = [&](bool hit, int ra, int rb) {
-            const unsigned hits = __ballot_sync(0xFFFFFFFFu, hit);
-            if (!hits) return;
+            if (!hit) return;
             if (pass == 1)
             {
-                if (hit) broad_emit(d, w, lo, sval, int(leaf[ra] & 0xFFF), int(leaf[rb] & 0xFFF), -1);
+                broad_emit(d, w, lo, sval, int(leaf[ra] & 0xFFF), int(leaf[rb] & 0xFFF), -1);
                 return;
             }
-            const int c = __popc(hits);
-            if (c > cleft)
+            const uint32_t e = uint32_t(ra) | (uint32_t(rb) << 12);
+            if (own < SLICE)
+                queue[own * THREADS + tid] = e;
+            else
             {
-                hole(cbase, cleft);
-                int b0 = 0;
-                if (lane == 0) b0 = atomicAdd(&fill, kBroadChunk);
-                cbase = __shfl_sync(0xFFFFFFFFu, b0, 0);
-                cleft = kBroadChunk;
+                const int o = atomicAdd(&ofill, 1);
+                if (o < OCAP) queue[SLICE * THREADS + o] = e;
             }
-            const int q = cbase + __popc(hits & ((1u << lane) - 1u));
-            if (hit && q < QCAP) queue[q] = uint32_t(ra) | (uint32_t(rb) << 12);
-            cbase += c;
-            cleft -= c;
+            ++own;
         };
-        // a warp tests sorted position ra against positions [from, to), 64 a turn
-        auto sweep_warp = [&](int ra, int from, int to) {
-            float qa[6];
+        // a warp tests sorted position ra against positions [from, to), 64 a turn, taking every
+        // `step`-th block of 64
+        auto sweep_warp = [&](int ra, int from, int to, int step) {
+            float qa[6], qs[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) qa[k] = box[6 * ra + k];
+            if constexpr (sizeof(T) == 8) shrink(qa, qs);
             const bool a_static = (leaf[ra] & 0x8000) != 0;
-            for (int base = from; base < to; base += 64)
+            for (int base = from; base < to; base += 64 * step)
             {
                 const int s0 = base + lane, s1 = base + 32 + lane;
-                const bool h0 = (s0 < to) & overlaps(ra, qa, a_static, min(s0, n - 1));
-                const bool h1 = (s1 < to) & overlaps(ra, qa, a_static, min(s1, n - 1));
+                const bool h0 = (s0 < to) & overlaps(ra, qa, qs, a_static, min(s0, n - 1));
+                const bool h1 = (s1 < to) & overlaps(ra, qa, qs, a_static, min(s1, n - 1));
                 push(h0, ra, s0);
                 push(h1, ra, s1);
             }
@@ -1075,12 +1090,12 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
         // A warp takes 32 consecutive sorted positions, one per lane; each lane finds the end of
         // its window and tests up to kBroadLaneSpan candidates of it, four a turn (neighbouring
         // positions have windows of similar length). The rest of longer windows, such as those of
-        // static walls that span the world, is tested by the whole warp.
+        // static walls that span the world, is listed and shared out to all warps afterwards.
         for (int g = warp * 32; g < n - 1; g += nw * 32)
         {
             const int r = g + lane;
             const bool has = r < n - 1;
-            float qa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float qa[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, qs[6];
             bool a_static = false;
             int end = r + 1;
             if (has)
@@ -1090,28 +1105,47 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
                 a_static = (leaf[r] & 0x8000) != 0;
                 end = window_end(r, ax == 0 ? qa[3] : (ax == 1 ? qa[4] : qa[5]));
             }
+            if constexpr (sizeof(T) == 8) shrink(qa, qs);
             const int lane_end = min(end, r + 1 + kBroadLaneSpan);
             for (int k = r + 1; __any_sync(0xFFFFFFFFu, k < lane_end); k += 4)
             {
                 bool h[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) h[u] = (k + u < lane_end) & overlaps(r, qa, a_static, min(k + u, n - 1));
+                for (int u = 0; u < 4; ++u)
+                    h[u] = (k + u < lane_end) & overlaps(r, qa, qs, a_static, min(k + u, n - 1));
 #pragma unroll
                 for (int u = 0; u < 4; ++u) push(h[u], r, k + u);
             }
-            unsigned rest = __ballot_sync(0xFFFFFFFFu, end > lane_end);
-            while (rest)
+            const bool longer = end > lane_end;
+            const unsigned rest = __ballot_sync(0xFFFFFFFFu, longer);
+            if (rest)
             {
-                const int l = __ffs(rest) - 1;
-                rest &= rest - 1;
-                sweep_warp(g + l, __shfl_sync(0xFFFFFFFFu, lane_end, l), __shfl_sync(0xFFFFFFFFu, end, l));
+                int at = 0;
+                if (lane == 0) at = atomicAdd(&nlong, __popc(rest));
+                at = __shfl_sync(0xFFFFFFFFu, at, 0) + __popc(rest & ((1u << lane) - 1u));
+                if (longer && at < kBroadLong)
+                {
+                    long_at[at] = r;
+                    long_from[at] = lane_end;
+                    long_to[at] = end;
+                }
+                // a full list: this warp tests its own
+                unsigned own = __ballot_sync(0xFFFFFFFFu, longer && at >= kBroadLong);
+                while (own)
+                {
+                    const int l = __ffs(own) - 1;
+                    own &= own - 1;
+                    sweep_warp(g + l, __shfl_sync(0xFFFFFFFFu, lane_end, l), __shfl_sync(0xFFFFFFFFu, end, l), 1);
+                }
             }
         }
-        if (pass == 0) hole(cbase, cleft);
+        __syncthreads();
+        for (int k = 0, nl = min(nlong, kBroadLong); k < nl; ++k)
+            sweep_warp(long_at[k], long_from[k] + 64 * warp, long_to[k], nw);
         __syncthreads();
     }
-    const int nq = fill;
-    if (nq > QCAP) return; // emitted by the second sweep
+    if (ofill > OCAP) return; // emitted by the second sweep
+    const int mine_own = min(own, SLICE), novf = ofill;
     // Per sorted position its device slot and world-local index, in the space of the boxes (no
     // longer read): the pair checks and writes below then read shared memory only.
     uint32_t *pslot = reinterpret_cast<uint32_t *>(box), *ploc = pslot + n;
@@ -1126,11 +1160,16 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
     // pair has a dynamic end, so where each dynamic body was reinserted at or after the newest
     // creation in the world, every pair is allowed and the check is skipped.
     const bool young = oldest_reinserted < newest_created;
+    // a thread's entries: its slice, then every bs-th entry of the overflow region
+    auto entry_at = [&](int k) {
+        return k < mine_own ? k * THREADS + tid : SLICE * THREADS + tid + (k - mine_own) * THREADS;
+    };
+    const int nmine = mine_own + (novf > tid ? (novf - tid + THREADS - 1) / THREADS : 0);
     int mine = 0;
-    for (int q = tid; q < nq; q += bs)
+    for (int k = 0; k < nmine; ++k)
     {
+        const int q = entry_at(k);
         const uint32_t e = queue[q];
-        if (e & 0x80000000u) continue; // a hole
         if (!young || pair_allowed<T>(d.meta[pslot[e & 0xFFFu]], d.meta[pslot[(e >> 12) & 0xFFFu]]))
             ++mine;
         else
@@ -1158,9 +1197,9 @@ __global__ void __launch_bounds__(THREADS) k_broad_small(Dev<T> d, const uint64_
     __syncthreads();
     int slot = cta_base + warp_count[warp] + before - mine;
     const uint64_t wkey = uint64_t(w) << (2 * d.lbits);
-    for (int q = tid; q < nq; q += bs)
+    for (int k = 0; k < nmine; ++k)
     {
-        const uint32_t e = queue[q];
+        const uint32_t e = queue[entry_at(k)];
         if (e & 0x80000000u) continue;
         const int ra = int(e & 0xFFFu), rb = int((e >> 12) & 0xFFFu);
         const uint32_t la = ploc[ra], lb = ploc[rb];
