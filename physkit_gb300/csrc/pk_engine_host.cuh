@@ -216,8 +216,10 @@ public:
         PK_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
         PK_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         PK_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        PK_CUDA(cudaStreamCreateWithFlags(&st3_, cudaStreamNonBlocking));
         PK_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
         PK_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
+        PK_CUDA(cudaEventCreateWithFlags(&join3_, cudaEventDisableTiming));
         PK_CUDA(cudaStreamCreateWithFlags(&cs_, cudaStreamNonBlocking));
         for (int k = 0; k < 2; ++k)
         {
@@ -1237,7 +1239,8 @@ private:
     Dev<T> d_{};
     cudaStream_t st_ = nullptr;
     cudaStream_t st2_ = nullptr; // the solver's small-world launches run beside the large-world one
-    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    cudaStream_t st3_ = nullptr; // with st2_: the sweep's size classes run side by side
+    cudaEvent_t fork_ = nullptr, join_ = nullptr, join3_ = nullptr;
     int sms_ = 1;
     int nslots_ = 0;
     int parity_ = 0;
@@ -1333,11 +1336,11 @@ private:
         return cudaMalloc(const_cast<void **>(reinterpret_cast<const void **>(p)), sizeof(U) * n);
     }
     static int solve_threads(int t) { return t < solve_max_threads<T>() ? t : solve_max_threads<T>(); }
-    template <int C> void launch_broad(const Dev<T> &d, const uint64_t *skey, const uint64_t *sval)
+    template <int C> void launch_broad(const Dev<T> &d, const uint64_t *skey, const uint64_t *sval, cudaStream_t st)
     {
         constexpr BroadClass c = kBroadClasses[C];
         k_broad_small<T, c.minn, c.maxn, c.qcap, c.threads>
-            <<<cfg_.max_worlds, c.threads, broad_smem_bytes<c.maxn, c.qcap>(), st_>>>(d, skey, sval);
+            <<<cfg_.max_worlds, c.threads, broad_smem_bytes<c.maxn, c.qcap>(), st>>>(d, skey, sval);
     }
     // The joint-free instances serve batches that never had joints (buffers unallocated).
     void launch_solve(int blocks, int threads, size_t smem, const Dev<T> &d, const uint64_t *pv, int first, int cache,
@@ -1399,9 +1402,12 @@ private:
         st_ = nullptr;
         if (st2_) cudaStreamDestroy(st2_);
         st2_ = nullptr;
+        if (st3_) cudaStreamDestroy(st3_);
+        st3_ = nullptr;
         if (fork_) cudaEventDestroy(fork_);
         if (join_) cudaEventDestroy(join_);
-        fork_ = join_ = nullptr;
+        if (join3_) cudaEventDestroy(join3_);
+        fork_ = join_ = join3_ = nullptr;
     }
 
     int enqueue_step(T dt, int parity)
@@ -1435,9 +1441,19 @@ private:
         k_lbvh_refit<T><<<gb, 256, 0, st_>>>(d, sval, true);
         PK_CUDA(mark(3));
         k_traverse<T><<<(N + tune_.traverse_threads - 1) / tune_.traverse_threads, tune_.traverse_threads, 0, st_>>>(d, sval);
-        launch_broad<0>(d, skey, sval);
-        launch_broad<1>(d, skey, sval);
-        launch_broad<2>(d, skey, sval);
+        // The sweep's three size classes run side by side, so that the SMs one class's last wave
+        // leaves idle take the others' CTAs. Their worlds are disjoint, and the pair list they
+        // append to is sorted after them.
+        PK_CUDA(cudaEventRecord(fork_, st_));
+        PK_CUDA(cudaStreamWaitEvent(st2_, fork_, 0));
+        PK_CUDA(cudaStreamWaitEvent(st3_, fork_, 0));
+        launch_broad<2>(d, skey, sval, st_);
+        launch_broad<1>(d, skey, sval, st2_);
+        launch_broad<0>(d, skey, sval, st3_);
+        PK_CUDA(cudaEventRecord(join_, st2_));
+        PK_CUDA(cudaEventRecord(join3_, st3_));
+        PK_CUDA(cudaStreamWaitEvent(st_, join_, 0));
+        PK_CUDA(cudaStreamWaitEvent(st_, join3_, 0));
         k_clamp_pairs<T><<<1, 1, 0, st_>>>(d);
         k_kept_count<T><<<cfg_.max_worlds, 256, 0, st_>>>(d);
         PK_CUDA(mark(4));
