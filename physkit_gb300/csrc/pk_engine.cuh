@@ -783,15 +783,16 @@ __device__ __forceinline__ void broad_emit(const Dev<T> &d, int w, int lo, const
 //  3. each sorted leaf a tests the leaves after it up to the first whose lower bound passes a's
 //     upper bound (found by binary search), so every pair overlapping on the axis is met once,
 //     from its earlier leaf: a lane per leaf, four candidates a turn, and the whole warp for the
-//     rest of long windows; the overlapping pairs are queued in shared memory;
+//     rest of long windows; each thread queues the overlapping pairs it finds in its own slice of
+//     a queue in shared memory;
 //  4. the CTA drops queued pairs the reference does not pair yet (pair_allowed; only checked in a
 //     world where some dynamic body was not reinserted since the newest creation), reserves its
 //     range of the pair list with one atomic and writes the pairs there.
 // A world's static leaves sort after its dynamic ones in the leaf list, so "leaf >= first static"
 // marks them and static-static pairs are skipped. The pair test is the traversal's (closed
 // intervals on the exact fat boxes), so the pair set is the same; sweep bounds are rounded outward
-// to FP32, which only widens the window. A world whose overlaps overflow the queue sweeps again and
-// emits straight to the pair list.
+// to FP32, which only widens the window. A world whose pairs overflow the queue (the slices and the
+// shared region after them) sweeps again and emits straight to the pair list.
 constexpr int kBroadPow2 = 4096;  // sort capacity, a power of two >= kBroadMax, indices in 12 bits
 constexpr int kBroadQueue = 10240; // queued pairs per world (two 12-bit sorted positions each)
 static_assert(kBroadPow2 >= kBroadMax && kBroadPow2 <= 4096, "sort capacity");
